@@ -1,0 +1,283 @@
+/*
+ * tval3_c.h -- C ABI of the GB300 (sm_103a) TVAL3 reconstructor.
+ *
+ * Drop-in boundary for the reference's tval3_gpu_3d / tval3_gpu entry points
+ * and its mat_vec_mul operator interface (modk/tval3-gpu).  Plain C types and
+ * pointers only; every function returns a tval3_status and, on failure, sets
+ * a thread-local message readable with tval3_last_error_message().  The C++
+ * header tval3.hpp restores the reference's overloads, container classes and
+ * exception types on top of these functions.
+ *
+ * Data layout: volumes are column-major with y fastest (the reference's
+ * mat_host with dim_y, dim_x, dim_z; 3d/tval3_gpu_3d_kernels.cu:1501):
+ * voxel (y, x, z) is element y + dim_y*(x + dim_x*z).  Sparse matrices are
+ * A (rays x voxels) in CSR, plus optionally the CSR of A^T (the reference's
+ * CSC arrays, 3d/tval3_gpu_3d.cpp:1463).
+ */
+#ifndef TVAL3_C_H_
+#define TVAL3_C_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define TVAL3_API
+#else
+#define TVAL3_API __attribute__((visibility("default")))
+#endif
+
+/* Status codes.  Replace the reference's exceptions (tval3_gpu_exception,
+ * cuda_exception, illegal_mat_gpu_assignment; 2d/tval3_types.h:45-49,
+ * 2d/handle_error.h:14-41). */
+typedef enum tval3_status {
+    TVAL3_OK = 0,
+    TVAL3_ERR_ARG = 1,        /* argument error (reference: "Argument error: ...") */
+    TVAL3_ERR_SHAPE = 2,      /* inconsistent dimensions */
+    TVAL3_ERR_CUDA = 3,       /* CUDA runtime error */
+    TVAL3_ERR_NOMEM = 4,      /* device or host allocation failed */
+    TVAL3_ERR_TIMEOUT = 5,    /* a bounded device wait expired */
+    TVAL3_ERR_NONFINITE = 6,  /* NaN/Inf in an input */
+    TVAL3_ERR_UNSUPPORTED = 7 /* combination not provided by this build */
+} tval3_status;
+
+typedef enum tval3_tv { TVAL3_TV_ANISO = 0, TVAL3_TV_ISO = 1 } tval3_tv;
+
+/* Storage precision of operator values. */
+typedef enum tval3_precision {
+    TVAL3_PREC_FP32 = 0,
+    TVAL3_PREC_FP64 = 1,
+    TVAL3_PREC_BF16 = 2, /* BF16 values with per-row FP32 scale, FP32 accumulation */
+    TVAL3_PREC_FP16 = 3, /* FP16 values with per-row FP32 scale, FP32 accumulation */
+    TVAL3_PREC_FP32_F64VEC = 4 /* FP32 values, FP64 vectors, products and reductions */
+} tval3_precision;
+
+typedef enum tval3_trans { TVAL3_OP_N = 0, TVAL3_OP_T = 1 } tval3_trans;
+
+/* Options: the fields of tval3_options (2d/tval3_types.h:7-35) and the 3D
+ * skip-multiplication fields (3d/tval3_gpu_3d.cpp:194-197), plus tv_type.
+ * tval3_options_default() sets the reference defaults (2d/tval3_types.h:29-33). */
+typedef struct tval3_options {
+    double mu;        /* maximum mu */
+    double mu0;       /* initial mu */
+    double beta;      /* maximum beta */
+    double beta0;     /* initial beta */
+    double rate_cnt;  /* continuation rate of mu and beta */
+    double tol;       /* outer tolerance */
+    double tol_inn;   /* inner tolerance */
+    int maxcnt;       /* maximum outer iterations */
+    int maxit;        /* maximum total iterations */
+    double c;         /* Armijo parameter */
+    double gamma;     /* backtracking factor */
+    double gam;       /* nonmonotone weight */
+    double rate_gam;  /* shrink rate of gam after a failed backtracking */
+    int isreal;       /* kept for interface compatibility (unused, as in the reference) */
+    int nonneg;       /* project onto U >= 0 */
+    unsigned numInitIterations; /* skip heuristic: must be 0 / skipMulRatio 0 (exact products) */
+    double skipMulRatio;
+    double maxRelativeChange;
+    int tv_type;      /* tval3_tv; the reference is anisotropic */
+} tval3_options;
+
+/* Result summary (tval3_info, 2d/tval3_types.h:37-43; outer_secs
+ * 3d/tval3_gpu_3d.cpp:1507) plus line-search counters. */
+typedef struct tval3_info {
+    int total_iters;
+    int outer_iters;
+    double rel_chg;
+    double rel_error;
+    double secs;
+    double outer_secs;
+    int backtracks;
+    int restarts;
+    double final_f;
+} tval3_info;
+
+/* Sparse matrix in host memory (sparse_mat_host, 2d/container_host.h:78-127).
+ * rows = m (measurements, reference A.dim_y), cols = n (voxels, A.dim_x).
+ * format: 1 = CSR only, 2 = CSC only, 3 = both (the 3D reference requires 3,
+ * 3d/tval3_gpu_3d.cpp:1463; this library builds whichever part is missing).
+ * val_type: TVAL3_PREC_FP32 or TVAL3_PREC_FP64 (type of csr_val / csc_val). */
+typedef struct tval3_sparse_host {
+    int rows, cols, nnz;
+    int format;
+    int val_type;
+    const int* csr_ptr;
+    const int* csr_ind;
+    const void* csr_val;
+    const int* csc_ptr;
+    const int* csc_ind;
+    const void* csc_val;
+} tval3_sparse_host;
+
+#define TVAL3_SPARSE_CSR 1
+#define TVAL3_SPARSE_CSC 2
+#define TVAL3_SPARSE_BOTH 3
+
+/* Dense matrix in host memory (mat_host, column-major by default;
+ * 3d/tval3_gpu_3d.cpp:1404 requires column-major). row_major = 1 accepts a
+ * row-major array too.  rows = m, cols = n. */
+typedef struct tval3_dense_host {
+    int rows, cols;
+    int row_major;
+    int val_type;
+    const void* data;
+} tval3_dense_host;
+
+/* Measurement geometry (geometry_host; fields read by geometry_device,
+ * 3d/container_device.h:683-750).  Coordinates are voxel indices per
+ * measurement position: x_emitters[numMPs*num_emitters] etc.  use_path
+ * (num_emitters*num_receivers flags, may be NULL = all) selects the rays; the
+ * ray list is compacted as in 3d/mat_vec_mul_dynamic.h:477-556.
+ * traversal 0 = integer Bresenham (dyn_calc_kernel, weight scale_factor);
+ * traversal 1 = Siddon exact path lengths from the continuous coordinates
+ * *_pos (voxel units, NULL = voxel centres of the integer coordinates),
+ * multiplied by scale_factor. */
+typedef struct tval3_geometry_host {
+    int numMPs;
+    int num_emitters, num_receivers;
+    const int *x_emitters, *y_emitters, *z_emitters;
+    const int *x_receivers, *y_receivers, *z_receivers;
+    const unsigned* use_path;
+    int rv_x, rv_y, rv_z;
+    float scale_factor;
+    int traversal;
+    const double *xe_pos, *ye_pos, *ze_pos;
+    const double *xr_pos, *yr_pos, *zr_pos;
+} tval3_geometry_host;
+
+#define TVAL3_TRAVERSAL_BRESENHAM 0
+#define TVAL3_TRAVERSAL_SIDDON 1
+
+/* ---------------------------------------------------------------------- */
+TVAL3_API void tval3_options_default(tval3_options* opts);
+TVAL3_API const char* tval3_last_error_message(void);
+TVAL3_API const char* tval3_version(void);
+
+/* ---------------------------------------------------------------------- *
+ * Reference entry points.  U (dim_y x dim_x x dim_z, column-major) is output
+ * only; A and b are read; Ut (length n or NULL) enables info->rel_error.
+ * pagelocked / mainGPU / numGPUs / gpuArray are accepted for compatibility;
+ * this library runs on the current device only (one GPU).
+ * ---------------------------------------------------------------------- */
+
+/* tval3_gpu_3d(U, sparse_mat_host<float> A, b, opts, Ut, ...),
+ * 3d/tval3_gpu_3d.cpp:23-27 and :1454-1530 */
+TVAL3_API tval3_status tval3_gpu_3d_sparse_f32(float* U, int dim_y, int dim_x, int dim_z,
+                                               const tval3_sparse_host* A, const float* b, int b_len,
+                                               const tval3_options* opts, const float* Ut, int Ut_len,
+                                               int pagelocked, int mainGPU, int numGPUs, const int* gpuArray,
+                                               tval3_info* info);
+/* double instantiation, 3d/tval3_gpu_3d.cpp:46-50 */
+TVAL3_API tval3_status tval3_gpu_3d_sparse_f64(double* U, int dim_y, int dim_x, int dim_z,
+                                               const tval3_sparse_host* A, const double* b, int b_len,
+                                               const tval3_options* opts, const double* Ut, int Ut_len,
+                                               int pagelocked, int mainGPU, int numGPUs, const int* gpuArray,
+                                               tval3_info* info);
+/* tval3_gpu_3d(U, mat_host<float> A, ...), 3d/tval3_gpu_3d.cpp:29-33, :1395-1448 */
+TVAL3_API tval3_status tval3_gpu_3d_dense_f32(float* U, int dim_y, int dim_x, int dim_z,
+                                              const tval3_dense_host* A, const float* b, int b_len,
+                                              const tval3_options* opts, const float* Ut, int Ut_len,
+                                              int pagelocked, int mainGPU, int numGPUs, const int* gpuArray,
+                                              tval3_info* info);
+TVAL3_API tval3_status tval3_gpu_3d_dense_f64(double* U, int dim_y, int dim_x, int dim_z,
+                                              const tval3_dense_host* A, const double* b, int b_len,
+                                              const tval3_options* opts, const double* Ut, int Ut_len,
+                                              int pagelocked, int mainGPU, int numGPUs, const int* gpuArray,
+                                              tval3_info* info);
+/* tval3_gpu_3d(U, geometry_host A, ...), 3d/tval3_gpu_3d.cpp:35-39, :1533-1600 */
+TVAL3_API tval3_status tval3_gpu_3d_geometry_f32(float* U, int dim_y, int dim_x, int dim_z,
+                                                 const tval3_geometry_host* A, const float* b, int b_len,
+                                                 const tval3_options* opts, const float* Ut, int Ut_len,
+                                                 int pagelocked, int mainGPU, int numGPUs, const int* gpuArray,
+                                                 tval3_info* info);
+/* tval3_gpu_3d(U, geometry_host, sparse_mat_host, ...) (on-the-fly A*x,
+ * sparse A^T*y; sparse_geom_mm), 3d/tval3_gpu_3d.cpp:41-44, :1606-1667 */
+TVAL3_API tval3_status tval3_gpu_3d_geometry_sparse_f32(float* U, int dim_y, int dim_x, int dim_z,
+                                                        const tval3_geometry_host* A_geo,
+                                                        const tval3_sparse_host* A_mat, const float* b,
+                                                        int b_len, const tval3_options* opts, const float* Ut,
+                                                        int Ut_len, int pagelocked, int mainGPU, int numGPUs,
+                                                        const int* gpuArray, tval3_info* info);
+/* 2D: tval3_gpu(U, sparse_mat_host A, b, opts, Ut, pagelocked), 2d/tval3_gpu.h:9-13;
+ * U is rows x cols (dim_y x dim_x), periodic D in 2D (2d/tval3.cu:202-331). */
+TVAL3_API tval3_status tval3_gpu_sparse(float* U, int rows, int cols, const tval3_sparse_host* A, const float* b,
+                                        int b_len, const tval3_options* opts, const float* Ut, int Ut_len,
+                                        int pagelocked, tval3_info* info);
+/* 2D dense: tval3_gpu(U, mat_host A, ...), 2d/tval3_gpu.h:15-19 */
+TVAL3_API tval3_status tval3_gpu_dense(float* U, int rows, int cols, const tval3_dense_host* A, const float* b,
+                                       int b_len, const tval3_options* opts, const float* Ut, int Ut_len,
+                                       int pagelocked, tval3_info* info);
+
+/* ---------------------------------------------------------------------- *
+ * Operator handles: the mat_vec_mul interface (3d/mat_vec_mul_sparse.h:1703,
+ * 3d/mat_vec_mul_dense.h:37, 3d/mat_vec_mul_dynamic.h:683,
+ * 3d/mat_vec_mul.h:733).  A handle owns device copies of the operator; the
+ * products take DEVICE pointers and a stream.
+ * ---------------------------------------------------------------------- */
+typedef struct tval3_op_s* tval3_op;
+
+/* From host CSR (+ optional CSR of A^T).  precision selects the stored value
+ * type: FP32, BF16 or FP16 (the vector type of products is FP32), or FP64
+ * (vector type FP64).  The transpose is built on the device when absent. */
+TVAL3_API tval3_status tval3_op_create_sparse(tval3_op* op, const tval3_sparse_host* A, int precision);
+/* From device CSR arrays (copied; the caller keeps ownership).  val is FP32. */
+TVAL3_API tval3_status tval3_op_create_sparse_device(tval3_op* op, int rows, int cols, int nnz, const int* d_ptr,
+                                                     const int* d_ind, const float* d_val, int precision,
+                                                     void* stream);
+/* From a geometry: the ray matrix (Bresenham or Siddon) is built on the
+ * device.  mode 0: stored as CSR; mode 1: on-the-fly traversal (A*x gathers,
+ * A^T*y scatters), nothing stored. */
+TVAL3_API tval3_status tval3_op_create_geometry(tval3_op* op, const tval3_geometry_host* G, int mode, int precision);
+TVAL3_API tval3_status tval3_op_create_dense(tval3_op* op, const tval3_dense_host* A, int precision);
+TVAL3_API tval3_status tval3_op_destroy(tval3_op op);
+TVAL3_API tval3_status tval3_op_shape(tval3_op op, int* rows, int* cols, int64_t* nnz);
+/* Copy the device CSR (A and A^T) of a stored operator to host arrays
+ * (ptr: rows+1 / cols+1 ints, ind: nnz ints, val: nnz floats); any pointer may
+ * be NULL to skip that array.  Values are FP32 (dequantised for BF16/FP16). */
+TVAL3_API tval3_status tval3_op_export_csr(tval3_op op, int* ptr, int* ind, float* val, int* tptr, int* tind,
+                                           float* tval);
+/* mat_vec_mul(trans, A, x, y, stream): y = A x (trans = 0) or y = A^T x.
+ * x, y are device pointers of the operator's vector type (float, or double for
+ * FP64 operators).  Batched multi-RHS form: nrhs columns, leading dimension =
+ * vector length (the reference's `layers`, 2d/mat_vec_mul.h:65-71, :96-99). */
+TVAL3_API tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, void* stream);
+TVAL3_API tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, void* Y, void* stream);
+
+/* ---------------------------------------------------------------------- *
+ * Device-resident solver: a workspace bound to an operator and a volume;
+ * solve() takes DEVICE b and writes DEVICE U.  Repeated solves reuse the
+ * workspace (no allocation per call).
+ * ---------------------------------------------------------------------- */
+typedef struct tval3_solver_s* tval3_solver;
+TVAL3_API tval3_status tval3_solver_create(tval3_solver* s, tval3_op A, int dim_y, int dim_x, int dim_z,
+                                           const tval3_options* opts);
+/* mode 0: host-driven loop with device-resident scalars; mode 1: the whole
+ * solve as one CUDA graph with conditional nodes (no host round trips). */
+TVAL3_API tval3_status tval3_solver_set_mode(tval3_solver s, int mode);
+TVAL3_API tval3_status tval3_solver_solve(tval3_solver s, const void* d_b, void* d_U, const void* d_Ut,
+                                          tval3_info* info, void* stream);
+/* Record ||U_k/scl - xstar|| after every iteration k (xstar on device, length
+ * n; NULL disables).  Read with tval3_solver_trace (host array of maxit). */
+TVAL3_API tval3_status tval3_solver_set_trace(tval3_solver s, const void* d_xstar);
+TVAL3_API tval3_status tval3_solver_trace(tval3_solver s, double* host_err, int len);
+TVAL3_API tval3_status tval3_solver_destroy(tval3_solver s);
+
+/* ---------------------------------------------------------------------- *
+ * Stencil operators on device arrays (D_gpu / Dt_gpu, 3d/tval3_gpu_3d.cpp:
+ * 271-361).  DU holds 3 consecutive n-vectors (along y, x, z).
+ * ---------------------------------------------------------------------- */
+TVAL3_API tval3_status tval3_D_f32(int dim_y, int dim_x, int dim_z, const float* d_U, float* d_DU, void* stream);
+TVAL3_API tval3_status tval3_Dt_f32(int dim_y, int dim_x, int dim_z, const float* d_V, float* d_out, void* stream);
+TVAL3_API tval3_status tval3_D_f64(int dim_y, int dim_x, int dim_z, const double* d_U, double* d_DU, void* stream);
+TVAL3_API tval3_status tval3_Dt_f64(int dim_y, int dim_x, int dim_z, const double* d_V, double* d_out,
+                                    void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TVAL3_C_H_ */

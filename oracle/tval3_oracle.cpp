@@ -1,0 +1,799 @@
+/*
+ * tval3_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the oracle).
+ *
+ * A CPU restatement of the modk/tval3-gpu reconstruction path, written from the
+ * reference's behaviour.  It is the checker for tests/, for
+ * __graft_entry__.smoke() and for the cpu_baseline leg of bench.py; nothing in
+ * the shipped library links, loads or calls it.
+ *
+ * What it restates (paths are relative to the reference project):
+ *   - the TVAL3 3D main loop and its step functions, 3d/tval3_gpu_3d.cpp:85-1345
+ *     (b scaling :226-266, get_g :366-572, get_tau :577-666, descend :671-701,
+ *     update_g :706-818, min_u :823-891, get_gradient :896-919, shrinkage
+ *     :924-960, update_W :965-1029, update_mlp :1034-1083, loop :1089-1345);
+ *   - the periodic forward-difference operator D and its adjoint,
+ *     3d/tval3_gpu_3d_kernels.cu:170-215 and :479-510 (2D: 2d/tval3.cu:202-331);
+ *   - anisotropic shrinkage, 3d/tval3_gpu_3d_kernels.cu:1249-1300;
+ *   - the integer 3D Bresenham ray walk of dyn_calc_kernel,
+ *     3d/tval3_gpu_3d_kernels.cu:1612-1764, and the ray list compaction of
+ *     3d/mat_vec_mul_dynamic.h:477-556;
+ *   - CSR A*x and the CSC-as-CSR A^T*y of 3d/mat_vec_mul_sparse.h:1703-1780.
+ * Deliberate differences from the reference follow the intended mathematics
+ * where the reference is defective: lam2/lam4 read Vz (not Vy twice,
+ * 3d/tval3_gpu_3d_kernels.cu:740), sigmaY/sigmaZ are passed in order
+ * (3d/tval3_gpu_3d.cpp:512-514), and b is left unscaled when max|b| and min|b|
+ * coincide (3d/tval3_gpu_3d.cpp:253-256 divides by zero).
+ * Additions that the reference does not have: isotropic shrinkage (TVAL3
+ * paper's isotropic TV) and the Siddon ray builder with exact path lengths.
+ *
+ * Parity status: the reference does not compile and ships no tests, fixtures
+ * or golden vectors, so this oracle is "parity unpinned" against the
+ * reference's own outputs.  It is pinned to hand-derived known answers
+ * (tests/golden/), adjoint identities and FP64 self-consistency.
+ *
+ * Determinism: every reduction is a fixed-chunk sum (independent of the number
+ * of OpenMP threads); compile with -ffp-contract=off so the Siddon arithmetic
+ * rounds exactly like the library's non-contracted device code.
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+const long kChunk = 8192;
+
+// Deterministic double-precision sum of f(i) for i in [0, n).
+template <class F>
+double dsum(long n, F f) {
+    long nch = (n + kChunk - 1) / kChunk;
+    std::vector<double> part(std::max<long>(nch, 1), 0.0);
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < nch; ++c) {
+        double s = 0.0;
+        long e = std::min(n, (c + 1) * kChunk);
+        for (long i = c * kChunk; i < e; ++i) s += f(i);
+        part[c] = s;
+    }
+    double s = 0.0;
+    for (long c = 0; c < nch; ++c) s += part[c];
+    return s;
+}
+
+template <class F>
+void pfor(long n, F f) {
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; ++i) f(i);
+}
+
+struct Dims {
+    int p, q, r;  // dim_y (fastest), dim_x, dim_z
+    long n() const { return (long)p * q * r; }
+};
+
+// D: periodic forward differences.  Component 0 runs along the fastest axis
+// (the reference's Uy), 1 along dim_x (Ux), 2 along dim_z (Uz).
+// 3d/tval3_gpu_3d.cpp:271-314 with 3d/tval3_gpu_3d_kernels.cu:170-215.
+template <class T>
+void D_op(const Dims& g, const T* U, T* D0, T* D1, T* D2) {
+    const long pq = (long)g.p * g.q;
+    pfor((long)g.q * g.r, [&](long xz) {
+        long x = xz % g.q, z = xz / g.q;
+        long base = x * g.p + z * pq;
+        long bx = (x + 1 < g.q) ? base + g.p : z * pq;               // x+1 wraps to 0
+        long bz = (z + 1 < g.r) ? base + pq : x * g.p;                // z+1 wraps to 0
+        for (long y = 0; y < g.p; ++y) {
+            long i = base + y;
+            T u = U[i];
+            T uy = (y + 1 < g.p) ? U[i + 1] : U[base];
+            D0[i] = uy - u;
+            D1[i] = U[bx + y] - u;
+            D2[i] = U[bz + y] - u;
+        }
+    });
+}
+
+// D^T: 3d/tval3_gpu_3d_kernels.cu:479-510; res = (xp - X) + (yp - Y) + (zp - Z).
+template <class T>
+void Dt_op(const Dims& g, const T* V0, const T* V1, const T* V2, T* res) {
+    const long pq = (long)g.p * g.q;
+    pfor((long)g.q * g.r, [&](long xz) {
+        long x = xz % g.q, z = xz / g.q;
+        long base = x * g.p + z * pq;
+        long bx = (x > 0) ? base - g.p : base + (long)(g.q - 1) * g.p;
+        long bz = (z > 0) ? base - pq : base + (long)(g.r - 1) * pq;
+        for (long y = 0; y < g.p; ++y) {
+            long i = base + y;
+            T v0p = (y > 0) ? V0[i - 1] : V0[base + g.p - 1];
+            T v1p = V1[bx + y];
+            T v2p = V2[bz + y];
+            res[i] = v0p - V0[i] + v1p - V1[i] + v2p - V2[i];
+        }
+    });
+}
+
+// ---------------------------------------------------------------------------
+// Linear operators A (m x n).  Values are stored in float (the reference's
+// sparse_mat_host<float>), products are formed in T.
+// ---------------------------------------------------------------------------
+template <class T>
+struct Op {
+    long m = 0, n = 0;
+    virtual void N(const T* x, T* y) const = 0;   // y = A x
+    virtual void Tr(const T* y, T* x) const = 0;  // x = A^T y
+    virtual ~Op() {}
+};
+
+template <class T>
+struct CsrOp : Op<T> {
+    const int *ptr, *ind, *tptr, *tind;
+    const float *val, *tval;
+    void N(const T* x, T* y) const override {
+        pfor(this->m, [&](long r) {
+            T s = 0;
+            for (int k = ptr[r]; k < ptr[r + 1]; ++k) s += (T)val[k] * x[ind[k]];
+            y[r] = s;
+        });
+    }
+    void Tr(const T* y, T* x) const override {
+        pfor(this->n, [&](long c) {
+            T s = 0;
+            for (int k = tptr[c]; k < tptr[c + 1]; ++k) s += (T)tval[k] * y[tind[k]];
+            x[c] = s;
+        });
+    }
+};
+
+// Dense A, row-major m x n (row = ray).  3d/mat_vec_mul_dense.h:14-73.
+template <class T>
+struct DenseOp : Op<T> {
+    const float* a;
+    void N(const T* x, T* y) const override {
+        pfor(this->m, [&](long r) {
+            const float* row = a + r * this->n;
+            T s = 0;
+            for (long c = 0; c < this->n; ++c) s += (T)row[c] * x[c];
+            y[r] = s;
+        });
+    }
+    void Tr(const T* y, T* x) const override {
+        const long nb = 256;
+        pfor((this->n + nb - 1) / nb, [&](long b) {
+            long c0 = b * nb, c1 = std::min(this->n, c0 + nb);
+            for (long c = c0; c < c1; ++c) x[c] = 0;
+            for (long r = 0; r < this->m; ++r) {
+                const float* row = a + r * this->n;
+                T yr = y[r];
+                for (long c = c0; c < c1; ++c) x[c] += (T)row[c] * yr;
+            }
+        });
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+struct oracle_opts {
+    double mu, mu0, beta, beta0, rate_cnt, tol, tol_inn;
+    int maxcnt, maxit;
+    double c, gamma, gam, rate_gam;
+    int nonneg;
+    int tv_iso;  // 0: anisotropic (reference), 1: isotropic
+};
+
+struct oracle_info {
+    int total_iters, outer_iters;
+    double rel_chg, rel_error;
+    int backtracks, restarts;
+    double final_f;
+    double scl;
+};
+
+}  // extern "C"
+
+namespace {
+
+template <class T>
+struct Solver {
+    Dims g;
+    long n, m;
+    const Op<T>& A;
+    const oracle_opts& o;
+    // penalty parameters and Lagrangian terms (3d/tval3_gpu_3d.cpp:86-114)
+    double mu, beta, muDbeta, f = 0, lam1 = 0, lam2 = 0, lam3 = 0, lam4 = 0, lam5 = 0;
+    std::vector<T> delta, b, U, Up, dU, uup, Atb, Au, Aup, dAu, d, gv, gp, dg, g2, g2p, dg2, DtsAtd;
+    std::vector<T> DU[3], DUp[3], dDU[3], W[3], sig[3], V[3];
+    int backtracks = 0, restarts = 0;
+
+    Solver(Dims g_, const Op<T>& A_, const oracle_opts& o_) : g(g_), n(g_.n()), m(A_.m), A(A_), o(o_) {
+        auto N = [&](std::vector<T>& v) { v.assign(n, T(0)); };
+        auto M = [&](std::vector<T>& v) { v.assign(m, T(0)); };
+        M(delta); M(b); M(Au); M(Aup); M(dAu);
+        N(U); N(Up); N(dU); N(uup); N(Atb); N(d); N(gv); N(gp); N(dg); N(g2); N(g2p); N(dg2); N(DtsAtd);
+        for (int a = 0; a < 3; ++a) { N(DU[a]); N(DUp[a]); N(dDU[a]); N(W[a]); N(sig[a]); N(V[a]); }
+    }
+
+    double dot(const std::vector<T>& x, const std::vector<T>& y) const {
+        return dsum((long)x.size(), [&](long i) { return (double)x[i] * (double)y[i]; });
+    }
+
+    void D(const std::vector<T>& u, std::vector<T>* out) { D_op(g, u.data(), out[0].data(), out[1].data(), out[2].data()); }
+
+    // V = DU - W; lam2 = ||V||^2; lam4 = <sigma, V>; g2 = D^T V.
+    void lam24_g2() {
+        for (int a = 0; a < 3; ++a) pfor(n, [&](long i) { V[a][i] = DU[a][i] - W[a][i]; });
+        lam2 = dsum(n, [&](long i) {
+            return (double)V[0][i] * V[0][i] + (double)V[1][i] * V[1][i] + (double)V[2][i] * V[2][i];
+        });
+        lam4 = dsum(n, [&](long i) {
+            return (double)V[0][i] * sig[0][i] + (double)V[1][i] * sig[1][i] + (double)V[2][i] * sig[2][i];
+        });
+        Dt_op(g, V[0].data(), V[1].data(), V[2].data(), g2.data());
+    }
+    void lam35() {
+        lam3 = dsum(m, [&](long i) { double r = (double)Au[i] - b[i]; return r * r; });
+        lam5 = dsum(m, [&](long i) { return (double)delta[i] * ((double)Au[i] - b[i]); });
+    }
+    void fval() { f = lam1 + beta / 2 * lam2 + mu / 2 * lam3 - lam4 - lam5; }
+
+    // get_g_gpu, 3d/tval3_gpu_3d.cpp:366-572 (skipMulRatio == 0: always multiply)
+    void get_g() {
+        A.N(U.data(), Au.data());
+        A.Tr(Au.data(), gv.data());
+        lam35();
+        lam24_g2();
+        pfor(n, [&](long i) { gv[i] = gv[i] - Atb[i]; });
+        fval();
+    }
+
+    // get_tau_gpu, :577-666
+    double get_tau(bool fst) {
+        if (fst) {
+            D(d, V);
+            double dDd = dot(V[0], V[0]) + dot(V[1], V[1]) + dot(V[2], V[2]);
+            double dd = dot(d, d);
+            std::vector<T> Ad(m);
+            A.N(d.data(), Ad.data());
+            double Add = dot(Ad, Ad);
+            return std::fabs(dd / (dDd + muDbeta * Add));
+        }
+        double ss = dsum(n, [&](long i) { return (double)uup[i] * uup[i]; });
+        double sy = dsum(n, [&](long i) {
+            double dgi = (double)gv[i] - gp[i], dg2i = (double)g2[i] - g2p[i];
+            return (double)uup[i] * (dg2i + muDbeta * dgi);
+        });
+        return std::fabs(ss / sy);
+    }
+
+    // descend_gpu, :671-701
+    void descend(double tau) {
+        const T mt = (T)(-tau);
+        pfor(n, [&](long i) {
+            T v = U[i] + mt * d[i];
+            if (o.nonneg && v < 0) v = 0;
+            U[i] = v;
+        });
+        D(U, DU);
+        get_g();
+    }
+
+    // update_g_gpu, :706-818
+    void update_g(double alpha) {
+        const T al = (T)alpha;
+        pfor(n, [&](long i) {
+            gv[i] = gp[i] + al * dg[i];
+            g2[i] = g2p[i] + al * dg2[i];
+            U[i] = Up[i] + al * dU[i];
+            for (int a = 0; a < 3; ++a) DU[a][i] = DUp[a][i] + al * dDU[a][i];
+        });
+        pfor(m, [&](long i) { Au[i] = Aup[i] + al * dAu[i]; });
+        for (int a = 0; a < 3; ++a) pfor(n, [&](long i) { V[a][i] = DU[a][i] - W[a][i]; });
+        lam35();
+        lam2 = dsum(n, [&](long i) {
+            return (double)V[0][i] * V[0][i] + (double)V[1][i] * V[1][i] + (double)V[2][i] * V[2][i];
+        });
+        lam4 = dsum(n, [&](long i) {
+            return (double)V[0][i] * sig[0][i] + (double)V[1][i] * sig[1][i] + (double)V[2][i] * sig[2][i];
+        });
+        fval();
+    }
+
+    // min_u_gpu, :823-891
+    void min_u(double& gam, double C, bool fst) {
+        double tau = get_tau(fst);
+        Up = U; gp = gv; g2p = g2; Aup = Au;
+        for (int a = 0; a < 3; ++a) DUp[a] = DU[a];
+        descend(tau);
+        double alpha = 1;
+        pfor(n, [&](long i) { dU[i] = U[i] - Up[i]; });
+        double c_armij = dot(d, d) * tau * o.c * beta;
+        if (std::fabs(f) > std::fabs(C - alpha * c_armij)) {
+            pfor(n, [&](long i) {
+                dg[i] = gv[i] - gp[i];
+                dg2[i] = g2[i] - g2p[i];
+                for (int a = 0; a < 3; ++a) dDU[a][i] = DU[a][i] - DUp[a][i];
+            });
+            pfor(m, [&](long i) { dAu[i] = Au[i] - Aup[i]; });
+            int cnt = 0;
+            while (std::fabs(f) > std::fabs(C - alpha * c_armij)) {
+                if (cnt == 5) {
+                    gam *= o.rate_gam;
+                    tau = get_tau(true);
+                    U = Up;
+                    descend(tau);
+                    ++restarts;
+                    break;
+                }
+                alpha *= o.gamma;
+                update_g(alpha);
+                ++backtracks;
+                ++cnt;
+            }
+        }
+    }
+
+    // get_gradient_gpu, :896-919: d = g2 + muDbeta*g + DtsAtd
+    void get_gradient() {
+        const T mdb = (T)muDbeta;
+        pfor(n, [&](long i) { d[i] = mdb * gv[i] + g2[i] + DtsAtd[i]; });
+    }
+
+    // shrinkage_gpu, :924-960 (anisotropic); isotropic per TVAL3's isotropic TV.
+    void shrinkage() {
+        const T ib = (T)(1.0 / beta);
+        const T bt = (T)beta;
+        if (!o.tv_iso) {
+            lam1 = dsum(n, [&](long i) {
+                double s = 0;
+                for (int a = 0; a < 3; ++a) {
+                    T ub = DU[a][i] - sig[a][i] / bt;
+                    T t = std::fabs(ub) - ib;
+                    t = (t >= 0) ? t : T(0);
+                    W[a][i] = (ub >= 0) ? t : -t;
+                    s += t;
+                }
+                return s;
+            });
+        } else {
+            lam1 = dsum(n, [&](long i) {
+                T ub[3];
+                for (int a = 0; a < 3; ++a) ub[a] = DU[a][i] - sig[a][i] / bt;
+                T nv = std::sqrt(ub[0] * ub[0] + ub[1] * ub[1] + ub[2] * ub[2]);
+                T t = nv - ib;
+                t = (t > 0) ? t : T(0);
+                T sc = (nv > 0) ? t / nv : T(0);
+                for (int a = 0; a < 3; ++a) W[a][i] = ub[a] * sc;
+                return (double)t;
+            });
+        }
+    }
+
+    // update_W_gpu, :965-1029
+    void update_W() {
+        f -= (lam1 + beta / 2 * lam2 - lam4);
+        shrinkage();
+        lam24_g2();
+        f += (lam1 + beta / 2 * lam2 - lam4);
+    }
+
+    // update_mlp_gpu, :1034-1083
+    void update_mlp() {
+        f += (lam4 + lam5);
+        const T bt = (T)beta, mut = (T)mu;
+        for (int a = 0; a < 3; ++a)
+            pfor(n, [&](long i) {
+                V[a][i] = DU[a][i] - W[a][i];
+                sig[a][i] = sig[a][i] - bt * V[a][i];
+            });
+        lam4 = dsum(n, [&](long i) {
+            return (double)sig[0][i] * V[0][i] + (double)sig[1][i] * V[1][i] + (double)sig[2][i] * V[2][i];
+        });
+        std::vector<T> Aub(m);
+        pfor(m, [&](long i) {
+            Aub[i] = Au[i] - b[i];
+            delta[i] = delta[i] - mut * Aub[i];
+        });
+        lam5 = dot(delta, Aub);
+        f -= (lam4 + lam5);
+    }
+};
+
+// scaleb_gpu, 3d/tval3_gpu_3d.cpp:226-266
+template <class T>
+double scale_b(const T* b, long m) {
+    if (m <= 0) return 1.0;
+    double bmin = b[0], bmax = b[0], amin = std::fabs(bmin), amax = amin;
+    for (long i = 0; i < m; ++i) {
+        double v = b[i], a = std::fabs(v);
+        if (a < amin) { bmin = v; amin = a; }
+        if (a > amax) { bmax = v; amax = a; }
+    }
+    double dif = std::fabs(bmax - bmin);
+    if (dif == 0.0) return 1.0;
+    if (dif < 0.5) return 0.5 / dif;
+    if (dif > 1.5) return 1.5 / dif;
+    return 1.0;
+}
+
+// tval3_gpu_3d main loop, 3d/tval3_gpu_3d.cpp:1089-1345
+template <class T>
+int solve(Dims g, const Op<T>& A, const T* b_in, const oracle_opts& o, T* U_out, const T* Ut,
+          oracle_info* info, double* trace_f, const double* xstar = nullptr, double* trace_err = nullptr) {
+    Solver<T> s(g, A, o);
+    const long n = s.n, m = s.m;
+    double scl = scale_b(b_in, m);
+    const T sclT = (T)scl;
+    for (long i = 0; i < m; ++i) s.b[i] = (scl == 1.0) ? b_in[i] : b_in[i] * sclT;
+    A.Tr(s.b.data(), s.Atb.data());
+    s.U = s.Atb;
+    const double muf = o.mu, betaf = o.beta;
+    double gam = o.gam;
+    s.mu = o.mu0; s.beta = o.beta0;
+    if (s.mu > muf) s.mu = muf;
+    if (s.beta > betaf) s.beta = betaf;
+    s.muDbeta = s.mu / s.beta;
+    std::vector<T> rcdU = s.U;
+    s.D(s.U, s.DU);
+    s.shrinkage();
+    s.get_g();
+    s.get_gradient();
+    double Q = 1, Qp, C = s.f;
+    int count_outer = 0, count_total = 0;
+    double RelChg = 0, RelChgOut = 0, nrmup = 0;
+    while (count_outer < o.maxcnt && count_total < o.maxit) {
+        bool fst = true;
+        while (count_total < o.maxit) {
+            s.min_u(gam, C, fst);
+            s.update_W();
+            Qp = Q; Q = gam * Qp + 1; C = (gam * Qp * C + s.f) / Q;
+            pfor(n, [&](long i) { s.uup[i] = s.U[i] - s.Up[i]; });
+            s.get_gradient();
+            if (trace_f) trace_f[count_total] = s.f;
+            if (xstar && trace_err) {
+                // relative error of U_k (unscaled) against a given solution
+                double num = dsum(n, [&](long i) { double v = (double)s.U[i] / scl - xstar[i]; return v * v; });
+                double den = dsum(n, [&](long i) { return xstar[i] * xstar[i]; });
+                trace_err[count_total] = std::sqrt(num / den);
+            }
+            ++count_total;
+            nrmup = std::sqrt(s.dot(s.Up, s.Up));
+            RelChg = std::sqrt(s.dot(s.uup, s.uup)) / nrmup;
+            if (RelChg < o.tol_inn && !fst) break;
+            fst = false;
+        }
+        ++count_outer;
+        double dn = dsum(n, [&](long i) { double v = (double)s.U[i] - rcdU[i]; return v * v; });
+        RelChgOut = std::sqrt(dn) / nrmup;
+        rcdU = s.U;
+        if (RelChgOut < o.tol) break;
+        s.update_mlp();
+        double beta0 = s.beta;
+        s.beta *= o.rate_cnt;
+        s.mu *= o.rate_cnt;
+        if (s.beta > betaf) s.beta = betaf;
+        if (s.mu > muf) s.mu = muf;
+        s.muDbeta = s.mu / s.beta;
+        s.fval();
+        const T ratio = (T)(beta0 / s.beta);
+        pfor(n, [&](long i) { s.DtsAtd[i] = ratio * s.d[i]; });
+        s.get_gradient();
+        gam = o.gam; Q = 1; C = s.f;
+    }
+    for (long i = 0; i < n; ++i) U_out[i] = (scl == 1.0) ? s.U[i] : (T)(s.U[i] / sclT);
+    if (info) {
+        info->total_iters = count_total;
+        info->outer_iters = count_outer;
+        info->rel_chg = RelChgOut;
+        info->backtracks = s.backtracks;
+        info->restarts = s.restarts;
+        info->final_f = s.f;
+        info->scl = scl;
+        info->rel_error = 0;
+        if (Ut) {
+            double num = dsum(n, [&](long i) { double v = (double)Ut[i] - U_out[i]; return v * v; });
+            double den = dsum(n, [&](long i) { return (double)Ut[i] * Ut[i]; });
+            info->rel_error = std::sqrt(num) / std::sqrt(den);
+        }
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Ray builders
+// ---------------------------------------------------------------------------
+
+inline long lin_index(int x, int y, int z, int rv_x, int rv_y) {
+    // column-major, y fastest: 3d/tval3_gpu_3d_kernels.cu:1501
+    return (long)z * rv_x * rv_y + (long)x * rv_y + y;
+}
+
+// One Bresenham ray, 3d/tval3_gpu_3d_kernels.cu:1649-1763.  Calls emit(index)
+// for the emitter voxel and for every one of the m1 steps.
+template <class F>
+void bresenham_walk(int xs, int ys, int zs, int xe, int ye, int ze, int rv_x, int rv_y, F emit) {
+    int x = xs, y = ys, z = zs;
+    emit(lin_index(x, y, z, rv_x, rv_y));
+    int d1 = xe - x, d2 = ye - y, d3 = ze - z;
+    int m1 = std::abs(d1), m2 = std::abs(d2), m3 = std::abs(d3);
+    int *p1, *p2, *p3;
+    if (m1 >= m2 && m1 >= m3) {
+        p1 = &x; p2 = &y; p3 = &z;
+    } else if (m2 >= m1 && m2 >= m3) {
+        std::swap(d1, d2);
+        p1 = &y; p2 = &x; p3 = &z;
+    } else {
+        int t = d1; d1 = d3; d3 = d2; d2 = t;
+        p1 = &z; p2 = &x; p3 = &y;
+    }
+    int inc1 = d1 < 0 ? -1 : 1, inc2 = d2 < 0 ? -1 : 1, inc3 = d3 < 0 ? -1 : 1;
+    m1 = std::abs(d1); m2 = std::abs(d2); m3 = std::abs(d3);
+    int e1 = 2 * m2 - m1, e2 = 2 * m3 - m1;
+    for (int j = 1; j < m1 + 1; ++j) {
+        if (e1 > 0) { *p2 += inc2; e1 -= 2 * m1; }
+        if (e2 > 0) { *p3 += inc3; e2 -= 2 * m1; }
+        e1 += 2 * m2; e2 += 2 * m3;
+        *p1 += inc1;
+        emit(lin_index(x, y, z, rv_x, rv_y));
+    }
+}
+
+// One Siddon ray through the grid [0,nx) x [0,ny) x [0,nz) (voxel units):
+// exact intersection lengths.  Calls emit(index, length*scale as float) for
+// every segment of positive length, in order along the ray.
+template <class F>
+void siddon_walk(const double P0[3], const double P1[3], const int N[3], double scale, F emit) {
+    // axis order in P0/P1/N: 0 = x (dim_x), 1 = y (dim_y), 2 = z (dim_z)
+    double dv[3] = {P1[0] - P0[0], P1[1] - P0[1], P1[2] - P0[2]};
+    double L = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    if (!(L > 0)) return;
+    double tmin = 0.0, tmax = 1.0;
+    for (int a = 0; a < 3; ++a) {
+        if (dv[a] == 0.0) {
+            if (!(P0[a] >= 0.0 && P0[a] < (double)N[a])) return;
+        } else {
+            double t0 = (0.0 - P0[a]) / dv[a];
+            double t1 = ((double)N[a] - P0[a]) / dv[a];
+            double lo = std::min(t0, t1), hi = std::max(t0, t1);
+            tmin = std::max(tmin, lo);
+            tmax = std::min(tmax, hi);
+        }
+    }
+    if (!(tmin < tmax)) return;
+    double tn[3];
+    long k[3];
+    int st[3];
+    for (int a = 0; a < 3; ++a) {
+        if (dv[a] == 0.0) { tn[a] = INFINITY; k[a] = 0; st[a] = 0; continue; }
+        st[a] = dv[a] > 0 ? 1 : -1;
+        double pos = P0[a] + tmin * dv[a];
+        k[a] = (st[a] > 0) ? (long)std::floor(pos) + 1 : (long)std::ceil(pos) - 1;
+        tn[a] = ((double)k[a] - P0[a]) / dv[a];
+        while (tn[a] <= tmin) {
+            k[a] += st[a];
+            tn[a] = ((double)k[a] - P0[a]) / dv[a];
+        }
+    }
+    double t = tmin;
+    while (t < tmax) {
+        double te = std::min(std::min(tn[0], tn[1]), std::min(tn[2], tmax));
+        if (te > t) {
+            double mid = 0.5 * (t + te);
+            int idx[3];
+            for (int a = 0; a < 3; ++a) {
+                double c = P0[a] + mid * dv[a];
+                long v = (long)std::floor(c);
+                if (v < 0) v = 0;
+                if (v > N[a] - 1) v = N[a] - 1;
+                idx[a] = (int)v;
+            }
+            double len = (te - t) * L;
+            emit(lin_index(idx[0], idx[1], idx[2], N[0], N[1]), (float)(len * scale));
+        }
+        for (int a = 0; a < 3; ++a)
+            if (tn[a] == te) {
+                k[a] += st[a];
+                tn[a] = ((double)k[a] - P0[a]) / dv[a];
+            }
+        t = te;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// Ray list of 3d/mat_vec_mul_dynamic.h:477-556: for every signal i of
+// numMPs * E * R with use_path[i % (E*R)] != 0, emit (emitter, receiver) with
+// emitter = i / R and receiver = (i / (E*R)) * R + i % R.  Returns the count;
+// pairs may be NULL to count only.
+long oracle_ray_list(int numMPs, int E, int R, const unsigned* use_path, unsigned* pairs) {
+    long cnt = 0;
+    long per = (long)E * R;
+    for (long i = 0; i < per * numMPs; ++i) {
+        if (use_path && use_path[i % per] == 0) continue;
+        if (pairs) {
+            pairs[2 * cnt] = (unsigned)(i / R);
+            pairs[2 * cnt + 1] = (unsigned)((i / per) * R + (i % R));
+        }
+        ++cnt;
+    }
+    return cnt;
+}
+
+// Bresenham CSR.  row_ptr must hold nrays+1 entries; col/val may be NULL
+// (count pass).  Coordinates are voxel indices (x -> rv_x, y -> rv_y fastest,
+// z -> rv_z).  Returns nnz, or -1 if an endpoint lies outside the volume.
+long oracle_bresenham_csr(long nrays, const unsigned* pairs, const int* xe, const int* ye, const int* ze,
+                          const int* xr, const int* yr, const int* zr, int rv_x, int rv_y, int rv_z,
+                          float scale, int* row_ptr, int* col, float* val) {
+    for (long r = 0; r < nrays; ++r) {
+        unsigned e = pairs[2 * r], q = pairs[2 * r + 1];
+        int c[6] = {xe[e], ye[e], ze[e], xr[q], yr[q], zr[q]};
+        int lim[6] = {rv_x, rv_y, rv_z, rv_x, rv_y, rv_z};
+        for (int j = 0; j < 6; ++j)
+            if (c[j] < 0 || c[j] >= lim[j]) return -1;
+    }
+    if (!col) {
+        row_ptr[0] = 0;
+        for (long r = 0; r < nrays; ++r) {
+            unsigned e = pairs[2 * r], q = pairs[2 * r + 1];
+            int m1 = std::max(std::abs(xr[q] - xe[e]), std::max(std::abs(yr[q] - ye[e]), std::abs(zr[q] - ze[e])));
+            row_ptr[r + 1] = row_ptr[r] + m1 + 1;
+        }
+        return row_ptr[nrays];
+    }
+    pfor(nrays, [&](long r) {
+        unsigned e = pairs[2 * r], q = pairs[2 * r + 1];
+        long k = row_ptr[r];
+        bresenham_walk(xe[e], ye[e], ze[e], xr[q], yr[q], zr[q], rv_x, rv_y, [&](long idx) {
+            col[k] = (int)idx;
+            val[k] = scale;
+            ++k;
+        });
+    });
+    return row_ptr[nrays];
+}
+
+// Siddon CSR from continuous emitter/receiver coordinates (voxel units).
+// Same two-pass protocol as oracle_bresenham_csr.
+long oracle_siddon_csr(long nrays, const unsigned* pairs, const double* xe, const double* ye, const double* ze,
+                       const double* xr, const double* yr, const double* zr, int dim_x, int dim_y, int dim_z,
+                       double scale, int* row_ptr, int* col, float* val) {
+    const int N[3] = {dim_x, dim_y, dim_z};
+    if (!col) {
+        std::vector<int> cnt(nrays, 0);
+        pfor(nrays, [&](long r) {
+            unsigned e = pairs[2 * r], q = pairs[2 * r + 1];
+            double P0[3] = {xe[e], ye[e], ze[e]}, P1[3] = {xr[q], yr[q], zr[q]};
+            int c = 0;
+            siddon_walk(P0, P1, N, scale, [&](long, float) { ++c; });
+            cnt[r] = c;
+        });
+        row_ptr[0] = 0;
+        for (long r = 0; r < nrays; ++r) row_ptr[r + 1] = row_ptr[r] + cnt[r];
+        return row_ptr[nrays];
+    }
+    pfor(nrays, [&](long r) {
+        unsigned e = pairs[2 * r], q = pairs[2 * r + 1];
+        double P0[3] = {xe[e], ye[e], ze[e]}, P1[3] = {xr[q], yr[q], zr[q]};
+        long k = row_ptr[r];
+        siddon_walk(P0, P1, N, scale, [&](long idx, float v) {
+            col[k] = (int)idx;
+            val[k] = v;
+            ++k;
+        });
+    });
+    return row_ptr[nrays];
+}
+
+// CSR of A^T by a stable counting sort: inside every column the rows are in
+// ascending order, so the result is the reference's CSC arrays.
+void oracle_csr_transpose(long m, long n, const int* ptr, const int* ind, const float* val, int* tptr, int* tind,
+                          float* tval) {
+    std::vector<long> cnt(n + 1, 0);
+    for (long k = 0; k < ptr[m]; ++k) cnt[ind[k] + 1]++;
+    for (long c = 0; c < n; ++c) cnt[c + 1] += cnt[c];
+    for (long c = 0; c <= n; ++c) tptr[c] = (int)cnt[c];
+    std::vector<long> pos(cnt.begin(), cnt.end() - 1);
+    for (long r = 0; r < m; ++r)
+        for (int k = ptr[r]; k < ptr[r + 1]; ++k) {
+            long p = pos[ind[k]]++;
+            tind[p] = (int)r;
+            tval[p] = val[k];
+        }
+}
+
+void oracle_spmv_f64(long m, const int* ptr, const int* ind, const float* val, const double* x, double* y) {
+    pfor(m, [&](long r) {
+        double s = 0;
+        for (int k = ptr[r]; k < ptr[r + 1]; ++k) s += (double)val[k] * x[ind[k]];
+        y[r] = s;
+    });
+}
+
+void oracle_D_f64(int p, int q, int r, const double* U, double* D0, double* D1, double* D2) {
+    D_op(Dims{p, q, r}, U, D0, D1, D2);
+}
+
+void oracle_Dt_f64(int p, int q, int r, const double* V0, const double* V1, const double* V2, double* res) {
+    Dt_op(Dims{p, q, r}, V0, V1, V2, res);
+}
+
+// Shrinkage on given DU and sigma; returns lam1.
+double oracle_shrink_f64(long n, const double* D0, const double* D1, const double* D2, const double* s0,
+                         const double* s1, const double* s2, double beta, int iso, double* W0, double* W1,
+                         double* W2) {
+    const double* DU[3] = {D0, D1, D2};
+    const double* sg[3] = {s0, s1, s2};
+    double* W[3] = {W0, W1, W2};
+    double lam1 = 0;
+    for (long i = 0; i < n; ++i) {
+        double ub[3];
+        for (int a = 0; a < 3; ++a) ub[a] = DU[a][i] - sg[a][i] / beta;
+        if (!iso) {
+            for (int a = 0; a < 3; ++a) {
+                double t = std::fabs(ub[a]) - 1.0 / beta;
+                t = t >= 0 ? t : 0;
+                W[a][i] = ub[a] >= 0 ? t : -t;
+                lam1 += t;
+            }
+        } else {
+            double nv = std::sqrt(ub[0] * ub[0] + ub[1] * ub[1] + ub[2] * ub[2]);
+            double t = nv - 1.0 / beta;
+            t = t > 0 ? t : 0;
+            double sc = nv > 0 ? t / nv : 0;
+            for (int a = 0; a < 3; ++a) W[a][i] = ub[a] * sc;
+            lam1 += t;
+        }
+    }
+    return lam1;
+}
+
+// TVAL3 with a CSR matrix (and its transpose as CSR).  prec 0: FP64 vectors,
+// 1: FP32 vectors (the CPU baseline); scalars and reductions in FP64 either way.
+int oracle_tval3_csr(int prec, int p, int q, int r, long m, const int* ptr, const int* ind, const float* val,
+                     const int* tptr, const int* tind, const float* tval, const void* b, const oracle_opts* o,
+                     void* U_out, const void* Ut, oracle_info* info, double* trace_f, const double* xstar,
+                     double* trace_err) {
+    Dims g{p, q, r};
+    if (prec == 0) {
+        CsrOp<double> A;
+        A.m = m; A.n = g.n(); A.ptr = ptr; A.ind = ind; A.val = val; A.tptr = tptr; A.tind = tind; A.tval = tval;
+        return solve<double>(g, A, (const double*)b, *o, (double*)U_out, (const double*)Ut, info, trace_f, xstar,
+                             trace_err);
+    }
+    CsrOp<float> A;
+    A.m = m; A.n = g.n(); A.ptr = ptr; A.ind = ind; A.val = val; A.tptr = tptr; A.tind = tind; A.tval = tval;
+    return solve<float>(g, A, (const float*)b, *o, (float*)U_out, (const float*)Ut, info, trace_f, xstar, trace_err);
+}
+
+// TVAL3 with a dense row-major m x n matrix.
+int oracle_tval3_dense(int prec, int p, int q, int r, long m, const float* a, const void* b, const oracle_opts* o,
+                       void* U_out, const void* Ut, oracle_info* info, double* trace_f) {
+    Dims g{p, q, r};
+    if (prec == 0) {
+        DenseOp<double> A;
+        A.m = m; A.n = g.n(); A.a = a;
+        return solve<double>(g, A, (const double*)b, *o, (double*)U_out, (const double*)Ut, info, trace_f);
+    }
+    DenseOp<float> A;
+    A.m = m; A.n = g.n(); A.a = a;
+    return solve<float>(g, A, (const float*)b, *o, (float*)U_out, (const float*)Ut, info, trace_f);
+}
+
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+}  // extern "C"

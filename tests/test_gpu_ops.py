@@ -1,0 +1,174 @@
+"""GPU parity of the operators (A, A^T, D, D^T) and of the device ray-matrix
+builders against the CPU oracle, through the C ABI."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _small_3d(n=24, ne=20, seed=0):
+    from tval3_gb300 import workloads as W
+    return W.config_3d(n, ne, ne, seed=seed)
+
+
+@pytest.mark.parametrize("which", ["ring", "hemi"])
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_device_ray_matrix_bitexact(cuda, oracle, which, traversal):
+    """The device-built CSR (row pointers, voxel indices, values) equals the
+    oracle's construction bit for bit (Bresenham: dyn_calc_kernel's walk)."""
+    from tval3_gb300 import Operator
+    from tval3_gb300 import workloads as W
+    geo = W.ring_geometry(64, 128) if which == "ring" else _small_3d(40, 48)[1]
+    geo = geo.with_traversal(traversal)
+    ref = oracle.bresenham_csr(geo) if traversal == 0 else oracle.siddon_csr(geo)
+    op = Operator.from_geometry(geo, mode=0)
+    ptr, ind, val, tptr, tind, tval = op.export_csr()
+    assert np.array_equal(ptr, ref[0])
+    assert np.array_equal(ind, ref[1])
+    assert np.array_equal(val.view(np.uint32), ref[2].view(np.uint32))
+    rt = oracle.transpose(ptr.size - 1, op.cols, *ref)
+    assert np.array_equal(tptr, rt[0]) and np.array_equal(tind, rt[1]) and np.array_equal(tval, rt[2])
+
+
+def _vecs(torch, op, dtype, seed=0):
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    x = torch.randn(op.cols, generator=g, dtype=torch.float64)
+    y = torch.randn(op.rows, generator=g, dtype=torch.float64)
+    return x, y
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2, 3])
+def test_spmv_parity_and_adjoint(cuda, oracle, prec):
+    """A x and A^T y against the oracle's FP64 products (FP32 storage:
+    1e-5 relative; FP64: 1e-12; BF16/FP16: against the dequantised matrix),
+    and the dot-product test <Ax, y> = <x, A^T y>."""
+    torch = _torch()
+    from tval3_gb300 import Operator, SparseMatrix
+    cfg, geo, x0 = _small_3d()
+    ptr, ind, val = oracle.siddon_csr(geo)
+    m, n = ptr.size - 1, x0.size
+    tptr, tind, tval = oracle.transpose(m, n, ptr, ind, val)
+    A = SparseMatrix(m, n, ptr, ind, val.astype(np.float64) if prec == 1 else val,
+                     tptr, tind, tval.astype(np.float64) if prec == 1 else tval)
+    op = Operator.from_sparse(A, precision=prec)
+    vt = torch.float64 if prec == 1 else torch.float32
+    x, y = _vecs(torch, op, vt)
+    xd, yd = x.to(cuda, vt), y.to(cuda, vt)
+    Ax = torch.empty(m, device=cuda, dtype=vt)
+    Aty = torch.empty(n, device=cuda, dtype=vt)
+    op.mat_vec_mul(0, xd, Ax)
+    op.mat_vec_mul(1, yd, Aty)
+    torch.cuda.synchronize()
+    if prec in (2, 3):
+        qptr, qind, qval, qtptr, qtind, qtval = op.export_csr()
+        assert np.array_equal(qind, ind) and np.array_equal(qtind, tind)
+        ref_val, ref_tval = qval, qtval
+        # round-to-nearest of v / rowmax: half an ulp relative (2^-8 BF16, 2^-11
+        # FP16), plus FP16's subnormal spacing 2^-24 of the row maximum
+        rowmax = np.maximum.reduceat(np.abs(val), ptr[:-1])[np.repeat(np.arange(m), np.diff(ptr))] \
+            if val.size else val
+        bound = (2.0 ** -8 if prec == 2 else 2.0 ** -11) * np.abs(val) + (0 if prec == 2 else 2.0 ** -24) * rowmax
+        assert np.all(np.abs(qval.astype(np.float64) - val) <= bound * 1.001 + 1e-30)
+        tol = 1e-5
+    else:
+        ref_val, ref_tval = val, tval
+        tol = 1e-12 if prec == 1 else 1e-5
+    ref_Ax = oracle.spmv(ptr, ind, ref_val, x.numpy())
+    ref_Aty = oracle.spmv(tptr, tind, ref_tval, y.numpy())
+    got_Ax = Ax.double().cpu().numpy()
+    got_Aty = Aty.double().cpu().numpy()
+    assert np.linalg.norm(got_Ax - ref_Ax) <= tol * np.linalg.norm(ref_Ax)
+    assert np.linalg.norm(got_Aty - ref_Aty) <= tol * np.linalg.norm(ref_Aty)
+    lhs = float(np.dot(got_Ax, y.numpy()))
+    rhs = float(np.dot(x.numpy(), got_Aty))
+    assert abs(lhs - rhs) <= (1e-12 if prec == 1 else 1e-5) * max(abs(lhs), 1.0)
+
+
+def test_on_the_fly_bresenham_matches_csr(cuda, oracle):
+    """On-the-fly traversal (dyn_calc_kernel's mode) equals the stored CSR
+    product: A x within FP32 summation order, A^T y (atomic scatter) likewise."""
+    torch = _torch()
+    from tval3_gb300 import Operator
+    cfg, geo, _ = _small_3d(40, 48)
+    geo = geo.with_traversal(0)
+    ptr, ind, val = oracle.bresenham_csr(geo)
+    tptr, tind, tval = oracle.transpose(ptr.size - 1, 40 ** 3, ptr, ind, val)
+    op = Operator.from_geometry(geo, mode=1)
+    x, y = _vecs(torch, op, torch.float32)
+    Ax = torch.empty(op.rows, device=cuda)
+    Aty = torch.empty(op.cols, device=cuda)
+    op.mat_vec_mul(0, x.to(cuda, torch.float32), Ax)
+    op.mat_vec_mul(1, y.to(cuda, torch.float32), Aty)
+    torch.cuda.synchronize()
+    ref_Ax = oracle.spmv(ptr, ind, val, x.numpy())
+    ref_Aty = oracle.spmv(tptr, tind, tval, y.numpy())
+    assert np.linalg.norm(Ax.double().cpu().numpy() - ref_Ax) <= 1e-5 * np.linalg.norm(ref_Ax)
+    assert np.linalg.norm(Aty.double().cpu().numpy() - ref_Aty) <= 1e-5 * np.linalg.norm(ref_Aty)
+
+
+@pytest.mark.parametrize("dims", [(7, 5, 3), (64, 64, 1), (33, 17, 9)])
+@pytest.mark.parametrize("f64", [False, True])
+def test_D_Dt_parity(cuda, oracle, dims, f64):
+    torch = _torch()
+    from tval3_gb300 import D, Dt
+    p, q, r = dims
+    n = p * q * r
+    dt = torch.float64 if f64 else torch.float32
+    g = torch.Generator().manual_seed(3)
+    U = torch.randn(n, generator=g, dtype=torch.float64)
+    P = torch.randn(3 * n, generator=g, dtype=torch.float64)
+    DU = torch.empty(3 * n, device=cuda, dtype=dt)
+    DtP = torch.empty(n, device=cuda, dtype=dt)
+    D(U.to(cuda, dt), dims, DU)
+    Dt(P.to(cuda, dt), dims, DtP)
+    torch.cuda.synchronize()
+    tol = 1e-15 if f64 else 1e-6
+    ref = oracle.D(U.numpy(), dims).reshape(-1)
+    assert np.abs(DU.double().cpu().numpy() - ref).max() <= tol * 10
+    ref_t = oracle.Dt(P.numpy(), dims)
+    assert np.abs(DtP.double().cpu().numpy() - ref_t).max() <= tol * 20
+    lhs = float((DU.double().cpu() * P).sum())
+    rhs = float((U * DtP.double().cpu()).sum())
+    assert abs(lhs - rhs) <= (1e-12 if f64 else 1e-5) * max(abs(lhs), 1.0)
+
+
+def test_dense_operator_parity(cuda):
+    torch = _torch()
+    from tval3_gb300 import DenseMatrix, Operator
+    rng = np.random.default_rng(0)
+    A = rng.normal(size=(300, 200)).astype(np.float32)
+    x = rng.normal(size=200)
+    y = rng.normal(size=300)
+    for prec, tol in ((0, 1e-5), (2, 1e-2)):
+        op = Operator.from_dense(DenseMatrix(A), precision=prec)
+        Ax = torch.empty(300, device=cuda)
+        Aty = torch.empty(200, device=cuda)
+        op.mat_vec_mul(0, torch.tensor(x, dtype=torch.float32, device=cuda), Ax)
+        op.mat_vec_mul(1, torch.tensor(y, dtype=torch.float32, device=cuda), Aty)
+        torch.cuda.synchronize()
+        assert np.linalg.norm(Ax.cpu().numpy() - A @ x) <= tol * np.linalg.norm(A @ x)
+        assert np.linalg.norm(Aty.cpu().numpy() - A.T @ y) <= tol * np.linalg.norm(A.T @ y)
+
+
+def test_empty_rays_and_empty_matrix(cuda, oracle):
+    """Rays that miss the grid give empty rows; a matrix with no nonzeros is valid."""
+    torch = _torch()
+    from tval3_gb300 import Geometry, Operator
+    geo = Geometry(rv_x=8, rv_y=8, rv_z=1, x_emitters=[0, 0], y_emitters=[0, 0], z_emitters=[0, 0],
+                   x_receivers=[0, 0], y_receivers=[0, 0], z_receivers=[0, 0], traversal=1,
+                   pos=(np.array([-2.0, 1.0]), np.array([-2.0, 1.0]), np.array([0.5, 0.5]),
+                        np.array([-2.0, 7.0]), np.array([9.0, 7.0]), np.array([0.5, 0.5])))
+    op = Operator.from_geometry(geo, mode=0)
+    ref = oracle.siddon_csr(geo)
+    ptr, ind, val, *_ = op.export_csr()
+    assert np.array_equal(ptr, ref[0]) and np.array_equal(ind, ref[1])
+    assert ptr[1] == ptr[0]  # the ray outside the grid is an empty row
+    y = torch.zeros(op.rows, device=cuda)
+    op.mat_vec_mul(0, torch.ones(op.cols, device=cuda), y)
+    torch.cuda.synchronize()
+    assert float(y[0]) == 0.0

@@ -1,0 +1,553 @@
+// C ABI (include/tval3/tval3_c.h).  Every entry point validates its
+// arguments like the reference's check_params_1/2 (3d/tval3_gpu_3d.cpp:
+// 1351-1380), converts internal errors to a status code plus a thread-local
+// message (the reference throws tval3_gpu_exception, :1439-1445), and runs on
+// the caller's current device.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+#include "solver.h"
+#include "tval3/tval3_c.h"
+
+using namespace tv3;
+
+struct tval3_op_s {
+    int dbl = 0;  // vector type double?
+    int precision = 0;
+    LinOp<float>* f = nullptr;
+    LinOp<double>* d = nullptr;
+    ~tval3_op_s() {
+        delete f;
+        delete d;
+    }
+};
+
+struct tval3_solver_s {
+    int dbl = 0;
+    Solver<float>* f = nullptr;
+    Solver<double>* d = nullptr;
+    ~tval3_solver_s() {
+        delete f;
+        delete d;
+    }
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+tval3_status fail(int st, const std::string& msg) {
+    g_err = msg;
+    return (tval3_status)st;
+}
+
+template <class F>
+tval3_status guard(F f) {
+    try {
+        g_err.clear();
+        f();
+        return TVAL3_OK;
+    } catch (const Error& e) {
+        return fail(e.status, e.msg);
+    } catch (const std::bad_alloc&) {
+        return fail(TVAL3_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(TVAL3_ERR_ARG, std::string("Internal error: ") + e.what());
+    }
+}
+
+[[noreturn]] void arg_error(int st, const std::string& msg) { throw Error{st, msg}; }
+
+template <class T>
+struct HostVec {
+    T* p = nullptr;
+};
+
+void check_sparse(const tval3_sparse_host* A) {
+    if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+    if (A->rows < 0 || A->cols < 0 || A->nnz < 0) arg_error(TVAL3_ERR_SHAPE, "Argument error: negative matrix size!");
+    if (A->format < 1 || A->format > 3) arg_error(TVAL3_ERR_ARG, "Argument error: unknown sparse format!");
+    if (A->val_type != TVAL3_PREC_FP32 && A->val_type != TVAL3_PREC_FP64)
+        arg_error(TVAL3_ERR_ARG, "Argument error: sparse values must be FP32 or FP64!");
+    auto chk = [&](const int* ptr, const int* ind, const void* val, long rows, long cols, const char* what) {
+        if (!ptr || (A->nnz > 0 && (!ind || !val)))
+            arg_error(TVAL3_ERR_ARG, std::string("Argument error: missing ") + what + " arrays!");
+        if (ptr[0] != 0 || ptr[rows] != A->nnz)
+            arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: inconsistent ") + what + " pointer array!");
+        for (long r = 0; r < rows; ++r)
+            if (ptr[r + 1] < ptr[r]) arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: decreasing ") + what + " pointers!");
+        for (long k = 0; k < A->nnz; ++k)
+            if (ind[k] < 0 || ind[k] >= cols)
+                arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: ") + what + " index out of range!");
+        if (A->val_type == TVAL3_PREC_FP32) {
+            const float* v = (const float*)val;
+            for (long k = 0; k < A->nnz; ++k)
+                if (!std::isfinite(v[k])) arg_error(TVAL3_ERR_NONFINITE, "Argument error: non-finite matrix value!");
+        } else {
+            const double* v = (const double*)val;
+            for (long k = 0; k < A->nnz; ++k)
+                if (!std::isfinite(v[k])) arg_error(TVAL3_ERR_NONFINITE, "Argument error: non-finite matrix value!");
+        }
+    };
+    if (A->format & TVAL3_SPARSE_CSR) chk(A->csr_ptr, A->csr_ind, A->csr_val, A->rows, A->cols, "CSR");
+    if (A->format & TVAL3_SPARSE_CSC) chk(A->csc_ptr, A->csc_ind, A->csc_val, A->cols, A->rows, "CSC");
+}
+
+template <class T>
+void to_device(DBuf<T>& d, const void* h, long n, int src_type) {
+    d.alloc(std::max<long>(n, 1));
+    if (n <= 0) return;
+    bool src_double = (src_type == TVAL3_PREC_FP64);
+    if (src_double == (sizeof(T) == 8)) {
+        TV3_CUDA(cudaMemcpy(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<T> tmp(n);
+        if (src_double)
+            for (long i = 0; i < n; ++i) tmp[i] = (T)((const double*)h)[i];
+        else
+            for (long i = 0; i < n; ++i) tmp[i] = (T)((const float*)h)[i];
+        TV3_CUDA(cudaMemcpy(d.p, tmp.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+    }
+}
+
+// device operator from a host sparse matrix
+template <class T>
+LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision) {
+    check_sparse(A);
+    const long m = A->rows, n = A->cols, nnz = A->nnz;
+    DBuf<int> ptr, ind, tptr, tind;
+    DBuf<T> val, tval;
+    cudaStream_t s = 0;
+    if (A->format & TVAL3_SPARSE_CSR) {
+        ptr.alloc(m + 1);
+        ind.alloc(std::max<long>(nnz, 1));
+        TV3_CUDA(cudaMemcpy(ptr.p, A->csr_ptr, (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        if (nnz) TV3_CUDA(cudaMemcpy(ind.p, A->csr_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
+        to_device(val, A->csr_val, nnz, A->val_type);
+    }
+    if (A->format & TVAL3_SPARSE_CSC) {
+        tptr.alloc(n + 1);
+        tind.alloc(std::max<long>(nnz, 1));
+        TV3_CUDA(cudaMemcpy(tptr.p, A->csc_ptr, (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        if (nnz) TV3_CUDA(cudaMemcpy(tind.p, A->csc_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
+        to_device(tval, A->csc_val, nnz, A->val_type);
+    }
+    if (!(A->format & TVAL3_SPARSE_CSR)) {
+        // only CSC given: its transpose is the CSR of A
+        ptr.alloc(m + 1);
+        ind.alloc(std::max<long>(nnz, 1));
+        val.alloc(std::max<long>(nnz, 1));
+        csr_transpose_device<T>(n, m, nnz, tptr.p, tind.p, tval.p, ptr.p, ind.p, val.p, s);
+    }
+    return make_csr_op_device<T>(m, n, nnz, ptr.p, ind.p, val.p, tptr.p ? tptr.p : nullptr,
+                                 tptr.p ? tind.p : nullptr, tptr.p ? tval.p : nullptr, precision, s);
+}
+
+void check_opts(const tval3_options* o) {
+    if (!o) arg_error(TVAL3_ERR_ARG, "Argument error: opts is NULL!");
+    if (o->skipMulRatio != 0.0 || o->numInitIterations != 0)
+        arg_error(TVAL3_ERR_UNSUPPORTED, "skipMulRatio/numInitIterations: only exact products (0) are provided");
+    if (!(o->beta > 0) || !(o->mu > 0) || !(o->beta0 > 0) || !(o->mu0 > 0))
+        arg_error(TVAL3_ERR_ARG, "Argument error: mu, mu0, beta, beta0 must be positive!");
+}
+
+template <class T>
+void check_vec(const T* v, long n, const char* what) {
+    for (long i = 0; i < n; ++i)
+        if (!std::isfinite((double)v[i])) arg_error(TVAL3_ERR_NONFINITE, std::string("Argument error: non-finite ") + what + "!");
+}
+
+// the common body of the reference entry points: host U/b/Ut, operator built
+template <class T>
+void solve_host(LinOp<T>* op, T* U, int dim_y, int dim_x, int dim_z, const T* b, int b_len, const tval3_options* opts,
+                const T* Ut, int Ut_len, tval3_info* info, std::chrono::steady_clock::time_point t0) {
+    std::unique_ptr<LinOp<T>> hold(op);
+    const long n = (long)dim_y * dim_x * dim_z;
+    DBuf<T> db, dU, dUt;
+    db.alloc(std::max<long>(b_len, 1));
+    dU.alloc(std::max<long>(n, 1));
+    if (b_len) TV3_CUDA(cudaMemcpy(db.p, b, b_len * sizeof(T), cudaMemcpyHostToDevice));
+    const bool use_ut = Ut && Ut_len == n && n > 0;
+    if (use_ut) {
+        dUt.alloc(n);
+        TV3_CUDA(cudaMemcpy(dUt.p, Ut, n * sizeof(T), cudaMemcpyHostToDevice));
+    }
+    Solver<T> s(op, dim_y, dim_x, dim_z, *opts);
+    tval3_info inf{};
+    s.solve(db.p, dU.p, use_ut ? dUt.p : nullptr, &inf, 0);
+    TV3_CUDA(cudaMemcpy(U, dU.p, n * sizeof(T), cudaMemcpyDeviceToHost));
+    inf.outer_secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (info) *info = inf;
+}
+
+template <class T>
+void check_problem(const T* U, int dim_y, int dim_x, int dim_z, long A_rows, long A_cols, const T* b, int b_len,
+                   const T* Ut, int Ut_len) {
+    if (!U || dim_y <= 0 || dim_x <= 0 || dim_z <= 0) arg_error(TVAL3_ERR_ARG, "Argument error: U must be a non-empty volume!");
+    const long n = (long)dim_y * dim_x * dim_z;
+    if (Ut && Ut_len > 0 && Ut_len != n) arg_error(TVAL3_ERR_SHAPE, "Argument error: U and Ut must have the same size!");
+    if (n != A_cols) arg_error(TVAL3_ERR_SHAPE, "Argument error: the length of U must be equal to A.dim_x!");
+    if (b_len != A_rows) arg_error(TVAL3_ERR_SHAPE, "Argument error: b.len must be equal to A.dim_y!");
+    if (b_len > 0 && !b) arg_error(TVAL3_ERR_ARG, "Argument error: b is NULL!");
+    check_vec(b, b_len, "measurement b");
+}
+
+}  // namespace
+
+extern "C" {
+
+void tval3_options_default(tval3_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->mu = 256.0; o->mu0 = 256.0; o->beta = 32.0; o->beta0 = 32.0; o->rate_cnt = 2.0;
+    o->tol = 1e-6; o->tol_inn = 1e-3; o->maxcnt = 10; o->maxit = 1025; o->c = 1e-5;
+    o->gamma = 0.6; o->gam = 0.9995; o->rate_gam = 0.9; o->isreal = 1; o->nonneg = 1;
+    o->numInitIterations = 0; o->skipMulRatio = 0.0; o->maxRelativeChange = 0.0;
+    o->tv_type = TVAL3_TV_ANISO;
+}
+
+const char* tval3_last_error_message(void) { return g_err.c_str(); }
+const char* tval3_version(void) { return "tval3-gb300 0.1 (sm_103a)"; }
+
+tval3_status tval3_gpu_3d_sparse_f32(float* U, int dim_y, int dim_x, int dim_z, const tval3_sparse_host* A,
+                                     const float* b, int b_len, const tval3_options* opts, const float* Ut,
+                                     int Ut_len, int, int, int, const int*, tval3_info* info) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_opts(opts);
+        if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+        check_problem(U, dim_y, dim_x, dim_z, A->rows, A->cols, b, b_len, Ut, Ut_len);
+        solve_host<float>(sparse_op<float>(A, TVAL3_PREC_FP32), U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len,
+                          info, t0);
+    });
+}
+
+tval3_status tval3_gpu_3d_sparse_f64(double* U, int dim_y, int dim_x, int dim_z, const tval3_sparse_host* A,
+                                     const double* b, int b_len, const tval3_options* opts, const double* Ut,
+                                     int Ut_len, int, int, int, const int*, tval3_info* info) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_opts(opts);
+        if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+        check_problem(U, dim_y, dim_x, dim_z, A->rows, A->cols, b, b_len, Ut, Ut_len);
+        solve_host<double>(sparse_op<double>(A, TVAL3_PREC_FP64), U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len,
+                           info, t0);
+    });
+}
+
+tval3_status tval3_gpu_sparse(float* U, int rows, int cols, const tval3_sparse_host* A, const float* b, int b_len,
+                              const tval3_options* opts, const float* Ut, int Ut_len, int pagelocked,
+                              tval3_info* info) {
+    return tval3_gpu_3d_sparse_f32(U, rows, cols, 1, A, b, b_len, opts, Ut, Ut_len, pagelocked, -1, 0, nullptr, info);
+}
+
+tval3_status tval3_gpu_3d_dense_f32(float* U, int dim_y, int dim_x, int dim_z, const tval3_dense_host* A,
+                                    const float* b, int b_len, const tval3_options* opts, const float* Ut,
+                                    int Ut_len, int, int, int, const int*, tval3_info* info) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_opts(opts);
+        if (!A || !A->data || A->rows < 0 || A->cols < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad dense matrix!");
+        check_problem(U, dim_y, dim_x, dim_z, A->rows, A->cols, b, b_len, Ut, Ut_len);
+        solve_host<float>(make_dense_op<float>(A->rows, A->cols, A->data, A->row_major, A->val_type, TVAL3_PREC_FP32, 0),
+                          U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len, info, t0);
+    });
+}
+
+tval3_status tval3_gpu_3d_dense_f64(double* U, int dim_y, int dim_x, int dim_z, const tval3_dense_host* A,
+                                    const double* b, int b_len, const tval3_options* opts, const double* Ut,
+                                    int Ut_len, int, int, int, const int*, tval3_info* info) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_opts(opts);
+        if (!A || !A->data || A->rows < 0 || A->cols < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad dense matrix!");
+        check_problem(U, dim_y, dim_x, dim_z, A->rows, A->cols, b, b_len, Ut, Ut_len);
+        solve_host<double>(make_dense_op<double>(A->rows, A->cols, A->data, A->row_major, A->val_type, TVAL3_PREC_FP64, 0),
+                           U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len, info, t0);
+    });
+}
+
+tval3_status tval3_gpu_dense(float* U, int rows, int cols, const tval3_dense_host* A, const float* b, int b_len,
+                             const tval3_options* opts, const float* Ut, int Ut_len, int pagelocked,
+                             tval3_info* info) {
+    return tval3_gpu_3d_dense_f32(U, rows, cols, 1, A, b, b_len, opts, Ut, Ut_len, pagelocked, -1, 0, nullptr, info);
+}
+
+tval3_status tval3_gpu_3d_geometry_f32(float* U, int dim_y, int dim_x, int dim_z, const tval3_geometry_host* A,
+                                       const float* b, int b_len, const tval3_options* opts, const float* Ut,
+                                       int Ut_len, int, int, int, const int*, tval3_info* info) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_opts(opts);
+        if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+        if (A->rv_y != dim_y || A->rv_x != dim_x || A->rv_z != dim_z)
+            arg_error(TVAL3_ERR_SHAPE, "Argument error: the volume of U must equal the geometry's rv_y x rv_x x rv_z!");
+        // the reference evaluates this overload on the fly (geom_mm_multGPU); Bresenham runs on the fly here too
+        const int mode = (A->traversal == TVAL3_TRAVERSAL_BRESENHAM) ? 1 : 0;
+        LinOp<float>* op = make_geometry_op<float>(A, mode, TVAL3_PREC_FP32, 0);
+        try {
+            check_problem(U, dim_y, dim_x, dim_z, op->m, op->n, b, b_len, Ut, Ut_len);
+        } catch (...) {
+            delete op;
+            throw;
+        }
+        solve_host<float>(op, U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len, info, t0);
+    });
+}
+
+tval3_status tval3_gpu_3d_geometry_sparse_f32(float* U, int dim_y, int dim_x, int dim_z,
+                                              const tval3_geometry_host* A_geo, const tval3_sparse_host* A_mat,
+                                              const float* b, int b_len, const tval3_options* opts, const float* Ut,
+                                              int Ut_len, int, int, int, const int*, tval3_info* info) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_opts(opts);
+        if (!A_geo || !A_mat) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+        check_problem(U, dim_y, dim_x, dim_z, A_mat->rows, A_mat->cols, b, b_len, Ut, Ut_len);
+        std::unique_ptr<LinOp<float>> geo(make_geometry_op<float>(A_geo, 1, TVAL3_PREC_FP32, 0));
+        std::unique_ptr<LinOp<float>> mat(sparse_op<float>(A_mat, TVAL3_PREC_FP32));
+        if (geo->m != mat->m || geo->n != mat->n)
+            arg_error(TVAL3_ERR_SHAPE, "Argument error: geometry and sparse matrix disagree in shape!");
+        solve_host<float>(new SplitOp<float>(std::move(geo), std::move(mat)), U, dim_y, dim_x, dim_z, b, b_len, opts,
+                          Ut, Ut_len, info, t0);
+    });
+}
+
+// ---------------------------------------------------------------------------
+// operators
+// ---------------------------------------------------------------------------
+tval3_status tval3_op_create_sparse(tval3_op* op, const tval3_sparse_host* A, int precision) {
+    return guard([&] {
+        if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
+        if (precision < 0 || precision > 4) arg_error(TVAL3_ERR_ARG, "Argument error: unknown precision!");
+        auto* h = new tval3_op_s();
+        try {
+            h->precision = precision;
+            if (precision == TVAL3_PREC_FP64 || precision == TVAL3_PREC_FP32_F64VEC) {
+                h->dbl = 1;
+                h->d = sparse_op<double>(A, precision);
+            } else {
+                h->f = sparse_op<float>(A, precision);
+            }
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *op = h;
+    });
+}
+
+tval3_status tval3_op_create_sparse_device(tval3_op* op, int rows, int cols, int nnz, const int* d_ptr,
+                                           const int* d_ind, const float* d_val, int precision, void* stream) {
+    return guard([&] {
+        if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
+        if (rows < 0 || cols < 0 || nnz < 0 || !d_ptr) arg_error(TVAL3_ERR_ARG, "Argument error: bad device CSR!");
+        if (precision == TVAL3_PREC_FP64 || precision < 0 || precision > 3)
+            arg_error(TVAL3_ERR_UNSUPPORTED, "device CSR input takes FP32 values (FP32/BF16/FP16 storage)");
+        auto* h = new tval3_op_s();
+        try {
+            h->precision = precision;
+            h->f = make_csr_op_device<float>(rows, cols, nnz, d_ptr, d_ind, d_val, nullptr, nullptr, nullptr, precision,
+                                             (cudaStream_t)stream);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *op = h;
+    });
+}
+
+tval3_status tval3_op_create_geometry(tval3_op* op, const tval3_geometry_host* G, int mode, int precision) {
+    return guard([&] {
+        if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
+        if (mode < 0 || mode > 1) arg_error(TVAL3_ERR_ARG, "Argument error: unknown geometry mode!");
+        if (precision == TVAL3_PREC_FP64 || precision < 0 || precision > 4)
+            arg_error(TVAL3_ERR_UNSUPPORTED, "geometry operators store FP32/BF16/FP16 values");
+        if (mode == 1 && precision != TVAL3_PREC_FP32)
+            arg_error(TVAL3_ERR_UNSUPPORTED, "on-the-fly traversal stores nothing; use FP32");
+        auto* h = new tval3_op_s();
+        try {
+            h->precision = precision;
+            if (precision == TVAL3_PREC_FP32_F64VEC) {
+                h->dbl = 1;
+                h->d = make_geometry_op<double>(G, mode, precision, 0);
+            } else {
+                h->f = make_geometry_op<float>(G, mode, precision, 0);
+            }
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *op = h;
+    });
+}
+
+tval3_status tval3_op_create_dense(tval3_op* op, const tval3_dense_host* A, int precision) {
+    return guard([&] {
+        if (!op || !A || !A->data || A->rows < 0 || A->cols < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad dense matrix!");
+        if (precision == TVAL3_PREC_FP16 || precision < 0 || precision > 3)
+            arg_error(TVAL3_ERR_UNSUPPORTED, "dense storage: FP32, FP64 or BF16");
+        auto* h = new tval3_op_s();
+        try {
+            h->precision = precision;
+            if (precision == TVAL3_PREC_FP64) {
+                h->dbl = 1;
+                h->d = make_dense_op<double>(A->rows, A->cols, A->data, A->row_major, A->val_type, precision, 0);
+            } else {
+                h->f = make_dense_op<float>(A->rows, A->cols, A->data, A->row_major, A->val_type, precision, 0);
+            }
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *op = h;
+    });
+}
+
+tval3_status tval3_op_destroy(tval3_op op) {
+    return guard([&] { delete op; });
+}
+
+tval3_status tval3_op_shape(tval3_op op, int* rows, int* cols, int64_t* nnz) {
+    return guard([&] {
+        if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
+        long m = op->dbl ? op->d->m : op->f->m, n = op->dbl ? op->d->n : op->f->n;
+        long z = op->dbl ? op->d->nnz : op->f->nnz;
+        if (rows) *rows = (int)m;
+        if (cols) *cols = (int)n;
+        if (nnz) *nnz = z;
+    });
+}
+
+tval3_status tval3_op_export_csr(tval3_op op, int* ptr, int* ind, float* val, int* tptr, int* tind, float* tval) {
+    return guard([&] {
+        if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
+        if (op->dbl) op->d->export_csr(ptr, ind, val, tptr, tind, tval);
+        else op->f->export_csr(ptr, ind, val, tptr, tind, tval);
+    });
+}
+
+tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, void* stream) {
+    return guard([&] {
+        if (!op || !x || !y) arg_error(TVAL3_ERR_ARG, "Argument error: NULL operator or vector!");
+        cudaStream_t s = (cudaStream_t)stream;
+        if (op->dbl) op->d->apply(trans ? 1 : 0, plain_io<double>((const double*)x, (double*)y), SPMV_PLAIN, s);
+        else op->f->apply(trans ? 1 : 0, plain_io<float>((const float*)x, (float*)y), SPMV_PLAIN, s);
+    });
+}
+
+tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, void* Y, void* stream) {
+    return guard([&] {
+        if (!op || !X || !Y || nrhs < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad multi-RHS product!");
+        cudaStream_t s = (cudaStream_t)stream;
+        if (op->dbl) op->d->apply_multi(trans ? 1 : 0, nrhs, (const double*)X, (double*)Y, s);
+        else op->f->apply_multi(trans ? 1 : 0, nrhs, (const float*)X, (float*)Y, s);
+    });
+}
+
+// ---------------------------------------------------------------------------
+// device-resident solver
+// ---------------------------------------------------------------------------
+tval3_status tval3_solver_create(tval3_solver* s, tval3_op A, int dim_y, int dim_x, int dim_z,
+                                 const tval3_options* opts) {
+    return guard([&] {
+        if (!s || !A) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver or operator!");
+        check_opts(opts);
+        const long n = (long)dim_y * dim_x * dim_z;
+        long cols = A->dbl ? A->d->n : A->f->n;
+        if (dim_y <= 0 || dim_x <= 0 || dim_z <= 0 || n != cols)
+            arg_error(TVAL3_ERR_SHAPE, "Argument error: the length of U must be equal to A.dim_x!");
+        auto* h = new tval3_solver_s();
+        try {
+            h->dbl = A->dbl;
+            if (A->dbl) h->d = new Solver<double>(A->d, dim_y, dim_x, dim_z, *opts);
+            else h->f = new Solver<float>(A->f, dim_y, dim_x, dim_z, *opts);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *s = h;
+    });
+}
+
+tval3_status tval3_solver_set_mode(tval3_solver s, int mode) {
+    return guard([&] {
+        if (!s || mode < 0 || mode > 1) arg_error(TVAL3_ERR_ARG, "Argument error: bad solver mode!");
+        if (s->dbl) s->d->mode = mode;
+        else s->f->mode = mode;
+    });
+}
+
+tval3_status tval3_solver_solve(tval3_solver s, const void* d_b, void* d_U, const void* d_Ut, tval3_info* info,
+                                void* stream) {
+    return guard([&] {
+        if (!s || !d_b || !d_U) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver or vector!");
+        if (s->dbl) s->d->solve((const double*)d_b, (double*)d_U, (const double*)d_Ut, info, (cudaStream_t)stream);
+        else s->f->solve((const float*)d_b, (float*)d_U, (const float*)d_Ut, info, (cudaStream_t)stream);
+    });
+}
+
+tval3_status tval3_solver_set_trace(tval3_solver s, const void* d_xstar) {
+    return guard([&] {
+        if (!s) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver!");
+        if (s->dbl) {
+            s->d->xstar = (const double*)d_xstar;
+            s->d->gexec ? (void)cudaGraphExecDestroy(s->d->gexec) : (void)0;
+            s->d->gexec = nullptr;
+        } else {
+            s->f->xstar = (const float*)d_xstar;
+            s->f->gexec ? (void)cudaGraphExecDestroy(s->f->gexec) : (void)0;
+            s->f->gexec = nullptr;
+        }
+    });
+}
+
+tval3_status tval3_solver_trace(tval3_solver s, double* host_err, int len) {
+    return guard([&] {
+        if (!s || !host_err) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver or buffer!");
+        if (s->dbl) s->d->read_trace(host_err, len);
+        else s->f->read_trace(host_err, len);
+    });
+}
+
+tval3_status tval3_solver_destroy(tval3_solver s) {
+    return guard([&] { delete s; });
+}
+
+// ---------------------------------------------------------------------------
+// stencils
+// ---------------------------------------------------------------------------
+tval3_status tval3_D_f32(int dim_y, int dim_x, int dim_z, const float* U, float* DU, void* stream) {
+    return guard([&] {
+        if (dim_y <= 0 || dim_x <= 0 || dim_z <= 0 || !U || !DU) arg_error(TVAL3_ERR_ARG, "Argument error: bad volume!");
+        launch_D_plain<float>(dim_y, dim_x, dim_z, U, DU, (cudaStream_t)stream);
+        TV3_CUDA(cudaGetLastError());
+    });
+}
+tval3_status tval3_Dt_f32(int dim_y, int dim_x, int dim_z, const float* V, float* out, void* stream) {
+    return guard([&] {
+        if (dim_y <= 0 || dim_x <= 0 || dim_z <= 0 || !V || !out) arg_error(TVAL3_ERR_ARG, "Argument error: bad volume!");
+        launch_Dt_plain<float>(dim_y, dim_x, dim_z, V, out, (cudaStream_t)stream);
+        TV3_CUDA(cudaGetLastError());
+    });
+}
+tval3_status tval3_D_f64(int dim_y, int dim_x, int dim_z, const double* U, double* DU, void* stream) {
+    return guard([&] {
+        if (dim_y <= 0 || dim_x <= 0 || dim_z <= 0 || !U || !DU) arg_error(TVAL3_ERR_ARG, "Argument error: bad volume!");
+        launch_D_plain<double>(dim_y, dim_x, dim_z, U, DU, (cudaStream_t)stream);
+        TV3_CUDA(cudaGetLastError());
+    });
+}
+tval3_status tval3_Dt_f64(int dim_y, int dim_x, int dim_z, const double* V, double* out, void* stream) {
+    return guard([&] {
+        if (dim_y <= 0 || dim_x <= 0 || dim_z <= 0 || !V || !out) arg_error(TVAL3_ERR_ARG, "Argument error: bad volume!");
+        launch_Dt_plain<double>(dim_y, dim_x, dim_z, V, out, (cudaStream_t)stream);
+        TV3_CUDA(cudaGetLastError());
+    });
+}
+
+}  // extern "C"

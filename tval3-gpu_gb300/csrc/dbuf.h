@@ -1,0 +1,49 @@
+// Owning device buffer (cudaMalloc / cudaFree), move-only.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include "ops.h"
+
+namespace tv3 {
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() {}
+    explicit DBuf(size_t n_) { alloc(n_); }
+    void alloc(size_t n_) {
+        release();
+        if (n_) {
+            void* q = nullptr;
+            TV3_CUDA(cudaMalloc(&q, n_ * sizeof(T)));
+            p = static_cast<T*>(q);
+            n = n_;
+        }
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DBuf() { release(); }
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) {
+        o.p = nullptr;
+        o.n = 0;
+    }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p;
+            n = o.n;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
+};
+
+}  // namespace tv3

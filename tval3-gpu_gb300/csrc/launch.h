@@ -1,0 +1,105 @@
+// Host-side launch interface of the kernels (internal to the library).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace tv3 {
+
+struct Ctl;
+
+enum SpmvEpi : int { SPMV_PLAIN = 0, SPMV_SUB = 1, SPMV_LAM35 = 2, SPMV_NORM2 = 3 };
+
+// Arguments of one CSR product y = M x (M is A or the CSR of A^T).  x and y
+// are ping-pong pairs: with by_parity set, the kernel uses slot ctl->parity.
+template <class T, class V>
+struct SpmvArgs {
+    long rows;
+    const int* ptr;
+    const int* ind;
+    const V* val;
+    const float* rscale;  // per-row scale applied to the row sum (A*x), or null
+    const float* xscale;  // per-entry scale of the gathered x (A^T*y), or null
+    const T* x[2];
+    T* y[2];
+    int by_parity;
+    const T* sub;    // SPMV_SUB: y = Mx - sub
+    const T* b;      // SPMV_LAM35
+    const T* delta;  // SPMV_LAM35
+    Ctl* ctl;
+    double* part;
+    unsigned* ticket;
+};
+
+template <class T, class V>
+void launch_spmv(const SpmvArgs<T, V>& a, int epi, int G, int grid, cudaStream_t s);
+
+// Buffers of one solve (see solver.cu).  Slot arrays are ping-pong pairs
+// indexed by ctl->parity ("current") and 1 - parity ("previous").
+template <class T>
+struct SolverBufs {
+    int p, q, r;   // dim_y (fastest), dim_x, dim_z
+    long n, m;
+    T* U[2];
+    T* g[2];
+    T* g2[2];
+    T* Au[2];
+    T* DU[2];      // 3n each
+    T* d;
+    T* DtsAtd;
+    T* Atb;
+    T* W;          // 3n
+    T* sig;        // 3n
+    T* dU;
+    T* dg;
+    T* dg2;
+    T* dDU;        // 3n
+    T* dAu;        // m
+    T* b;          // m, scaled
+    T* delta;      // m
+    T* rcdU;
+    const T* xstar;   // optional reference solution (unscaled) for the relerr trace
+    double* trace;    // optional per-iteration relative error vs xstar
+    int use_dtsatd;
+    Ctl* ctl;
+    double* part;
+    unsigned* ticket;
+    int grid;         // grid of the reducing kernels
+    // CUDA graph conditional handles (whole-solve graph only): the epilogues
+    // that decide a branch set the matching handle when use_graph is set.
+    int use_graph;
+    unsigned long long h_inner;  // WHILE: continue the inner loop
+    unsigned long long h_arm;    // IF: Armijo test failed after the descent
+    unsigned long long h_bt;     // WHILE: take another backtracking step
+    unsigned long long h_mlp;    // IF: outer loop continues (multiplier update)
+};
+
+// Flags that the tiny condition kernel copies from the control block into a
+// conditional handle.
+enum CondSrc : int { COND_FST = 0, COND_RESTART = 1, COND_ONE = 2, COND_NOT_DONE = 3 };
+void launch_cond(Ctl* ctl, unsigned long long handle, int src, cudaStream_t s);
+
+// stencil.cu
+template <class T> void launch_scale_b(const T* b_in, SolverBufs<T>& B, cudaStream_t s);
+template <class T> void launch_D_only(SolverBufs<T>& B, cudaStream_t s);
+template <class T> void launch_descend(SolverBufs<T>& B, int restart, cudaStream_t s);
+template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s);
+template <class T> void launch_tau(SolverBufs<T>& B, cudaStream_t s);
+template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s);
+template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s);
+template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t s);
+template <class T> void launch_backtrack(SolverBufs<T>& B, int setup, cudaStream_t s);
+template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s);
+template <class T> void launch_mlp(SolverBufs<T>& B, cudaStream_t s);
+template <class T> void launch_outer_grad(SolverBufs<T>& B, cudaStream_t s);
+template <class T> void launch_finalize(SolverBufs<T>& B, T* U_out, const T* Ut, cudaStream_t s);
+
+// Standalone operators (tval3_D / tval3_Dt entry points).
+template <class T> void launch_D_plain(int p, int q, int r, const T* U, T* DU3, cudaStream_t s);
+template <class T> void launch_Dt_plain(int p, int q, int r, const T* V3, T* out, cudaStream_t s);
+
+int num_sms();
+
+}  // namespace tv3

@@ -1,0 +1,401 @@
+// CSR operator: device copies of A and of the CSR of A^T, value storage in
+// FP32 / FP64 / BF16 / FP16 (16-bit values carry a per-ray FP32 scale), and the
+// device-side transpose (replaces cusparseScsr2csc, 2d/mat_vec_mul.h:23-28).
+// The single-GPU counterpart in the reference is sparse_mm
+// (3d/mat_vec_mul_sparse.h:1599-1781).
+#include <cub/cub.cuh>
+#include <algorithm>
+#include <vector>
+#include "dbuf.h"
+#include "ops.h"
+
+namespace tv3 {
+
+void throw_cuda(cudaError_t e, const char* what) {
+    int st = (e == cudaErrorMemoryAllocation) ? 4 : 3;
+    cudaGetLastError();  // clear a sticky launch error where possible
+    throw Error{st, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+static int pick_lanes(double avg) {
+    if (avg > 48) return 32;
+    if (avg > 20) return 16;
+    if (avg > 8) return 8;
+    return 4;
+}
+
+static int spmv_grid(long rows, int G) {
+    long need = (rows * G + 255) / 256;
+    long cap = (long)num_sms() * 8;
+    return (int)std::max<long>(1, std::min(need, cap));
+}
+
+// ---------------------------------------------------------------------------
+// quantisation helpers
+// ---------------------------------------------------------------------------
+template <class V> __device__ __forceinline__ V to_v(float x);
+template <> __device__ __forceinline__ __nv_bfloat16 to_v<__nv_bfloat16>(float x) { return __float2bfloat16_rn(x); }
+template <> __device__ __forceinline__ __half to_v<__half>(float x) { return __float2half_rn(x); }
+template <class V> __device__ __forceinline__ float from_v(V x);
+template <> __device__ __forceinline__ float from_v<__nv_bfloat16>(__nv_bfloat16 x) { return __bfloat162float(x); }
+template <> __device__ __forceinline__ float from_v<__half>(__half x) { return __half2float(x); }
+
+// per-row scale = max |a_r| (1 for an empty or all-zero row); one warp per row
+__global__ void k_rowmax(long rows, const int* __restrict__ ptr, const float* __restrict__ val, float* __restrict__ s) {
+    const int lane = threadIdx.x & 31;
+    for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += ((long)gridDim.x * blockDim.x) >> 5) {
+        float mx = 0.f;
+        for (int k = ptr[r] + lane; k < ptr[r + 1]; k += 32) mx = fmaxf(mx, fabsf(val[k]));
+        for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
+        if (lane == 0) s[r] = (mx > 0.f) ? mx : 1.f;
+    }
+}
+
+template <class V>
+__global__ void k_quant_rows(long rows, const int* __restrict__ ptr, const float* __restrict__ val,
+                             const float* __restrict__ s, V* __restrict__ q) {
+    const int lane = threadIdx.x & 31;
+    for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += ((long)gridDim.x * blockDim.x) >> 5) {
+        const float inv = s[r];
+        for (int k = ptr[r] + lane; k < ptr[r + 1]; k += 32) q[k] = to_v<V>(val[k] / inv);
+    }
+}
+
+template <class V>
+__global__ void k_quant_entries(long nnz, const int* __restrict__ rowidx, const float* __restrict__ val,
+                                const float* __restrict__ s, V* __restrict__ q) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x)
+        q[k] = to_v<V>(val[k] / s[rowidx[k]]);
+}
+
+template <class V>
+__global__ void k_dequant_rows(long rows, const int* __restrict__ ptr, const V* __restrict__ q,
+                               const float* __restrict__ s, float* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += ((long)gridDim.x * blockDim.x) >> 5)
+        for (int k = ptr[r] + lane; k < ptr[r + 1]; k += 32) out[k] = from_v<V>(q[k]) * s[r];
+}
+
+template <class V>
+__global__ void k_dequant_entries(long nnz, const int* __restrict__ rowidx, const V* __restrict__ q,
+                                  const float* __restrict__ s, float* __restrict__ out) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x)
+        out[k] = from_v<V>(q[k]) * s[rowidx[k]];
+}
+
+template <class A, class B>
+__global__ void k_convert(long n, const A* __restrict__ in, B* __restrict__ out) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+        out[k] = (B)in[k];
+}
+
+// ---------------------------------------------------------------------------
+// device transpose (stable radix sort of the column indices)
+// ---------------------------------------------------------------------------
+__global__ void k_iota(long n, int* __restrict__ v) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) v[k] = (int)k;
+}
+
+__global__ void k_expand_rows(long rows, const int* __restrict__ ptr, int* __restrict__ rowof) {
+    const int lane = threadIdx.x & 31;
+    for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += ((long)gridDim.x * blockDim.x) >> 5)
+        for (int k = ptr[r] + lane; k < ptr[r + 1]; k += 32) rowof[k] = (int)r;
+}
+
+__global__ void k_hist(long nnz, const int* __restrict__ ind, int* __restrict__ cnt) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x)
+        atomicAdd(cnt + ind[k], 1);
+}
+
+template <class V>
+__global__ void k_gather_t(long nnz, const int* __restrict__ perm, const int* __restrict__ rowof,
+                           const V* __restrict__ val, int* __restrict__ tind, V* __restrict__ tval) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
+        int p = perm[k];
+        tind[k] = rowof[p];
+        tval[k] = val[p];
+    }
+}
+
+static int ew(long n) {
+    long g = (n + 255) / 256;
+    long cap = (long)num_sms() * 32;
+    return (int)std::max<long>(1, std::min(g, cap));
+}
+
+template <class V>
+void csr_transpose_device(long rows, long cols, long nnz, const int* ptr, const int* ind, const V* val, int* tptr,
+                          int* tind, V* tval, cudaStream_t s) {
+    DBuf<int> cnt(cols + 1);
+    TV3_CUDA(cudaMemsetAsync(cnt.p, 0, (cols + 1) * sizeof(int), s));
+    if (nnz > 0) {
+        DBuf<int> keys_out(nnz), perm_in(nnz), perm_out(nnz), rowof(nnz);
+        k_iota<<<ew(nnz), 256, 0, s>>>(nnz, perm_in.p);
+        k_expand_rows<<<ew(rows * 32), 256, 0, s>>>(rows, ptr, rowof.p);
+        k_hist<<<ew(nnz), 256, 0, s>>>(nnz, ind, cnt.p);
+        int end_bit = 1;
+        while (end_bit < 31 && (1L << end_bit) < cols) ++end_bit;
+        size_t tmp_bytes = 0;
+        TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, ind, keys_out.p, perm_in.p, perm_out.p, (int)nnz,
+                                                 0, end_bit, s));
+        DBuf<char> tmp(tmp_bytes);
+        TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, ind, keys_out.p, perm_in.p, perm_out.p, (int)nnz,
+                                                 0, end_bit, s));
+        k_gather_t<V><<<ew(nnz), 256, 0, s>>>(nnz, perm_out.p, rowof.p, val, tind, tval);
+        TV3_CUDA(cudaGetLastError());
+        size_t scan_bytes = 0;
+        TV3_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, cnt.p, tptr, (int)(cols + 1), s));
+        DBuf<char> tmp2(scan_bytes);
+        TV3_CUDA(cub::DeviceScan::ExclusiveSum(tmp2.p, scan_bytes, cnt.p, tptr, (int)(cols + 1), s));
+        TV3_CUDA(cudaStreamSynchronize(s));  // temporaries are freed on return
+    } else {
+        TV3_CUDA(cudaMemsetAsync(tptr, 0, (cols + 1) * sizeof(int), s));
+        TV3_CUDA(cudaStreamSynchronize(s));
+    }
+}
+
+template void csr_transpose_device<float>(long, long, long, const int*, const int*, const float*, int*, int*, float*,
+                                          cudaStream_t);
+template void csr_transpose_device<double>(long, long, long, const int*, const int*, const double*, int*, int*,
+                                           double*, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// the operator
+// ---------------------------------------------------------------------------
+template <class T, class V>
+struct CsrOp : LinOp<T> {
+    DBuf<int> ptr, ind, tptr, tind, rowof_t;
+    DBuf<V> val, tval;
+    DBuf<float> rs;  // per-ray scale (16-bit storage only)
+    int Gn = 32, Gt = 8, grid_n = 1, grid_t = 1;
+
+    void apply(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const override {
+        SpmvArgs<T, V> a{};
+        if (!trans) {
+            a.rows = this->m; a.ptr = ptr.p; a.ind = ind.p; a.val = val.p; a.rscale = rs.p; a.xscale = nullptr;
+        } else {
+            a.rows = this->n; a.ptr = tptr.p; a.ind = tind.p; a.val = tval.p; a.rscale = nullptr; a.xscale = rs.p;
+        }
+        a.x[0] = io.x[0]; a.x[1] = io.x[1];
+        a.y[0] = io.y[0]; a.y[1] = io.y[1];
+        a.by_parity = io.by_parity;
+        a.sub = io.sub; a.b = io.b; a.delta = io.delta;
+        a.ctl = io.ctl; a.part = io.part; a.ticket = io.ticket;
+        launch_spmv<T, V>(a, epi, trans ? Gt : Gn, trans ? grid_t : grid_n, s);
+        TV3_CUDA(cudaGetLastError());
+    }
+
+    void export_csr(int* hptr, int* hind, float* hval, int* htptr, int* htind, float* htval) const override;
+};
+
+template <class T, class V>
+static void export_vals(const CsrOp<T, V>& op, float* hval, float* htval);
+
+template <>
+void export_vals<float, float>(const CsrOp<float, float>& op, float* hval, float* htval) {
+    if (hval) TV3_CUDA(cudaMemcpy(hval, op.val.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
+    if (htval) TV3_CUDA(cudaMemcpy(htval, op.tval.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
+}
+template <>
+void export_vals<double, double>(const CsrOp<double, double>& op, float* hval, float* htval) {
+    DBuf<float> tmp(std::max<long>(op.nnz, 1));
+    if (hval) {
+        k_convert<double, float><<<ew(op.nnz), 256>>>(op.nnz, op.val.p, tmp.p);
+        TV3_CUDA(cudaMemcpy(hval, tmp.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    if (htval) {
+        k_convert<double, float><<<ew(op.nnz), 256>>>(op.nnz, op.tval.p, tmp.p);
+        TV3_CUDA(cudaMemcpy(htval, tmp.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+}
+template <class V>
+static void export_q(const CsrOp<float, V>& op, float* hval, float* htval) {
+    DBuf<float> tmp(std::max<long>(op.nnz, 1));
+    if (hval) {
+        k_dequant_rows<V><<<ew(op.m * 32), 256>>>(op.m, op.ptr.p, op.val.p, op.rs.p, tmp.p);
+        TV3_CUDA(cudaMemcpy(hval, tmp.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    if (htval) {
+        k_dequant_entries<V><<<ew(op.nnz), 256>>>(op.nnz, op.tind.p, op.tval.p, op.rs.p, tmp.p);
+        TV3_CUDA(cudaMemcpy(htval, tmp.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+}
+template <>
+void export_vals<float, __nv_bfloat16>(const CsrOp<float, __nv_bfloat16>& op, float* hval, float* htval) {
+    export_q(op, hval, htval);
+}
+template <>
+void export_vals<float, __half>(const CsrOp<float, __half>& op, float* hval, float* htval) {
+    export_q(op, hval, htval);
+}
+
+template <class T, class V>
+void CsrOp<T, V>::export_csr(int* hptr, int* hind, float* hval, int* htptr, int* htind, float* htval) const {
+    if (hptr) TV3_CUDA(cudaMemcpy(hptr, ptr.p, (this->m + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    if (hind) TV3_CUDA(cudaMemcpy(hind, ind.p, this->nnz * sizeof(int), cudaMemcpyDeviceToHost));
+    if (htptr) TV3_CUDA(cudaMemcpy(htptr, tptr.p, (this->n + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    if (htind) TV3_CUDA(cudaMemcpy(htind, tind.p, this->nnz * sizeof(int), cudaMemcpyDeviceToHost));
+    export_vals<T, V>(*this, hval, htval);
+}
+
+template <class T, class V>
+static void finish_layout(CsrOp<T, V>* op) {
+    op->Gn = pick_lanes(op->m ? (double)op->nnz / op->m : 0.0);
+    op->Gt = pick_lanes(op->n ? (double)op->nnz / op->n : 0.0);
+    op->grid_n = spmv_grid(op->m, op->Gn);
+    op->grid_t = spmv_grid(op->n, op->Gt);
+}
+
+// Build from device arrays (FP32 values for the FP32/BF16/FP16 precisions,
+// FP64 values for FP64).  The transpose is built when d_tptr is null.
+template <class T>
+LinOp<T>* make_csr_op_device(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind, const T* d_val,
+                             const int* d_tptr, const int* d_tind, const T* d_tval, int precision,
+                             cudaStream_t s);
+
+template <class T>
+static void copy_structure(LinOp<T>* base, DBuf<int>& ptr, DBuf<int>& ind, DBuf<int>& tptr, DBuf<int>& tind,
+                           long rows, long cols, long nnz, const int* d_ptr, const int* d_ind) {
+    base->m = rows; base->n = cols; base->nnz = nnz; base->kind = 0;
+    ptr.alloc(rows + 1);
+    ind.alloc(std::max<long>(nnz, 1));
+    tptr.alloc(cols + 1);
+    tind.alloc(std::max<long>(nnz, 1));
+    TV3_CUDA(cudaMemcpy(ptr.p, d_ptr, (rows + 1) * sizeof(int), cudaMemcpyDeviceToDevice));
+    if (nnz) TV3_CUDA(cudaMemcpy(ind.p, d_ind, nnz * sizeof(int), cudaMemcpyDeviceToDevice));
+}
+
+template <>
+void export_vals<double, float>(const CsrOp<double, float>& op, float* hval, float* htval) {
+    if (hval) TV3_CUDA(cudaMemcpy(hval, op.val.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
+    if (htval) TV3_CUDA(cudaMemcpy(htval, op.tval.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
+}
+
+// FP32 values with FP64 vectors: the matrix stream is that of the FP32
+// operator, the products, vectors and reductions are FP64.
+LinOp<double>* make_csr_op_f64vec(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind,
+                                  const float* d_val, const int* d_tptr, const int* d_tind, const float* d_tval,
+                                  cudaStream_t s) {
+    auto* op = new CsrOp<double, float>();
+    try {
+        copy_structure<double>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
+        op->val.alloc(std::max<long>(nnz, 1));
+        op->tval.alloc(std::max<long>(nnz, 1));
+        if (nnz) TV3_CUDA(cudaMemcpy(op->val.p, d_val, nnz * sizeof(float), cudaMemcpyDeviceToDevice));
+        if (d_tptr) {
+            TV3_CUDA(cudaMemcpy(op->tptr.p, d_tptr, (cols + 1) * sizeof(int), cudaMemcpyDeviceToDevice));
+            if (nnz) {
+                TV3_CUDA(cudaMemcpy(op->tind.p, d_tind, nnz * sizeof(int), cudaMemcpyDeviceToDevice));
+                TV3_CUDA(cudaMemcpy(op->tval.p, d_tval, nnz * sizeof(float), cudaMemcpyDeviceToDevice));
+            }
+        } else {
+            csr_transpose_device<float>(rows, cols, nnz, op->ptr.p, op->ind.p, op->val.p, op->tptr.p, op->tind.p,
+                                        op->tval.p, s);
+        }
+        finish_layout(op);
+    } catch (...) {
+        delete op;
+        throw;
+    }
+    return op;
+}
+
+template <>
+LinOp<double>* make_csr_op_device<double>(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind,
+                                          const double* d_val, const int* d_tptr, const int* d_tind,
+                                          const double* d_tval, int precision, cudaStream_t s) {
+    if (precision == 4) {
+        DBuf<float> v(std::max<long>(nnz, 1)), tv(std::max<long>(nnz, 1));
+        if (nnz) k_convert<double, float><<<ew(nnz), 256, 0, s>>>(nnz, d_val, v.p);
+        if (nnz && d_tptr) k_convert<double, float><<<ew(nnz), 256, 0, s>>>(nnz, d_tval, tv.p);
+        TV3_CUDA(cudaGetLastError());
+        TV3_CUDA(cudaStreamSynchronize(s));
+        return make_csr_op_f64vec(rows, cols, nnz, d_ptr, d_ind, v.p, d_tptr, d_tind, d_tptr ? tv.p : nullptr, s);
+    }
+    auto* op = new CsrOp<double, double>();
+    try {
+        copy_structure<double>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
+        op->val.alloc(std::max<long>(nnz, 1));
+        op->tval.alloc(std::max<long>(nnz, 1));
+        if (nnz) TV3_CUDA(cudaMemcpy(op->val.p, d_val, nnz * sizeof(double), cudaMemcpyDeviceToDevice));
+        if (d_tptr) {
+            TV3_CUDA(cudaMemcpy(op->tptr.p, d_tptr, (cols + 1) * sizeof(int), cudaMemcpyDeviceToDevice));
+            if (nnz) {
+                TV3_CUDA(cudaMemcpy(op->tind.p, d_tind, nnz * sizeof(int), cudaMemcpyDeviceToDevice));
+                TV3_CUDA(cudaMemcpy(op->tval.p, d_tval, nnz * sizeof(double), cudaMemcpyDeviceToDevice));
+            }
+        } else {
+            csr_transpose_device<double>(rows, cols, nnz, op->ptr.p, op->ind.p, op->val.p, op->tptr.p, op->tind.p,
+                                         op->tval.p, s);
+        }
+        finish_layout(op);
+    } catch (...) {
+        delete op;
+        throw;
+    }
+    return op;
+}
+
+template <class V>
+static LinOp<float>* make_q(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind, const float* d_val,
+                            const int* d_tptr, const int* d_tind, const float* d_tval, cudaStream_t s) {
+    auto* op = new CsrOp<float, V>();
+    try {
+        copy_structure<float>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
+        DBuf<float> tv(std::max<long>(nnz, 1));
+        if (d_tptr) {
+            TV3_CUDA(cudaMemcpy(op->tptr.p, d_tptr, (cols + 1) * sizeof(int), cudaMemcpyDeviceToDevice));
+            if (nnz) {
+                TV3_CUDA(cudaMemcpy(op->tind.p, d_tind, nnz * sizeof(int), cudaMemcpyDeviceToDevice));
+                TV3_CUDA(cudaMemcpy(tv.p, d_tval, nnz * sizeof(float), cudaMemcpyDeviceToDevice));
+            }
+        } else {
+            csr_transpose_device<float>(rows, cols, nnz, op->ptr.p, op->ind.p, d_val, op->tptr.p, op->tind.p, tv.p, s);
+        }
+        op->rs.alloc(std::max<long>(rows, 1));
+        op->val.alloc(std::max<long>(nnz, 1));
+        op->tval.alloc(std::max<long>(nnz, 1));
+        k_rowmax<<<ew(rows * 32), 256, 0, s>>>(rows, op->ptr.p, d_val, op->rs.p);
+        k_quant_rows<V><<<ew(rows * 32), 256, 0, s>>>(rows, op->ptr.p, d_val, op->rs.p, op->val.p);
+        if (nnz) k_quant_entries<V><<<ew(nnz), 256, 0, s>>>(nnz, op->tind.p, tv.p, op->rs.p, op->tval.p);
+        TV3_CUDA(cudaGetLastError());
+        TV3_CUDA(cudaStreamSynchronize(s));
+        finish_layout(op);
+    } catch (...) {
+        delete op;
+        throw;
+    }
+    return op;
+}
+
+template <>
+LinOp<float>* make_csr_op_device<float>(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind,
+                                        const float* d_val, const int* d_tptr, const int* d_tind, const float* d_tval,
+                                        int precision, cudaStream_t s) {
+    if (precision == 2) return make_q<__nv_bfloat16>(rows, cols, nnz, d_ptr, d_ind, d_val, d_tptr, d_tind, d_tval, s);
+    if (precision == 3) return make_q<__half>(rows, cols, nnz, d_ptr, d_ind, d_val, d_tptr, d_tind, d_tval, s);
+    auto* op = new CsrOp<float, float>();
+    try {
+        copy_structure<float>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
+        op->val.alloc(std::max<long>(nnz, 1));
+        op->tval.alloc(std::max<long>(nnz, 1));
+        if (nnz) TV3_CUDA(cudaMemcpy(op->val.p, d_val, nnz * sizeof(float), cudaMemcpyDeviceToDevice));
+        if (d_tptr) {
+            TV3_CUDA(cudaMemcpy(op->tptr.p, d_tptr, (cols + 1) * sizeof(int), cudaMemcpyDeviceToDevice));
+            if (nnz) {
+                TV3_CUDA(cudaMemcpy(op->tind.p, d_tind, nnz * sizeof(int), cudaMemcpyDeviceToDevice));
+                TV3_CUDA(cudaMemcpy(op->tval.p, d_tval, nnz * sizeof(float), cudaMemcpyDeviceToDevice));
+            }
+        } else {
+            csr_transpose_device<float>(rows, cols, nnz, op->ptr.p, op->ind.p, op->val.p, op->tptr.p, op->tind.p,
+                                        op->tval.p, s);
+        }
+        finish_layout(op);
+    } catch (...) {
+        delete op;
+        throw;
+    }
+    return op;
+}
+
+}  // namespace tv3

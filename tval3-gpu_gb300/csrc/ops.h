@@ -1,0 +1,113 @@
+// Linear operators A (rays x voxels) behind the mat_vec_mul interface
+// (3d/mat_vec_mul_sparse.h:1703, 3d/mat_vec_mul_dense.h:37,
+// 3d/mat_vec_mul_dynamic.h:683, 3d/mat_vec_mul.h:733).  Internal to the
+// library; the C ABI wraps them in tval3_op handles.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <memory>
+#include <string>
+#include "launch.h"
+#include "tval3_internal.cuh"
+
+namespace tv3 {
+
+// I/O of one product inside the solver.  x and y are ping-pong pairs selected
+// by ctl->parity when by_parity is set; epilogues as in SpmvEpi.
+template <class T>
+struct MatIO {
+    const T* x[2];
+    T* y[2];
+    int by_parity;
+    const T* sub;
+    const T* b;
+    const T* delta;
+    Ctl* ctl;
+    double* part;
+    unsigned* ticket;
+};
+
+template <class T>
+MatIO<T> plain_io(const T* x, T* y) {
+    MatIO<T> io{};
+    io.x[0] = io.x[1] = x;
+    io.y[0] = io.y[1] = y;
+    return io;
+}
+
+// Error raised inside the library; converted to a status at the C ABI.
+struct Error {
+    int status;
+    std::string msg;
+};
+
+void throw_cuda(cudaError_t e, const char* what);
+#define TV3_CUDA(call)                                           \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) ::tv3::throw_cuda(e_, #call);     \
+    } while (0)
+
+template <class T>
+struct LinOp {
+    long m = 0, n = 0, nnz = 0;
+    int kind = 0;  // 0 CSR, 1 dense, 2 on-the-fly geometry
+    virtual ~LinOp() {}
+    // trans 0: y[rows m] = A x ; trans 1: y[rows n] = A^T x
+    virtual void apply(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const = 0;
+    // multi-RHS products: columns of length n (trans 0: X n x k -> Y m x k)
+    virtual void apply_multi(int trans, int k, const T* X, T* Y, cudaStream_t s) const {
+        const long lx = trans ? m : n, ly = trans ? n : m;
+        for (int j = 0; j < k; ++j) apply(trans, plain_io<T>(X + j * lx, Y + j * ly), SPMV_PLAIN, s);
+    }
+    // export the stored matrix as FP32 CSR (stored operators only)
+    virtual void export_csr(int*, int*, float*, int*, int*, float*) const {
+        throw Error{7, "operator has no stored CSR"};
+    }
+};
+
+// A*x from one operator, A^T*y from another: the reference's sparse_geom_mm
+// (on-the-fly ray traversal for A*x, stored sparse matrix for A^T*y,
+// 3d/mat_vec_mul.h:733-756).
+template <class T>
+struct SplitOp : LinOp<T> {
+    std::unique_ptr<LinOp<T>> nop, top;
+    SplitOp(std::unique_ptr<LinOp<T>> a, std::unique_ptr<LinOp<T>> b) : nop(std::move(a)), top(std::move(b)) {
+        this->m = nop->m;
+        this->n = nop->n;
+        this->nnz = top->nnz;
+        this->kind = 3;
+    }
+    void apply(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const override {
+        (trans ? top : nop)->apply(trans, io, epi, s);
+    }
+};
+
+// CSR operator: A and the CSR of A^T on the device.
+template <class T>
+LinOp<T>* make_csr_op_device(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind, const T* d_val,
+                             const int* d_tptr, const int* d_tind, const T* d_tval, int precision,
+                             cudaStream_t s);
+
+// FP32 stored values, FP64 vectors (precision TVAL3_PREC_FP32_F64VEC).
+LinOp<double>* make_csr_op_f64vec(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind,
+                                  const float* d_val, const int* d_tptr, const int* d_tind, const float* d_tval,
+                                  cudaStream_t s);
+
+// Ray-geometry operators (ray.cu).
+struct RayList;  // compacted ray list and geometry on the device
+template <class T>
+LinOp<T>* make_geometry_op(const void* geometry_host, int mode, int precision, cudaStream_t s);
+
+// Dense operator (dense.cu).
+template <class T>
+LinOp<T>* make_dense_op(long rows, long cols, const void* h_data, int row_major, int val_type, int precision,
+                        cudaStream_t s);
+
+// Device CSR transpose: (ptr, ind, val) of rows x cols -> CSR of A^T with rows
+// ascending inside every column (the reference's CSC order).
+template <class V>
+void csr_transpose_device(long rows, long cols, long nnz, const int* ptr, const int* ind, const V* val, int* tptr,
+                          int* tind, V* tval, cudaStream_t s);
+
+}  // namespace tv3

@@ -1,0 +1,383 @@
+// The TVAL3 loop (3d/tval3_gpu_3d.cpp:1089-1345) driven from the host over
+// device-resident state, in two forms:
+//   mode 0: the host enqueues the kernels of one inner iteration and reads the
+//           two branch flags (Armijo, inner break) from the control block;
+//   mode 1: the whole solve is one CUDA graph.  The loops and branches of the
+//           reference (outer while, inner while, first-iteration step size,
+//           Armijo backtracking with at most five steps, restart, multiplier
+//           update) are conditional graph nodes whose conditions are set on
+//           the device by the epilogues that decide them.  One launch per
+//           solve, no host round trip.
+// Both forms run the same kernels in the same order, so they give identical
+// results.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <vector>
+#include "solver.h"
+
+namespace tv3 {
+
+template <class T>
+Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_)
+    : A(A_), p(p_), q(q_), r(r_), n((long)p_ * q_ * r_), m(A_->m), o(o_) {
+    const long nvec = 28, mvec = 5;
+    nv.alloc(nvec * n);
+    mv.alloc(mvec * std::max<long>(m, 1));
+    ctl.alloc(1);
+    part.alloc(4 * 16384);
+    ticket.alloc(1);
+    trace.alloc(std::max(1, o.maxit));
+    TV3_CUDA(cudaMemset(ticket.p, 0, sizeof(unsigned)));
+    TV3_CUDA(cudaMallocHost(&hctl, sizeof(Ctl)));
+    T* v = nv.p;
+    auto take = [&](long k) { T* t = v; v += k * n; return t; };
+    B.p = p; B.q = q; B.r = r; B.n = n; B.m = m;
+    B.U[0] = take(1); B.U[1] = take(1);
+    B.g[0] = take(1); B.g[1] = take(1);
+    B.g2[0] = take(1); B.g2[1] = take(1);
+    B.DU[0] = take(3); B.DU[1] = take(3);
+    B.d = take(1); B.DtsAtd = take(1); B.Atb = take(1);
+    B.W = take(3); B.sig = take(3);
+    B.dU = take(1); B.dg = take(1); B.dg2 = take(1); B.dDU = take(3);
+    B.rcdU = take(1);
+    T* w = mv.p;
+    const long mm = std::max<long>(m, 1);
+    B.Au[0] = w; B.Au[1] = w + mm; B.dAu = w + 2 * mm; B.b = w + 3 * mm; B.delta = w + 4 * mm;
+    B.ctl = ctl.p; B.part = part.p; B.ticket = ticket.p;
+    // reduction grid: a fixed multiple of the SM count (partials fit in `part`)
+    B.grid = std::max(1, std::min(num_sms() * 4, 8192));
+    B.trace = trace.p;
+}
+
+template <class T>
+Solver<T>::~Solver() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (hctl) cudaFreeHost(hctl);
+}
+
+template <class T>
+MatIO<T> Solver<T>::io_AU() const {
+    MatIO<T> io{};
+    io.x[0] = B.U[0]; io.x[1] = B.U[1];
+    io.y[0] = B.Au[0]; io.y[1] = B.Au[1];
+    io.by_parity = 1;
+    io.b = B.b; io.delta = B.delta;
+    io.ctl = B.ctl; io.part = B.part; io.ticket = B.ticket;
+    return io;
+}
+template <class T>
+MatIO<T> Solver<T>::io_AtAu() const {
+    MatIO<T> io{};
+    io.x[0] = B.Au[0]; io.x[1] = B.Au[1];
+    io.y[0] = B.g[0]; io.y[1] = B.g[1];
+    io.by_parity = 1;
+    io.sub = B.Atb;
+    io.ctl = B.ctl; io.part = B.part; io.ticket = B.ticket;
+    return io;
+}
+template <class T>
+MatIO<T> Solver<T>::io_Ad() const {
+    MatIO<T> io{};
+    io.x[0] = io.x[1] = B.d;
+    io.y[0] = io.y[1] = nullptr;
+    io.ctl = B.ctl; io.part = B.part; io.ticket = B.ticket;
+    return io;
+}
+
+__global__ void k_init_ctl(Ctl* c, Ctl v) { *c = v; }
+
+template <class T>
+void Solver<T>::init_ctl(cudaStream_t s) {
+    Ctl c;
+    std::memset(&c, 0, sizeof(c));
+    c.mu_max = o.mu; c.beta_max = o.beta; c.rate_cnt = o.rate_cnt;
+    c.tol = o.tol; c.tol_inn = o.tol_inn; c.c_arm = o.c; c.gamma = o.gamma;
+    c.gam0 = o.gam; c.rate_gam = o.rate_gam;
+    c.maxcnt = o.maxcnt; c.maxit = o.maxit; c.nonneg = o.nonneg ? 1 : 0; c.iso = (o.tv_type == TVAL3_TV_ISO);
+    c.mu = std::min(o.mu0, o.mu);
+    c.beta = std::min(o.beta0, o.beta);
+    c.muDbeta = c.mu / c.beta;
+    c.gam = o.gam;
+    c.Q = 1.0;
+    c.fst = 1;
+    c.scl = 1.0;
+    k_init_ctl<<<1, 1, 0, s>>>(ctl.p, c);
+    TV3_CUDA(cudaGetLastError());
+}
+
+template <class T>
+void Solver<T>::read_ctl(cudaStream_t s) {
+    TV3_CUDA(cudaMemcpyAsync(hctl, ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    TV3_CUDA(cudaStreamSynchronize(s));
+}
+
+// get_g_gpu (:366-572): Au = A U, g = A^T Au - Atb, g2 = D^T(DU - W), f.
+template <class T>
+void Solver<T>::get_g(int epi, cudaStream_t s) {
+    A->apply(0, io_AU(), SPMV_LAM35, s);
+    A->apply(1, io_AtAu(), SPMV_SUB, s);
+    launch_g2<T>(B, epi, s);
+}
+
+// first-iteration step size (:583-611): ||Dd||^2, <d,d>, ||Ad||^2 -> tau
+template <class T>
+void Solver<T>::tau_first(cudaStream_t s) {
+    launch_Dd_norm<T>(B, s);
+    A->apply(0, io_Ad(), SPMV_NORM2, s);
+}
+
+// start-up (:1115-1149)
+template <class T>
+void Solver<T>::setup(const T* d_b, cudaStream_t s) {
+    init_ctl(s);
+    TV3_CUDA(cudaMemsetAsync(B.sig, 0, 3 * n * sizeof(T), s));
+    TV3_CUDA(cudaMemsetAsync(B.DtsAtd, 0, n * sizeof(T), s));
+    if (m > 0) TV3_CUDA(cudaMemsetAsync(B.delta, 0, m * sizeof(T), s));
+    launch_scale_b<T>(d_b, B, s);                                    // scaleb_gpu
+    A->apply(1, plain_io<T>(B.b, B.Atb), SPMV_PLAIN, s);             // Atb = A^T b
+    TV3_CUDA(cudaMemcpyAsync(B.U[0], B.Atb, n * sizeof(T), cudaMemcpyDeviceToDevice, s));   // U = Atb
+    TV3_CUDA(cudaMemcpyAsync(B.rcdU, B.Atb, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    launch_D_only<T>(B, s);
+    launch_shrink<T>(B, EPI_G2_INIT, s);
+    get_g(EPI_G2_INIT, s);
+    launch_gradient<T>(B, 0, s);
+    TV3_CUDA(cudaGetLastError());
+}
+
+template <class T>
+void Solver<T>::run_host(cudaStream_t s) {
+    if (!(o.maxcnt > 0 && o.maxit > 0)) return;
+    bool fst = true;
+    for (;;) {
+        // ---- min_u (:823-891)
+        if (fst) tau_first(s);
+        else launch_tau<T>(B, s);
+        launch_descend<T>(B, 0, s);
+        get_g(EPI_G2_DESCEND, s);
+        read_ctl(s);
+        if (hctl->armijo_fail) {
+            launch_backtrack<T>(B, 1, s);
+            read_ctl(s);
+            while (hctl->armijo_fail && hctl->cnt < 5) {
+                launch_backtrack<T>(B, 0, s);
+                read_ctl(s);
+            }
+            if (hctl->armijo_fail) {  // cnt == 5: exact step from Up
+                tau_first(s);
+                launch_descend<T>(B, 1, s);
+                get_g(EPI_G2_RESTART, s);
+            }
+        }
+        // ---- update_W (:965-1029), reference values, gradient, RelChg
+        launch_shrink<T>(B, EPI_G2_UPDATE_W, s);
+        launch_g2<T>(B, EPI_G2_UPDATE_W, s);
+        launch_gradient<T>(B, 1, s);
+        read_ctl(s);
+        fst = false;
+        if (hctl->inner_break) {
+            launch_outer_relchg<T>(B, s);
+            read_ctl(s);
+            if (hctl->done) break;
+            launch_mlp<T>(B, s);
+            launch_outer_grad<T>(B, s);
+            read_ctl(s);
+            if (hctl->done) break;
+            fst = true;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// whole-solve graph
+// ---------------------------------------------------------------------------
+namespace {
+
+// A body graph being filled by stream capture.  Between captured sequences,
+// conditional nodes are appended with the current tail as dependencies.
+struct Body {
+    cudaGraph_t g;
+    std::vector<cudaGraphNode_t> deps;
+    cudaStream_t s;
+    bool capturing = false;
+    void begin() {
+        TV3_CUDA(cudaStreamBeginCaptureToGraph(s, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                               cudaStreamCaptureModeThreadLocal));
+        capturing = true;
+    }
+    void end() {
+        cudaStreamCaptureStatus st;
+        const cudaGraphNode_t* d = nullptr;
+        size_t nd = 0;
+        TV3_CUDA(cudaStreamGetCaptureInfo(s, &st, nullptr, nullptr, &d, nullptr, &nd));
+        std::vector<cudaGraphNode_t> tail(d, d + nd);
+        cudaGraph_t out = g;
+        TV3_CUDA(cudaStreamEndCapture(s, &out));
+        deps = tail;
+        capturing = false;
+    }
+    // append a conditional node; returns its body graphs
+    std::vector<cudaGraph_t> cond(cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, unsigned size) {
+        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+        np.conditional.handle = h;
+        np.conditional.type = type;
+        np.conditional.size = size;
+        cudaGraphNode_t node;
+        TV3_CUDA(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &np));
+        deps.assign(1, node);
+        return std::vector<cudaGraph_t>(np.conditional.phGraph_out, np.conditional.phGraph_out + size);
+    }
+};
+
+}  // namespace
+
+template <class T>
+void Solver<T>::build_graph(const T* d_b, T* d_U, const T* d_Ut, cudaStream_t s) {
+    if (gexec) {
+        cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+    }
+    cudaGraph_t top;
+    TV3_CUDA(cudaGraphCreate(&top, 0));
+    cudaStream_t cs;
+    TV3_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    try {
+        const unsigned run = (o.maxcnt > 0 && o.maxit > 0) ? 1u : 0u;
+        cudaGraphConditionalHandle h_outer, h_inner, h_fst, h_arm, h_bt, h_restart, h_mlp;
+        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_outer, top, run, cudaGraphCondAssignDefault));
+        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_inner, top, 1, cudaGraphCondAssignDefault));
+        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_fst, top, 1, cudaGraphCondAssignDefault));
+        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_arm, top, 0, cudaGraphCondAssignDefault));
+        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_bt, top, 0, cudaGraphCondAssignDefault));
+        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_restart, top, 0, cudaGraphCondAssignDefault));
+        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_mlp, top, 0, cudaGraphCondAssignDefault));
+        B.use_graph = 1;
+        B.h_inner = h_inner; B.h_arm = h_arm; B.h_bt = h_bt; B.h_mlp = h_mlp;
+
+        Body tb{top, {}, cs};
+        tb.begin();
+        setup(d_b, cs);
+        tb.end();
+        // outer while
+        Body ob{tb.cond(h_outer, cudaGraphCondTypeWhile, 1)[0], {}, cs};
+        ob.begin();
+        launch_cond(B.ctl, h_inner, COND_ONE, cs);
+        ob.end();
+        {
+            Body ib{ob.cond(h_inner, cudaGraphCondTypeWhile, 1)[0], {}, cs};
+            ib.begin();
+            launch_cond(B.ctl, h_fst, COND_FST, cs);
+            ib.end();
+            auto fb = ib.cond(h_fst, cudaGraphCondTypeIf, 2);
+            {
+                Body t{fb[0], {}, cs};
+                t.begin(); tau_first(cs); t.end();
+                Body e{fb[1], {}, cs};
+                e.begin(); launch_tau<T>(B, cs); e.end();
+            }
+            ib.begin();
+            launch_descend<T>(B, 0, cs);
+            get_g(EPI_G2_DESCEND, cs);  // sets h_arm
+            ib.end();
+            {
+                Body ab{ib.cond(h_arm, cudaGraphCondTypeIf, 1)[0], {}, cs};
+                ab.begin();
+                launch_backtrack<T>(B, 1, cs);  // sets h_bt
+                ab.end();
+                {
+                    Body bb{ab.cond(h_bt, cudaGraphCondTypeWhile, 1)[0], {}, cs};
+                    bb.begin(); launch_backtrack<T>(B, 0, cs); bb.end();
+                }
+                ab.begin();
+                launch_cond(B.ctl, h_restart, COND_RESTART, cs);
+                ab.end();
+                {
+                    Body rb{ab.cond(h_restart, cudaGraphCondTypeIf, 1)[0], {}, cs};
+                    rb.begin();
+                    tau_first(cs);
+                    launch_descend<T>(B, 1, cs);
+                    get_g(EPI_G2_RESTART, cs);
+                    rb.end();
+                }
+            }
+            ib.begin();
+            launch_shrink<T>(B, EPI_G2_UPDATE_W, cs);
+            launch_g2<T>(B, EPI_G2_UPDATE_W, cs);
+            launch_gradient<T>(B, 1, cs);  // sets h_inner
+            ib.end();
+        }
+        ob.begin();
+        launch_outer_relchg<T>(B, cs);  // sets h_mlp
+        ob.end();
+        {
+            Body mb{ob.cond(h_mlp, cudaGraphCondTypeIf, 1)[0], {}, cs};
+            mb.begin();
+            launch_mlp<T>(B, cs);
+            launch_outer_grad<T>(B, cs);
+            mb.end();
+        }
+        ob.begin();
+        launch_cond(B.ctl, h_outer, COND_NOT_DONE, cs);
+        ob.end();
+        tb.begin();
+        launch_finalize<T>(B, d_U, d_Ut, cs);
+        tb.end();
+        B.use_graph = 0;
+        TV3_CUDA(cudaGraphInstantiate(&gexec, top, 0));
+    } catch (...) {
+        B.use_graph = 0;
+        cudaStreamDestroy(cs);
+        cudaGraphDestroy(top);
+        throw;
+    }
+    cudaStreamDestroy(cs);
+    cudaGraphDestroy(top);
+    g_b = d_b; g_U = d_U; g_Ut = d_Ut; g_stream = s;
+}
+
+template <class T>
+void Solver<T>::solve(const T* d_b, T* d_U, const T* d_Ut, tval3_info* info, cudaStream_t s) {
+    B.xstar = xstar;
+    cudaEvent_t e0, e1;
+    TV3_CUDA(cudaEventCreate(&e0));
+    TV3_CUDA(cudaEventCreate(&e1));
+    TV3_CUDA(cudaEventRecord(e0, s));
+    if (mode == 1) {
+        if (!gexec || g_b != d_b || g_U != d_U || g_Ut != d_Ut) build_graph(d_b, d_U, d_Ut, s);
+        TV3_CUDA(cudaGraphLaunch(gexec, s));
+    } else {
+        B.use_graph = 0;
+        setup(d_b, s);
+        run_host(s);
+        launch_finalize<T>(B, d_U, d_Ut, s);
+    }
+    TV3_CUDA(cudaEventRecord(e1, s));
+    TV3_CUDA(cudaGetLastError());
+    read_ctl(s);
+    float ms = 0.f;
+    TV3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (hctl->err) throw Error{TVAL3_ERR_CUDA, "device-side error word set during the solve"};
+    if (info) {
+        info->total_iters = hctl->count_total;
+        info->outer_iters = hctl->count_outer;
+        info->rel_chg = hctl->relchgout;
+        info->rel_error = hctl->rel_error;
+        info->secs = ms / 1000.0;
+        info->backtracks = hctl->backtracks;
+        info->restarts = hctl->restarts;
+        info->final_f = hctl->f;
+    }
+}
+
+template <class T>
+void Solver<T>::read_trace(double* host, int len) {
+    int k = std::min(len, (int)trace.n);
+    if (k > 0) TV3_CUDA(cudaMemcpy(host, trace.p, k * sizeof(double), cudaMemcpyDeviceToHost));
+}
+
+template struct Solver<float>;
+template struct Solver<double>;
+
+}  // namespace tv3

@@ -1,0 +1,659 @@
+// Volume kernels of the TVAL3 loop: the periodic difference operator D and
+// its adjoint, shrinkage, the step-size, gradient, backtracking and multiplier
+// updates, each fused with the reductions the loop needs.  Every reducing
+// kernel ends in a deterministic grid reduction whose last block updates the
+// device control block (tval3_internal.cuh), so no value crosses to the host.
+//
+// Reference counterparts (3d/tval3_gpu_3d.cpp unless noted):
+//   k_D_only / k_descend   D_gpu :271-314 (+ axpy and nonneg_kernel, :671-701)
+//   k_Dd_norm              get_tau_gpu first iteration :583-600
+//   k_tau                  get_tau_kernel, 3d/tval3_gpu_3d_kernels.cu:1017-1067
+//   k_g2                   V = DU - W, lam2_4_kernel, Dt_gpu (get_g_gpu :484-571)
+//   k_shrink               shrinkage_kernel, 3d/tval3_gpu_3d_kernels.cu:1249-1300
+//   k_gradient             get_gradient_gpu :896-919 and the RelChg test :1178-1200
+//   k_backtrack            min_u_gpu Armijo branch :848-890 with update_g_gpu :706-818
+//   k_outer_relchg         :1204-1220
+//   k_mlp                  update_mlp_gpu :1034-1083 and continuation :1222-1237
+//   k_outer_grad           DtsAtd and get_gradient :1238-1249
+#include <math.h>
+#include "tval3_internal.cuh"
+#include "launch.h"
+
+namespace tv3 {
+
+struct Nb {
+    long yp, ym, xp, xm, zp, zm;
+};
+
+__device__ __forceinline__ Nb neighbours(int p, int q, int r, long i) {
+    const long pq = (long)p * q;
+    const int y = (int)(i % p);
+    const long t = i / p;
+    const int x = (int)(t % q);
+    const int z = (int)(t / q);
+    Nb o;
+    o.yp = (y + 1 < p) ? i + 1 : i - y;
+    o.ym = (y > 0) ? i - 1 : i + (p - 1);
+    o.xp = (x + 1 < q) ? i + p : i - (long)x * p;
+    o.xm = (x > 0) ? i - p : i + (long)(q - 1) * p;
+    o.zp = (z + 1 < r) ? i + pq : i - (long)z * pq;
+    o.zm = (z > 0) ? i - pq : i + (long)(r - 1) * pq;
+    return o;
+}
+
+#define GRID_STRIDE(i, N) for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < (N); i += (long)gridDim.x * blockDim.x)
+
+template <class T> __device__ __forceinline__ T proj(T v, int nonneg) { return (nonneg && v < T(0)) ? T(0) : v; }
+
+// ---------------------------------------------------------------------------
+// b scaling (scaleb_gpu :226-266): one block finds the entries of smallest and
+// largest |b| (first occurrence on ties, as the reference's strict scan), the
+// next kernel writes b*scl.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(1024) k_scale_find(const T* __restrict__ b, long m, Ctl* ctl) {
+    double amin = INFINITY, amax = -1.0;
+    long imin = -1, imax = -1;
+    for (long i = threadIdx.x; i < m; i += blockDim.x) {
+        double a = fabs((double)b[i]);
+        if (a < amin) { amin = a; imin = i; }
+        if (a > amax) { amax = a; imax = i; }
+    }
+    __shared__ double sa[2][1024];
+    __shared__ long si[2][1024];
+    sa[0][threadIdx.x] = amin; si[0][threadIdx.x] = imin;
+    sa[1][threadIdx.x] = amax; si[1][threadIdx.x] = imax;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o; o >>= 1) {
+        if (threadIdx.x < o) {
+            int j = threadIdx.x + o;
+            double a0 = sa[0][j]; long i0 = si[0][j];
+            if (i0 >= 0 && (si[0][threadIdx.x] < 0 || a0 < sa[0][threadIdx.x] ||
+                            (a0 == sa[0][threadIdx.x] && i0 < si[0][threadIdx.x]))) {
+                sa[0][threadIdx.x] = a0; si[0][threadIdx.x] = i0;
+            }
+            double a1 = sa[1][j]; long i1 = si[1][j];
+            if (i1 >= 0 && (si[1][threadIdx.x] < 0 || a1 > sa[1][threadIdx.x] ||
+                            (a1 == sa[1][threadIdx.x] && i1 < si[1][threadIdx.x]))) {
+                sa[1][threadIdx.x] = a1; si[1][threadIdx.x] = i1;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double scl = 1.0;
+        if (m > 0 && si[0][0] >= 0 && si[1][0] >= 0) {
+            double dif = fabs((double)b[si[1][0]] - (double)b[si[0][0]]);
+            // the reference divides by zero when dif == 0; a constant-|b| input keeps scl = 1
+            if (dif > 0.0) {
+                if (dif < 0.5) scl = 0.5 / dif;
+                else if (dif > 1.5) scl = 1.5 / dif;
+            }
+        }
+        ctl->scl = scl;
+    }
+}
+
+template <class T>
+__global__ void k_scale_apply(const T* __restrict__ b_in, T* __restrict__ b, long m, const Ctl* ctl) {
+    const double scl = ctl->scl;
+    const T s = (T)scl;
+    GRID_STRIDE(i, m) b[i] = (scl == 1.0) ? b_in[i] : b_in[i] * s;
+}
+
+// ---------------------------------------------------------------------------
+// D at start-up: DU[0] = D U[0]
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_D_only(SolverBufs<T> B) {
+    const T* __restrict__ U = B.U[0];
+    T* __restrict__ DU = B.DU[0];
+    GRID_STRIDE(i, B.n) {
+        Nb nb = neighbours(B.p, B.q, B.r, i);
+        T u = U[i];
+        DU[i] = U[nb.yp] - u;
+        DU[B.n + i] = U[nb.xp] - u;
+        DU[2 * B.n + i] = U[nb.zp] - u;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// descent step fused with D: U = P(Up - tau d), DU = D U.  U at the forward
+// neighbours is recomputed from Up and d (same expression, so bit-identical
+// to the stored value).  Normal mode reads the current slot, writes the other
+// one and flips the parity (the previous values become Up, gp, g2p, Aup, DUp
+// without copies, :831-833); restart mode reads the previous slot (U = Up,
+// :878) and writes the current one.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_descend(SolverBufs<T> B, int restart) {
+    Ctl* ctl = B.ctl;
+    const int cur = ctl->parity;
+    const int src = restart ? 1 - cur : cur, dst = restart ? cur : 1 - cur;
+    const T* __restrict__ Up = B.U[src];
+    const T* __restrict__ d = B.d;
+    T* __restrict__ U = B.U[dst];
+    T* __restrict__ DU = B.DU[dst];
+    const T mt = (T)(-ctl->tau);
+    const int nn = ctl->nonneg;
+    GRID_STRIDE(i, B.n) {
+        Nb nb = neighbours(B.p, B.q, B.r, i);
+        T uc = proj(Up[i] + mt * d[i], nn);
+        T uy = proj(Up[nb.yp] + mt * d[nb.yp], nn);
+        T ux = proj(Up[nb.xp] + mt * d[nb.xp], nn);
+        T uz = proj(Up[nb.zp] + mt * d[nb.zp], nn);
+        U[i] = uc;
+        DU[i] = uy - uc;
+        DU[B.n + i] = ux - uc;
+        DU[2 * B.n + i] = uz - uc;
+    }
+    if (!restart) {
+        double v[1] = {0.0}, tot[1];
+        if (grid_reduce<1>(v, B.part, B.ticket, tot) && threadIdx.x == 0) ctl->parity = 1 - cur;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// first inner iteration: ||D d||^2 and <d,d>
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_Dd_norm(SolverBufs<T> B) {
+    const T* __restrict__ d = B.d;
+    double s0 = 0.0, s1 = 0.0;
+    GRID_STRIDE(i, B.n) {
+        Nb nb = neighbours(B.p, B.q, B.r, i);
+        T dc = d[i];
+        T a = d[nb.yp] - dc, b = d[nb.xp] - dc, c = d[nb.zp] - dc;
+        s0 += (double)a * a + (double)b * b + (double)c * c;
+        s1 += (double)dc * dc;
+    }
+    double v[2] = {s0, s1}, tot[2];
+    if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        B.ctl->dDd = tot[0];
+        B.ctl->dd = tot[1];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// BB step: ss = <uup,uup>, sy = <uup, dg2 + mu/beta dg>, tau = |ss/sy|
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_tau(SolverBufs<T> B) {
+    Ctl* ctl = B.ctl;
+    const int cur = ctl->parity, prv = 1 - cur;
+    const double mdb = ctl->muDbeta;
+    const T *__restrict__ U = B.U[cur], *__restrict__ Up = B.U[prv];
+    const T *__restrict__ g = B.g[cur], *__restrict__ gp = B.g[prv];
+    const T *__restrict__ g2 = B.g2[cur], *__restrict__ g2p = B.g2[prv];
+    double ss = 0.0, sy = 0.0;
+    GRID_STRIDE(i, B.n) {
+        double u = (double)U[i] - (double)Up[i];
+        double dg = (double)g[i] - (double)gp[i];
+        double dg2 = (double)g2[i] - (double)g2p[i];
+        ss += u * u;
+        sy += u * (dg2 + mdb * dg);
+    }
+    double v[2] = {ss, sy}, tot[2];
+    if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) ctl->tau = fabs(tot[0] / tot[1]);
+}
+
+__device__ __forceinline__ double fval(const Ctl* c) {
+    return c->lam1 + c->beta / 2 * c->lam2 + c->mu / 2 * c->lam3 - c->lam4 - c->lam5;
+}
+
+__device__ __forceinline__ void armijo(Ctl* c) {
+    // |f| > |C - alpha * c_armij| : step rejected (:848, :855)
+    const int fail = fabs(c->f) > fabs(c->C - c->alpha * c->c_armij);
+    c->armijo_fail = fail;
+}
+
+// ---------------------------------------------------------------------------
+// g2 = D^T (DU - W) with lam2 = ||DU - W||^2 and lam4 = <sigma, DU - W>.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_g2(SolverBufs<T> B, int mode) {
+    Ctl* ctl = B.ctl;
+    const int cur = ctl->parity;
+    const long n = B.n;
+    const T* __restrict__ DU = B.DU[cur];
+    const T* __restrict__ W = B.W;
+    const T* __restrict__ S = B.sig;
+    T* __restrict__ g2 = B.g2[cur];
+    double l2 = 0.0, l4 = 0.0;
+    GRID_STRIDE(i, n) {
+        Nb nb = neighbours(B.p, B.q, B.r, i);
+        T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
+        T v0m = DU[nb.ym] - W[nb.ym];
+        T v1m = DU[n + nb.xm] - W[n + nb.xm];
+        T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
+        g2[i] = v0m - v0 + v1m - v1 + v2m - v2;
+        l2 += (double)v0 * v0 + (double)v1 * v1 + (double)v2 * v2;
+        l4 += (double)v0 * S[i] + (double)v1 * S[n + i] + (double)v2 * S[2 * n + i];
+    }
+    double v[2] = {l2, l4}, tot[2];
+    if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        ctl->lam2 = tot[0];
+        ctl->lam4 = tot[1];
+        if (mode == EPI_G2_UPDATE_W) {
+            ctl->f += ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
+            // nonmonotone reference values (:1176-1177)
+            double Qp = ctl->Q;
+            ctl->Q = ctl->gam * Qp + 1.0;
+            ctl->C = (ctl->gam * Qp * ctl->C + ctl->f) / ctl->Q;
+        } else {
+            ctl->f = fval(ctl);
+            if (mode == EPI_G2_DESCEND) {
+                ctl->alpha = 1.0;
+                ctl->cnt = 0;
+                ctl->c_armij = ctl->dd * ctl->tau * ctl->c_arm * ctl->beta;
+                armijo(ctl);
+                if (ctl->armijo_fail) ctl->alpha *= ctl->gamma;
+                if (B.use_graph) cudaGraphSetConditional(B.h_arm, ctl->armijo_fail ? 1u : 0u);
+            } else {
+                ctl->armijo_fail = 0;
+                if (mode == EPI_G2_RESTART) ctl->restarts += 1;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// shrinkage: W = shrink(DU - sigma/beta, 1/beta), lam1 = TV(W)
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_shrink(SolverBufs<T> B, int mode) {
+    Ctl* ctl = B.ctl;
+    const int cur = ctl->parity;
+    const long n = B.n;
+    const T* __restrict__ DU = B.DU[cur];
+    const T* __restrict__ S = B.sig;
+    T* __restrict__ W = B.W;
+    const T bt = (T)ctl->beta, ib = (T)(1.0 / ctl->beta);
+    const int iso = ctl->iso;
+    double l1 = 0.0;
+    GRID_STRIDE(i, n) {
+        T u0 = DU[i] - S[i] / bt, u1 = DU[n + i] - S[n + i] / bt, u2 = DU[2 * n + i] - S[2 * n + i] / bt;
+        if (!iso) {
+            T t0 = fabs(u0) - ib, t1 = fabs(u1) - ib, t2 = fabs(u2) - ib;
+            t0 = (t0 >= T(0)) ? t0 : T(0);
+            t1 = (t1 >= T(0)) ? t1 : T(0);
+            t2 = (t2 >= T(0)) ? t2 : T(0);
+            W[i] = (u0 >= T(0)) ? t0 : -t0;
+            W[n + i] = (u1 >= T(0)) ? t1 : -t1;
+            W[2 * n + i] = (u2 >= T(0)) ? t2 : -t2;
+            l1 += (double)t0 + (double)t1 + (double)t2;
+        } else {
+            T nv = sqrt(u0 * u0 + u1 * u1 + u2 * u2);
+            T t = nv - ib;
+            t = (t > T(0)) ? t : T(0);
+            T sc = (nv > T(0)) ? t / nv : T(0);
+            W[i] = u0 * sc;
+            W[n + i] = u1 * sc;
+            W[2 * n + i] = u2 * sc;
+            l1 += (double)t;
+        }
+    }
+    double v[1] = {l1}, tot[1];
+    if (grid_reduce<1>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        if (mode == EPI_G2_UPDATE_W) ctl->f -= ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
+        ctl->lam1 = tot[0];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// d = mu/beta g + g2 + DtsAtd, with ||Up||, ||U - Up|| (RelChg) and <d,d>
+// (mode 0: start-up, mode 1: inner iteration)
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_gradient(SolverBufs<T> B, int iter) {
+    Ctl* ctl = B.ctl;
+    const int cur = ctl->parity, prv = 1 - cur;
+    const T mdb = (T)ctl->muDbeta;
+    const T *__restrict__ g = B.g[cur], *__restrict__ g2 = B.g2[cur], *__restrict__ dts = B.DtsAtd;
+    const T *__restrict__ U = B.U[cur], *__restrict__ Up = B.U[prv];
+    const T* __restrict__ xs = B.xstar;
+    const double iscl = 1.0 / ctl->scl;
+    T* __restrict__ d = B.d;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    GRID_STRIDE(i, B.n) {
+        T di = mdb * g[i] + g2[i] + dts[i];
+        d[i] = di;
+        s2 += (double)di * di;
+        if (iter) {
+            T u = U[i], up = Up[i];
+            T du = u - up;
+            s0 += (double)up * up;
+            s1 += (double)du * du;
+            if (xs) {
+                double e = (double)u * iscl - (double)xs[i];
+                s3 += e * e;
+            }
+        }
+    }
+    double v[4] = {s0, s1, s2, s3}, tot[4];
+    if (grid_reduce<4>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        ctl->dd = tot[2];
+        if (!iter) {
+            ctl->Q = 1.0;
+            ctl->C = ctl->f;
+        } else {
+            ctl->nrmup = sqrt(tot[0]);
+            ctl->relchg = sqrt(tot[1]) / ctl->nrmup;
+            if (B.trace && xs) B.trace[ctl->count_total] = sqrt(tot[3]);
+            ctl->count_total += 1;
+            ctl->inner_break = ((ctl->relchg < ctl->tol_inn) && !ctl->fst) || (ctl->count_total >= ctl->maxit);
+            ctl->fst = 0;
+            if (B.use_graph) cudaGraphSetConditional(B.h_inner, ctl->inner_break ? 0u : 1u);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// backtracking: X = Xp + alpha*dX for U, g, g2, DU (n) and Au (m), then
+// lam2..lam5, f and the Armijo test.  The setup call first forms dX = X - Xp.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_backtrack(SolverBufs<T> B, int setup) {
+    Ctl* ctl = B.ctl;
+    const int cur = ctl->parity, prv = 1 - cur;
+    const long n = B.n, m = B.m;
+    const T al = (T)ctl->alpha;
+    T *__restrict__ U = B.U[cur], *__restrict__ g = B.g[cur], *__restrict__ g2 = B.g2[cur];
+    T *__restrict__ DU = B.DU[cur], *__restrict__ Au = B.Au[cur];
+    const T *__restrict__ Up = B.U[prv], *__restrict__ gp = B.g[prv], *__restrict__ g2p = B.g2[prv];
+    const T *__restrict__ DUp = B.DU[prv], *__restrict__ Aup = B.Au[prv];
+    const T *__restrict__ W = B.W, *__restrict__ S = B.sig, *__restrict__ bb = B.b, *__restrict__ dl = B.delta;
+    double l2 = 0.0, l4 = 0.0, l3 = 0.0, l5 = 0.0;
+    const long N = n > m ? n : m;
+    GRID_STRIDE(i, N) {
+        if (i < n) {
+            T du, dgv, dg2v, d0, d1, d2;
+            if (setup) {
+                du = U[i] - Up[i];
+                dgv = g[i] - gp[i];
+                dg2v = g2[i] - g2p[i];
+                d0 = DU[i] - DUp[i];
+                d1 = DU[n + i] - DUp[n + i];
+                d2 = DU[2 * n + i] - DUp[2 * n + i];
+                B.dU[i] = du; B.dg[i] = dgv; B.dg2[i] = dg2v;
+                B.dDU[i] = d0; B.dDU[n + i] = d1; B.dDU[2 * n + i] = d2;
+            } else {
+                du = B.dU[i]; dgv = B.dg[i]; dg2v = B.dg2[i];
+                d0 = B.dDU[i]; d1 = B.dDU[n + i]; d2 = B.dDU[2 * n + i];
+            }
+            g[i] = gp[i] + al * dgv;
+            g2[i] = g2p[i] + al * dg2v;
+            U[i] = Up[i] + al * du;
+            T e0 = DUp[i] + al * d0, e1 = DUp[n + i] + al * d1, e2 = DUp[2 * n + i] + al * d2;
+            DU[i] = e0; DU[n + i] = e1; DU[2 * n + i] = e2;
+            T v0 = e0 - W[i], v1 = e1 - W[n + i], v2 = e2 - W[2 * n + i];
+            l2 += (double)v0 * v0 + (double)v1 * v1 + (double)v2 * v2;
+            l4 += (double)v0 * S[i] + (double)v1 * S[n + i] + (double)v2 * S[2 * n + i];
+        }
+        if (i < m) {
+            T da;
+            if (setup) {
+                da = Au[i] - Aup[i];
+                B.dAu[i] = da;
+            } else {
+                da = B.dAu[i];
+            }
+            T a = Aup[i] + al * da;
+            Au[i] = a;
+            double t = (double)a - (double)bb[i];
+            l3 += t * t;
+            l5 += (double)dl[i] * t;
+        }
+    }
+    double v[4] = {l2, l4, l3, l5}, tot[4];
+    if (grid_reduce<4>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        ctl->lam2 = tot[0];
+        ctl->lam4 = tot[1];
+        ctl->lam3 = tot[2];
+        ctl->lam5 = tot[3];
+        ctl->f = fval(ctl);
+        ctl->cnt += 1;
+        ctl->backtracks += 1;
+        armijo(ctl);
+        if (ctl->armijo_fail) {
+            if (ctl->cnt == 5) ctl->gam *= ctl->rate_gam;  // restart follows (:876-882)
+            else ctl->alpha *= ctl->gamma;
+        }
+        if (B.use_graph) cudaGraphSetConditional(B.h_bt, (ctl->armijo_fail && ctl->cnt < 5) ? 1u : 0u);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// outer loop: RelChgOut = ||U - rcdU|| / ||Up||, rcdU = U
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_outer_relchg(SolverBufs<T> B) {
+    Ctl* ctl = B.ctl;
+    const T* __restrict__ U = B.U[ctl->parity];
+    T* __restrict__ R = B.rcdU;
+    double s = 0.0;
+    GRID_STRIDE(i, B.n) {
+        T u = U[i];
+        double e = (double)u - (double)R[i];
+        s += e * e;
+        R[i] = u;
+    }
+    double v[1] = {s}, tot[1];
+    if (grid_reduce<1>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        ctl->count_outer += 1;
+        ctl->relchgout = sqrt(tot[0]) / ctl->nrmup;
+        ctl->done = (ctl->relchgout < ctl->tol);
+        if (B.use_graph) cudaGraphSetConditional(B.h_mlp, ctl->done ? 0u : 1u);
+    }
+}
+
+// copies one control flag into a graph conditional handle
+__global__ void k_cond(const Ctl* ctl, unsigned long long h, int src) {
+    unsigned v = 0;
+    switch (src) {
+        case COND_FST: v = ctl->fst ? 1u : 0u; break;
+        case COND_RESTART: v = ctl->armijo_fail ? 1u : 0u; break;
+        case COND_ONE: v = 1u; break;
+        default: v = ctl->done ? 0u : 1u; break;
+    }
+    cudaGraphSetConditional(h, v);
+}
+
+void launch_cond(Ctl* ctl, unsigned long long handle, int src, cudaStream_t s) {
+    k_cond<<<1, 1, 0, s>>>(ctl, handle, src);
+}
+
+// ---------------------------------------------------------------------------
+// multiplier update and continuation
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_mlp(SolverBufs<T> B) {
+    Ctl* ctl = B.ctl;
+    const int cur = ctl->parity;
+    const long n = B.n, m = B.m;
+    const T bt = (T)ctl->beta, mut = (T)ctl->mu;
+    const T *__restrict__ DU = B.DU[cur], *__restrict__ W = B.W, *__restrict__ Au = B.Au[cur], *__restrict__ bb = B.b;
+    T *__restrict__ S = B.sig, *__restrict__ dl = B.delta;
+    double l4 = 0.0, l5 = 0.0;
+    const long N = n > m ? n : m;
+    GRID_STRIDE(i, N) {
+        if (i < n) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                T v = DU[a * n + i] - W[a * n + i];
+                T s = S[a * n + i] - bt * v;
+                S[a * n + i] = s;
+                l4 += (double)s * v;
+            }
+        }
+        if (i < m) {
+            T aub = Au[i] - bb[i];
+            T dv = dl[i] - mut * aub;
+            dl[i] = dv;
+            l5 += (double)dv * aub;
+        }
+    }
+    double v[2] = {l4, l5}, tot[2];
+    if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        ctl->f += ctl->lam4 + ctl->lam5;
+        ctl->lam4 = tot[0];
+        ctl->lam5 = tot[1];
+        ctl->f -= ctl->lam4 + ctl->lam5;
+        ctl->beta_prev = ctl->beta;
+        ctl->beta *= ctl->rate_cnt;
+        ctl->mu *= ctl->rate_cnt;
+        if (ctl->beta > ctl->beta_max) ctl->beta = ctl->beta_max;
+        if (ctl->mu > ctl->mu_max) ctl->mu = ctl->mu_max;
+        ctl->muDbeta = ctl->mu / ctl->beta;
+        ctl->f = fval(ctl);
+    }
+}
+
+template <class T>
+__global__ void k_outer_grad(SolverBufs<T> B) {
+    Ctl* ctl = B.ctl;
+    const int cur = ctl->parity;
+    const T ratio = (T)(ctl->beta_prev / ctl->beta);
+    const T mdb = (T)ctl->muDbeta;
+    const T *__restrict__ g = B.g[cur], *__restrict__ g2 = B.g2[cur];
+    T *__restrict__ d = B.d, *__restrict__ dts = B.DtsAtd;
+    double s = 0.0;
+    GRID_STRIDE(i, B.n) {
+        T t = ratio * d[i];
+        dts[i] = t;
+        T di = mdb * g[i] + g2[i] + t;
+        d[i] = di;
+        s += (double)di * di;
+    }
+    double v[1] = {s}, tot[1];
+    if (grid_reduce<1>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        ctl->dd = tot[0];
+        ctl->gam = ctl->gam0;
+        ctl->Q = 1.0;
+        ctl->C = ctl->f;
+        ctl->fst = 1;
+        ctl->done = !(ctl->count_outer < ctl->maxcnt && ctl->count_total < ctl->maxit);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// U_out = U / scl (:1272-1277) and rel_error vs Ut (:1308-1324)
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_finalize(SolverBufs<T> B, T* __restrict__ out, const T* __restrict__ Ut) {
+    Ctl* ctl = B.ctl;
+    const T* __restrict__ U = B.U[ctl->parity];
+    const double scl = ctl->scl;
+    const T s = (T)scl;
+    double e = 0.0, t = 0.0;
+    GRID_STRIDE(i, B.n) {
+        T u = (scl == 1.0) ? U[i] : U[i] / s;
+        out[i] = u;
+        if (Ut) {
+            double dv = (double)Ut[i] - (double)u;
+            e += dv * dv;
+            t += (double)Ut[i] * Ut[i];
+        }
+    }
+    double v[2] = {e, t}, tot[2];
+    if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0)
+        ctl->rel_error = Ut ? sqrt(tot[0]) / sqrt(tot[1]) : 0.0;
+}
+
+// standalone D and D^T (operator entry points)
+template <class T>
+__global__ void k_D_plain(int p, int q, int r, long n, const T* __restrict__ U, T* __restrict__ DU) {
+    GRID_STRIDE(i, n) {
+        Nb nb = neighbours(p, q, r, i);
+        T u = U[i];
+        DU[i] = U[nb.yp] - u;
+        DU[n + i] = U[nb.xp] - u;
+        DU[2 * n + i] = U[nb.zp] - u;
+    }
+}
+
+template <class T>
+__global__ void k_Dt_plain(int p, int q, int r, long n, const T* __restrict__ V, T* __restrict__ out) {
+    GRID_STRIDE(i, n) {
+        Nb nb = neighbours(p, q, r, i);
+        out[i] = V[nb.ym] - V[i] + V[n + nb.xm] - V[n + i] + V[2 * n + nb.zm] - V[2 * n + i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static int g_sms = 0;
+int num_sms() {
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+    }
+    return g_sms;
+}
+
+static int ew_grid(long n) {
+    long g = (n + 255) / 256;
+    long cap = (long)num_sms() * 16;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+template <class T> void launch_scale_b(const T* b_in, SolverBufs<T>& B, cudaStream_t s) {
+    k_scale_find<T><<<1, 1024, 0, s>>>(b_in, B.m, B.ctl);
+    k_scale_apply<T><<<ew_grid(B.m), 256, 0, s>>>(b_in, B.b, B.m, B.ctl);
+}
+template <class T> void launch_D_only(SolverBufs<T>& B, cudaStream_t s) { k_D_only<T><<<ew_grid(B.n), 256, 0, s>>>(B); }
+template <class T> void launch_descend(SolverBufs<T>& B, int restart, cudaStream_t s) {
+    k_descend<T><<<B.grid, 256, 0, s>>>(B, restart);
+}
+template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s) { k_Dd_norm<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_tau(SolverBufs<T>& B, cudaStream_t s) { k_tau<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s) { k_g2<T><<<B.grid, 256, 0, s>>>(B, mode); }
+template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s) {
+    k_shrink<T><<<B.grid, 256, 0, s>>>(B, mode);
+}
+template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t s) {
+    k_gradient<T><<<B.grid, 256, 0, s>>>(B, mode);
+}
+template <class T> void launch_backtrack(SolverBufs<T>& B, int setup, cudaStream_t s) {
+    k_backtrack<T><<<B.grid, 256, 0, s>>>(B, setup);
+}
+template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s) { k_outer_relchg<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_mlp(SolverBufs<T>& B, cudaStream_t s) { k_mlp<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_outer_grad(SolverBufs<T>& B, cudaStream_t s) { k_outer_grad<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_finalize(SolverBufs<T>& B, T* U_out, const T* Ut, cudaStream_t s) {
+    k_finalize<T><<<B.grid, 256, 0, s>>>(B, U_out, Ut);
+}
+template <class T> void launch_D_plain(int p, int q, int r, const T* U, T* DU3, cudaStream_t s) {
+    long n = (long)p * q * r;
+    k_D_plain<T><<<ew_grid(n), 256, 0, s>>>(p, q, r, n, U, DU3);
+}
+template <class T> void launch_Dt_plain(int p, int q, int r, const T* V3, T* out, cudaStream_t s) {
+    long n = (long)p * q * r;
+    k_Dt_plain<T><<<ew_grid(n), 256, 0, s>>>(p, q, r, n, V3, out);
+}
+
+#define INST(T)                                                                   \
+    template void launch_scale_b<T>(const T*, SolverBufs<T>&, cudaStream_t);      \
+    template void launch_D_only<T>(SolverBufs<T>&, cudaStream_t);                 \
+    template void launch_descend<T>(SolverBufs<T>&, int, cudaStream_t);           \
+    template void launch_Dd_norm<T>(SolverBufs<T>&, cudaStream_t);                \
+    template void launch_tau<T>(SolverBufs<T>&, cudaStream_t);                    \
+    template void launch_g2<T>(SolverBufs<T>&, int, cudaStream_t);                \
+    template void launch_shrink<T>(SolverBufs<T>&, int, cudaStream_t);            \
+    template void launch_gradient<T>(SolverBufs<T>&, int, cudaStream_t);          \
+    template void launch_backtrack<T>(SolverBufs<T>&, int, cudaStream_t);         \
+    template void launch_outer_relchg<T>(SolverBufs<T>&, cudaStream_t);           \
+    template void launch_mlp<T>(SolverBufs<T>&, cudaStream_t);                    \
+    template void launch_outer_grad<T>(SolverBufs<T>&, cudaStream_t);             \
+    template void launch_finalize<T>(SolverBufs<T>&, T*, const T*, cudaStream_t); \
+    template void launch_D_plain<T>(int, int, int, const T*, T*, cudaStream_t);   \
+    template void launch_Dt_plain<T>(int, int, int, const T*, T*, cudaStream_t);
+INST(float)
+INST(double)
+
+}  // namespace tv3

@@ -1,0 +1,158 @@
+// Internal definitions shared by the sm_103a kernels and the host solver.
+//
+// Layout in HBM (column-major, y fastest, as in the reference's
+// 3d/tval3_gpu_3d_kernels.cu:1501): voxel (y, x, z) of a p x q x r volume sits
+// at y + p*(x + q*z).  The three components of D*U are stored as three
+// consecutive n-vectors (component 0 along y, 1 along x, 2 along z; the
+// reference calls them Uy, Ux, Uz).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace tv3 {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Device-resident control block of one solve.  All scalars of the TVAL3 loop
+// (penalties, Lagrangian terms, step sizes, nonmonotone reference values,
+// counters and branch flags) live here, so the loop runs without host round
+// trips; kernels read their scalar inputs from it and the last block of each
+// reducing kernel writes the results back.  Mirrors tval3_data_gpu
+// (3d/tval3_gpu_3d.cpp:86-199) plus the loop locals of :1089-1345.
+// ---------------------------------------------------------------------------
+struct Ctl {
+    // options (constant during a solve)
+    double mu_max, beta_max, rate_cnt, tol, tol_inn, c_arm, gamma, gam0, rate_gam;
+    int maxcnt, maxit, nonneg, iso;
+    // penalties
+    double mu, beta, muDbeta, beta_prev;
+    // Lagrangian and its terms
+    double f, lam1, lam2, lam3, lam4, lam5;
+    // line search
+    double tau, alpha, c_armij, C, Q, gam, dd, dDd, Add;
+    // stopping tests
+    double nrmup, relchg, relchgout, scl, rel_error;
+    // counters and flags
+    int count_outer, count_total, fst, cnt;
+    int armijo_fail;   // 1: the Armijo test failed for the current step
+    int inner_break;   // 1: the inner loop ends after this iteration
+    int done;          // 1: the solve is finished
+    int parity;        // slot index of the "current" ping-pong buffers
+    int backtracks, restarts;
+    int err;           // device-side error word (0 = none)
+    int pad_;
+};
+
+// Epilogue selectors of the reducing kernels.
+enum Epi : int {
+    EPI_NONE = 0,
+    EPI_LAM35 = 1,        // A*U: lam3, lam5
+    EPI_ADD = 2,          // A*d at the first inner iteration: ||Ad||^2 -> tau
+    EPI_G2_INIT = 3,      // get_g at start-up: f
+    EPI_G2_DESCEND = 4,   // get_g after a descent step: f and the Armijo test
+    EPI_G2_RESTART = 5,   // get_g after the restart descent: f
+    EPI_G2_UPDATE_W = 6,  // update_W: f, Q, C
+};
+
+// ---------------------------------------------------------------------------
+// Value loads.  Matrix streams are read once per product: load them with the
+// evict-first policy (__ldcs) so they do not push x out of L2.
+// ---------------------------------------------------------------------------
+template <class V> __device__ __forceinline__ float ldv_f(const V* p);
+template <> __device__ __forceinline__ float ldv_f<float>(const float* p) { return __ldcs(p); }
+template <> __device__ __forceinline__ float ldv_f<__nv_bfloat16>(const __nv_bfloat16* p) {
+    unsigned short u = __ldcs(reinterpret_cast<const unsigned short*>(p));
+    return __uint_as_float(((unsigned)u) << 16);
+}
+template <> __device__ __forceinline__ float ldv_f<__half>(const __half* p) {
+    unsigned short u = __ldcs(reinterpret_cast<const unsigned short*>(p));
+    return __half2float(__ushort_as_half(u));
+}
+
+template <class T, class V> struct Acc;
+template <> struct Acc<float, float> {
+    __device__ static __forceinline__ float load(const float* p) { return __ldcs(p); }
+};
+template <> struct Acc<double, double> {
+    __device__ static __forceinline__ double load(const double* p) { return __ldcs(p); }
+};
+template <> struct Acc<float, __nv_bfloat16> {
+    __device__ static __forceinline__ float load(const __nv_bfloat16* p) { return ldv_f(p); }
+};
+template <> struct Acc<float, __half> {
+    __device__ static __forceinline__ float load(const __half* p) { return ldv_f(p); }
+};
+template <> struct Acc<double, float> {
+    __device__ static __forceinline__ double load(const float* p) { return (double)__ldcs(p); }
+};
+
+// ---------------------------------------------------------------------------
+// Deterministic grid reduction.  Every block reduces NV doubles with warp
+// shuffles, writes its partials to part[k*gridDim.x + block], and takes a
+// ticket; the last block sums the partials in block order (so the result
+// depends only on the grid size, never on scheduling), resets the ticket and
+// returns true with the totals in tot[] (valid in all threads of that block).
+// ---------------------------------------------------------------------------
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double* part, unsigned* ticket, double (&tot)[NV]) {
+    __shared__ double sh[NV][32];
+    __shared__ int is_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double t = v[k];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) t += __shfl_down_sync(FULL, t, o);
+        if (lane == 0) sh[k][warp] = t;
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double t = (lane < nw) ? sh[k][lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) t += __shfl_down_sync(FULL, t, o);
+            if (lane == 0) part[(size_t)k * gridDim.x + blockIdx.x] = t;
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned t = atomicAdd(ticket, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+    // fixed-order sum of the partials: thread j adds blocks j, j+B, ...; then a
+    // fixed shuffle tree.
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double t = 0.0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) t += __ldcg(part + (size_t)k * gridDim.x + b);
+#pragma unroll
+        for (int o = 16; o; o >>= 1) t += __shfl_down_sync(FULL, t, o);
+        if (lane == 0) sh[k][warp] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double t = 0.0;
+        for (int w = 0; w < nw; ++w) t += sh[k][w];
+        tot[k] = t;
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
+}
+
+// Voxel coordinates from a linear index.
+struct Vol {
+    int p, q, r;  // dim_y (fastest), dim_x, dim_z
+    long n;       // p*q*r
+    long pq;
+};
+
+}  // namespace tv3

@@ -1,0 +1,370 @@
+"""Python mirror of the reference's TVAL3 interface over the C ABI.
+
+Names follow modk/tval3-gpu: ``tval3_gpu_3d`` (3d/tval3_gpu_3d.cpp:23-69) and
+``tval3_gpu`` (2d/tval3_gpu.h:9-19) take U's shape, the matrix A (sparse,
+dense or geometry), b, the options and an optional true image Ut, and return
+the reconstruction with a ``tval3_info``; errors raise ``Tval3Error`` (the
+reference raises tval3_gpu_exception).  ``Operator.mat_vec_mul`` is the
+reference's ``mat_vec_mul(trans, A, x, y, stream)``.
+
+Volumes are numpy arrays indexed [z, x, y] (C order), which is the
+reference's column-major layout with y fastest.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+from .capi import (PREC_BF16, PREC_FP16, PREC_FP32, PREC_FP64, SPARSE_BOTH, SPARSE_CSC, SPARSE_CSR,
+                   TRAV_BRESENHAM, TRAV_SIDDON, Info, Options, check, default_options, load)
+
+__all__ = ["SparseMatrix", "DenseMatrix", "Geometry", "tval3_gpu_3d", "tval3_gpu", "Operator", "Solver",
+           "D", "Dt", "default_options", "Options", "Info"]
+
+
+def _ptr(a) -> int | None:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return int(a)
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                return torch.cuda.current_stream().cuda_stream
+        except ImportError:
+            pass
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return stream.cuda_stream
+    return int(stream)
+
+
+@dataclass
+class SparseMatrix:
+    """sparse_mat_host: A (rows = rays, cols = voxels) as CSR and/or the CSC arrays."""
+    rows: int
+    cols: int
+    csr_ptr: np.ndarray | None = None
+    csr_ind: np.ndarray | None = None
+    csr_val: np.ndarray | None = None
+    csc_ptr: np.ndarray | None = None
+    csc_ind: np.ndarray | None = None
+    csc_val: np.ndarray | None = None
+
+    def __post_init__(self):
+        def c(a, dt):
+            return None if a is None else np.ascontiguousarray(a, dtype=dt)
+        vt = np.float64 if (self.csr_val is not None and np.asarray(self.csr_val).dtype == np.float64) or \
+            (self.csr_val is None and self.csc_val is not None and np.asarray(self.csc_val).dtype == np.float64) \
+            else np.float32
+        self.csr_ptr, self.csr_ind, self.csr_val = c(self.csr_ptr, np.int32), c(self.csr_ind, np.int32), c(self.csr_val, vt)
+        self.csc_ptr, self.csc_ind, self.csc_val = c(self.csc_ptr, np.int32), c(self.csc_ind, np.int32), c(self.csc_val, vt)
+
+    @property
+    def nnz(self) -> int:
+        return int(self.csr_ind.size if self.csr_ind is not None else self.csc_ind.size)
+
+    @property
+    def format(self) -> int:
+        return (SPARSE_CSR if self.csr_ptr is not None else 0) | (SPARSE_CSC if self.csc_ptr is not None else 0)
+
+    def struct(self) -> capi.SparseHost:
+        s = capi.SparseHost()
+        s.rows, s.cols, s.nnz, s.format = self.rows, self.cols, self.nnz, self.format
+        v = self.csr_val if self.csr_val is not None else self.csc_val
+        s.val_type = PREC_FP64 if v.dtype == np.float64 else PREC_FP32
+        s.csr_ptr, s.csr_ind, s.csr_val = _ptr(self.csr_ptr), _ptr(self.csr_ind), _ptr(self.csr_val)
+        s.csc_ptr, s.csc_ind, s.csc_val = _ptr(self.csc_ptr), _ptr(self.csc_ind), _ptr(self.csc_val)
+        return s
+
+
+@dataclass
+class DenseMatrix:
+    """mat_host A (rows x cols).  ``data`` is row-major unless row_major=False."""
+    data: np.ndarray
+    row_major: bool = True
+
+    def __post_init__(self):
+        dt = np.float64 if self.data.dtype == np.float64 else np.float32
+        self.data = np.ascontiguousarray(self.data, dtype=dt)
+
+    @property
+    def rows(self):
+        return self.data.shape[0] if self.row_major else self.data.shape[1]
+
+    @property
+    def cols(self):
+        return self.data.shape[1] if self.row_major else self.data.shape[0]
+
+    def struct(self) -> capi.DenseHost:
+        s = capi.DenseHost()
+        s.rows, s.cols, s.row_major = self.rows, self.cols, 1 if self.row_major else 0
+        s.val_type = PREC_FP64 if self.data.dtype == np.float64 else PREC_FP32
+        s.data = _ptr(self.data)
+        return s
+
+
+@dataclass
+class Geometry:
+    """geometry_host: transducer voxel coordinates per measurement position,
+    use_path flags (E*R) and the volume size; optional continuous positions for
+    Siddon traversal (voxel units)."""
+    rv_x: int
+    rv_y: int
+    rv_z: int
+    x_emitters: np.ndarray
+    y_emitters: np.ndarray
+    z_emitters: np.ndarray
+    x_receivers: np.ndarray
+    y_receivers: np.ndarray
+    z_receivers: np.ndarray
+    num_emitters: int = 0
+    num_receivers: int = 0
+    numMPs: int = 1
+    use_path: np.ndarray | None = None
+    scale_factor: float = 1.0
+    traversal: int = TRAV_BRESENHAM
+    pos: tuple | None = None  # (xe, ye, ze, xr, yr, zr) float64 arrays
+    _keep: list = field(default_factory=list, repr=False)
+
+    def __post_init__(self):
+        for k in ("x_emitters", "y_emitters", "z_emitters", "x_receivers", "y_receivers", "z_receivers"):
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.int32))
+        if not self.num_emitters:
+            self.num_emitters = self.x_emitters.size // self.numMPs
+        if not self.num_receivers:
+            self.num_receivers = self.x_receivers.size // self.numMPs
+        if self.use_path is not None:
+            self.use_path = np.ascontiguousarray(self.use_path, dtype=np.uint32)
+        if self.pos is not None:
+            self.pos = tuple(np.ascontiguousarray(p, dtype=np.float64) for p in self.pos)
+
+    def with_traversal(self, traversal: int) -> "Geometry":
+        return Geometry(self.rv_x, self.rv_y, self.rv_z, self.x_emitters, self.y_emitters, self.z_emitters,
+                        self.x_receivers, self.y_receivers, self.z_receivers, self.num_emitters,
+                        self.num_receivers, self.numMPs, self.use_path, self.scale_factor, traversal, self.pos)
+
+    def ray_pairs(self) -> np.ndarray:
+        """(emitter, receiver) of every ray in the reference's compaction order."""
+        E, R, M = self.num_emitters, self.num_receivers, self.numMPs
+        i = np.arange(M * E * R, dtype=np.int64)
+        if self.use_path is not None:
+            i = i[self.use_path[i % (E * R)] != 0]
+        return np.stack([i // R, (i // (E * R)) * R + i % R], axis=1).astype(np.uint32)
+
+    @property
+    def nrays(self) -> int:
+        if self.use_path is None:
+            return self.numMPs * self.num_emitters * self.num_receivers
+        return int(self.numMPs * np.count_nonzero(self.use_path))
+
+    def struct(self) -> capi.GeometryHost:
+        s = capi.GeometryHost()
+        s.numMPs, s.num_emitters, s.num_receivers = self.numMPs, self.num_emitters, self.num_receivers
+        s.x_emitters, s.y_emitters, s.z_emitters = _ptr(self.x_emitters), _ptr(self.y_emitters), _ptr(self.z_emitters)
+        s.x_receivers, s.y_receivers, s.z_receivers = (_ptr(self.x_receivers), _ptr(self.y_receivers),
+                                                       _ptr(self.z_receivers))
+        s.use_path = _ptr(self.use_path)
+        s.rv_x, s.rv_y, s.rv_z = self.rv_x, self.rv_y, self.rv_z
+        s.scale_factor = self.scale_factor
+        s.traversal = self.traversal
+        if self.pos is not None:
+            s.xe_pos, s.ye_pos, s.ze_pos, s.xr_pos, s.yr_pos, s.zr_pos = (_ptr(p) for p in self.pos)
+        return s
+
+
+def _opts(opts) -> Options:
+    if opts is None:
+        return default_options()
+    if isinstance(opts, Options):
+        return opts
+    return default_options(**opts)
+
+
+def tval3_gpu_3d(shape, A, b, opts=None, Ut=None, *, dtype=np.float32, pagelocked=True, mainGPU=-1,
+                 numGPUs=0, gpuArray=None):
+    """Reconstruct U (shape (dim_y, dim_x, dim_z)) from b = A U.  Returns
+    (U as a [z, x, y] array, info dict).  A: SparseMatrix, DenseMatrix or
+    Geometry, or (Geometry, SparseMatrix) for the combined operator."""
+    lib = load()
+    dim_y, dim_x, dim_z = shape
+    n = dim_y * dim_x * dim_z
+    dt = np.float64 if dtype == np.float64 else np.float32
+    b = np.ascontiguousarray(b, dtype=dt)
+    U = np.zeros((dim_z, dim_x, dim_y), dtype=dt)
+    Ut_a = None if Ut is None else np.ascontiguousarray(Ut, dtype=dt).reshape(-1)
+    o = _opts(opts)
+    info = Info()
+    common = (_ptr(b), b.size, C.byref(o), _ptr(Ut_a), 0 if Ut_a is None else Ut_a.size, int(pagelocked),
+              mainGPU, numGPUs, None, C.byref(info))
+    if isinstance(A, tuple):
+        geo, mat = A
+        gs, ms = geo.struct(), mat.struct()
+        st = lib.tval3_gpu_3d_geometry_sparse_f32(_ptr(U), dim_y, dim_x, dim_z, C.byref(gs), C.byref(ms), *common)
+    elif isinstance(A, SparseMatrix):
+        s = A.struct()
+        fn = lib.tval3_gpu_3d_sparse_f64 if dt == np.float64 else lib.tval3_gpu_3d_sparse_f32
+        st = fn(_ptr(U), dim_y, dim_x, dim_z, C.byref(s), *common)
+    elif isinstance(A, DenseMatrix):
+        s = A.struct()
+        fn = lib.tval3_gpu_3d_dense_f64 if dt == np.float64 else lib.tval3_gpu_3d_dense_f32
+        st = fn(_ptr(U), dim_y, dim_x, dim_z, C.byref(s), *common)
+    elif isinstance(A, Geometry):
+        s = A.struct()
+        st = lib.tval3_gpu_3d_geometry_f32(_ptr(U), dim_y, dim_x, dim_z, C.byref(s), *common)
+    else:
+        raise TypeError(f"unsupported matrix type {type(A).__name__}")
+    check(st)
+    assert U.size == n
+    return U, info.as_dict()
+
+
+def tval3_gpu(shape, A, b, opts=None, Ut=None, pagelocked=True):
+    """2D entry (2d/tval3_gpu.h:9-19): shape = (rows, cols); returns U [cols, rows]."""
+    lib = load()
+    rows, cols = shape
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    U = np.zeros((cols, rows), dtype=np.float32)
+    Ut_a = None if Ut is None else np.ascontiguousarray(Ut, dtype=np.float32).reshape(-1)
+    o = _opts(opts)
+    info = Info()
+    s = A.struct()
+    fn = lib.tval3_gpu_sparse if isinstance(A, SparseMatrix) else lib.tval3_gpu_dense
+    check(fn(_ptr(U), rows, cols, C.byref(s), _ptr(b), b.size, C.byref(o), _ptr(Ut_a),
+             0 if Ut_a is None else Ut_a.size, int(pagelocked), C.byref(info)))
+    return U, info.as_dict()
+
+
+class Operator:
+    """A device operator (tval3_op): the reference's mat_vec_mul interface."""
+
+    def __init__(self, handle: C.c_void_p, keep=None):
+        self._h = handle
+        self._keep = keep
+        r, c, z = C.c_int(), C.c_int(), C.c_int64()
+        check(load().tval3_op_shape(self._h, C.byref(r), C.byref(c), C.byref(z)))
+        self.rows, self.cols, self.nnz = r.value, c.value, z.value
+
+    @classmethod
+    def from_sparse(cls, A: SparseMatrix, precision: int = PREC_FP32) -> "Operator":
+        h = C.c_void_p()
+        s = A.struct()
+        check(load().tval3_op_create_sparse(C.byref(h), C.byref(s), precision))
+        return cls(h)
+
+    @classmethod
+    def from_device_csr(cls, rows, cols, ptr, ind, val, precision=PREC_FP32, stream=None) -> "Operator":
+        h = C.c_void_p()
+        check(load().tval3_op_create_sparse_device(C.byref(h), rows, cols, int(ind.numel()), _ptr(ptr), _ptr(ind),
+                                                   _ptr(val), precision, _stream(stream)))
+        return cls(h)
+
+    @classmethod
+    def from_geometry(cls, G: Geometry, mode: int = 0, precision: int = PREC_FP32) -> "Operator":
+        h = C.c_void_p()
+        s = G.struct()
+        check(load().tval3_op_create_geometry(C.byref(h), C.byref(s), mode, precision))
+        return cls(h)
+
+    @classmethod
+    def from_dense(cls, A: DenseMatrix, precision: int = PREC_FP32) -> "Operator":
+        h = C.c_void_p()
+        s = A.struct()
+        check(load().tval3_op_create_dense(C.byref(h), C.byref(s), precision))
+        return cls(h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def mat_vec_mul(self, trans: int, x, y, stream=None) -> None:
+        check(load().tval3_mat_vec_mul(self._h, int(trans), _ptr(x), _ptr(y), _stream(stream)))
+
+    def mat_mat_mul(self, trans: int, nrhs: int, X, Y, stream=None) -> None:
+        check(load().tval3_mat_mat_mul(self._h, int(trans), nrhs, _ptr(X), _ptr(Y), _stream(stream)))
+
+    def export_csr(self):
+        m, n, z = self.rows, self.cols, self.nnz
+        ptr, tptr = np.empty(m + 1, np.int32), np.empty(n + 1, np.int32)
+        ind, tind = np.empty(z, np.int32), np.empty(z, np.int32)
+        val, tval = np.empty(z, np.float32), np.empty(z, np.float32)
+        check(load().tval3_op_export_csr(self._h, _ptr(ptr), _ptr(ind), _ptr(val), _ptr(tptr), _ptr(tind),
+                                         _ptr(tval)))
+        return ptr, ind, val, tptr, tind, tval
+
+    def close(self):
+        if self._h:
+            load().tval3_op_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """Device-resident workspace (tval3_solver) for repeated solves."""
+
+    def __init__(self, op: Operator, shape, opts=None, mode: int = 0):
+        self.op = op
+        self.shape = shape
+        self._h = C.c_void_p()
+        o = _opts(opts)
+        self.maxit = o.maxit
+        check(load().tval3_solver_create(C.byref(self._h), op.handle, *shape, C.byref(o)))
+        self.set_mode(mode)
+
+    def set_mode(self, mode: int):
+        check(load().tval3_solver_set_mode(self._h, mode))
+
+    def set_trace(self, xstar_dev):
+        check(load().tval3_solver_set_trace(self._h, _ptr(xstar_dev)))
+
+    def trace(self) -> np.ndarray:
+        out = np.zeros(max(self.maxit, 1), dtype=np.float64)
+        check(load().tval3_solver_trace(self._h, _ptr(out), out.size))
+        return out
+
+    def solve(self, b_dev, U_dev, Ut_dev=None, stream=None) -> dict:
+        info = Info()
+        check(load().tval3_solver_solve(self._h, _ptr(b_dev), _ptr(U_dev), _ptr(Ut_dev), C.byref(info),
+                                        _stream(stream)))
+        return info.as_dict()
+
+    def close(self):
+        if self._h:
+            load().tval3_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def D(U_dev, shape, DU_dev, stream=None):
+    """DU (3 n-vectors along y, x, z) = D U on device arrays (float32 or float64)."""
+    f = load().tval3_D_f64 if _is_f64(U_dev) else load().tval3_D_f32
+    check(f(*shape, _ptr(U_dev), _ptr(DU_dev), _stream(stream)))
+
+
+def Dt(V_dev, shape, out_dev, stream=None):
+    f = load().tval3_Dt_f64 if _is_f64(V_dev) else load().tval3_Dt_f32
+    check(f(*shape, _ptr(V_dev), _ptr(out_dev), _stream(stream)))
+
+
+def _is_f64(t) -> bool:
+    return str(getattr(t, "dtype", "")) in ("torch.float64", "float64")
