@@ -575,13 +575,13 @@ void siddon_walk(const double P0[3], const double P1[3], const int N[3], double 
         double pos = P0[a] + tmin * dv[a];
         k[a] = (st[a] > 0) ? (long)std::floor(pos) + 1 : (long)std::ceil(pos) - 1;
         tn[a] = ((double)k[a] - P0[a]) / dv[a];
-        while (tn[a] <= tmin) {
+        for (int guard = 0; tn[a] <= tmin && guard < 4; ++guard) {
             k[a] += st[a];
             tn[a] = ((double)k[a] - P0[a]) / dv[a];
         }
     }
     double t = tmin;
-    while (t < tmax) {
+    for (int guard = N[0] + N[1] + N[2] + 8; t < tmax && guard > 0; --guard) {
         double te = std::min(std::min(tn[0], tn[1]), std::min(tn[2], tmax));
         if (te > t) {
             double mid = 0.5 * (t + te);

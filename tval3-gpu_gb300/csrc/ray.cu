@@ -119,13 +119,14 @@ __device__ void siddon_walk_dev(const double P0[3], const double P1[3], const in
         double pos = __dadd_rn(P0[a], __dmul_rn(tmin, dv[a]));
         k[a] = (st[a] > 0) ? (long)floor(pos) + 1 : (long)ceil(pos) - 1;
         tn[a] = __ddiv_rn(__dsub_rn((double)k[a], P0[a]), dv[a]);
-        while (tn[a] <= tmin) {
+        for (int guard = 0; tn[a] <= tmin && guard < 4; ++guard) {
             k[a] += st[a];
             tn[a] = __ddiv_rn(__dsub_rn((double)k[a], P0[a]), dv[a]);
         }
     }
     double t = tmin;
-    while (t < tmax) {
+    // at most one segment per crossed plane (the guard only bounds degenerate input)
+    for (int guard = N[0] + N[1] + N[2] + 8; t < tmax && guard > 0; --guard) {
         double te = dmin_(dmin_(tn[0], tn[1]), dmin_(tn[2], tmax));
         if (te > t) {
             double mid = __dmul_rn(0.5, __dadd_rn(t, te));
@@ -396,11 +397,13 @@ static void upload_geometry(const tval3_geometry_host* G, RayGeom& g) {
             for (long e = 0; e < g.ne; ++e) {
                 double v = have_pos ? src[a][e] : ie[a * g.ne + e] + 0.5;
                 if (!std::isfinite(v)) throw Error{6, "Argument error: non-finite coordinate!"};
+                if (std::fabs(v) > 1e6) throw Error{1, "Argument error: coordinate beyond 1e6 voxels!"};
                 pe[a * g.ne + e] = v;
             }
             for (long q = 0; q < g.nr; ++q) {
                 double v = have_pos ? src[3 + a][q] : ie[3 * g.ne + a * g.nr + q] + 0.5;
                 if (!std::isfinite(v)) throw Error{6, "Argument error: non-finite coordinate!"};
+                if (std::fabs(v) > 1e6) throw Error{1, "Argument error: coordinate beyond 1e6 voxels!"};
                 pe[3 * g.ne + a * g.nr + q] = v;
             }
         }
