@@ -94,6 +94,7 @@ typedef struct tval3_info {
     int backtracks;
     int restarts;
     double final_f;
+    int launches;     /* kernels the solve ran on the device */
 } tval3_info;
 
 /* Sparse matrix in host memory (sparse_mat_host, 2d/container_host.h:78-127).

@@ -177,6 +177,7 @@ void solve_host(LinOp<T>* op, T* U, int dim_y, int dim_x, int dim_z, const T* b,
         TV3_CUDA(cudaMemcpy(dUt.p, Ut, n * sizeof(T), cudaMemcpyHostToDevice));
     }
     Solver<T> s(op, dim_y, dim_x, dim_z, *opts);
+    s.mode = 1;  // the whole solve as one graph launch
     tval3_info inf{};
     s.solve(db.p, dU.p, use_ut ? dUt.p : nullptr, &inf, 0);
     TV3_CUDA(cudaMemcpy(U, dU.p, n * sizeof(T), cudaMemcpyDeviceToHost));
@@ -234,8 +235,9 @@ tval3_status tval3_gpu_3d_sparse_f64(double* U, int dim_y, int dim_x, int dim_z,
         check_opts(opts);
         if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
         check_problem(U, dim_y, dim_x, dim_z, A->rows, A->cols, b, b_len, Ut, Ut_len);
-        solve_host<double>(sparse_op<double>(A, TVAL3_PREC_FP64), U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len,
-                           info, t0);
+        // FP32 matrix values keep their storage (FP64 vectors and reductions)
+        const int prec = (A->val_type == TVAL3_PREC_FP32) ? TVAL3_PREC_FP32_F64VEC : TVAL3_PREC_FP64;
+        solve_host<double>(sparse_op<double>(A, prec), U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len, info, t0);
     });
 }
 

@@ -15,6 +15,7 @@ namespace tv3 {
 template <class T, class V, int EPI>
 __global__ void __launch_bounds__(256) k_dense_N(long m, long n, const V* __restrict__ A, const float* __restrict__ rs,
                                                  MatIO<T> io) {
+    count_launch(io.ctl);
     const int lane = threadIdx.x & 31;
     const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = ((long)gridDim.x * blockDim.x) >> 5;
     const int sel = io.by_parity ? io.ctl->parity : 0;
@@ -59,6 +60,7 @@ __global__ void __launch_bounds__(256) k_dense_N(long m, long n, const V* __rest
 template <class T, class V>
 __global__ void __launch_bounds__(256) k_dense_T_part(long m, long n, long rows_per_slab, const V* __restrict__ A,
                                                       const float* __restrict__ rs, MatIO<T> io, T* __restrict__ part) {
+    count_launch(io.ctl);
     const int sel = io.by_parity ? io.ctl->parity : 0;
     const T* __restrict__ yv = io.x[sel];
     const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -76,6 +78,7 @@ __global__ void __launch_bounds__(256) k_dense_T_part(long m, long n, long rows_
 
 template <class T>
 __global__ void k_dense_T_sum(long n, int slabs, const T* __restrict__ part, MatIO<T> io, int sub) {
+    count_launch(io.ctl);
     const int sel = io.by_parity ? io.ctl->parity : 0;
     T* __restrict__ out = io.y[sel];
     for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {

@@ -227,6 +227,7 @@ __global__ void k_ray_fill(GeomView g, int traversal, const int* __restrict__ pt
 // ---------------------------------------------------------------------------
 template <int G, int EPI>
 __global__ void __launch_bounds__(256) k_bres_N(GeomView g, MatIO<float> io) {
+    count_launch(io.ctl);
     const int lane = threadIdx.x % G;
     const long grp = ((long)blockIdx.x * blockDim.x + threadIdx.x) / G;
     const long ngrp = ((long)gridDim.x * blockDim.x) / G;
@@ -275,6 +276,7 @@ __global__ void __launch_bounds__(256) k_bres_N(GeomView g, MatIO<float> io) {
 // A^T y by scattering: out must be zero on entry
 template <int G>
 __global__ void __launch_bounds__(256) k_bres_T(GeomView g, MatIO<float> io) {
+    count_launch(io.ctl);
     const int lane = threadIdx.x % G;
     const long grp = ((long)blockIdx.x * blockDim.x + threadIdx.x) / G;
     const long ngrp = ((long)gridDim.x * blockDim.x) / G;
@@ -293,12 +295,14 @@ __global__ void __launch_bounds__(256) k_bres_T(GeomView g, MatIO<float> io) {
 }
 
 __global__ void k_zero_sel(MatIO<float> io, long n) {
+    count_launch(io.ctl);
     const int sel = io.by_parity ? io.ctl->parity : 0;
     float* y = io.y[sel];
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) y[i] = 0.f;
 }
 
 __global__ void k_sub_sel(MatIO<float> io, long n) {
+    count_launch(io.ctl);
     const int sel = io.by_parity ? io.ctl->parity : 0;
     float* y = io.y[sel];
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) y[i] -= io.sub[i];

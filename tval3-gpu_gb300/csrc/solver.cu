@@ -102,6 +102,7 @@ void Solver<T>::init_ctl(cudaStream_t s) {
     c.Q = 1.0;
     c.fst = 1;
     c.scl = 1.0;
+    c.launches = 1;  // this kernel
     k_init_ctl<<<1, 1, 0, s>>>(ctl.p, c);
     TV3_CUDA(cudaGetLastError());
 }
@@ -135,7 +136,9 @@ void Solver<T>::setup(const T* d_b, cudaStream_t s) {
     TV3_CUDA(cudaMemsetAsync(B.DtsAtd, 0, n * sizeof(T), s));
     if (m > 0) TV3_CUDA(cudaMemsetAsync(B.delta, 0, m * sizeof(T), s));
     launch_scale_b<T>(d_b, B, s);                                    // scaleb_gpu
-    A->apply(1, plain_io<T>(B.b, B.Atb), SPMV_PLAIN, s);             // Atb = A^T b
+    MatIO<T> io_atb = plain_io<T>(B.b, B.Atb);
+    io_atb.ctl = B.ctl;
+    A->apply(1, io_atb, SPMV_PLAIN, s);                              // Atb = A^T b
     TV3_CUDA(cudaMemcpyAsync(B.U[0], B.Atb, n * sizeof(T), cudaMemcpyDeviceToDevice, s));   // U = Atb
     TV3_CUDA(cudaMemcpyAsync(B.rcdU, B.Atb, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
     launch_D_only<T>(B, s);
@@ -368,6 +371,7 @@ void Solver<T>::solve(const T* d_b, T* d_U, const T* d_Ut, tval3_info* info, cud
         info->backtracks = hctl->backtracks;
         info->restarts = hctl->restarts;
         info->final_f = hctl->f;
+        info->launches = (int)hctl->launches;
     }
 }
 

@@ -22,6 +22,7 @@ namespace tv3 {
 
 template <class T, class V, int G, int EPI>
 __global__ void __launch_bounds__(256) k_spmv(SpmvArgs<T, V> a) {
+    count_launch(a.ctl);
     const int lane = threadIdx.x % G;
     const long grp = ((long)blockIdx.x * blockDim.x + threadIdx.x) / G;
     const long ngrp = ((long)gridDim.x * blockDim.x) / G;

@@ -52,6 +52,7 @@ template <class T> __device__ __forceinline__ T proj(T v, int nonneg) { return (
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(1024) k_scale_find(const T* __restrict__ b, long m, Ctl* ctl) {
+    count_launch(ctl);
     double amin = INFINITY, amax = -1.0;
     long imin = -1, imax = -1;
     for (long i = threadIdx.x; i < m; i += blockDim.x) {
@@ -95,7 +96,8 @@ __global__ void __launch_bounds__(1024) k_scale_find(const T* __restrict__ b, lo
 }
 
 template <class T>
-__global__ void k_scale_apply(const T* __restrict__ b_in, T* __restrict__ b, long m, const Ctl* ctl) {
+__global__ void k_scale_apply(const T* __restrict__ b_in, T* __restrict__ b, long m, Ctl* ctl) {
+    count_launch(ctl);
     const double scl = ctl->scl;
     const T s = (T)scl;
     GRID_STRIDE(i, m) b[i] = (scl == 1.0) ? b_in[i] : b_in[i] * s;
@@ -106,6 +108,7 @@ __global__ void k_scale_apply(const T* __restrict__ b_in, T* __restrict__ b, lon
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void k_D_only(SolverBufs<T> B) {
+    count_launch(B.ctl);
     const T* __restrict__ U = B.U[0];
     T* __restrict__ DU = B.DU[0];
     GRID_STRIDE(i, B.n) {
@@ -128,6 +131,7 @@ __global__ void k_D_only(SolverBufs<T> B) {
 template <class T>
 __global__ void k_descend(SolverBufs<T> B, int restart) {
     Ctl* ctl = B.ctl;
+    count_launch(ctl);
     const int cur = ctl->parity;
     const int src = restart ? 1 - cur : cur, dst = restart ? cur : 1 - cur;
     const T* __restrict__ Up = B.U[src];
@@ -158,6 +162,7 @@ __global__ void k_descend(SolverBufs<T> B, int restart) {
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void k_Dd_norm(SolverBufs<T> B) {
+    count_launch(B.ctl);
     const T* __restrict__ d = B.d;
     double s0 = 0.0, s1 = 0.0;
     GRID_STRIDE(i, B.n) {
@@ -180,6 +185,7 @@ __global__ void k_Dd_norm(SolverBufs<T> B) {
 template <class T>
 __global__ void k_tau(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
+    count_launch(ctl);
     const int cur = ctl->parity, prv = 1 - cur;
     const double mdb = ctl->muDbeta;
     const T *__restrict__ U = B.U[cur], *__restrict__ Up = B.U[prv];
@@ -213,6 +219,7 @@ __device__ __forceinline__ void armijo(Ctl* c) {
 template <class T>
 __global__ void k_g2(SolverBufs<T> B, int mode) {
     Ctl* ctl = B.ctl;
+    count_launch(ctl);
     const int cur = ctl->parity;
     const long n = B.n;
     const T* __restrict__ DU = B.DU[cur];
@@ -263,6 +270,7 @@ __global__ void k_g2(SolverBufs<T> B, int mode) {
 template <class T>
 __global__ void k_shrink(SolverBufs<T> B, int mode) {
     Ctl* ctl = B.ctl;
+    count_launch(ctl);
     const int cur = ctl->parity;
     const long n = B.n;
     const T* __restrict__ DU = B.DU[cur];
@@ -307,6 +315,7 @@ __global__ void k_shrink(SolverBufs<T> B, int mode) {
 template <class T>
 __global__ void k_gradient(SolverBufs<T> B, int iter) {
     Ctl* ctl = B.ctl;
+    count_launch(ctl);
     const int cur = ctl->parity, prv = 1 - cur;
     const T mdb = (T)ctl->muDbeta;
     const T *__restrict__ g = B.g[cur], *__restrict__ g2 = B.g2[cur], *__restrict__ dts = B.DtsAtd;
@@ -355,6 +364,7 @@ __global__ void k_gradient(SolverBufs<T> B, int iter) {
 template <class T>
 __global__ void k_backtrack(SolverBufs<T> B, int setup) {
     Ctl* ctl = B.ctl;
+    count_launch(ctl);
     const int cur = ctl->parity, prv = 1 - cur;
     const long n = B.n, m = B.m;
     const T al = (T)ctl->alpha;
@@ -429,6 +439,7 @@ __global__ void k_backtrack(SolverBufs<T> B, int setup) {
 template <class T>
 __global__ void k_outer_relchg(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
+    count_launch(ctl);
     const T* __restrict__ U = B.U[ctl->parity];
     T* __restrict__ R = B.rcdU;
     double s = 0.0;
@@ -448,7 +459,8 @@ __global__ void k_outer_relchg(SolverBufs<T> B) {
 }
 
 // copies one control flag into a graph conditional handle
-__global__ void k_cond(const Ctl* ctl, unsigned long long h, int src) {
+__global__ void k_cond(Ctl* ctl, unsigned long long h, int src) {
+    count_launch(ctl);
     unsigned v = 0;
     switch (src) {
         case COND_FST: v = ctl->fst ? 1u : 0u; break;
@@ -469,6 +481,7 @@ void launch_cond(Ctl* ctl, unsigned long long handle, int src, cudaStream_t s) {
 template <class T>
 __global__ void k_mlp(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
+    count_launch(ctl);
     const int cur = ctl->parity;
     const long n = B.n, m = B.m;
     const T bt = (T)ctl->beta, mut = (T)ctl->mu;
@@ -512,6 +525,7 @@ __global__ void k_mlp(SolverBufs<T> B) {
 template <class T>
 __global__ void k_outer_grad(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
+    count_launch(ctl);
     const int cur = ctl->parity;
     const T ratio = (T)(ctl->beta_prev / ctl->beta);
     const T mdb = (T)ctl->muDbeta;
@@ -542,6 +556,7 @@ __global__ void k_outer_grad(SolverBufs<T> B) {
 template <class T>
 __global__ void k_finalize(SolverBufs<T> B, T* __restrict__ out, const T* __restrict__ Ut) {
     Ctl* ctl = B.ctl;
+    count_launch(ctl);
     const T* __restrict__ U = B.U[ctl->parity];
     const double scl = ctl->scl;
     const T s = (T)scl;

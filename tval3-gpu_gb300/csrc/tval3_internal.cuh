@@ -44,8 +44,13 @@ struct Ctl {
     int parity;        // slot index of the "current" ping-pong buffers
     int backtracks, restarts;
     int err;           // device-side error word (0 = none)
-    int pad_;
+    unsigned launches; // kernels of this solve that ran (each counts itself once)
 };
+
+// every solver kernel counts itself once (block 0, thread 0)
+__device__ __forceinline__ void count_launch(Ctl* c) {
+    if (c && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c->launches, 1u);
+}
 
 // Epilogue selectors of the reducing kernels.
 enum Epi : int {
