@@ -1,0 +1,451 @@
+#!/usr/bin/env python
+"""Benchmark: time for the 128^3 TVAL3 reconstruction to reach relative L2
+error 1e-3 against the FP64 CPU oracle's solution, on one GB300.
+
+Workload (seeded, synthetic): 128^3 voxels, 512 emitters x 512 receivers on a
+Fibonacci hemisphere of radius 0.95 (262,144 rays), Siddon path lengths stored
+as CSR (built on the device), 12 ellipsoids (0.9-1.1 on 1.0), 0.5 % noise,
+isotropic TV, mu 2^9, beta 2^6, tol 1e-4, maxit 200.
+
+One step = one reconstruction, run up to the first iteration K* at which the
+iterate is within 1e-3 of the oracle's FP64 solution x* (K* is found by an
+instrumented run that records ||x_k - x*|| / ||x*|| on the device after every
+iteration; the timed runs stop at K*, so their output meets the bound, which
+is checked).  Every precision mode of the library is traced; modes that never
+reach 1e-3 are reported with their final error.
+
+value   : seconds per step with b, the operator and all state resident in HBM
+          (one CUDA-graph launch per step, CUDA events on the solver stream).
+e2e     : the same through the reference-facing C-ABI entry point
+          tval3_gpu_3d_sparse_f64 with host CSR + CSC, host b and host U
+          (all host<->device copies inside the timed region).
+roofline: the dominant kernel (CSR SpMV), algorithmic bytes / measured launch
+          time vs the measured HBM copy bandwidth.
+cpu_baseline: the oracle's FP64 solve of the same workload on the host cores.
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle port; the reference itself does not compile) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (str(ROOT / "tval3-gpu_gb300"), str(ROOT)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "128^3 time-to-1e-3 relerr vs FP64 oracle (s per reconstruction)"
+UNIT = "s"
+L2_BYTES = 129 * 2 ** 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=128, help="volume edge (the metric is quoted at 128)")
+    ap.add_argument("--rays", type=int, default=512, help="emitters = receivers")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline timing (development only)")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier_max(value: float, ws: int) -> float:
+    """Barrier and max over ranks (replicas)."""
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.15)
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            hbm = d.get("hbm_gbs") or d.get("hbm_GBs") or d.get("hbm")
+            if isinstance(hbm, dict):
+                hbm = hbm.get("value")
+            if hbm:
+                return float(hbm), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def workload(size, rays):
+    from tval3_gb300 import workloads as W
+    cfg, geo, x = W.config_3d(size, rays, rays)
+    return cfg, geo, x
+
+
+def spmv_bytes(nnz, m, n, sv=4, sx=4, trans=False):
+    """Algorithmic bytes of one CSR product: values + column indices, row
+    pointers, x read once, y written once."""
+    rows = n if trans else m
+    nin, nout = (m, n) if trans else (n, m)
+    return nnz * (sv + 4) + 4 * (rows + 1) + sx * nin + sx * nout
+
+
+def relerr(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64).reshape(-1) - np.asarray(b, np.float64).reshape(-1)) /
+                 np.linalg.norm(np.asarray(b, np.float64).reshape(-1)))
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import tval3_gb300 as T
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    T.load()
+
+    cfg, geo, x_true = workload(args.size, args.rays)
+    dims = cfg.dims
+    n = int(np.prod(dims))
+    stream = torch.cuda.Stream(device=dev)
+
+    # ---- operator built on the device (Siddon), b = A x + noise
+    t0 = time.time()
+    op32 = T.Operator.from_geometry(geo, mode=0, precision=T.PREC_FP32)
+    build_s = time.time() - t0
+    m, nnz = op32.rows, op32.nnz
+    xd = torch.tensor(x_true.reshape(-1), device=dev)
+    Ax = torch.empty(m, device=dev)
+    op32.mat_vec_mul(0, xd, Ax, stream=torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    from tval3_gb300.workloads import add_noise
+    b = add_noise(Ax.double().cpu().numpy(), cfg.noise, cfg.seed).astype(np.float64)
+    ptr, ind, val, tptr, tind, tval = op32.export_csr()
+
+    # ---- the checker: FP64 oracle solve on the host cores (also the CPU baseline)
+    cpu = {}
+    xstar = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        t0 = time.time()
+        xstar, oinfo = O.tval3_csr(dims, ptr, ind, val, b, cfg.opts, prec=0, tptr=tptr, tind=tind, tval=tval)
+        cpu_s = time.time() - t0
+        cpu = dict(seconds=cpu_s, iters=oinfo["total_iters"], info=oinfo, threads=O.num_threads())
+    if ws > 1:
+        # replicas: rank 0's x* is broadcast so every replica checks the same bound
+        buf = torch.zeros(n, dtype=torch.float64, device=dev)
+        if rank == 0:
+            buf.copy_(torch.tensor(xstar.reshape(-1)))
+        import torch.distributed as dist
+        dist.broadcast(buf, 0)
+        xstar = buf.cpu().numpy()
+    xs_dev = torch.tensor(np.asarray(xstar).reshape(-1), dtype=torch.float64, device=dev)
+    xs_norm = float(np.linalg.norm(xstar))
+
+    # ---- trace every precision mode against x*
+    modes = [("fp64vec", T.PREC_FP32_F64VEC, torch.float64), ("fp32", T.PREC_FP32, torch.float32),
+             ("bf16", T.PREC_BF16, torch.float32), ("fp16", T.PREC_FP16, torch.float32)]
+    traced = {}
+    ops = {}
+    for name, prec, dt in modes:
+        op = op32 if prec == T.PREC_FP32 else T.Operator.from_geometry(geo, mode=0, precision=prec)
+        ops[name] = op
+        s = T.Solver(op, dims, cfg.opts, mode=1)
+        xs_t = xs_dev.to(dt)
+        s.set_trace(xs_t)
+        bd = torch.tensor(b, dtype=dt, device=dev)
+        U = torch.empty(n, dtype=dt, device=dev)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            info = s.solve(bd, U, stream=stream)
+        torch.cuda.synchronize()
+        tr = s.trace()[: info["total_iters"]] / xs_norm
+        hit = np.nonzero(tr <= 1e-3)[0]
+        traced[name] = dict(prec=prec, dtype=dt, info=info, final_relerr=relerr(U.double().cpu().numpy(), xstar),
+                            kstar=int(hit[0]) + 1 if hit.size else None, trace=tr)
+        s.close()
+
+    reach = [k for k in traced if traced[k]["kstar"] is not None]
+    head = "fp64vec" if "fp64vec" in reach else (reach[0] if reach else "fp64vec")
+    hm = traced[head]
+    kstar = hm["kstar"] or hm["info"]["total_iters"]
+    opts_k = dict(cfg.opts, maxit=kstar)
+
+    # ---- timed region: K steps of the device-resident reconstruction
+    dt = hm["dtype"]
+    op = ops[head]
+    solver = T.Solver(op, dims, opts_k, mode=1)
+    bd = torch.tensor(b, dtype=dt, device=dev)
+    U = torch.empty(n, dtype=dt, device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    launches = 0
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            solver.solve(bd, U, stream=stream)
+    torch.cuda.synchronize()
+    times = []
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)  # L2 flush between steps (outside the events)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                info = solver.solve(bd, U, stream=stream)
+                e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1000.0)
+            launches += info["launches"]
+        torch.cuda.synchronize()
+    barrier(ws)
+    step_s = barrier_max(float(np.mean(times)), ws)
+    out_err = relerr(U.double().cpu().numpy(), xstar)
+    assert out_err <= 1e-3 or hm["kstar"] is None, out_err
+    solver.close()
+
+    # ---- roofline of the dominant kernel: CSR SpMV, live CUDA-event timing
+    sx = 8 if dt == torch.float64 else 4
+    xv = torch.randn(n, dtype=dt, device=dev)
+    yv = torch.randn(m, dtype=dt, device=dev)
+    outm = torch.empty(m, dtype=dt, device=dev)
+    outn = torch.empty(n, dtype=dt, device=dev)
+    torch.cuda.synchronize()
+
+    def time_op(trans, reps=20):
+        src, dst = (yv, outn) if trans else (xv, outm)
+        for _ in range(3):
+            op.mat_vec_mul(trans, src, dst, stream=stream)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        tot = 0.0
+        for _ in range(reps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                ev[0].record(stream)
+                op.mat_vec_mul(trans, src, dst, stream=stream)
+                ev[1].record(stream)
+            ev[1].synchronize()
+            tot += ev[0].elapsed_time(ev[1]) / 1000.0
+        return tot / reps
+    tN, tT = time_op(0), time_op(1)
+    bN = spmv_bytes(nnz, m, n, 4, sx, False)
+    bT = spmv_bytes(nnz, m, n, 4, sx, True)
+    peak, peak_kind = peaks()
+    dom = ("spmv_AT", tT, bT) if tT >= tN else ("spmv_A", tN, bN)
+    ach = dom[2] / dom[1] / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "spmv_traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(f"{dom[0]}_{args.size}")
+        except Exception:
+            traffic = None
+    roofline = {"kernel": dom[0], "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                "bytes_per_launch": dom[2], "launch_us": round(dom[1] * 1e6, 2),
+                "pair": {"A_us": round(tN * 1e6, 2), "AT_us": round(tT * 1e6, 2),
+                         "pair_GBs": round((bN + bT) / (tN + tT) / 1e9, 1)}}
+
+    # ---- e2e: reference-facing entry point with host buffers
+    e2e = None
+    if head in ("fp64vec", "fp32"):
+        A_host = T.SparseMatrix(m, n, ptr, ind, val, tptr, tind, tval)
+        dtn = np.float64 if head == "fp64vec" else np.float32
+        h2d = (ptr.nbytes + ind.nbytes + val.nbytes + tptr.nbytes + tind.nbytes + tval.nbytes +
+               b.astype(dtn).nbytes)
+        d2h = n * np.dtype(dtn).itemsize
+        T.tval3_gpu_3d(dims, A_host, b, opts_k, dtype=dtn)  # warm-up
+        torch.cuda.synchronize()
+        et = []
+        for _ in range(max(1, args.e2e_steps)):
+            t0 = time.perf_counter()
+            Ue, ie = T.tval3_gpu_3d(dims, A_host, b, opts_k, dtype=dtn)
+            et.append(time.perf_counter() - t0)
+        e2e = {"value": round(barrier_max(float(np.mean(et)), ws), 5), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "relerr_vs_oracle": relerr(Ue, xstar),
+               "entry": "tval3_gpu_3d_sparse_f64 (FP32 CSR+CSC values, host arrays)"}
+
+    if rank != 0:
+        return None
+    cpu_baseline = None
+    if cpu:
+        per_it = cpu["seconds"] / max(cpu["iters"], 1)
+        cpu_baseline = {"value": round(per_it * kstar, 4), "unit": UNIT, "cores": cpu["threads"], "kind": "port",
+                        "sample": f"full FP64 oracle solve of this workload ({cpu['iters']} iterations, "
+                                  f"{cpu['seconds']:.2f} s); value = its per-iteration time x K*={kstar}"}
+    modes_out = {k: {"kstar": v["kstar"], "final_relerr": round(v["final_relerr"], 6),
+                     "iters": v["info"]["total_iters"], "backtracks": v["info"]["backtracks"],
+                     "restarts": v["info"]["restarts"], "solve_s": round(v["info"]["secs"], 5)}
+                 for k, v in traced.items()}
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": round(step_s, 6), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(step_s * 1e3, 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if dt == torch.float64 else "f32",
+        "data": "synthetic (seeded phantom and geometry)",
+        "config": {"workload": f"tval3 3d {args.size}^3, {args.rays}x{args.rays} hemisphere rays, Siddon CSR",
+                   "voxels": n, "rays": m, "nnz": nnz, "mode": head, "matrix_values": "f32", "kstar": kstar,
+                   "tv": "isotropic", "mu": cfg.opts["mu"], "beta": cfg.opts["beta"], "maxit": cfg.opts["maxit"],
+                   "l2": "inputs larger than L2 (matrix %.0f MB) and a %d MB flush between steps" %
+                         (nnz * 8 / 1e6 * 2, 2 * L2_BYTES // 2 ** 20),
+                   "parallelism": f"replicas x{ws}", "device_build_s": round(build_s, 3),
+                   "output_relerr_vs_oracle": round(out_err, 8)},
+        "modes": modes_out,
+        "roofline": roofline,
+        "cpu_baseline": cpu_baseline,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    return line
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    """The reference algorithm on the host cores (the oracle port; the
+    reference's own sources do not compile), same workload, same metric."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+    from tval3_gb300.workloads import add_noise
+    cfg, geo, x_true = workload(args.size, args.rays)
+    dims = cfg.dims
+    ptr, ind, val = O.siddon_csr(geo)
+    tptr, tind, tval = O.transpose(ptr.size - 1, x_true.size, ptr, ind, val)
+    b = add_noise(O.spmv(ptr, ind, val, x_true), cfg.noise, cfg.seed).astype(np.float64)
+    xstar, info = O.tval3_csr(dims, ptr, ind, val, b, cfg.opts, prec=0, tptr=tptr, tind=tind, tval=tval)
+    _, _, tr = O.tval3_csr(dims, ptr, ind, val, b, cfg.opts, prec=0, tptr=tptr, tind=tind, tval=tval, xstar=xstar)
+    hit = np.nonzero(tr[: info["total_iters"]] <= 1e-3)[0]
+    kstar = int(hit[0]) + 1 if hit.size else info["total_iters"]
+    opts_k = dict(cfg.opts, maxit=kstar)
+    for _ in range(args.warmup):
+        O.tval3_csr(dims, ptr, ind, val, b, opts_k, prec=0, tptr=tptr, tind=tind, tval=tval)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        U, _ = O.tval3_csr(dims, ptr, ind, val, b, opts_k, prec=0, tptr=tptr, tind=tind, tval=tval)
+        ts.append(time.perf_counter() - t0)
+    v = float(np.mean(ts))
+    cores = O.num_threads()
+    return {
+        "metric": METRIC, "value": round(v, 5), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(v * 1e3, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded phantom and geometry)",
+        "config": {"workload": f"tval3 3d {args.size}^3, {args.rays}x{args.rays} hemisphere rays, Siddon CSR",
+                   "voxels": int(np.prod(dims)), "rays": int(ptr.size - 1), "nnz": int(ind.size), "kstar": kstar,
+                   "output_relerr_vs_oracle": relerr(U, xstar)},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(v, 5), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"FP64 CPU restatement of the reference loop (the reference does not compile), "
+                                   f"{kstar} iterations per step, OpenMP on {cores} threads"},
+        "e2e": {"value": round(v, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    ws, _, _ = dist_env()
+    if ws > 1 and args.impl != "reference":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
