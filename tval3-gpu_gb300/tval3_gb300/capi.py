@@ -14,7 +14,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libtval3_gb300.so"
 TVAL3_OK = 0
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_SHAPE", 3: "ERR_CUDA", 4: "ERR_NOMEM", 5: "ERR_TIMEOUT",
           6: "ERR_NONFINITE", 7: "ERR_UNSUPPORTED"}
-PREC_FP32, PREC_FP64, PREC_BF16, PREC_FP16 = 0, 1, 2, 3
+PREC_FP32, PREC_FP64, PREC_BF16, PREC_FP16, PREC_FP32_F64VEC = 0, 1, 2, 3, 4
 TV_ANISO, TV_ISO = 0, 1
 SPARSE_CSR, SPARSE_CSC, SPARSE_BOTH = 1, 2, 3
 TRAV_BRESENHAM, TRAV_SIDDON = 0, 1
