@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--rays", type=int, default=512, help="emitters = receivers")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline timing (development only)")
+    ap.add_argument("--modes", default="fp64vec,fp32,bf16,fp16", help="precision modes to trace")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-API measurement (profiling runs)")
     return ap.parse_args()
 
 
@@ -235,6 +237,8 @@ def run_ours(args):
     # ---- trace every precision mode against x*
     modes = [("fp64vec", T.PREC_FP32_F64VEC, torch.float64), ("fp32", T.PREC_FP32, torch.float32),
              ("bf16", T.PREC_BF16, torch.float32), ("fp16", T.PREC_FP16, torch.float32)]
+    wanted = set(args.modes.split(","))
+    modes = [md for md in modes if md[0] in wanted]
     traced = {}
     ops = {}
     for name, prec, dt in modes:
@@ -340,7 +344,7 @@ def run_ours(args):
 
     # ---- e2e: reference-facing entry point with host buffers
     e2e = None
-    if head in ("fp64vec", "fp32"):
+    if head in ("fp64vec", "fp32") and not args.no_e2e:
         A_host = T.SparseMatrix(m, n, ptr, ind, val, tptr, tind, tval)
         dtn = np.float64 if head == "fp64vec" else np.float32
         h2d = (ptr.nbytes + ind.nbytes + val.nbytes + tptr.nbytes + tind.nbytes + tval.nbytes +
