@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline timing (development only)")
     ap.add_argument("--modes", default="fp64vec,fp32,bf16,fp16", help="precision modes to trace")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-API measurement (profiling runs)")
+    ap.add_argument("--solver-mode", type=int, default=1,
+                    help="1: whole solve as one CUDA graph; 0: host-driven loop (same kernels; profilers "
+                         "cannot see kernels inside graphs with conditional nodes)")
     return ap.parse_args()
 
 
@@ -244,7 +247,7 @@ def run_ours(args):
     for name, prec, dt in modes:
         op = op32 if prec == T.PREC_FP32 else T.Operator.from_geometry(geo, mode=0, precision=prec)
         ops[name] = op
-        s = T.Solver(op, dims, cfg.opts, mode=1)
+        s = T.Solver(op, dims, cfg.opts, mode=args.solver_mode)
         xs_t = xs_dev.to(dt)
         s.set_trace(xs_t)
         bd = torch.tensor(b, dtype=dt, device=dev)
@@ -268,7 +271,7 @@ def run_ours(args):
     # ---- timed region: K steps of the device-resident reconstruction
     dt = hm["dtype"]
     op = ops[head]
-    solver = T.Solver(op, dims, opts_k, mode=1)
+    solver = T.Solver(op, dims, opts_k, mode=args.solver_mode)
     bd = torch.tensor(b, dtype=dt, device=dev)
     U = torch.empty(n, dtype=dt, device=dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)

@@ -12,6 +12,11 @@ struct Ctl;
 
 enum SpmvEpi : int { SPMV_PLAIN = 0, SPMV_SUB = 1, SPMV_LAM35 = 2, SPMV_NORM2 = 3 };
 
+// Slack (elements) behind the index and value arrays of a CSR operator: the
+// SpMV reads four-element chunks from a 4-aligned base, at most 4*G + 3
+// elements past the last nonzero (G <= 32).  The slack is zero-filled.
+constexpr long SPMV_PAD = 256;
+
 // Arguments of one CSR product y = M x (M is A or the CSR of A^T).  x and y
 // are ping-pong pairs: with by_parity set, the kernel uses slot ctl->parity.
 template <class T, class V>

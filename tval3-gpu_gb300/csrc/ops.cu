@@ -17,6 +17,14 @@ void throw_cuda(cudaError_t e, const char* what) {
     throw Error{st, std::string(what) + ": " + cudaGetErrorString(e)};
 }
 
+// index / value arrays of a CSR operator: nnz elements plus zeroed slack
+// that the four-element loads of the SpMV may touch
+template <class X>
+static void alloc_padded(DBuf<X>& b, long nnz) {
+    b.alloc(nnz + SPMV_PAD);
+    TV3_CUDA(cudaMemset(b.p, 0, (nnz + SPMV_PAD) * sizeof(X)));
+}
+
 static int pick_lanes(double avg) {
     if (avg > 48) return 32;
     if (avg > 20) return 16;
@@ -238,12 +246,49 @@ void CsrOp<T, V>::export_csr(int* hptr, int* hind, float* hval, int* htptr, int*
     export_vals<T, V>(*this, hval, htval);
 }
 
+// Autotuner: for matrices big enough to matter, time every lanes-per-row
+// choice of both products on the operator itself (CUDA events, zero vectors,
+// three launches each after one warm-up) and keep the fastest; small matrices
+// use the nonzeros-per-row heuristic.
+template <class T, class V>
+static void tune_lanes(CsrOp<T, V>* op) {
+    const long m = op->m, n = op->n;
+    DBuf<T> x(std::max(m, n) + 1), y(std::max(m, n) + 1);
+    TV3_CUDA(cudaMemset(x.p, 0, (std::max(m, n) + 1) * sizeof(T)));
+    cudaEvent_t e0, e1;
+    TV3_CUDA(cudaEventCreate(&e0));
+    TV3_CUDA(cudaEventCreate(&e1));
+    const int cand[4] = {4, 8, 16, 32};
+    for (int trans = 0; trans < 2; ++trans) {
+        float best = 1e30f;
+        int bestG = trans ? op->Gt : op->Gn;
+        for (int G : cand) {
+            if (trans) { op->Gt = G; op->grid_t = spmv_grid(n, G); }
+            else { op->Gn = G; op->grid_n = spmv_grid(m, G); }
+            MatIO<T> io = plain_io<T>(x.p, y.p);
+            op->apply(trans, io, SPMV_PLAIN, 0);
+            TV3_CUDA(cudaEventRecord(e0, 0));
+            for (int r = 0; r < 3; ++r) op->apply(trans, io, SPMV_PLAIN, 0);
+            TV3_CUDA(cudaEventRecord(e1, 0));
+            TV3_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            TV3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) { best = ms; bestG = G; }
+        }
+        if (trans) { op->Gt = bestG; op->grid_t = spmv_grid(n, bestG); }
+        else { op->Gn = bestG; op->grid_n = spmv_grid(m, bestG); }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+}
+
 template <class T, class V>
 static void finish_layout(CsrOp<T, V>* op) {
     op->Gn = pick_lanes(op->m ? (double)op->nnz / op->m : 0.0);
     op->Gt = pick_lanes(op->n ? (double)op->nnz / op->n : 0.0);
     op->grid_n = spmv_grid(op->m, op->Gn);
     op->grid_t = spmv_grid(op->n, op->Gt);
+    if (op->nnz >= (1L << 22)) tune_lanes(op);
 }
 
 // Build from device arrays (FP32 values for the FP32/BF16/FP16 precisions,
@@ -258,9 +303,9 @@ static void copy_structure(LinOp<T>* base, DBuf<int>& ptr, DBuf<int>& ind, DBuf<
                            long rows, long cols, long nnz, const int* d_ptr, const int* d_ind) {
     base->m = rows; base->n = cols; base->nnz = nnz; base->kind = 0;
     ptr.alloc(rows + 1);
-    ind.alloc(std::max<long>(nnz, 1));
+    alloc_padded(ind, nnz);
     tptr.alloc(cols + 1);
-    tind.alloc(std::max<long>(nnz, 1));
+    alloc_padded(tind, nnz);
     TV3_CUDA(cudaMemcpy(ptr.p, d_ptr, (rows + 1) * sizeof(int), cudaMemcpyDeviceToDevice));
     if (nnz) TV3_CUDA(cudaMemcpy(ind.p, d_ind, nnz * sizeof(int), cudaMemcpyDeviceToDevice));
 }
@@ -279,8 +324,8 @@ LinOp<double>* make_csr_op_f64vec(long rows, long cols, long nnz, const int* d_p
     auto* op = new CsrOp<double, float>();
     try {
         copy_structure<double>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
-        op->val.alloc(std::max<long>(nnz, 1));
-        op->tval.alloc(std::max<long>(nnz, 1));
+        alloc_padded(op->val, nnz);
+        alloc_padded(op->tval, nnz);
         if (nnz) TV3_CUDA(cudaMemcpy(op->val.p, d_val, nnz * sizeof(float), cudaMemcpyDeviceToDevice));
         if (d_tptr) {
             TV3_CUDA(cudaMemcpy(op->tptr.p, d_tptr, (cols + 1) * sizeof(int), cudaMemcpyDeviceToDevice));
@@ -315,8 +360,8 @@ LinOp<double>* make_csr_op_device<double>(long rows, long cols, long nnz, const 
     auto* op = new CsrOp<double, double>();
     try {
         copy_structure<double>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
-        op->val.alloc(std::max<long>(nnz, 1));
-        op->tval.alloc(std::max<long>(nnz, 1));
+        alloc_padded(op->val, nnz);
+        alloc_padded(op->tval, nnz);
         if (nnz) TV3_CUDA(cudaMemcpy(op->val.p, d_val, nnz * sizeof(double), cudaMemcpyDeviceToDevice));
         if (d_tptr) {
             TV3_CUDA(cudaMemcpy(op->tptr.p, d_tptr, (cols + 1) * sizeof(int), cudaMemcpyDeviceToDevice));
@@ -353,8 +398,8 @@ static LinOp<float>* make_q(long rows, long cols, long nnz, const int* d_ptr, co
             csr_transpose_device<float>(rows, cols, nnz, op->ptr.p, op->ind.p, d_val, op->tptr.p, op->tind.p, tv.p, s);
         }
         op->rs.alloc(std::max<long>(rows, 1));
-        op->val.alloc(std::max<long>(nnz, 1));
-        op->tval.alloc(std::max<long>(nnz, 1));
+        alloc_padded(op->val, nnz);
+        alloc_padded(op->tval, nnz);
         k_rowmax<<<ew(rows * 32), 256, 0, s>>>(rows, op->ptr.p, d_val, op->rs.p);
         k_quant_rows<V><<<ew(rows * 32), 256, 0, s>>>(rows, op->ptr.p, d_val, op->rs.p, op->val.p);
         if (nnz) k_quant_entries<V><<<ew(nnz), 256, 0, s>>>(nnz, op->tind.p, tv.p, op->rs.p, op->tval.p);
@@ -377,8 +422,8 @@ LinOp<float>* make_csr_op_device<float>(long rows, long cols, long nnz, const in
     auto* op = new CsrOp<float, float>();
     try {
         copy_structure<float>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
-        op->val.alloc(std::max<long>(nnz, 1));
-        op->tval.alloc(std::max<long>(nnz, 1));
+        alloc_padded(op->val, nnz);
+        alloc_padded(op->tval, nnz);
         if (nnz) TV3_CUDA(cudaMemcpy(op->val.p, d_val, nnz * sizeof(float), cudaMemcpyDeviceToDevice));
         if (d_tptr) {
             TV3_CUDA(cudaMemcpy(op->tptr.p, d_tptr, (cols + 1) * sizeof(int), cudaMemcpyDeviceToDevice));

@@ -3,13 +3,17 @@
 // 3d/mat_vec_mul_sparse.h:1727-1745).  Replaces cusparseScsrmv
 // (3d/blas_wrapper.h:241-289).
 //
-// One group of G lanes per row, grid-stride over rows; G = 32 for the long
-// ray rows of A, smaller for the short voxel rows of A^T.  Matrix values and
-// column indices are streamed with the evict-first policy; x is gathered
-// through L1/L2 (it fits in L2 for every configuration of this library).
-// Values may be FP32, FP64, BF16 or FP16; for the 16-bit formats a per-row
-// FP32 scale of A is applied to the row sum (A*x) or to the gathered y (A^T*y),
-// so A^T is the exact adjoint of the quantised A.
+// One group of G lanes per row, grid-stride over rows.  Every lane reads four
+// consecutive nonzeros with one 16-byte load of column indices and one
+// 16-byte (FP32), 32-byte (FP64) or 8-byte (BF16/FP16) load of values, from a
+// 4-aligned base below the row start; elements outside [row start, row end)
+// are masked.  The index and value arrays are allocated with SPMV_PAD
+// elements of slack so these loads never leave the allocation.  Two such
+// chunks are issued before their gathers, so each lane keeps 4 streaming
+// loads and 8 gathers in flight.  Matrix streams use the evict-first policy;
+// x is gathered through L1/L2 (it fits in L2 for every configuration).
+// For 16-bit values a per-ray FP32 scale of A is applied to the row sum (A*x)
+// or to the gathered y (A^T*y), so A^T is the exact adjoint of the quantised A.
 //
 // Optional fused epilogues (solver only): lam3 = ||Au - b||^2 and
 // lam5 = <delta, Au - b> (3d/tval3_gpu_3d_kernels.cu:876-919), ||Ad||^2 for the
@@ -20,9 +24,43 @@
 
 namespace tv3 {
 
+// four consecutive values from a 16-byte aligned element index
+template <class V> struct Vec4;
+template <> struct Vec4<float> {
+    __device__ static __forceinline__ void load(const float* p, float (&o)[4]) {
+        float4 v = __ldcs(reinterpret_cast<const float4*>(p));
+        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    }
+};
+template <> struct Vec4<double> {
+    __device__ static __forceinline__ void load(const double* p, double (&o)[4]) {
+        double2 a = __ldcs(reinterpret_cast<const double2*>(p));
+        double2 b = __ldcs(reinterpret_cast<const double2*>(p) + 1);
+        o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+    }
+};
+template <> struct Vec4<__nv_bfloat16> {
+    __device__ static __forceinline__ void load(const __nv_bfloat16* p, float (&o)[4]) {
+        uint2 u = __ldcs(reinterpret_cast<const uint2*>(p));
+        o[0] = __uint_as_float(u.x << 16); o[1] = __uint_as_float(u.x & 0xffff0000u);
+        o[2] = __uint_as_float(u.y << 16); o[3] = __uint_as_float(u.y & 0xffff0000u);
+    }
+};
+template <> struct Vec4<__half> {
+    __device__ static __forceinline__ void load(const __half* p, float (&o)[4]) {
+        uint2 u = __ldcs(reinterpret_cast<const uint2*>(p));
+        __half2 a = *reinterpret_cast<__half2*>(&u.x), b = *reinterpret_cast<__half2*>(&u.y);
+        float2 fa = __half22float2(a), fb = __half22float2(b);
+        o[0] = fa.x; o[1] = fa.y; o[2] = fb.x; o[3] = fb.y;
+    }
+};
+template <class V> struct VT { using type = float; };
+template <> struct VT<double> { using type = double; };
+
 template <class T, class V, int G, int EPI>
 __global__ void __launch_bounds__(256) k_spmv(SpmvArgs<T, V> a) {
     count_launch(a.ctl);
+    using VV = typename VT<V>::type;
     const int lane = threadIdx.x % G;
     const long grp = ((long)blockIdx.x * blockDim.x + threadIdx.x) / G;
     const long ngrp = ((long)gridDim.x * blockDim.x) / G;
@@ -33,32 +71,31 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs<T, V> a) {
     const int* __restrict__ ptr = a.ptr;
     const int* __restrict__ ind = a.ind;
     const V* __restrict__ val = a.val;
+    const float* __restrict__ xs = a.xscale;
     double acc0 = 0.0, acc1 = 0.0;
-    // the group mask for the shuffles: G consecutive lanes
     const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
     for (long r = grp; r < a.rows; r += ngrp) {
         const int beg = __ldg(ptr + r), end = __ldg(ptr + r + 1);
         T s = T(0);
-        int k = beg + lane;
-        if (a.xscale) {
-            const float* __restrict__ xs = a.xscale;
-            for (; k < end; k += G) {
-                int c = __ldcs(ind + k);
-                s += (T)Acc<T, V>::load(val + k) * (x[c] * (T)__ldg(xs + c));
+        for (int base = (beg & ~3) + 4 * lane; base < end; base += 8 * G) {
+            const int base2 = base + 4 * G;
+            int4 c0 = __ldcs(reinterpret_cast<const int4*>(ind + base));
+            int4 c1 = __ldcs(reinterpret_cast<const int4*>(ind + base2));
+            VV v0[4], v1[4];
+            Vec4<V>::load(val + base, v0);
+            Vec4<V>::load(val + base2, v1);
+            const int cc[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+            T xv[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int k = (e < 4 ? base : base2) + (e & 3);
+                xv[e] = (k >= beg && k < end) ? x[cc[e]] : T(0);
+                if (xs && k >= beg && k < end) xv[e] *= (T)__ldg(xs + cc[e]);
             }
-        } else {
-            for (; k + 3 * G < end; k += 4 * G) {
-                int c0 = __ldcs(ind + k), c1 = __ldcs(ind + k + G), c2 = __ldcs(ind + k + 2 * G),
-                    c3 = __ldcs(ind + k + 3 * G);
-                T v0 = (T)Acc<T, V>::load(val + k), v1 = (T)Acc<T, V>::load(val + k + G),
-                  v2 = (T)Acc<T, V>::load(val + k + 2 * G), v3 = (T)Acc<T, V>::load(val + k + 3 * G);
-                T x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
-                s += v0 * x0;
-                s += v1 * x1;
-                s += v2 * x2;
-                s += v3 * x3;
-            }
-            for (; k < end; k += G) s += (T)Acc<T, V>::load(val + k) * x[__ldcs(ind + k)];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) s += (T)v0[e] * xv[e];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) s += (T)v1[e] * xv[4 + e];
         }
 #pragma unroll
         for (int o = G / 2; o; o >>= 1) s += __shfl_down_sync(gmask, s, o, G);
