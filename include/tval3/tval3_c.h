@@ -52,7 +52,9 @@ typedef enum tval3_precision {
     TVAL3_PREC_FP64 = 1,
     TVAL3_PREC_BF16 = 2, /* BF16 values with per-row FP32 scale, FP32 accumulation */
     TVAL3_PREC_FP16 = 3, /* FP16 values with per-row FP32 scale, FP32 accumulation */
-    TVAL3_PREC_FP32_F64VEC = 4 /* FP32 values, FP64 vectors, products and reductions */
+    TVAL3_PREC_FP32_F64VEC = 4, /* FP32 values, FP64 vectors, products and reductions */
+    TVAL3_PREC_FP32_DF64 = 5    /* FP32 values; vectors, products and reductions in double-float
+                                   (pairs of FP32, ~48 bits) on the FP32 pipes; FP64 at the interface */
 } tval3_precision;
 
 typedef enum tval3_trans { TVAL3_OP_N = 0, TVAL3_OP_T = 1 } tval3_trans;
@@ -80,6 +82,9 @@ typedef struct tval3_options {
     double skipMulRatio;
     double maxRelativeChange;
     int tv_type;      /* tval3_tv; the reference is anisotropic */
+    int precision;    /* internal arithmetic of the host entry points: -1 = the entry point's
+                         type; TVAL3_PREC_FP32_DF64 with an _f64 entry and FP32 matrix values
+                         runs the solve in double-float */
 } tval3_options;
 
 /* Result summary (tval3_info, 2d/tval3_types.h:37-43; outer_secs

@@ -45,6 +45,33 @@ def test_fp64_solve_matches_oracle(cuda, oracle, iso):
 
 
 @pytest.mark.parametrize("iso", [0, 1])
+def test_double_float_solve_matches_fp64_oracle(cuda, oracle, iso):
+    """Double-float vectors (FP32 pairs, ~48 bits) over the FP32 matrix follow
+    the FP64 oracle: the same control flow and the result well inside 1e-3
+    after a full solve of the 64^2 ring problem."""
+    import torch
+    from tval3_gb300 import PREC_FP32_DF64, Operator, Solver, SparseMatrix, tval3_gpu_3d
+    geo, x, ptr, ind, val, b = _problem(oracle, 64, 128, seed=0)
+    o = dict(OPTS, tv_type=iso, mu0=256., beta0=32.)
+    Uo, io = oracle.tval3_csr((64, 64, 1), ptr, ind, val, b.astype(np.float64), o, prec=0, Ut=x)
+    op = Operator.from_sparse(SparseMatrix(ptr.size - 1, x.size, ptr, ind, val), precision=PREC_FP32_DF64)
+    for mode in (0, 1):
+        s = Solver(op, (64, 64, 1), o, mode=mode)
+        U = torch.empty(x.size, dtype=torch.float64, device=cuda)
+        ig = s.solve(torch.tensor(b, dtype=torch.float64, device=cuda), U)
+        torch.cuda.synchronize()
+        assert (ig["total_iters"], ig["outer_iters"], ig["backtracks"], ig["restarts"]) == \
+            (io["total_iters"], io["outer_iters"], io["backtracks"], io["restarts"])
+        assert np.linalg.norm(U.cpu().numpy() - Uo.reshape(-1)) <= 1e-4 * np.linalg.norm(Uo)
+        s.close()
+    # the reference-facing FP64 entry point with FP32 values, run in double-float
+    Uh, ih = tval3_gpu_3d((64, 64, 1), SparseMatrix(ptr.size - 1, x.size, ptr, ind, val), b.astype(np.float64),
+                          dict(o, precision=PREC_FP32_DF64), dtype=np.float64)
+    assert ih["total_iters"] == io["total_iters"]
+    assert np.linalg.norm(Uh - Uo) <= 1e-4 * np.linalg.norm(Uo)
+
+
+@pytest.mark.parametrize("iso", [0, 1])
 def test_fp32_solve_matches_oracle_short_horizon(cuda, oracle, iso):
     from tval3_gb300 import SparseMatrix, tval3_gpu_3d
     geo, x, ptr, ind, val, b = _problem(oracle, 64, 128, seed=0)

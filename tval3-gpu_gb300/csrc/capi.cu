@@ -16,11 +16,13 @@
 using namespace tv3;
 
 struct tval3_op_s {
-    int dbl = 0;  // vector type double?
+    int dbl = 0;  // caller-facing vector type double?
     int precision = 0;
     LinOp<float>* f = nullptr;
     LinOp<double>* d = nullptr;
+    LinOp<df64>* q = nullptr;  // double-float view of d (TVAL3_PREC_FP32_DF64)
     ~tval3_op_s() {
+        delete q;
         delete f;
         delete d;
     }
@@ -30,9 +32,11 @@ struct tval3_solver_s {
     int dbl = 0;
     Solver<float>* f = nullptr;
     Solver<double>* d = nullptr;
+    Solver<df64>* q = nullptr;
     ~tval3_solver_s() {
         delete f;
         delete d;
+        delete q;
     }
 };
 
@@ -155,6 +159,14 @@ void check_opts(const tval3_options* o) {
         arg_error(TVAL3_ERR_ARG, "Argument error: mu, mu0, beta, beta0 must be positive!");
 }
 
+// calls f on whichever solver the handle holds (float, double or double-float)
+template <class F>
+void with_solver(tval3_solver s, F f) {
+    if (s->q) f(*s->q);
+    else if (s->d) f(*s->d);
+    else f(*s->f);
+}
+
 template <class T>
 void check_vec(const T* v, long n, const char* what) {
     for (long i = 0; i < n; ++i)
@@ -163,24 +175,26 @@ void check_vec(const T* v, long n, const char* what) {
 
 // the common body of the reference entry points: host U/b/Ut, operator built
 template <class T>
-void solve_host(LinOp<T>* op, T* U, int dim_y, int dim_x, int dim_z, const T* b, int b_len, const tval3_options* opts,
-                const T* Ut, int Ut_len, tval3_info* info, std::chrono::steady_clock::time_point t0) {
+void solve_host(LinOp<T>* op, Ext<T>* U, int dim_y, int dim_x, int dim_z, const Ext<T>* b, int b_len,
+                const tval3_options* opts, const Ext<T>* Ut, int Ut_len, tval3_info* info,
+                std::chrono::steady_clock::time_point t0) {
+    using E = Ext<T>;
     std::unique_ptr<LinOp<T>> hold(op);
     const long n = (long)dim_y * dim_x * dim_z;
-    DBuf<T> db, dU, dUt;
+    DBuf<E> db, dU, dUt;
     db.alloc(std::max<long>(b_len, 1));
     dU.alloc(std::max<long>(n, 1));
-    if (b_len) TV3_CUDA(cudaMemcpy(db.p, b, b_len * sizeof(T), cudaMemcpyHostToDevice));
+    if (b_len) TV3_CUDA(cudaMemcpy(db.p, b, b_len * sizeof(E), cudaMemcpyHostToDevice));
     const bool use_ut = Ut && Ut_len == n && n > 0;
     if (use_ut) {
         dUt.alloc(n);
-        TV3_CUDA(cudaMemcpy(dUt.p, Ut, n * sizeof(T), cudaMemcpyHostToDevice));
+        TV3_CUDA(cudaMemcpy(dUt.p, Ut, n * sizeof(E), cudaMemcpyHostToDevice));
     }
     Solver<T> s(op, dim_y, dim_x, dim_z, *opts);
     s.mode = 1;  // the whole solve as one graph launch
     tval3_info inf{};
     s.solve(db.p, dU.p, use_ut ? dUt.p : nullptr, &inf, 0);
-    TV3_CUDA(cudaMemcpy(U, dU.p, n * sizeof(T), cudaMemcpyDeviceToHost));
+    TV3_CUDA(cudaMemcpy(U, dU.p, n * sizeof(E), cudaMemcpyDeviceToHost));
     inf.outer_secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (info) *info = inf;
 }
@@ -209,6 +223,7 @@ void tval3_options_default(tval3_options* o) {
     o->gamma = 0.6; o->gam = 0.9995; o->rate_gam = 0.9; o->isreal = 1; o->nonneg = 1;
     o->numInitIterations = 0; o->skipMulRatio = 0.0; o->maxRelativeChange = 0.0;
     o->tv_type = TVAL3_TV_ANISO;
+    o->precision = -1;
 }
 
 const char* tval3_last_error_message(void) { return g_err.c_str(); }
@@ -237,6 +252,13 @@ tval3_status tval3_gpu_3d_sparse_f64(double* U, int dim_y, int dim_x, int dim_z,
         check_problem(U, dim_y, dim_x, dim_z, A->rows, A->cols, b, b_len, Ut, Ut_len);
         // FP32 matrix values keep their storage (FP64 vectors and reductions)
         const int prec = (A->val_type == TVAL3_PREC_FP32) ? TVAL3_PREC_FP32_F64VEC : TVAL3_PREC_FP64;
+        if (prec == TVAL3_PREC_FP32_F64VEC && opts->precision == TVAL3_PREC_FP32_DF64) {
+            // double-float solve over the FP32 matrix; FP64 at the interface
+            std::unique_ptr<LinOp<double>> base(sparse_op<double>(A, prec));
+            solve_host<df64>(make_df64_view(base.get()), U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len, info,
+                             t0);
+            return;
+        }
         solve_host<double>(sparse_op<double>(A, prec), U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len, info, t0);
     });
 }
@@ -325,11 +347,15 @@ tval3_status tval3_gpu_3d_geometry_sparse_f32(float* U, int dim_y, int dim_x, in
 tval3_status tval3_op_create_sparse(tval3_op* op, const tval3_sparse_host* A, int precision) {
     return guard([&] {
         if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
-        if (precision < 0 || precision > 4) arg_error(TVAL3_ERR_ARG, "Argument error: unknown precision!");
+        if (precision < 0 || precision > 5) arg_error(TVAL3_ERR_ARG, "Argument error: unknown precision!");
         auto* h = new tval3_op_s();
         try {
             h->precision = precision;
-            if (precision == TVAL3_PREC_FP64 || precision == TVAL3_PREC_FP32_F64VEC) {
+            if (precision == TVAL3_PREC_FP32_DF64) {
+                h->dbl = 1;
+                h->d = sparse_op<double>(A, TVAL3_PREC_FP32_F64VEC);
+                h->q = make_df64_view(h->d);
+            } else if (precision == TVAL3_PREC_FP64 || precision == TVAL3_PREC_FP32_F64VEC) {
                 h->dbl = 1;
                 h->d = sparse_op<double>(A, precision);
             } else {
@@ -367,16 +393,17 @@ tval3_status tval3_op_create_geometry(tval3_op* op, const tval3_geometry_host* G
     return guard([&] {
         if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
         if (mode < 0 || mode > 1) arg_error(TVAL3_ERR_ARG, "Argument error: unknown geometry mode!");
-        if (precision == TVAL3_PREC_FP64 || precision < 0 || precision > 4)
+        if (precision == TVAL3_PREC_FP64 || precision < 0 || precision > 5)
             arg_error(TVAL3_ERR_UNSUPPORTED, "geometry operators store FP32/BF16/FP16 values");
         if (mode == 1 && precision != TVAL3_PREC_FP32)
             arg_error(TVAL3_ERR_UNSUPPORTED, "on-the-fly traversal stores nothing; use FP32");
         auto* h = new tval3_op_s();
         try {
             h->precision = precision;
-            if (precision == TVAL3_PREC_FP32_F64VEC) {
+            if (precision == TVAL3_PREC_FP32_F64VEC || precision == TVAL3_PREC_FP32_DF64) {
                 h->dbl = 1;
-                h->d = make_geometry_op<double>(G, mode, precision, 0);
+                h->d = make_geometry_op<double>(G, mode, TVAL3_PREC_FP32_F64VEC, 0);
+                if (precision == TVAL3_PREC_FP32_DF64) h->q = make_df64_view(h->d);
             } else {
                 h->f = make_geometry_op<float>(G, mode, precision, 0);
             }
@@ -466,7 +493,8 @@ tval3_status tval3_solver_create(tval3_solver* s, tval3_op A, int dim_y, int dim
         auto* h = new tval3_solver_s();
         try {
             h->dbl = A->dbl;
-            if (A->dbl) h->d = new Solver<double>(A->d, dim_y, dim_x, dim_z, *opts);
+            if (A->q) h->q = new Solver<df64>(A->q, dim_y, dim_x, dim_z, *opts);
+            else if (A->dbl) h->d = new Solver<double>(A->d, dim_y, dim_x, dim_z, *opts);
             else h->f = new Solver<float>(A->f, dim_y, dim_x, dim_z, *opts);
         } catch (...) {
             delete h;
@@ -479,8 +507,7 @@ tval3_status tval3_solver_create(tval3_solver* s, tval3_op A, int dim_y, int dim
 tval3_status tval3_solver_set_mode(tval3_solver s, int mode) {
     return guard([&] {
         if (!s || mode < 0 || mode > 1) arg_error(TVAL3_ERR_ARG, "Argument error: bad solver mode!");
-        if (s->dbl) s->d->mode = mode;
-        else s->f->mode = mode;
+        with_solver(s, [&](auto& v) { v.mode = mode; });
     });
 }
 
@@ -488,31 +515,25 @@ tval3_status tval3_solver_solve(tval3_solver s, const void* d_b, void* d_U, cons
                                 void* stream) {
     return guard([&] {
         if (!s || !d_b || !d_U) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver or vector!");
-        if (s->dbl) s->d->solve((const double*)d_b, (double*)d_U, (const double*)d_Ut, info, (cudaStream_t)stream);
-        else s->f->solve((const float*)d_b, (float*)d_U, (const float*)d_Ut, info, (cudaStream_t)stream);
+        with_solver(s, [&](auto& v) { v.solve(d_b, d_U, d_Ut, info, (cudaStream_t)stream); });
     });
 }
 
 tval3_status tval3_solver_set_trace(tval3_solver s, const void* d_xstar) {
     return guard([&] {
         if (!s) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver!");
-        if (s->dbl) {
-            s->d->xstar = (const double*)d_xstar;
-            s->d->gexec ? (void)cudaGraphExecDestroy(s->d->gexec) : (void)0;
-            s->d->gexec = nullptr;
-        } else {
-            s->f->xstar = (const float*)d_xstar;
-            s->f->gexec ? (void)cudaGraphExecDestroy(s->f->gexec) : (void)0;
-            s->f->gexec = nullptr;
-        }
+        with_solver(s, [&](auto& v) {
+            v.xstar = d_xstar;
+            if (v.gexec) cudaGraphExecDestroy(v.gexec);
+            v.gexec = nullptr;
+        });
     });
 }
 
 tval3_status tval3_solver_trace(tval3_solver s, double* host_err, int len) {
     return guard([&] {
         if (!s || !host_err) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver or buffer!");
-        if (s->dbl) s->d->read_trace(host_err, len);
-        else s->f->read_trace(host_err, len);
+        with_solver(s, [&](auto& v) { v.read_trace(host_err, len); });
     });
 }
 

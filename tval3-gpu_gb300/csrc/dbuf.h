@@ -11,6 +11,7 @@ template <class T>
 struct DBuf {
     T* p = nullptr;
     size_t n = 0;
+    bool own = true;  // false: a view of another buffer (never freed here)
     DBuf() {}
     explicit DBuf(size_t n_) { alloc(n_); }
     void alloc(size_t n_) {
@@ -22,15 +23,22 @@ struct DBuf {
             n = n_;
         }
     }
+    void view(T* q, size_t n_) {
+        release();
+        p = q;
+        n = n_;
+        own = false;
+    }
     void release() {
-        if (p) cudaFree(p);
+        if (p && own) cudaFree(p);
         p = nullptr;
         n = 0;
+        own = true;
     }
     ~DBuf() { release(); }
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
-    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) {
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), own(o.own) {
         o.p = nullptr;
         o.n = 0;
     }
@@ -39,6 +47,7 @@ struct DBuf {
             release();
             p = o.p;
             n = o.n;
+            own = o.own;
             o.p = nullptr;
             o.n = 0;
         }

@@ -65,8 +65,8 @@ struct SolverBufs {
     T* b;          // m, scaled
     T* delta;      // m
     T* rcdU;
-    const T* xstar;   // optional reference solution (unscaled) for the relerr trace
-    double* trace;    // optional per-iteration relative error vs xstar
+    const void* xstar;  // optional reference solution (unscaled, caller type) for the relerr trace
+    double* trace;      // optional per-iteration error norm vs xstar
     int use_dtsatd;
     Ctl* ctl;
     double* part;
@@ -87,7 +87,9 @@ enum CondSrc : int { COND_FST = 0, COND_RESTART = 1, COND_ONE = 2, COND_NOT_DONE
 void launch_cond(Ctl* ctl, unsigned long long handle, int src, cudaStream_t s);
 
 // stencil.cu
-template <class T> void launch_scale_b(const T* b_in, SolverBufs<T>& B, cudaStream_t s);
+// b_in, U_out and Ut are caller-facing arrays: float for float vectors,
+// double for double and double-float vectors.
+template <class T> void launch_scale_b(const void* b_in, SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_D_only(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_descend(SolverBufs<T>& B, int restart, cudaStream_t s);
 template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s);
@@ -99,7 +101,7 @@ template <class T> void launch_backtrack(SolverBufs<T>& B, int setup, cudaStream
 template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_mlp(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_outer_grad(SolverBufs<T>& B, cudaStream_t s);
-template <class T> void launch_finalize(SolverBufs<T>& B, T* U_out, const T* Ut, cudaStream_t s);
+template <class T> void launch_finalize(SolverBufs<T>& B, void* U_out, const void* Ut, cudaStream_t s);
 
 // Standalone operators (tval3_D / tval3_Dt entry points).
 template <class T> void launch_D_plain(int p, int q, int r, const T* U, T* DU3, cudaStream_t s);

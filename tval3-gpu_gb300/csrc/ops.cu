@@ -346,6 +346,34 @@ LinOp<double>* make_csr_op_f64vec(long rows, long cols, long nnz, const int* d_p
 }
 
 template <>
+void export_vals<df64, float>(const CsrOp<df64, float>& op, float* hval, float* htval) {
+    if (hval) TV3_CUDA(cudaMemcpy(hval, op.val.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
+    if (htval) TV3_CUDA(cudaMemcpy(htval, op.tval.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
+}
+
+// Double-float view of an FP32-value / FP64-vector CSR operator: the same
+// device arrays (not copied, not freed by the view), products in df64.
+LinOp<df64>* make_df64_view(const LinOp<double>* base) {
+    auto* b = dynamic_cast<const CsrOp<double, float>*>(base);
+    if (!b) throw Error{7, "double-float products need an FP32-value CSR operator"};
+    auto* op = new CsrOp<df64, float>();
+    op->m = b->m; op->n = b->n; op->nnz = b->nnz; op->kind = b->kind;
+    op->ptr.view(b->ptr.p, b->ptr.n);
+    op->ind.view(b->ind.p, b->ind.n);
+    op->tptr.view(b->tptr.p, b->tptr.n);
+    op->tind.view(b->tind.p, b->tind.n);
+    op->val.view(b->val.p, b->val.n);
+    op->tval.view(b->tval.p, b->tval.n);
+    try {
+        finish_layout(op);
+    } catch (...) {
+        delete op;
+        throw;
+    }
+    return op;
+}
+
+template <>
 LinOp<double>* make_csr_op_device<double>(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind,
                                           const double* d_val, const int* d_tptr, const int* d_tind,
                                           const double* d_tval, int precision, cudaStream_t s) {

@@ -94,6 +94,10 @@ LinOp<double>* make_csr_op_f64vec(long rows, long cols, long nnz, const int* d_p
                                   const float* d_val, const int* d_tptr, const int* d_tind, const float* d_tval,
                                   cudaStream_t s);
 
+// Double-float products over the arrays of an FP32-value / FP64-vector CSR
+// operator (precision TVAL3_PREC_FP32_DF64); the view does not own the arrays.
+LinOp<df64>* make_df64_view(const LinOp<double>* base);
+
 // Ray-geometry operators (ray.cu).
 struct RayList;  // compacted ray list and geometry on the device
 template <class T>

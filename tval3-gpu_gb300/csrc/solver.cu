@@ -130,7 +130,7 @@ void Solver<T>::tau_first(cudaStream_t s) {
 
 // start-up (:1115-1149)
 template <class T>
-void Solver<T>::setup(const T* d_b, cudaStream_t s) {
+void Solver<T>::setup(const void* d_b, cudaStream_t s) {
     init_ctl(s);
     TV3_CUDA(cudaMemsetAsync(B.sig, 0, 3 * n * sizeof(T), s));
     TV3_CUDA(cudaMemsetAsync(B.DtsAtd, 0, n * sizeof(T), s));
@@ -235,7 +235,7 @@ struct Body {
 }  // namespace
 
 template <class T>
-void Solver<T>::build_graph(const T* d_b, T* d_U, const T* d_Ut, cudaStream_t s) {
+void Solver<T>::build_graph(const void* d_b, void* d_U, const void* d_Ut, cudaStream_t s) {
     if (gexec) {
         cudaGraphExecDestroy(gexec);
         gexec = nullptr;
@@ -339,7 +339,7 @@ void Solver<T>::build_graph(const T* d_b, T* d_U, const T* d_Ut, cudaStream_t s)
 }
 
 template <class T>
-void Solver<T>::solve(const T* d_b, T* d_U, const T* d_Ut, tval3_info* info, cudaStream_t s) {
+void Solver<T>::solve(const void* d_b, void* d_U, const void* d_Ut, tval3_info* info, cudaStream_t s) {
     B.xstar = xstar;
     cudaEvent_t e0, e1;
     TV3_CUDA(cudaEventCreate(&e0));
@@ -383,5 +383,6 @@ void Solver<T>::read_trace(double* host, int len) {
 
 template struct Solver<float>;
 template struct Solver<double>;
+template struct Solver<df64>;
 
 }  // namespace tv3

@@ -93,12 +93,12 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs<T, V> a) {
                 if (xs && k >= beg && k < end) xv[e] *= (T)__ldg(xs + cc[e]);
             }
 #pragma unroll
-            for (int e = 0; e < 4; ++e) s += (T)v0[e] * xv[e];
+            for (int e = 0; e < 4; ++e) madd(s, v0[e], xv[e]);
 #pragma unroll
-            for (int e = 0; e < 4; ++e) s += (T)v1[e] * xv[4 + e];
+            for (int e = 0; e < 4; ++e) madd(s, v1[e], xv[4 + e]);
         }
 #pragma unroll
-        for (int o = G / 2; o; o >>= 1) s += __shfl_down_sync(gmask, s, o, G);
+        for (int o = G / 2; o; o >>= 1) s += shfl_down(gmask, s, o, G);
         if (lane == 0) {
             if (a.rscale) s *= (T)__ldg(a.rscale + r);
             if (EPI == SPMV_PLAIN) {
@@ -107,11 +107,12 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs<T, V> a) {
                 y[r] = s - a.sub[r];
             } else if (EPI == SPMV_LAM35) {
                 y[r] = s;
-                double t = (double)s - (double)a.b[r];
+                double t = acc_d(to_acc(s) - to_acc(a.b[r]));
                 acc0 += t * t;
-                acc1 += (double)a.delta[r] * t;
+                acc1 += acc_d(to_acc(a.delta[r])) * t;
             } else if (EPI == SPMV_NORM2) {
-                acc0 += (double)s * (double)s;
+                const double sd = acc_d(to_acc(s));
+                acc0 += sd * sd;
             }
         }
     }
@@ -154,6 +155,7 @@ void launch_spmv(const SpmvArgs<T, V>& a, int epi, int G, int grid, cudaStream_t
 template void launch_spmv<float, float>(const SpmvArgs<float, float>&, int, int, int, cudaStream_t);
 template void launch_spmv<double, double>(const SpmvArgs<double, double>&, int, int, int, cudaStream_t);
 template void launch_spmv<double, float>(const SpmvArgs<double, float>&, int, int, int, cudaStream_t);
+template void launch_spmv<df64, float>(const SpmvArgs<df64, float>&, int, int, int, cudaStream_t);
 template void launch_spmv<float, __nv_bfloat16>(const SpmvArgs<float, __nv_bfloat16>&, int, int, int, cudaStream_t);
 template void launch_spmv<float, __half>(const SpmvArgs<float, __half>&, int, int, int, cudaStream_t);
 

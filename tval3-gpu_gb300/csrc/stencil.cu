@@ -3,6 +3,8 @@
 // updates, each fused with the reductions the loop needs.  Every reducing
 // kernel ends in a deterministic grid reduction whose last block updates the
 // device control block (tval3_internal.cuh), so no value crosses to the host.
+// The element type T is float, double or df64 (double-float on the FP32
+// pipes); per-thread sums use acc_t<T>.
 //
 // Reference counterparts (3d/tval3_gpu_3d.cpp unless noted):
 //   k_D_only / k_descend   D_gpu :271-314 (+ axpy and nonneg_kernel, :671-701)
@@ -21,23 +23,50 @@
 
 namespace tv3 {
 
+// Division of a voxel index by the invariant dimensions with one high
+// multiply (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", 1994): q = (umulhi(i, M) + i) >> L with L = ceil(log2 d),
+// M = floor(2^32 (2^L - d) / d) + 1; exact for i < 2^31.
+struct FastDiv {
+    unsigned d, M, L;
+};
+static FastDiv make_div(unsigned d) {
+    FastDiv f;
+    f.d = d;
+    unsigned L = 0;
+    while ((1ull << L) < d) ++L;
+    f.L = L;
+    f.M = (unsigned)((((1ull << L) - d) << 32) / d + 1);
+    return f;
+}
+__device__ __forceinline__ unsigned fdiv(unsigned i, const FastDiv& f) {
+    return (unsigned)(((unsigned long long)__umulhi(i, f.M) + i) >> f.L);
+}
+
+struct Geo {
+    FastDiv p, q;
+    int r;
+};
+
 struct Nb {
     long yp, ym, xp, xm, zp, zm;
 };
 
-__device__ __forceinline__ Nb neighbours(int p, int q, int r, long i) {
-    const long pq = (long)p * q;
-    const int y = (int)(i % p);
-    const long t = i / p;
-    const int x = (int)(t % q);
-    const int z = (int)(t / q);
+__device__ __forceinline__ Nb neighbours(const Geo& g, long i) {
+    const unsigned ui = (unsigned)i;
+    const unsigned t = fdiv(ui, g.p);
+    const int y = (int)(ui - t * g.p.d);
+    const unsigned zz = fdiv(t, g.q);
+    const int x = (int)(t - zz * g.q.d);
+    const int z = (int)zz;
+    const long p = g.p.d, q = g.q.d, pq = p * q;
     Nb o;
-    o.yp = (y + 1 < p) ? i + 1 : i - y;
+    o.yp = (y + 1 < (int)p) ? i + 1 : i - y;
     o.ym = (y > 0) ? i - 1 : i + (p - 1);
-    o.xp = (x + 1 < q) ? i + p : i - (long)x * p;
-    o.xm = (x > 0) ? i - p : i + (long)(q - 1) * p;
-    o.zp = (z + 1 < r) ? i + pq : i - (long)z * pq;
-    o.zm = (z > 0) ? i - pq : i + (long)(r - 1) * pq;
+    o.xp = (x + 1 < (int)q) ? i + p : i - (long)x * p;
+    o.xm = (x > 0) ? i - p : i + (q - 1) * p;
+    o.zp = (z + 1 < g.r) ? i + pq : i - (long)z * pq;
+    o.zm = (z > 0) ? i - pq : i + (long)(g.r - 1) * pq;
     return o;
 }
 
@@ -45,13 +74,19 @@ __device__ __forceinline__ Nb neighbours(int p, int q, int r, long i) {
 
 template <class T> __device__ __forceinline__ T proj(T v, int nonneg) { return (nonneg && v < T(0)) ? T(0) : v; }
 
+// x / beta: division as in the reference for float and double; for df64 the
+// caller passes 1/beta and multiplies (same value to ~1e-15, a tenth of the
+// cost of a double-float division)
+template <class T> __device__ __forceinline__ T div_beta(T x, T bt, T) { return x / bt; }
+template <> __device__ __forceinline__ df64 div_beta<df64>(df64 x, df64, df64 ibt) { return x * ibt; }
+
 // ---------------------------------------------------------------------------
 // b scaling (scaleb_gpu :226-266): one block finds the entries of smallest and
 // largest |b| (first occurrence on ties, as the reference's strict scan), the
 // next kernel writes b*scl.
 // ---------------------------------------------------------------------------
-template <class T>
-__global__ void __launch_bounds__(1024) k_scale_find(const T* __restrict__ b, long m, Ctl* ctl) {
+template <class E>
+__global__ void __launch_bounds__(1024) k_scale_find(const E* __restrict__ b, long m, Ctl* ctl) {
     count_launch(ctl);
     double amin = INFINITY, amax = -1.0;
     long imin = -1, imax = -1;
@@ -96,23 +131,23 @@ __global__ void __launch_bounds__(1024) k_scale_find(const T* __restrict__ b, lo
 }
 
 template <class T>
-__global__ void k_scale_apply(const T* __restrict__ b_in, T* __restrict__ b, long m, Ctl* ctl) {
+__global__ void k_scale_apply(const Ext<T>* __restrict__ b_in, T* __restrict__ b, long m, Ctl* ctl) {
     count_launch(ctl);
     const double scl = ctl->scl;
-    const T s = (T)scl;
-    GRID_STRIDE(i, m) b[i] = (scl == 1.0) ? b_in[i] : b_in[i] * s;
+    const Ext<T> s = (Ext<T>)scl;
+    GRID_STRIDE(i, m) b[i] = from_ext<T>((scl == 1.0) ? b_in[i] : b_in[i] * s);
 }
 
 // ---------------------------------------------------------------------------
 // D at start-up: DU[0] = D U[0]
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void k_D_only(SolverBufs<T> B) {
+__global__ void k_D_only(SolverBufs<T> B, Geo g) {
     count_launch(B.ctl);
     const T* __restrict__ U = B.U[0];
     T* __restrict__ DU = B.DU[0];
     GRID_STRIDE(i, B.n) {
-        Nb nb = neighbours(B.p, B.q, B.r, i);
+        Nb nb = neighbours(g, i);
         T u = U[i];
         DU[i] = U[nb.yp] - u;
         DU[B.n + i] = U[nb.xp] - u;
@@ -129,7 +164,7 @@ __global__ void k_D_only(SolverBufs<T> B) {
 // :878) and writes the current one.
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void k_descend(SolverBufs<T> B, int restart) {
+__global__ void k_descend(SolverBufs<T> B, Geo g, int restart) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     const int cur = ctl->parity;
@@ -138,10 +173,10 @@ __global__ void k_descend(SolverBufs<T> B, int restart) {
     const T* __restrict__ d = B.d;
     T* __restrict__ U = B.U[dst];
     T* __restrict__ DU = B.DU[dst];
-    const T mt = (T)(-ctl->tau);
+    const T mt = scal<T>(-ctl->tau);
     const int nn = ctl->nonneg;
     GRID_STRIDE(i, B.n) {
-        Nb nb = neighbours(B.p, B.q, B.r, i);
+        Nb nb = neighbours(g, i);
         T uc = proj(Up[i] + mt * d[i], nn);
         T uy = proj(Up[nb.yp] + mt * d[nb.yp], nn);
         T ux = proj(Up[nb.xp] + mt * d[nb.xp], nn);
@@ -161,18 +196,19 @@ __global__ void k_descend(SolverBufs<T> B, int restart) {
 // first inner iteration: ||D d||^2 and <d,d>
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void k_Dd_norm(SolverBufs<T> B) {
+__global__ void k_Dd_norm(SolverBufs<T> B, Geo g) {
     count_launch(B.ctl);
+    using A = acc_t<T>;
     const T* __restrict__ d = B.d;
-    double s0 = 0.0, s1 = 0.0;
+    A s0(0.f), s1(0.f);
     GRID_STRIDE(i, B.n) {
-        Nb nb = neighbours(B.p, B.q, B.r, i);
+        Nb nb = neighbours(g, i);
         T dc = d[i];
-        T a = d[nb.yp] - dc, b = d[nb.xp] - dc, c = d[nb.zp] - dc;
-        s0 += (double)a * a + (double)b * b + (double)c * c;
-        s1 += (double)dc * dc;
+        A a = to_acc(d[nb.yp] - dc), b = to_acc(d[nb.xp] - dc), c = to_acc(d[nb.zp] - dc), e = to_acc(dc);
+        s0 += a * a + b * b + c * c;
+        s1 += e * e;
     }
-    double v[2] = {s0, s1}, tot[2];
+    double v[2] = {acc_d(s0), acc_d(s1)}, tot[2];
     if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         B.ctl->dDd = tot[0];
         B.ctl->dd = tot[1];
@@ -186,20 +222,21 @@ template <class T>
 __global__ void k_tau(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
+    using A = acc_t<T>;
     const int cur = ctl->parity, prv = 1 - cur;
-    const double mdb = ctl->muDbeta;
+    const A mdb = scal<A>(ctl->muDbeta);
     const T *__restrict__ U = B.U[cur], *__restrict__ Up = B.U[prv];
     const T *__restrict__ g = B.g[cur], *__restrict__ gp = B.g[prv];
     const T *__restrict__ g2 = B.g2[cur], *__restrict__ g2p = B.g2[prv];
-    double ss = 0.0, sy = 0.0;
+    A ss(0.f), sy(0.f);
     GRID_STRIDE(i, B.n) {
-        double u = (double)U[i] - (double)Up[i];
-        double dg = (double)g[i] - (double)gp[i];
-        double dg2 = (double)g2[i] - (double)g2p[i];
+        A u = to_acc(U[i]) - to_acc(Up[i]);
+        A dg = to_acc(g[i]) - to_acc(gp[i]);
+        A dg2 = to_acc(g2[i]) - to_acc(g2p[i]);
         ss += u * u;
         sy += u * (dg2 + mdb * dg);
     }
-    double v[2] = {ss, sy}, tot[2];
+    double v[2] = {acc_d(ss), acc_d(sy)}, tot[2];
     if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) ctl->tau = fabs(tot[0] / tot[1]);
 }
 
@@ -217,27 +254,29 @@ __device__ __forceinline__ void armijo(Ctl* c) {
 // g2 = D^T (DU - W) with lam2 = ||DU - W||^2 and lam4 = <sigma, DU - W>.
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void k_g2(SolverBufs<T> B, int mode) {
+__global__ void k_g2(SolverBufs<T> B, Geo g, int mode) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
+    using A = acc_t<T>;
     const int cur = ctl->parity;
     const long n = B.n;
     const T* __restrict__ DU = B.DU[cur];
     const T* __restrict__ W = B.W;
     const T* __restrict__ S = B.sig;
     T* __restrict__ g2 = B.g2[cur];
-    double l2 = 0.0, l4 = 0.0;
+    A l2(0.f), l4(0.f);
     GRID_STRIDE(i, n) {
-        Nb nb = neighbours(B.p, B.q, B.r, i);
+        Nb nb = neighbours(g, i);
         T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
         T v0m = DU[nb.ym] - W[nb.ym];
         T v1m = DU[n + nb.xm] - W[n + nb.xm];
         T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
         g2[i] = v0m - v0 + v1m - v1 + v2m - v2;
-        l2 += (double)v0 * v0 + (double)v1 * v1 + (double)v2 * v2;
-        l4 += (double)v0 * S[i] + (double)v1 * S[n + i] + (double)v2 * S[2 * n + i];
+        A a0 = to_acc(v0), a1 = to_acc(v1), a2 = to_acc(v2);
+        l2 += a0 * a0 + a1 * a1 + a2 * a2;
+        l4 += a0 * to_acc(S[i]) + a1 * to_acc(S[n + i]) + a2 * to_acc(S[2 * n + i]);
     }
-    double v[2] = {l2, l4}, tot[2];
+    double v[2] = {acc_d(l2), acc_d(l4)}, tot[2];
     if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->lam2 = tot[0];
         ctl->lam4 = tot[1];
@@ -271,16 +310,19 @@ template <class T>
 __global__ void k_shrink(SolverBufs<T> B, int mode) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
+    using A = acc_t<T>;
     const int cur = ctl->parity;
     const long n = B.n;
     const T* __restrict__ DU = B.DU[cur];
     const T* __restrict__ S = B.sig;
     T* __restrict__ W = B.W;
-    const T bt = (T)ctl->beta, ib = (T)(1.0 / ctl->beta);
+    const T bt = scal<T>(ctl->beta), ib = scal<T>(1.0 / ctl->beta);
     const int iso = ctl->iso;
-    double l1 = 0.0;
+    A l1(0.f);
     GRID_STRIDE(i, n) {
-        T u0 = DU[i] - S[i] / bt, u1 = DU[n + i] - S[n + i] / bt, u2 = DU[2 * n + i] - S[2 * n + i] / bt;
+        T u0 = DU[i] - div_beta(S[i], bt, ib);
+        T u1 = DU[n + i] - div_beta(S[n + i], bt, ib);
+        T u2 = DU[2 * n + i] - div_beta(S[2 * n + i], bt, ib);
         if (!iso) {
             T t0 = fabs(u0) - ib, t1 = fabs(u1) - ib, t2 = fabs(u2) - ib;
             t0 = (t0 >= T(0)) ? t0 : T(0);
@@ -289,19 +331,19 @@ __global__ void k_shrink(SolverBufs<T> B, int mode) {
             W[i] = (u0 >= T(0)) ? t0 : -t0;
             W[n + i] = (u1 >= T(0)) ? t1 : -t1;
             W[2 * n + i] = (u2 >= T(0)) ? t2 : -t2;
-            l1 += (double)t0 + (double)t1 + (double)t2;
+            l1 += to_acc(t0) + to_acc(t1) + to_acc(t2);
         } else {
             T nv = sqrt(u0 * u0 + u1 * u1 + u2 * u2);
             T t = nv - ib;
             t = (t > T(0)) ? t : T(0);
-            T sc = (nv > T(0)) ? t / nv : T(0);
+            T sc = (t > T(0)) ? t / nv : T(0);
             W[i] = u0 * sc;
             W[n + i] = u1 * sc;
             W[2 * n + i] = u2 * sc;
-            l1 += (double)t;
+            l1 += to_acc(t);
         }
     }
-    double v[1] = {l1}, tot[1];
+    double v[1] = {acc_d(l1)}, tot[1];
     if (grid_reduce<1>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         if (mode == EPI_G2_UPDATE_W) ctl->f -= ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
         ctl->lam1 = tot[0];
@@ -316,30 +358,33 @@ template <class T>
 __global__ void k_gradient(SolverBufs<T> B, int iter) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
+    using A = acc_t<T>;
     const int cur = ctl->parity, prv = 1 - cur;
-    const T mdb = (T)ctl->muDbeta;
+    const T mdb = scal<T>(ctl->muDbeta);
     const T *__restrict__ g = B.g[cur], *__restrict__ g2 = B.g2[cur], *__restrict__ dts = B.DtsAtd;
     const T *__restrict__ U = B.U[cur], *__restrict__ Up = B.U[prv];
-    const T* __restrict__ xs = B.xstar;
+    const Ext<T>* __restrict__ xs = static_cast<const Ext<T>*>(B.xstar);
     const double iscl = 1.0 / ctl->scl;
     T* __restrict__ d = B.d;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    A s0(0.f), s1(0.f), s2(0.f);
+    double s3 = 0.0;
     GRID_STRIDE(i, B.n) {
         T di = mdb * g[i] + g2[i] + dts[i];
         d[i] = di;
-        s2 += (double)di * di;
+        A ad = to_acc(di);
+        s2 += ad * ad;
         if (iter) {
-            T u = U[i], up = Up[i];
-            T du = u - up;
-            s0 += (double)up * up;
-            s1 += (double)du * du;
+            A u = to_acc(U[i]), up = to_acc(Up[i]);
+            A du = u - up;
+            s0 += up * up;
+            s1 += du * du;
             if (xs) {
-                double e = (double)u * iscl - (double)xs[i];
+                double e = acc_d(u) * iscl - (double)xs[i];
                 s3 += e * e;
             }
         }
     }
-    double v[4] = {s0, s1, s2, s3}, tot[4];
+    double v[4] = {acc_d(s0), acc_d(s1), acc_d(s2), s3}, tot[4];
     if (grid_reduce<4>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->dd = tot[2];
         if (!iter) {
@@ -365,15 +410,16 @@ template <class T>
 __global__ void k_backtrack(SolverBufs<T> B, int setup) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
+    using A = acc_t<T>;
     const int cur = ctl->parity, prv = 1 - cur;
     const long n = B.n, m = B.m;
-    const T al = (T)ctl->alpha;
+    const T al = scal<T>(ctl->alpha);
     T *__restrict__ U = B.U[cur], *__restrict__ g = B.g[cur], *__restrict__ g2 = B.g2[cur];
     T *__restrict__ DU = B.DU[cur], *__restrict__ Au = B.Au[cur];
     const T *__restrict__ Up = B.U[prv], *__restrict__ gp = B.g[prv], *__restrict__ g2p = B.g2[prv];
     const T *__restrict__ DUp = B.DU[prv], *__restrict__ Aup = B.Au[prv];
     const T *__restrict__ W = B.W, *__restrict__ S = B.sig, *__restrict__ bb = B.b, *__restrict__ dl = B.delta;
-    double l2 = 0.0, l4 = 0.0, l3 = 0.0, l5 = 0.0;
+    A l2(0.f), l4(0.f), l3(0.f), l5(0.f);
     const long N = n > m ? n : m;
     GRID_STRIDE(i, N) {
         if (i < n) {
@@ -396,9 +442,9 @@ __global__ void k_backtrack(SolverBufs<T> B, int setup) {
             U[i] = Up[i] + al * du;
             T e0 = DUp[i] + al * d0, e1 = DUp[n + i] + al * d1, e2 = DUp[2 * n + i] + al * d2;
             DU[i] = e0; DU[n + i] = e1; DU[2 * n + i] = e2;
-            T v0 = e0 - W[i], v1 = e1 - W[n + i], v2 = e2 - W[2 * n + i];
-            l2 += (double)v0 * v0 + (double)v1 * v1 + (double)v2 * v2;
-            l4 += (double)v0 * S[i] + (double)v1 * S[n + i] + (double)v2 * S[2 * n + i];
+            A v0 = to_acc(e0 - W[i]), v1 = to_acc(e1 - W[n + i]), v2 = to_acc(e2 - W[2 * n + i]);
+            l2 += v0 * v0 + v1 * v1 + v2 * v2;
+            l4 += v0 * to_acc(S[i]) + v1 * to_acc(S[n + i]) + v2 * to_acc(S[2 * n + i]);
         }
         if (i < m) {
             T da;
@@ -410,12 +456,12 @@ __global__ void k_backtrack(SolverBufs<T> B, int setup) {
             }
             T a = Aup[i] + al * da;
             Au[i] = a;
-            double t = (double)a - (double)bb[i];
+            A t = to_acc(a) - to_acc(bb[i]);
             l3 += t * t;
-            l5 += (double)dl[i] * t;
+            l5 += to_acc(dl[i]) * t;
         }
     }
-    double v[4] = {l2, l4, l3, l5}, tot[4];
+    double v[4] = {acc_d(l2), acc_d(l4), acc_d(l3), acc_d(l5)}, tot[4];
     if (grid_reduce<4>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->lam2 = tot[0];
         ctl->lam4 = tot[1];
@@ -440,16 +486,17 @@ template <class T>
 __global__ void k_outer_relchg(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
+    using A = acc_t<T>;
     const T* __restrict__ U = B.U[ctl->parity];
     T* __restrict__ R = B.rcdU;
-    double s = 0.0;
+    A s(0.f);
     GRID_STRIDE(i, B.n) {
         T u = U[i];
-        double e = (double)u - (double)R[i];
+        A e = to_acc(u) - to_acc(R[i]);
         s += e * e;
         R[i] = u;
     }
-    double v[1] = {s}, tot[1];
+    double v[1] = {acc_d(s)}, tot[1];
     if (grid_reduce<1>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->count_outer += 1;
         ctl->relchgout = sqrt(tot[0]) / ctl->nrmup;
@@ -482,12 +529,13 @@ template <class T>
 __global__ void k_mlp(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
+    using A = acc_t<T>;
     const int cur = ctl->parity;
     const long n = B.n, m = B.m;
-    const T bt = (T)ctl->beta, mut = (T)ctl->mu;
+    const T bt = scal<T>(ctl->beta), mut = scal<T>(ctl->mu);
     const T *__restrict__ DU = B.DU[cur], *__restrict__ W = B.W, *__restrict__ Au = B.Au[cur], *__restrict__ bb = B.b;
     T *__restrict__ S = B.sig, *__restrict__ dl = B.delta;
-    double l4 = 0.0, l5 = 0.0;
+    A l4(0.f), l5(0.f);
     const long N = n > m ? n : m;
     GRID_STRIDE(i, N) {
         if (i < n) {
@@ -496,17 +544,17 @@ __global__ void k_mlp(SolverBufs<T> B) {
                 T v = DU[a * n + i] - W[a * n + i];
                 T s = S[a * n + i] - bt * v;
                 S[a * n + i] = s;
-                l4 += (double)s * v;
+                l4 += to_acc(s) * to_acc(v);
             }
         }
         if (i < m) {
             T aub = Au[i] - bb[i];
             T dv = dl[i] - mut * aub;
             dl[i] = dv;
-            l5 += (double)dv * aub;
+            l5 += to_acc(dv) * to_acc(aub);
         }
     }
-    double v[2] = {l4, l5}, tot[2];
+    double v[2] = {acc_d(l4), acc_d(l5)}, tot[2];
     if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->f += ctl->lam4 + ctl->lam5;
         ctl->lam4 = tot[0];
@@ -526,20 +574,22 @@ template <class T>
 __global__ void k_outer_grad(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
+    using A = acc_t<T>;
     const int cur = ctl->parity;
-    const T ratio = (T)(ctl->beta_prev / ctl->beta);
-    const T mdb = (T)ctl->muDbeta;
+    const T ratio = scal<T>(ctl->beta_prev / ctl->beta);
+    const T mdb = scal<T>(ctl->muDbeta);
     const T *__restrict__ g = B.g[cur], *__restrict__ g2 = B.g2[cur];
     T *__restrict__ d = B.d, *__restrict__ dts = B.DtsAtd;
-    double s = 0.0;
+    A s(0.f);
     GRID_STRIDE(i, B.n) {
         T t = ratio * d[i];
         dts[i] = t;
         T di = mdb * g[i] + g2[i] + t;
         d[i] = di;
-        s += (double)di * di;
+        A a = to_acc(di);
+        s += a * a;
     }
-    double v[1] = {s}, tot[1];
+    double v[1] = {acc_d(s)}, tot[1];
     if (grid_reduce<1>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->dd = tot[0];
         ctl->gam = ctl->gam0;
@@ -554,15 +604,15 @@ __global__ void k_outer_grad(SolverBufs<T> B) {
 // U_out = U / scl (:1272-1277) and rel_error vs Ut (:1308-1324)
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void k_finalize(SolverBufs<T> B, T* __restrict__ out, const T* __restrict__ Ut) {
+__global__ void k_finalize(SolverBufs<T> B, Ext<T>* __restrict__ out, const Ext<T>* __restrict__ Ut) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     const T* __restrict__ U = B.U[ctl->parity];
     const double scl = ctl->scl;
-    const T s = (T)scl;
+    const T s = scal<T>(scl);
     double e = 0.0, t = 0.0;
     GRID_STRIDE(i, B.n) {
-        T u = (scl == 1.0) ? U[i] : U[i] / s;
+        Ext<T> u = to_ext<T>((scl == 1.0) ? U[i] : U[i] / s);
         out[i] = u;
         if (Ut) {
             double dv = (double)Ut[i] - (double)u;
@@ -577,9 +627,9 @@ __global__ void k_finalize(SolverBufs<T> B, T* __restrict__ out, const T* __rest
 
 // standalone D and D^T (operator entry points)
 template <class T>
-__global__ void k_D_plain(int p, int q, int r, long n, const T* __restrict__ U, T* __restrict__ DU) {
+__global__ void k_D_plain(Geo g, long n, const T* __restrict__ U, T* __restrict__ DU) {
     GRID_STRIDE(i, n) {
-        Nb nb = neighbours(p, q, r, i);
+        Nb nb = neighbours(g, i);
         T u = U[i];
         DU[i] = U[nb.yp] - u;
         DU[n + i] = U[nb.xp] - u;
@@ -588,9 +638,9 @@ __global__ void k_D_plain(int p, int q, int r, long n, const T* __restrict__ U, 
 }
 
 template <class T>
-__global__ void k_Dt_plain(int p, int q, int r, long n, const T* __restrict__ V, T* __restrict__ out) {
+__global__ void k_Dt_plain(Geo g, long n, const T* __restrict__ V, T* __restrict__ out) {
     GRID_STRIDE(i, n) {
-        Nb nb = neighbours(p, q, r, i);
+        Nb nb = neighbours(g, i);
         out[i] = V[nb.ym] - V[i] + V[n + nb.xm] - V[n + i] + V[2 * n + nb.zm] - V[2 * n + i];
     }
 }
@@ -617,17 +667,33 @@ static int ew_grid(long n) {
     return (int)g;
 }
 
-template <class T> void launch_scale_b(const T* b_in, SolverBufs<T>& B, cudaStream_t s) {
-    k_scale_find<T><<<1, 1024, 0, s>>>(b_in, B.m, B.ctl);
-    k_scale_apply<T><<<ew_grid(B.m), 256, 0, s>>>(b_in, B.b, B.m, B.ctl);
+static Geo geo_of(int p, int q, int r) {
+    Geo g;
+    g.p = make_div((unsigned)p);
+    g.q = make_div((unsigned)q);
+    g.r = r;
+    return g;
 }
-template <class T> void launch_D_only(SolverBufs<T>& B, cudaStream_t s) { k_D_only<T><<<ew_grid(B.n), 256, 0, s>>>(B); }
+template <class T> static Geo geo_of(const SolverBufs<T>& B) { return geo_of(B.p, B.q, B.r); }
+
+template <class T> void launch_scale_b(const void* b_in, SolverBufs<T>& B, cudaStream_t s) {
+    const Ext<T>* b = static_cast<const Ext<T>*>(b_in);
+    k_scale_find<Ext<T>><<<1, 1024, 0, s>>>(b, B.m, B.ctl);
+    k_scale_apply<T><<<ew_grid(B.m), 256, 0, s>>>(b, B.b, B.m, B.ctl);
+}
+template <class T> void launch_D_only(SolverBufs<T>& B, cudaStream_t s) {
+    k_D_only<T><<<ew_grid(B.n), 256, 0, s>>>(B, geo_of(B));
+}
 template <class T> void launch_descend(SolverBufs<T>& B, int restart, cudaStream_t s) {
-    k_descend<T><<<B.grid, 256, 0, s>>>(B, restart);
+    k_descend<T><<<B.grid, 256, 0, s>>>(B, geo_of(B), restart);
 }
-template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s) { k_Dd_norm<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s) {
+    k_Dd_norm<T><<<B.grid, 256, 0, s>>>(B, geo_of(B));
+}
 template <class T> void launch_tau(SolverBufs<T>& B, cudaStream_t s) { k_tau<T><<<B.grid, 256, 0, s>>>(B); }
-template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s) { k_g2<T><<<B.grid, 256, 0, s>>>(B, mode); }
+template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s) {
+    k_g2<T><<<B.grid, 256, 0, s>>>(B, geo_of(B), mode);
+}
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s) {
     k_shrink<T><<<B.grid, 256, 0, s>>>(B, mode);
 }
@@ -640,35 +706,38 @@ template <class T> void launch_backtrack(SolverBufs<T>& B, int setup, cudaStream
 template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s) { k_outer_relchg<T><<<B.grid, 256, 0, s>>>(B); }
 template <class T> void launch_mlp(SolverBufs<T>& B, cudaStream_t s) { k_mlp<T><<<B.grid, 256, 0, s>>>(B); }
 template <class T> void launch_outer_grad(SolverBufs<T>& B, cudaStream_t s) { k_outer_grad<T><<<B.grid, 256, 0, s>>>(B); }
-template <class T> void launch_finalize(SolverBufs<T>& B, T* U_out, const T* Ut, cudaStream_t s) {
-    k_finalize<T><<<B.grid, 256, 0, s>>>(B, U_out, Ut);
+template <class T> void launch_finalize(SolverBufs<T>& B, void* U_out, const void* Ut, cudaStream_t s) {
+    k_finalize<T><<<B.grid, 256, 0, s>>>(B, static_cast<Ext<T>*>(U_out), static_cast<const Ext<T>*>(Ut));
 }
 template <class T> void launch_D_plain(int p, int q, int r, const T* U, T* DU3, cudaStream_t s) {
     long n = (long)p * q * r;
-    k_D_plain<T><<<ew_grid(n), 256, 0, s>>>(p, q, r, n, U, DU3);
+    k_D_plain<T><<<ew_grid(n), 256, 0, s>>>(geo_of(p, q, r), n, U, DU3);
 }
 template <class T> void launch_Dt_plain(int p, int q, int r, const T* V3, T* out, cudaStream_t s) {
     long n = (long)p * q * r;
-    k_Dt_plain<T><<<ew_grid(n), 256, 0, s>>>(p, q, r, n, V3, out);
+    k_Dt_plain<T><<<ew_grid(n), 256, 0, s>>>(geo_of(p, q, r), n, V3, out);
 }
 
-#define INST(T)                                                                   \
-    template void launch_scale_b<T>(const T*, SolverBufs<T>&, cudaStream_t);      \
-    template void launch_D_only<T>(SolverBufs<T>&, cudaStream_t);                 \
-    template void launch_descend<T>(SolverBufs<T>&, int, cudaStream_t);           \
-    template void launch_Dd_norm<T>(SolverBufs<T>&, cudaStream_t);                \
-    template void launch_tau<T>(SolverBufs<T>&, cudaStream_t);                    \
-    template void launch_g2<T>(SolverBufs<T>&, int, cudaStream_t);                \
-    template void launch_shrink<T>(SolverBufs<T>&, int, cudaStream_t);            \
-    template void launch_gradient<T>(SolverBufs<T>&, int, cudaStream_t);          \
-    template void launch_backtrack<T>(SolverBufs<T>&, int, cudaStream_t);         \
-    template void launch_outer_relchg<T>(SolverBufs<T>&, cudaStream_t);           \
-    template void launch_mlp<T>(SolverBufs<T>&, cudaStream_t);                    \
-    template void launch_outer_grad<T>(SolverBufs<T>&, cudaStream_t);             \
-    template void launch_finalize<T>(SolverBufs<T>&, T*, const T*, cudaStream_t); \
-    template void launch_D_plain<T>(int, int, int, const T*, T*, cudaStream_t);   \
-    template void launch_Dt_plain<T>(int, int, int, const T*, T*, cudaStream_t);
+#define INST(T)                                                                     \
+    template void launch_scale_b<T>(const void*, SolverBufs<T>&, cudaStream_t);     \
+    template void launch_D_only<T>(SolverBufs<T>&, cudaStream_t);                   \
+    template void launch_descend<T>(SolverBufs<T>&, int, cudaStream_t);             \
+    template void launch_Dd_norm<T>(SolverBufs<T>&, cudaStream_t);                  \
+    template void launch_tau<T>(SolverBufs<T>&, cudaStream_t);                      \
+    template void launch_g2<T>(SolverBufs<T>&, int, cudaStream_t);                  \
+    template void launch_shrink<T>(SolverBufs<T>&, int, cudaStream_t);              \
+    template void launch_gradient<T>(SolverBufs<T>&, int, cudaStream_t);            \
+    template void launch_backtrack<T>(SolverBufs<T>&, int, cudaStream_t);           \
+    template void launch_outer_relchg<T>(SolverBufs<T>&, cudaStream_t);             \
+    template void launch_mlp<T>(SolverBufs<T>&, cudaStream_t);                      \
+    template void launch_outer_grad<T>(SolverBufs<T>&, cudaStream_t);               \
+    template void launch_finalize<T>(SolverBufs<T>&, void*, const void*, cudaStream_t);
 INST(float)
 INST(double)
+INST(df64)
+template void launch_D_plain<float>(int, int, int, const float*, float*, cudaStream_t);
+template void launch_D_plain<double>(int, int, int, const double*, double*, cudaStream_t);
+template void launch_Dt_plain<float>(int, int, int, const float*, float*, cudaStream_t);
+template void launch_Dt_plain<double>(int, int, int, const double*, double*, cudaStream_t);
 
 }  // namespace tv3

@@ -12,9 +12,50 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include "df64.cuh"
+
 namespace tv3 {
 
 constexpr unsigned FULL = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Vector element types: float, double, or df64 (double-float, FP32 pipes).
+// Per-thread accumulation of the loop's inner products uses acc_t<T>: double
+// for float and double vectors, df64 for df64 vectors (so no FP64 arithmetic
+// runs per element in the double-float mode); only the block partials become
+// double.  Ext<T> is the caller-facing element type (double for df64).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double to_acc(float v) { return (double)v; }
+__device__ __forceinline__ double to_acc(double v) { return v; }
+__device__ __forceinline__ df64 to_acc(df64 v) { return v; }
+template <class T> using acc_t = decltype(to_acc(T()));
+__device__ __forceinline__ double acc_d(double a) { return a; }
+__device__ __forceinline__ double acc_d(df64 a) { return (double)a; }
+
+template <class T> struct ExtT { using type = T; };
+template <> struct ExtT<df64> { using type = double; };
+template <class T> using Ext = typename ExtT<T>::type;
+
+// conversions between the caller-facing and the internal element type
+template <class T> __device__ __forceinline__ T from_ext(Ext<T> v) { return (T)v; }
+template <> __device__ __forceinline__ df64 from_ext<df64>(double v) { return df64(v); }
+template <class T> __device__ __forceinline__ Ext<T> to_ext(T v) { return (Ext<T>)v; }
+template <> __device__ __forceinline__ double to_ext<df64>(df64 v) { return (double)v; }
+// a double scalar from the control block as an element-type constant
+template <class T> __device__ __forceinline__ T scal(double v) { return (T)v; }
+template <> __device__ __forceinline__ df64 scal<df64>(double v) { return df64(v); }
+
+// s += v * x for an FP32/FP64 matrix value v
+__device__ __forceinline__ void madd(float& s, float v, float x) { s = fmaf(v, x, s); }
+__device__ __forceinline__ void madd(double& s, float v, double x) { s = fma((double)v, x, s); }
+__device__ __forceinline__ void madd(double& s, double v, double x) { s = fma(v, x, s); }
+__device__ __forceinline__ void madd(df64& s, float v, df64 x) { s = s + mul_f(x, v); }
+
+__device__ __forceinline__ float shfl_down(unsigned mask, float v, int o, int w) { return __shfl_down_sync(mask, v, o, w); }
+__device__ __forceinline__ double shfl_down(unsigned mask, double v, int o, int w) { return __shfl_down_sync(mask, v, o, w); }
+__device__ __forceinline__ df64 shfl_down(unsigned mask, df64 v, int o, int w) {
+    return df64(__shfl_down_sync(mask, v.hi, o, w), __shfl_down_sync(mask, v.lo, o, w));
+}
 
 // ---------------------------------------------------------------------------
 // Device-resident control block of one solve.  All scalars of the TVAL3 loop
@@ -93,6 +134,9 @@ template <> struct Acc<float, __half> {
 };
 template <> struct Acc<double, float> {
     __device__ static __forceinline__ double load(const float* p) { return (double)__ldcs(p); }
+};
+template <> struct Acc<df64, float> {
+    __device__ static __forceinline__ df64 load(const float* p) { return df64(__ldcs(p)); }
 };
 
 // ---------------------------------------------------------------------------

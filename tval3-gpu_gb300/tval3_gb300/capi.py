@@ -14,7 +14,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libtval3_gb300.so"
 TVAL3_OK = 0
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_SHAPE", 3: "ERR_CUDA", 4: "ERR_NOMEM", 5: "ERR_TIMEOUT",
           6: "ERR_NONFINITE", 7: "ERR_UNSUPPORTED"}
-PREC_FP32, PREC_FP64, PREC_BF16, PREC_FP16, PREC_FP32_F64VEC = 0, 1, 2, 3, 4
+PREC_FP32, PREC_FP64, PREC_BF16, PREC_FP16, PREC_FP32_F64VEC, PREC_FP32_DF64 = 0, 1, 2, 3, 4, 5
 TV_ANISO, TV_ISO = 0, 1
 SPARSE_CSR, SPARSE_CSC, SPARSE_BOTH = 1, 2, 3
 TRAV_BRESENHAM, TRAV_SIDDON = 0, 1
@@ -36,7 +36,7 @@ class Options(C.Structure):
                 ("maxcnt", C.c_int), ("maxit", C.c_int), ("c", C.c_double), ("gamma", C.c_double),
                 ("gam", C.c_double), ("rate_gam", C.c_double), ("isreal", C.c_int), ("nonneg", C.c_int),
                 ("numInitIterations", C.c_uint), ("skipMulRatio", C.c_double), ("maxRelativeChange", C.c_double),
-                ("tv_type", C.c_int)]
+                ("tv_type", C.c_int), ("precision", C.c_int)]
 
 
 class Info(C.Structure):
