@@ -312,10 +312,7 @@ def run_ours(args):
 
     # ---- roofline of the dominant kernel: CSR SpMV, live CUDA-event timing
     sx = 8 if dt == torch.float64 else 4
-    xv = torch.randn(n, dtype=dt, device=dev)
-    yv = torch.randn(m, dtype=dt, device=dev)
-    outm = torch.empty(m, dtype=dt, device=dev)
-    outn = torch.empty(n, dtype=dt, device=dev)
+    xv, yv, outm, outn = op_vectors(torch, head == "df64", dt, n, m, dev)
     torch.cuda.synchronize()
 
     def time_op(trans, reps=20):
@@ -410,6 +407,18 @@ def run_ours(args):
     return line
 
 
+def op_vectors(torch, pairs, dt, n, m, dev):
+    """x (n), y (m) and outputs in the operator's vector type; double-float
+    operators take {hi, lo} FP32 pairs (the values only need to be finite)."""
+    if pairs:
+        mk = lambda k: torch.randn(2 * k, dtype=torch.float32, device=dev) * torch.tensor(
+            [1.0, 1e-8], device=dev).repeat(k)
+        return mk(n), mk(m), torch.empty(2 * m, dtype=torch.float32, device=dev), \
+            torch.empty(2 * n, dtype=torch.float32, device=dev)
+    return (torch.randn(n, dtype=dt, device=dev), torch.randn(m, dtype=dt, device=dev),
+            torch.empty(m, dtype=dt, device=dev), torch.empty(n, dtype=dt, device=dev))
+
+
 def spmv_only(args, T, torch, geo, op32, n, m, nnz, dev):
     """A*x and A^T*y of one precision, 20 timed launches each (CUDA events on
     the launching stream, L2 flushed before every launch)."""
@@ -419,10 +428,7 @@ def spmv_only(args, T, torch, geo, op32, n, m, nnz, dev):
     prec, dt, sv, sx = precs[args.only_spmv]
     op = op32 if prec == T.PREC_FP32 else T.Operator.from_geometry(geo, mode=0, precision=prec)
     stream = torch.cuda.Stream(device=dev)
-    x = torch.randn(n, dtype=dt, device=dev)
-    y = torch.randn(m, dtype=dt, device=dev)
-    outm = torch.empty(m, dtype=dt, device=dev)
-    outn = torch.empty(n, dtype=dt, device=dev)
+    x, y, outm, outn = op_vectors(torch, args.only_spmv == "df64", dt, n, m, dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
     res = {}

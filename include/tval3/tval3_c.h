@@ -247,11 +247,17 @@ TVAL3_API tval3_status tval3_op_shape(tval3_op op, int* rows, int* cols, int64_t
 TVAL3_API tval3_status tval3_op_export_csr(tval3_op op, int* ptr, int* ind, float* val, int* tptr, int* tind,
                                            float* tval);
 /* mat_vec_mul(trans, A, x, y, stream): y = A x (trans = 0) or y = A^T x.
- * x, y are device pointers of the operator's vector type (float, or double for
- * FP64 operators).  Batched multi-RHS form: nrhs columns, leading dimension =
- * vector length (the reference's `layers`, 2d/mat_vec_mul.h:65-71, :96-99). */
+ * x, y are device pointers of the operator's vector type: float (FP32, BF16,
+ * FP16 operators), double (FP64, FP32_F64VEC), or double-float pairs
+ * {float hi, lo} (FP32_DF64; see tval3_df64_from_f64).  Batched multi-RHS
+ * form: nrhs columns, leading dimension = vector length (the reference's
+ * `layers`, 2d/mat_vec_mul.h:65-71, :96-99). */
 TVAL3_API tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, void* stream);
 TVAL3_API tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, void* Y, void* stream);
+/* Device conversions between double and the double-float pairs used by
+ * FP32_DF64 operators (hi = round(x), lo = round(x - hi)). */
+TVAL3_API tval3_status tval3_df64_from_f64(const double* d_in, void* d_pairs, int64_t n, void* stream);
+TVAL3_API tval3_status tval3_df64_to_f64(const void* d_pairs, double* d_out, int64_t n, void* stream);
 
 /* ---------------------------------------------------------------------- *
  * Device-resident solver: a workspace bound to an operator and a volume;

@@ -89,6 +89,42 @@ def test_spmv_parity_and_adjoint(cuda, oracle, prec):
     assert abs(lhs - rhs) <= (1e-12 if prec == 1 else 1e-5) * max(abs(lhs), 1.0)
 
 
+def test_double_float_products(cuda, oracle):
+    """FP32_DF64 operators take {hi, lo} FP32 pairs; their products agree with
+    the FP64 oracle to double-float accuracy (~1e-13), far below FP32."""
+    import ctypes as C
+    torch = _torch()
+    from tval3_gb300 import PREC_FP32_DF64, Operator, SparseMatrix, capi
+    cfg, geo, x0 = _small_3d()
+    ptr, ind, val = oracle.siddon_csr(geo)
+    m, n = ptr.size - 1, x0.size
+    op = Operator.from_sparse(SparseMatrix(m, n, ptr, ind, val), precision=PREC_FP32_DF64)
+    x, y = _vecs(torch, op, torch.float64, seed=2)
+    lib = capi.load()
+    def to_pairs(v):
+        out = torch.empty(2 * v.numel(), dtype=torch.float32, device=cuda)
+        capi.check(lib.tval3_df64_from_f64(v.to(cuda).data_ptr(), out.data_ptr(), v.numel(), None))
+        return out
+    def from_pairs(p, k):
+        out = torch.empty(k, dtype=torch.float64, device=cuda)
+        capi.check(lib.tval3_df64_to_f64(p.data_ptr(), out.data_ptr(), k, None))
+        return out
+    xp, yp = to_pairs(x), to_pairs(y)
+    Axp = torch.empty(2 * m, dtype=torch.float32, device=cuda)
+    Atyp = torch.empty(2 * n, dtype=torch.float32, device=cuda)
+    op.mat_vec_mul(0, xp, Axp)
+    op.mat_vec_mul(1, yp, Atyp)
+    torch.cuda.synchronize()
+    Ax = from_pairs(Axp, m).cpu().numpy()
+    Aty = from_pairs(Atyp, n).cpu().numpy()
+    torch.cuda.synchronize()
+    tptr, tind, tval = oracle.transpose(m, n, ptr, ind, val)
+    ref_Ax = oracle.spmv(ptr, ind, val, x.numpy())
+    ref_Aty = oracle.spmv(tptr, tind, tval, y.numpy())
+    assert np.linalg.norm(Ax - ref_Ax) <= 1e-12 * np.linalg.norm(ref_Ax)
+    assert np.linalg.norm(Aty - ref_Aty) <= 1e-12 * np.linalg.norm(ref_Aty)
+
+
 def test_on_the_fly_bresenham_matches_csr(cuda, oracle):
     """On-the-fly traversal (dyn_calc_kernel's mode) equals the stored CSR
     product: A x within FP32 summation order, A^T y (atomic scatter) likewise."""

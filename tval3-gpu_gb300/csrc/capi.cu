@@ -464,7 +464,8 @@ tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, v
     return guard([&] {
         if (!op || !x || !y) arg_error(TVAL3_ERR_ARG, "Argument error: NULL operator or vector!");
         cudaStream_t s = (cudaStream_t)stream;
-        if (op->dbl) op->d->apply(trans ? 1 : 0, plain_io<double>((const double*)x, (double*)y), SPMV_PLAIN, s);
+        if (op->q) op->q->apply(trans ? 1 : 0, plain_io<df64>((const df64*)x, (df64*)y), SPMV_PLAIN, s);
+        else if (op->dbl) op->d->apply(trans ? 1 : 0, plain_io<double>((const double*)x, (double*)y), SPMV_PLAIN, s);
         else op->f->apply(trans ? 1 : 0, plain_io<float>((const float*)x, (float*)y), SPMV_PLAIN, s);
     });
 }
@@ -473,8 +474,23 @@ tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, 
     return guard([&] {
         if (!op || !X || !Y || nrhs < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad multi-RHS product!");
         cudaStream_t s = (cudaStream_t)stream;
-        if (op->dbl) op->d->apply_multi(trans ? 1 : 0, nrhs, (const double*)X, (double*)Y, s);
+        if (op->q) op->q->apply_multi(trans ? 1 : 0, nrhs, (const df64*)X, (df64*)Y, s);
+        else if (op->dbl) op->d->apply_multi(trans ? 1 : 0, nrhs, (const double*)X, (double*)Y, s);
         else op->f->apply_multi(trans ? 1 : 0, nrhs, (const float*)X, (float*)Y, s);
+    });
+}
+
+tval3_status tval3_df64_from_f64(const double* d_in, void* d_pairs, int64_t n, void* stream) {
+    return guard([&] {
+        if (n < 0 || (n > 0 && (!d_in || !d_pairs))) arg_error(TVAL3_ERR_ARG, "Argument error: bad conversion!");
+        convert_to_df64(d_in, d_pairs, (long)n, (cudaStream_t)stream);
+    });
+}
+
+tval3_status tval3_df64_to_f64(const void* d_pairs, double* d_out, int64_t n, void* stream) {
+    return guard([&] {
+        if (n < 0 || (n > 0 && (!d_pairs || !d_out))) arg_error(TVAL3_ERR_ARG, "Argument error: bad conversion!");
+        convert_from_df64(d_pairs, d_out, (long)n, (cudaStream_t)stream);
     });
 }
 

@@ -351,6 +351,23 @@ void export_vals<df64, float>(const CsrOp<df64, float>& op, float* hval, float* 
     if (htval) TV3_CUDA(cudaMemcpy(htval, op.tval.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
 }
 
+__global__ void k_f64_to_df64(long n, const double* __restrict__ in, df64* __restrict__ out) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = df64(in[i]);
+}
+__global__ void k_df64_to_f64(long n, const df64* __restrict__ in, double* __restrict__ out) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+void convert_to_df64(const double* in, void* out, long n, cudaStream_t s) {
+    if (n > 0) k_f64_to_df64<<<ew(n), 256, 0, s>>>(n, in, static_cast<df64*>(out));
+    TV3_CUDA(cudaGetLastError());
+}
+void convert_from_df64(const void* in, double* out, long n, cudaStream_t s) {
+    if (n > 0) k_df64_to_f64<<<ew(n), 256, 0, s>>>(n, static_cast<const df64*>(in), out);
+    TV3_CUDA(cudaGetLastError());
+}
+
 // Double-float view of an FP32-value / FP64-vector CSR operator: the same
 // device arrays (not copied, not freed by the view), products in df64.
 LinOp<df64>* make_df64_view(const LinOp<double>* base) {

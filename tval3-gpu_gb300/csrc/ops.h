@@ -97,6 +97,8 @@ LinOp<double>* make_csr_op_f64vec(long rows, long cols, long nnz, const int* d_p
 // Double-float products over the arrays of an FP32-value / FP64-vector CSR
 // operator (precision TVAL3_PREC_FP32_DF64); the view does not own the arrays.
 LinOp<df64>* make_df64_view(const LinOp<double>* base);
+void convert_to_df64(const double* in, void* out, long n, cudaStream_t s);
+void convert_from_df64(const void* in, double* out, long n, cudaStream_t s);
 
 // Ray-geometry operators (ray.cu).
 struct RayList;  // compacted ray list and geometry on the device
