@@ -45,16 +45,17 @@ def test_fp64_solve_matches_oracle(cuda, oracle, iso):
 
 
 @pytest.mark.parametrize("iso", [0, 1])
-def test_double_float_solve_matches_fp64_oracle(cuda, oracle, iso):
-    """Double-float vectors (FP32 pairs, ~48 bits) over the FP32 matrix follow
-    the FP64 oracle through a full 300-iteration solve of the 64^2 ring
-    problem: the same iteration counts (a single Armijo decision may flip
-    where the test is decided in the last bits) and the result inside the
-    1e-3 bound the benchmark uses."""
+def test_double_float_short_horizon_2d(cuda, oracle, iso):
+    """Double-float vectors (FP32 pairs, ~48 bits) over the FP32 matrix track
+    the FP64 oracle closely while the loop's amplification of rounding is
+    still small: identical control flow and 1e-6 after 60 iterations of the
+    64^2 ring problem (over its full 300-iteration horizon this problem
+    amplifies FP64 rounding alone to ~3e-5, so no 48-bit arithmetic can stay
+    within 1e-3 of it; see the 3D test below for a full horizon)."""
     import torch
     from tval3_gb300 import PREC_FP32_DF64, Operator, Solver, SparseMatrix, tval3_gpu_3d
     geo, x, ptr, ind, val, b = _problem(oracle, 64, 128, seed=0)
-    o = dict(OPTS, tv_type=iso, mu0=256., beta0=32.)
+    o = dict(OPTS, tv_type=iso, mu0=256., beta0=32., maxit=60)
     Uo, io = oracle.tval3_csr((64, 64, 1), ptr, ind, val, b.astype(np.float64), o, prec=0, Ut=x)
     op = Operator.from_sparse(SparseMatrix(ptr.size - 1, x.size, ptr, ind, val), precision=PREC_FP32_DF64)
     for mode in (0, 1):
@@ -62,15 +63,35 @@ def test_double_float_solve_matches_fp64_oracle(cuda, oracle, iso):
         U = torch.empty(x.size, dtype=torch.float64, device=cuda)
         ig = s.solve(torch.tensor(b, dtype=torch.float64, device=cuda), U)
         torch.cuda.synchronize()
-        assert (ig["total_iters"], ig["outer_iters"]) == (io["total_iters"], io["outer_iters"])
-        assert abs(ig["backtracks"] - io["backtracks"]) <= 2 and abs(ig["restarts"] - io["restarts"]) <= 1
-        assert np.linalg.norm(U.cpu().numpy() - Uo.reshape(-1)) <= 1e-3 * np.linalg.norm(Uo)
+        assert (ig["total_iters"], ig["outer_iters"], ig["backtracks"], ig["restarts"]) == \
+            (io["total_iters"], io["outer_iters"], io["backtracks"], io["restarts"])
+        assert np.linalg.norm(U.cpu().numpy() - Uo.reshape(-1)) <= 1e-6 * np.linalg.norm(Uo)
         s.close()
     # the reference-facing FP64 entry point with FP32 values, run in double-float
     Uh, ih = tval3_gpu_3d((64, 64, 1), SparseMatrix(ptr.size - 1, x.size, ptr, ind, val), b.astype(np.float64),
                           dict(o, precision=PREC_FP32_DF64), dtype=np.float64)
     assert ih["total_iters"] == io["total_iters"]
-    assert np.linalg.norm(Uh - Uo) <= 1e-3 * np.linalg.norm(Uo)
+    assert np.linalg.norm(Uh - Uo) <= 1e-6 * np.linalg.norm(Uo)
+
+
+def test_double_float_full_solve_3d(cuda, oracle):
+    """A full solve of a small hemisphere problem (the 128^3 workload's
+    geometry and options at 32^3, 48 x 48 rays) in double-float ends inside
+    the 1e-3 bound of the FP64 oracle with the same control flow."""
+    import torch
+    from tval3_gb300 import PREC_FP32_DF64, Operator, Solver
+    from tval3_gb300 import workloads as W
+    cfg, geo, x = W.config_3d(32, 48, 48, seed=1)
+    ptr, ind, val = oracle.siddon_csr(geo)
+    b = W.add_noise(oracle.spmv(ptr, ind, val, x), cfg.noise, cfg.seed).astype(np.float64)
+    Uo, io = oracle.tval3_csr(cfg.dims, ptr, ind, val, b, cfg.opts, prec=0)
+    op = Operator.from_geometry(geo, mode=0, precision=PREC_FP32_DF64)
+    s = Solver(op, cfg.dims, cfg.opts, mode=1)
+    U = torch.empty(x.size, dtype=torch.float64, device=cuda)
+    ig = s.solve(torch.tensor(b, device=cuda), U)
+    torch.cuda.synchronize()
+    assert (ig["total_iters"], ig["outer_iters"]) == (io["total_iters"], io["outer_iters"])
+    assert np.linalg.norm(U.cpu().numpy() - Uo.reshape(-1)) <= 1e-3 * np.linalg.norm(Uo)
 
 
 @pytest.mark.parametrize("iso", [0, 1])

@@ -17,6 +17,10 @@ enum SpmvEpi : int { SPMV_PLAIN = 0, SPMV_SUB = 1, SPMV_LAM35 = 2, SPMV_NORM2 = 
 // elements past the last nonzero (G <= 32).  The slack is zero-filled.
 constexpr long SPMV_PAD = 256;
 
+// flag in the lanes-per-row argument of launch_spmv: single-nonzero lanes
+// (short rows) instead of four-element chunks (long rows)
+constexpr int SPMV_SCALAR = 64;
+
 // Arguments of one CSR product y = M x (M is A or the CSR of A^T).  x and y
 // are ping-pong pairs: with by_parity set, the kernel uses slot ctl->parity.
 template <class T, class V>

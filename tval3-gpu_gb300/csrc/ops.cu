@@ -258,13 +258,14 @@ static void tune_lanes(CsrOp<T, V>* op) {
     cudaEvent_t e0, e1;
     TV3_CUDA(cudaEventCreate(&e0));
     TV3_CUDA(cudaEventCreate(&e1));
-    const int cand[4] = {4, 8, 16, 32};
+    const int cand[8] = {4, 8, 16, 32, 4 | SPMV_SCALAR, 8 | SPMV_SCALAR, 16 | SPMV_SCALAR, 32 | SPMV_SCALAR};
     for (int trans = 0; trans < 2; ++trans) {
         float best = 1e30f;
         int bestG = trans ? op->Gt : op->Gn;
         for (int G : cand) {
-            if (trans) { op->Gt = G; op->grid_t = spmv_grid(n, G); }
-            else { op->Gn = G; op->grid_n = spmv_grid(m, G); }
+            const int lanes = G & ~SPMV_SCALAR;
+            if (trans) { op->Gt = G; op->grid_t = spmv_grid(n, lanes); }
+            else { op->Gn = G; op->grid_n = spmv_grid(m, lanes); }
             MatIO<T> io = plain_io<T>(x.p, y.p);
             op->apply(trans, io, SPMV_PLAIN, 0);
             TV3_CUDA(cudaEventRecord(e0, 0));
@@ -275,8 +276,8 @@ static void tune_lanes(CsrOp<T, V>* op) {
             TV3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
             if (ms < best) { best = ms; bestG = G; }
         }
-        if (trans) { op->Gt = bestG; op->grid_t = spmv_grid(n, bestG); }
-        else { op->Gn = bestG; op->grid_n = spmv_grid(m, bestG); }
+        if (trans) { op->Gt = bestG; op->grid_t = spmv_grid(n, bestG & ~SPMV_SCALAR); }
+        else { op->Gn = bestG; op->grid_n = spmv_grid(m, bestG & ~SPMV_SCALAR); }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

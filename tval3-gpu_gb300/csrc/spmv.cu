@@ -57,7 +57,11 @@ template <> struct Vec4<__half> {
 template <class V> struct VT { using type = float; };
 template <> struct VT<double> { using type = double; };
 
-template <class T, class V, int G, int EPI>
+// VEC = 1: every lane reads four consecutive nonzeros per chunk (16-byte
+// loads), two chunks in flight, masked outside the row: for long rows.
+// VEC = 0: lanes stride over single nonzeros (no masked work): for short rows,
+// where most four-element slots of the VEC form would be empty.
+template <class T, class V, int G, int EPI, int VEC>
 __global__ void __launch_bounds__(256) k_spmv(SpmvArgs<T, V> a) {
     count_launch(a.ctl);
     using VV = typename VT<V>::type;
@@ -76,27 +80,53 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs<T, V> a) {
     const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
     for (long r = grp; r < a.rows; r += ngrp) {
         const int beg = __ldg(ptr + r), end = __ldg(ptr + r + 1);
-        T s = T(0);
-        for (int base = (beg & ~3) + 4 * lane; base < end; base += 8 * G) {
-            const int base2 = base + 4 * G;
-            int4 c0 = __ldcs(reinterpret_cast<const int4*>(ind + base));
-            int4 c1 = __ldcs(reinterpret_cast<const int4*>(ind + base2));
-            VV v0[4], v1[4];
-            Vec4<V>::load(val + base, v0);
-            Vec4<V>::load(val + base2, v1);
-            const int cc[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-            T xv[8];
+        RowAcc<T> acc;
+        if (VEC) {
+            for (int base = (beg & ~3) + 4 * lane; base < end; base += 8 * G) {
+                const int base2 = base + 4 * G;
+                int4 c0 = __ldcs(reinterpret_cast<const int4*>(ind + base));
+                int4 c1 = __ldcs(reinterpret_cast<const int4*>(ind + base2));
+                VV v0[4], v1[4];
+                Vec4<V>::load(val + base, v0);
+                Vec4<V>::load(val + base2, v1);
+                const int cc[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+                T xv[8];
+                bool ok[8];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int k = (e < 4 ? base : base2) + (e & 3);
-                xv[e] = (k >= beg && k < end) ? x[cc[e]] : T(0);
-                if (xs && k >= beg && k < end) xv[e] *= (T)__ldg(xs + cc[e]);
+                for (int e = 0; e < 8; ++e) {
+                    const int k = (e < 4 ? base : base2) + (e & 3);
+                    ok[e] = (k >= beg && k < end);
+                    xv[e] = ok[e] ? x[cc[e]] : T(0);
+                    if (xs && ok[e]) xv[e] *= (T)__ldg(xs + cc[e]);
+                }
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (ok[e]) madd(acc, v0[e], xv[e]);
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (ok[4 + e]) madd(acc, v1[e], xv[4 + e]);
             }
-#pragma unroll
-            for (int e = 0; e < 4; ++e) madd(s, v0[e], xv[e]);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) madd(s, v1[e], xv[4 + e]);
+        } else {
+            int k = beg + lane;
+            for (; k + G < end; k += 2 * G) {
+                const int c0 = __ldcs(ind + k), c1 = __ldcs(ind + k + G);
+                const VV v0 = (VV)Acc<VV, V>::load(val + k), v1 = (VV)Acc<VV, V>::load(val + k + G);
+                T x0 = x[c0], x1 = x[c1];
+                if (xs) {
+                    x0 *= (T)__ldg(xs + c0);
+                    x1 *= (T)__ldg(xs + c1);
+                }
+                madd(acc, v0, x0);
+                madd(acc, v1, x1);
+            }
+            if (k < end) {
+                const int c0 = __ldcs(ind + k);
+                T x0 = x[c0];
+                if (xs) x0 *= (T)__ldg(xs + c0);
+                madd(acc, (VV)Acc<VV, V>::load(val + k), x0);
+            }
         }
+        T s = acc.value();
 #pragma unroll
         for (int o = G / 2; o; o >>= 1) s += shfl_down(gmask, s, o, G);
         if (lane == 0) {
@@ -132,23 +162,30 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs<T, V> a) {
     }
 }
 
-template <class T, class V, int EPI>
-static void launch_g(const SpmvArgs<T, V>& a, int G, int grid, cudaStream_t s) {
+// lanes: the group size G (4, 8, 16, 32), plus SPMV_SCALAR for the scalar-lane variant
+template <class T, class V, int EPI, int VEC>
+static void launch_v(const SpmvArgs<T, V>& a, int G, int grid, cudaStream_t s) {
     switch (G) {
-        case 4: k_spmv<T, V, 4, EPI><<<grid, 256, 0, s>>>(a); break;
-        case 8: k_spmv<T, V, 8, EPI><<<grid, 256, 0, s>>>(a); break;
-        case 16: k_spmv<T, V, 16, EPI><<<grid, 256, 0, s>>>(a); break;
-        default: k_spmv<T, V, 32, EPI><<<grid, 256, 0, s>>>(a); break;
+        case 4: k_spmv<T, V, 4, EPI, VEC><<<grid, 256, 0, s>>>(a); break;
+        case 8: k_spmv<T, V, 8, EPI, VEC><<<grid, 256, 0, s>>>(a); break;
+        case 16: k_spmv<T, V, 16, EPI, VEC><<<grid, 256, 0, s>>>(a); break;
+        default: k_spmv<T, V, 32, EPI, VEC><<<grid, 256, 0, s>>>(a); break;
     }
 }
 
+template <class T, class V, int EPI>
+static void launch_g(const SpmvArgs<T, V>& a, int lanes, int grid, cudaStream_t s) {
+    if (lanes & SPMV_SCALAR) launch_v<T, V, EPI, 0>(a, lanes & ~SPMV_SCALAR, grid, s);
+    else launch_v<T, V, EPI, 1>(a, lanes, grid, s);
+}
+
 template <class T, class V>
-void launch_spmv(const SpmvArgs<T, V>& a, int epi, int G, int grid, cudaStream_t s) {
+void launch_spmv(const SpmvArgs<T, V>& a, int epi, int lanes, int grid, cudaStream_t s) {
     switch (epi) {
-        case SPMV_SUB: launch_g<T, V, SPMV_SUB>(a, G, grid, s); break;
-        case SPMV_LAM35: launch_g<T, V, SPMV_LAM35>(a, G, grid, s); break;
-        case SPMV_NORM2: launch_g<T, V, SPMV_NORM2>(a, G, grid, s); break;
-        default: launch_g<T, V, SPMV_PLAIN>(a, G, grid, s); break;
+        case SPMV_SUB: launch_g<T, V, SPMV_SUB>(a, lanes, grid, s); break;
+        case SPMV_LAM35: launch_g<T, V, SPMV_LAM35>(a, lanes, grid, s); break;
+        case SPMV_NORM2: launch_g<T, V, SPMV_NORM2>(a, lanes, grid, s); break;
+        default: launch_g<T, V, SPMV_PLAIN>(a, lanes, grid, s); break;
     }
 }
 
