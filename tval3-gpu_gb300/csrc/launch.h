@@ -97,7 +97,6 @@ template <class T> void launch_scale_b(const void* b_in, SolverBufs<T>& B, cudaS
 template <class T> void launch_D_only(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_descend(SolverBufs<T>& B, int restart, cudaStream_t s);
 template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s);
-template <class T> void launch_tau(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s);
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s);
 template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t s);

@@ -153,9 +153,9 @@ void Solver<T>::run_host(cudaStream_t s) {
     if (!(o.maxcnt > 0 && o.maxit > 0)) return;
     bool fst = true;
     for (;;) {
-        // ---- min_u (:823-891)
+        // ---- min_u (:823-891); a non-first step size was formed by the
+        // previous iteration's gradient kernel
         if (fst) tau_first(s);
-        else launch_tau<T>(B, s);
         launch_descend<T>(B, 0, s);
         get_g(EPI_G2_DESCEND, s);
         read_ctl(s);
@@ -271,12 +271,9 @@ void Solver<T>::build_graph(const void* d_b, void* d_U, const void* d_Ut, cudaSt
             ib.begin();
             launch_cond(B.ctl, h_fst, COND_FST, cs);
             ib.end();
-            auto fb = ib.cond(h_fst, cudaGraphCondTypeIf, 2);
             {
-                Body t{fb[0], {}, cs};
+                Body t{ib.cond(h_fst, cudaGraphCondTypeIf, 1)[0], {}, cs};
                 t.begin(); tau_first(cs); t.end();
-                Body e{fb[1], {}, cs};
-                e.begin(); launch_tau<T>(B, cs); e.end();
             }
             ib.begin();
             launch_descend<T>(B, 0, cs);

@@ -9,7 +9,7 @@
 // Reference counterparts (3d/tval3_gpu_3d.cpp unless noted):
 //   k_D_only / k_descend   D_gpu :271-314 (+ axpy and nonneg_kernel, :671-701)
 //   k_Dd_norm              get_tau_gpu first iteration :583-600
-//   k_tau                  get_tau_kernel, 3d/tval3_gpu_3d_kernels.cu:1017-1067
+//   k_gradient (BB step)   get_tau_kernel, 3d/tval3_gpu_3d_kernels.cu:1017-1067
 //   k_g2                   V = DU - W, lam2_4_kernel, Dt_gpu (get_g_gpu :484-571)
 //   k_shrink               shrinkage_kernel, 3d/tval3_gpu_3d_kernels.cu:1249-1300
 //   k_gradient             get_gradient_gpu :896-919 and the RelChg test :1178-1200
@@ -215,31 +215,6 @@ __global__ void k_Dd_norm(SolverBufs<T> B, Geo g) {
     }
 }
 
-// ---------------------------------------------------------------------------
-// BB step: ss = <uup,uup>, sy = <uup, dg2 + mu/beta dg>, tau = |ss/sy|
-// ---------------------------------------------------------------------------
-template <class T>
-__global__ void k_tau(SolverBufs<T> B) {
-    Ctl* ctl = B.ctl;
-    count_launch(ctl);
-    using A = acc_t<T>;
-    const int cur = ctl->parity, prv = 1 - cur;
-    const A mdb = scal<A>(ctl->muDbeta);
-    const T *__restrict__ U = B.U[cur], *__restrict__ Up = B.U[prv];
-    const T *__restrict__ g = B.g[cur], *__restrict__ gp = B.g[prv];
-    const T *__restrict__ g2 = B.g2[cur], *__restrict__ g2p = B.g2[prv];
-    A ss(0.f), sy(0.f);
-    GRID_STRIDE(i, B.n) {
-        A u = to_acc(U[i]) - to_acc(Up[i]);
-        A dg = to_acc(g[i]) - to_acc(gp[i]);
-        A dg2 = to_acc(g2[i]) - to_acc(g2p[i]);
-        ss += u * u;
-        sy += u * (dg2 + mdb * dg);
-    }
-    double v[2] = {acc_d(ss), acc_d(sy)}, tot[2];
-    if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) ctl->tau = fabs(tot[0] / tot[1]);
-}
-
 __device__ __forceinline__ double fval(const Ctl* c) {
     return c->lam1 + c->beta / 2 * c->lam2 + c->mu / 2 * c->lam3 - c->lam4 - c->lam5;
 }
@@ -352,7 +327,12 @@ __global__ void k_shrink(SolverBufs<T> B, int mode) {
 
 // ---------------------------------------------------------------------------
 // d = mu/beta g + g2 + DtsAtd, with ||Up||, ||U - Up|| (RelChg) and <d,d>
-// (mode 0: start-up, mode 1: inner iteration)
+// (mode 0: start-up, mode 1: inner iteration).  In an inner iteration the
+// same pass forms the next iteration's Barzilai-Borwein step (get_tau_gpu,
+// :612-664): ss = ||U - Up||^2 and sy = <U - Up, (g2 - g2p) + mu/beta (g - gp)>
+// read exactly the vectors the next get_tau would (update_W changes only g2,
+// which is final here), so tau is ready when the next iteration starts; a
+// first iteration overwrites it with the exact step.
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void k_gradient(SolverBufs<T> B, int iter) {
@@ -361,15 +341,18 @@ __global__ void k_gradient(SolverBufs<T> B, int iter) {
     using A = acc_t<T>;
     const int cur = ctl->parity, prv = 1 - cur;
     const T mdb = scal<T>(ctl->muDbeta);
+    const A mdbA = scal<A>(ctl->muDbeta);
     const T *__restrict__ g = B.g[cur], *__restrict__ g2 = B.g2[cur], *__restrict__ dts = B.DtsAtd;
+    const T *__restrict__ gp = B.g[prv], *__restrict__ g2p = B.g2[prv];
     const T *__restrict__ U = B.U[cur], *__restrict__ Up = B.U[prv];
     const Ext<T>* __restrict__ xs = static_cast<const Ext<T>*>(B.xstar);
     const double iscl = 1.0 / ctl->scl;
     T* __restrict__ d = B.d;
-    A s0(0.f), s1(0.f), s2(0.f);
+    A s0(0.f), s1(0.f), s2(0.f), s4(0.f);
     double s3 = 0.0;
     GRID_STRIDE(i, B.n) {
-        T di = mdb * g[i] + g2[i] + dts[i];
+        const T gi = g[i], g2i = g2[i];
+        T di = mdb * gi + g2i + dts[i];
         d[i] = di;
         A ad = to_acc(di);
         s2 += ad * ad;
@@ -378,19 +361,23 @@ __global__ void k_gradient(SolverBufs<T> B, int iter) {
             A du = u - up;
             s0 += up * up;
             s1 += du * du;
+            A dg = to_acc(gi) - to_acc(gp[i]);
+            A dg2 = to_acc(g2i) - to_acc(g2p[i]);
+            s4 += du * (dg2 + mdbA * dg);
             if (xs) {
                 double e = acc_d(u) * iscl - (double)xs[i];
                 s3 += e * e;
             }
         }
     }
-    double v[4] = {acc_d(s0), acc_d(s1), acc_d(s2), s3}, tot[4];
-    if (grid_reduce<4>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+    double v[5] = {acc_d(s0), acc_d(s1), acc_d(s2), s3, acc_d(s4)}, tot[5];
+    if (grid_reduce<5>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->dd = tot[2];
         if (!iter) {
             ctl->Q = 1.0;
             ctl->C = ctl->f;
         } else {
+            ctl->tau = fabs(tot[1] / tot[4]);  // next iteration's BB step
             ctl->nrmup = sqrt(tot[0]);
             ctl->relchg = sqrt(tot[1]) / ctl->nrmup;
             if (B.trace && xs) B.trace[ctl->count_total] = sqrt(tot[3]);
@@ -690,7 +677,6 @@ template <class T> void launch_descend(SolverBufs<T>& B, int restart, cudaStream
 template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s) {
     k_Dd_norm<T><<<B.grid, 256, 0, s>>>(B, geo_of(B));
 }
-template <class T> void launch_tau(SolverBufs<T>& B, cudaStream_t s) { k_tau<T><<<B.grid, 256, 0, s>>>(B); }
 template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s) {
     k_g2<T><<<B.grid, 256, 0, s>>>(B, geo_of(B), mode);
 }
@@ -723,7 +709,6 @@ template <class T> void launch_Dt_plain(int p, int q, int r, const T* V3, T* out
     template void launch_D_only<T>(SolverBufs<T>&, cudaStream_t);                   \
     template void launch_descend<T>(SolverBufs<T>&, int, cudaStream_t);             \
     template void launch_Dd_norm<T>(SolverBufs<T>&, cudaStream_t);                  \
-    template void launch_tau<T>(SolverBufs<T>&, cudaStream_t);                      \
     template void launch_g2<T>(SolverBufs<T>&, int, cudaStream_t);                  \
     template void launch_shrink<T>(SolverBufs<T>&, int, cudaStream_t);              \
     template void launch_gradient<T>(SolverBufs<T>&, int, cudaStream_t);            \
