@@ -61,11 +61,6 @@ struct SolverBufs {
     T* Atb;
     T* W;          // 3n
     T* sig;        // 3n
-    T* dU;
-    T* dg;
-    T* dg2;
-    T* dDU;        // 3n
-    T* dAu;        // m
     T* b;          // m, scaled
     T* delta;      // m
     T* rcdU;
@@ -81,7 +76,6 @@ struct SolverBufs {
     int use_graph;
     unsigned long long h_inner;  // WHILE: continue the inner loop
     unsigned long long h_arm;    // IF: Armijo test failed after the descent
-    unsigned long long h_bt;     // WHILE: take another backtracking step
     unsigned long long h_mlp;    // IF: outer loop continues (multiplier update)
 };
 
@@ -100,7 +94,8 @@ template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s);
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s);
 template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t s);
-template <class T> void launch_backtrack(SolverBufs<T>& B, int setup, cudaStream_t s);
+template <class T> void launch_bt_coef(SolverBufs<T>& B, cudaStream_t s);
+template <class T> void launch_bt_apply(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_mlp(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_outer_grad(SolverBufs<T>& B, cudaStream_t s);

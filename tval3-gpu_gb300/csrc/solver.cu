@@ -4,10 +4,11 @@
 //           two branch flags (Armijo, inner break) from the control block;
 //   mode 1: the whole solve is one CUDA graph.  The loops and branches of the
 //           reference (outer while, inner while, first-iteration step size,
-//           Armijo backtracking with at most five steps, restart, multiplier
-//           update) are conditional graph nodes whose conditions are set on
-//           the device by the epilogues that decide them.  One launch per
-//           solve, no host round trip.
+//           Armijo failure, restart, multiplier update) are conditional graph
+//           nodes whose conditions are set on the device by the epilogues that
+//           decide them.  The (at most five) backtracking trials are evaluated
+//           in closed form by one kernel (k_bt_coef).  One launch per solve,
+//           no host round trip.
 // Both forms run the same kernels in the same order, so they give identical
 // results.
 #include <algorithm>
@@ -21,7 +22,7 @@ namespace tv3 {
 template <class T>
 Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_)
     : A(A_), p(p_), q(q_), r(r_), n((long)p_ * q_ * r_), m(A_->m), o(o_) {
-    const long nvec = 28, mvec = 5;
+    const long nvec = 22, mvec = 4;
     nv.alloc(nvec * n);
     mv.alloc(mvec * std::max<long>(m, 1));
     ctl.alloc(1);
@@ -39,11 +40,10 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
     B.DU[0] = take(3); B.DU[1] = take(3);
     B.d = take(1); B.DtsAtd = take(1); B.Atb = take(1);
     B.W = take(3); B.sig = take(3);
-    B.dU = take(1); B.dg = take(1); B.dg2 = take(1); B.dDU = take(3);
     B.rcdU = take(1);
     T* w = mv.p;
     const long mm = std::max<long>(m, 1);
-    B.Au[0] = w; B.Au[1] = w + mm; B.dAu = w + 2 * mm; B.b = w + 3 * mm; B.delta = w + 4 * mm;
+    B.Au[0] = w; B.Au[1] = w + mm; B.b = w + 2 * mm; B.delta = w + 3 * mm;
     B.ctl = ctl.p; B.part = part.p; B.ticket = ticket.p;
     // reduction grid: a fixed multiple of the SM count (partials fit in `part`)
     B.grid = std::max(1, std::min(num_sms() * 4, 8192));
@@ -160,12 +160,11 @@ void Solver<T>::run_host(cudaStream_t s) {
         get_g(EPI_G2_DESCEND, s);
         read_ctl(s);
         if (hctl->armijo_fail) {
-            launch_backtrack<T>(B, 1, s);
+            // the whole backtracking loop on the closed-form f(alpha), then the
+            // accepted point (nothing to apply when all five trials fail)
+            launch_bt_coef<T>(B, s);
+            launch_bt_apply<T>(B, s);
             read_ctl(s);
-            while (hctl->armijo_fail && hctl->cnt < 5) {
-                launch_backtrack<T>(B, 0, s);
-                read_ctl(s);
-            }
             if (hctl->armijo_fail) {  // cnt == 5: exact step from Up
                 tau_first(s);
                 launch_descend<T>(B, 1, s);
@@ -246,16 +245,15 @@ void Solver<T>::build_graph(const void* d_b, void* d_U, const void* d_Ut, cudaSt
     TV3_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     try {
         const unsigned run = (o.maxcnt > 0 && o.maxit > 0) ? 1u : 0u;
-        cudaGraphConditionalHandle h_outer, h_inner, h_fst, h_arm, h_bt, h_restart, h_mlp;
+        cudaGraphConditionalHandle h_outer, h_inner, h_fst, h_arm, h_restart, h_mlp;
         TV3_CUDA(cudaGraphConditionalHandleCreate(&h_outer, top, run, cudaGraphCondAssignDefault));
         TV3_CUDA(cudaGraphConditionalHandleCreate(&h_inner, top, 1, cudaGraphCondAssignDefault));
         TV3_CUDA(cudaGraphConditionalHandleCreate(&h_fst, top, 1, cudaGraphCondAssignDefault));
         TV3_CUDA(cudaGraphConditionalHandleCreate(&h_arm, top, 0, cudaGraphCondAssignDefault));
-        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_bt, top, 0, cudaGraphCondAssignDefault));
         TV3_CUDA(cudaGraphConditionalHandleCreate(&h_restart, top, 0, cudaGraphCondAssignDefault));
         TV3_CUDA(cudaGraphConditionalHandleCreate(&h_mlp, top, 0, cudaGraphCondAssignDefault));
         B.use_graph = 1;
-        B.h_inner = h_inner; B.h_arm = h_arm; B.h_bt = h_bt; B.h_mlp = h_mlp;
+        B.h_inner = h_inner; B.h_arm = h_arm; B.h_mlp = h_mlp;
 
         Body tb{top, {}, cs};
         tb.begin();
@@ -282,13 +280,8 @@ void Solver<T>::build_graph(const void* d_b, void* d_U, const void* d_Ut, cudaSt
             {
                 Body ab{ib.cond(h_arm, cudaGraphCondTypeIf, 1)[0], {}, cs};
                 ab.begin();
-                launch_backtrack<T>(B, 1, cs);  // sets h_bt
-                ab.end();
-                {
-                    Body bb{ab.cond(h_bt, cudaGraphCondTypeWhile, 1)[0], {}, cs};
-                    bb.begin(); launch_backtrack<T>(B, 0, cs); bb.end();
-                }
-                ab.begin();
+                launch_bt_coef<T>(B, cs);
+                launch_bt_apply<T>(B, cs);
                 launch_cond(B.ctl, h_restart, COND_RESTART, cs);
                 ab.end();
                 {

@@ -13,7 +13,7 @@
 //   k_g2                   V = DU - W, lam2_4_kernel, Dt_gpu (get_g_gpu :484-571)
 //   k_shrink               shrinkage_kernel, 3d/tval3_gpu_3d_kernels.cu:1249-1300
 //   k_gradient             get_gradient_gpu :896-919 and the RelChg test :1178-1200
-//   k_backtrack            min_u_gpu Armijo branch :848-890 with update_g_gpu :706-818
+//   k_bt_coef / k_bt_apply min_u_gpu Armijo branch :848-890 with update_g_gpu :706-818
 //   k_outer_relchg         :1204-1220
 //   k_mlp                  update_mlp_gpu :1034-1083 and continuation :1222-1237
 //   k_outer_grad           DtsAtd and get_gradient :1238-1249
@@ -390,14 +390,84 @@ __global__ void k_gradient(SolverBufs<T> B, int iter) {
 }
 
 // ---------------------------------------------------------------------------
-// backtracking: X = Xp + alpha*dX for U, g, g2, DU (n) and Au (m), then
-// lam2..lam5, f and the Armijo test.  The setup call first forms dX = X - Xp.
+// Backtracking in closed form.  update_g_gpu (:706-818) moves every quantity
+// along X(a) = Xp + a (X1 - Xp) (X1 the rejected full step) and re-evaluates
+// f(a) = lam1 + beta/2 lam2 + mu/2 lam3 - lam4 - lam5 for a = gamma, gamma^2,
+// ... (at most five, :859-888).  Along that segment lam2 and lam3 are exact
+// quadratics and lam4, lam5 exact linear functions of a, so one pass over
+// V0 = DUp - W, dV = DU1 - DUp, r0 = Aup - b, dr = Au1 - Aup gives their ten
+// coefficients; the epilogue then runs the whole Armijo loop on scalars and
+// either accepts the first admissible a or asks for the restart (cnt == 5,
+// :876-882).  k_bt_apply materialises the accepted point once.
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void k_backtrack(SolverBufs<T> B, int setup) {
+__global__ void k_bt_coef(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     using A = acc_t<T>;
+    const int cur = ctl->parity, prv = 1 - cur;
+    const long n = B.n, m = B.m;
+    const T *__restrict__ DU = B.DU[cur], *__restrict__ DUp = B.DU[prv];
+    const T *__restrict__ Au = B.Au[cur], *__restrict__ Aup = B.Au[prv];
+    const T *__restrict__ W = B.W, *__restrict__ S = B.sig, *__restrict__ bb = B.b, *__restrict__ dl = B.delta;
+    A a2(0.f), b2(0.f), c2(0.f), a4(0.f), b4(0.f), a3(0.f), b3(0.f), c3(0.f), a5(0.f), b5(0.f);
+    const long N = n > m ? n : m;
+    GRID_STRIDE(i, N) {
+        if (i < n) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const long k = c * n + i;
+                const T dp = DUp[k];
+                const A v0 = to_acc(dp - W[k]), dv = to_acc(DU[k] - dp), s = to_acc(S[k]);
+                a2 += v0 * v0;
+                b2 += v0 * dv;
+                c2 += dv * dv;
+                a4 += s * v0;
+                b4 += s * dv;
+            }
+        }
+        if (i < m) {
+            const T ap = Aup[i];
+            const A r0 = to_acc(ap) - to_acc(bb[i]), dr = to_acc(Au[i]) - to_acc(ap), d = to_acc(dl[i]);
+            a3 += r0 * r0;
+            b3 += r0 * dr;
+            c3 += dr * dr;
+            a5 += d * r0;
+            b5 += d * dr;
+        }
+    }
+    double v[10] = {acc_d(a2), acc_d(b2), acc_d(c2), acc_d(a4), acc_d(b4),
+                    acc_d(a3), acc_d(b3), acc_d(c3), acc_d(a5), acc_d(b5)},
+           tot[10];
+    if (grid_reduce<10>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        // alpha was already multiplied by gamma once by the Armijo epilogue of k_g2
+        int cnt = 0;
+        bool fail = true;
+        while (fail && cnt < 5) {
+            const double al = ctl->alpha;
+            ctl->lam2 = tot[0] + 2.0 * al * tot[1] + al * al * tot[2];
+            ctl->lam4 = tot[3] + al * tot[4];
+            ctl->lam3 = tot[5] + 2.0 * al * tot[6] + al * al * tot[7];
+            ctl->lam5 = tot[8] + al * tot[9];
+            ctl->f = fval(ctl);
+            ++cnt;
+            armijo(ctl);
+            fail = ctl->armijo_fail;
+            if (fail && cnt < 5) ctl->alpha *= ctl->gamma;
+        }
+        ctl->cnt = cnt;
+        ctl->backtracks += cnt;
+        if (fail) ctl->gam *= ctl->rate_gam;  // restart follows (:876-882)
+    }
+}
+
+// X = Xp + alpha (X1 - Xp) for U, g, g2, DU (n) and Au (m), in place in the
+// current slot (the full-step values X1 are read before they are replaced)
+template <class T>
+__global__ void k_bt_apply(SolverBufs<T> B) {
+    Ctl* ctl = B.ctl;
+    count_launch(ctl);
+    if (ctl->armijo_fail) return;  // restart path: nothing to apply
     const int cur = ctl->parity, prv = 1 - cur;
     const long n = B.n, m = B.m;
     const T al = scal<T>(ctl->alpha);
@@ -405,64 +475,25 @@ __global__ void k_backtrack(SolverBufs<T> B, int setup) {
     T *__restrict__ DU = B.DU[cur], *__restrict__ Au = B.Au[cur];
     const T *__restrict__ Up = B.U[prv], *__restrict__ gp = B.g[prv], *__restrict__ g2p = B.g2[prv];
     const T *__restrict__ DUp = B.DU[prv], *__restrict__ Aup = B.Au[prv];
-    const T *__restrict__ W = B.W, *__restrict__ S = B.sig, *__restrict__ bb = B.b, *__restrict__ dl = B.delta;
-    A l2(0.f), l4(0.f), l3(0.f), l5(0.f);
     const long N = n > m ? n : m;
     GRID_STRIDE(i, N) {
         if (i < n) {
-            T du, dgv, dg2v, d0, d1, d2;
-            if (setup) {
-                du = U[i] - Up[i];
-                dgv = g[i] - gp[i];
-                dg2v = g2[i] - g2p[i];
-                d0 = DU[i] - DUp[i];
-                d1 = DU[n + i] - DUp[n + i];
-                d2 = DU[2 * n + i] - DUp[2 * n + i];
-                B.dU[i] = du; B.dg[i] = dgv; B.dg2[i] = dg2v;
-                B.dDU[i] = d0; B.dDU[n + i] = d1; B.dDU[2 * n + i] = d2;
-            } else {
-                du = B.dU[i]; dgv = B.dg[i]; dg2v = B.dg2[i];
-                d0 = B.dDU[i]; d1 = B.dDU[n + i]; d2 = B.dDU[2 * n + i];
+            T p = Up[i];
+            U[i] = p + al * (U[i] - p);
+            p = gp[i];
+            g[i] = p + al * (g[i] - p);
+            p = g2p[i];
+            g2[i] = p + al * (g2[i] - p);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                p = DUp[c * n + i];
+                DU[c * n + i] = p + al * (DU[c * n + i] - p);
             }
-            g[i] = gp[i] + al * dgv;
-            g2[i] = g2p[i] + al * dg2v;
-            U[i] = Up[i] + al * du;
-            T e0 = DUp[i] + al * d0, e1 = DUp[n + i] + al * d1, e2 = DUp[2 * n + i] + al * d2;
-            DU[i] = e0; DU[n + i] = e1; DU[2 * n + i] = e2;
-            A v0 = to_acc(e0 - W[i]), v1 = to_acc(e1 - W[n + i]), v2 = to_acc(e2 - W[2 * n + i]);
-            l2 += v0 * v0 + v1 * v1 + v2 * v2;
-            l4 += v0 * to_acc(S[i]) + v1 * to_acc(S[n + i]) + v2 * to_acc(S[2 * n + i]);
         }
         if (i < m) {
-            T da;
-            if (setup) {
-                da = Au[i] - Aup[i];
-                B.dAu[i] = da;
-            } else {
-                da = B.dAu[i];
-            }
-            T a = Aup[i] + al * da;
-            Au[i] = a;
-            A t = to_acc(a) - to_acc(bb[i]);
-            l3 += t * t;
-            l5 += to_acc(dl[i]) * t;
+            T p = Aup[i];
+            Au[i] = p + al * (Au[i] - p);
         }
-    }
-    double v[4] = {acc_d(l2), acc_d(l4), acc_d(l3), acc_d(l5)}, tot[4];
-    if (grid_reduce<4>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
-        ctl->lam2 = tot[0];
-        ctl->lam4 = tot[1];
-        ctl->lam3 = tot[2];
-        ctl->lam5 = tot[3];
-        ctl->f = fval(ctl);
-        ctl->cnt += 1;
-        ctl->backtracks += 1;
-        armijo(ctl);
-        if (ctl->armijo_fail) {
-            if (ctl->cnt == 5) ctl->gam *= ctl->rate_gam;  // restart follows (:876-882)
-            else ctl->alpha *= ctl->gamma;
-        }
-        if (B.use_graph) cudaGraphSetConditional(B.h_bt, (ctl->armijo_fail && ctl->cnt < 5) ? 1u : 0u);
     }
 }
 
@@ -686,9 +717,8 @@ template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s
 template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t s) {
     k_gradient<T><<<B.grid, 256, 0, s>>>(B, mode);
 }
-template <class T> void launch_backtrack(SolverBufs<T>& B, int setup, cudaStream_t s) {
-    k_backtrack<T><<<B.grid, 256, 0, s>>>(B, setup);
-}
+template <class T> void launch_bt_coef(SolverBufs<T>& B, cudaStream_t s) { k_bt_coef<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_bt_apply(SolverBufs<T>& B, cudaStream_t s) { k_bt_apply<T><<<B.grid, 256, 0, s>>>(B); }
 template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s) { k_outer_relchg<T><<<B.grid, 256, 0, s>>>(B); }
 template <class T> void launch_mlp(SolverBufs<T>& B, cudaStream_t s) { k_mlp<T><<<B.grid, 256, 0, s>>>(B); }
 template <class T> void launch_outer_grad(SolverBufs<T>& B, cudaStream_t s) { k_outer_grad<T><<<B.grid, 256, 0, s>>>(B); }
@@ -712,7 +742,8 @@ template <class T> void launch_Dt_plain(int p, int q, int r, const T* V3, T* out
     template void launch_g2<T>(SolverBufs<T>&, int, cudaStream_t);                  \
     template void launch_shrink<T>(SolverBufs<T>&, int, cudaStream_t);              \
     template void launch_gradient<T>(SolverBufs<T>&, int, cudaStream_t);            \
-    template void launch_backtrack<T>(SolverBufs<T>&, int, cudaStream_t);           \
+    template void launch_bt_coef<T>(SolverBufs<T>&, cudaStream_t);                  \
+    template void launch_bt_apply<T>(SolverBufs<T>&, cudaStream_t);                 \
     template void launch_outer_relchg<T>(SolverBufs<T>&, cudaStream_t);             \
     template void launch_mlp<T>(SolverBufs<T>&, cudaStream_t);                      \
     template void launch_outer_grad<T>(SolverBufs<T>&, cudaStream_t);               \
