@@ -288,6 +288,21 @@ TVAL3_API tval3_status tval3_D_f64(int dim_y, int dim_x, int dim_z, const double
 TVAL3_API tval3_status tval3_Dt_f64(int dim_y, int dim_x, int dim_z, const double* d_V, double* d_out,
                                     void* stream);
 
+/* ---------------------------------------------------------------------- *
+ * Shrinkage as a differentiable operator (no reference counterpart as an
+ * entry point; the forward map is shrinkage_kernel,
+ * 3d/tval3_gpu_3d_kernels.cu:1249-1300, plus isotropic TV).  v, W, gW, gv
+ * hold 3 n-vectors; W = shrink(v, t) with threshold t (= 1/beta).  The
+ * adjoint writes gv = J^T gW and, when gt is not NULL, the n per-voxel terms
+ * of dL/dt (sum them for the scalar).  iso: tval3_tv.
+ * ---------------------------------------------------------------------- */
+TVAL3_API tval3_status tval3_shrink_f32(int64_t n, const float* d_v, double t, int iso, float* d_W, void* stream);
+TVAL3_API tval3_status tval3_shrink_f64(int64_t n, const double* d_v, double t, int iso, double* d_W, void* stream);
+TVAL3_API tval3_status tval3_shrink_adjoint_f32(int64_t n, const float* d_v, double t, int iso, const float* d_gW,
+                                                float* d_gv, float* d_gt, void* stream);
+TVAL3_API tval3_status tval3_shrink_adjoint_f64(int64_t n, const double* d_v, double t, int iso, const double* d_gW,
+                                                double* d_gv, double* d_gt, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

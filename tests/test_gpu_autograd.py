@@ -1,0 +1,126 @@
+"""Autograd binding: the hand-written adjoints (A^T, D^T, shrinkage
+subgradient) pass torch.autograd.gradcheck and dot-product tests in FP64,
+and the gradient of a loss through K unrolled TVAL3 iterations with respect
+to b, mu and beta agrees with central finite differences (h = 1e-3, FP64)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _op64(oracle, n=8, ne=6, seed=0):
+    from tval3_gb300 import PREC_FP64, Operator, SparseMatrix
+    from tval3_gb300 import workloads as W
+    cfg, geo, x = W.config_3d(n, ne, ne, seed=seed)
+    ptr, ind, val = oracle.siddon_csr(geo)
+    op = Operator.from_sparse(SparseMatrix(ptr.size - 1, x.size, ptr, ind, val.astype(np.float64)),
+                              precision=PREC_FP64)
+    return cfg, geo, x, op
+
+
+def test_gradcheck_operators(cuda, oracle):
+    import torch
+    from tval3_gb300 import autograd as AG
+    cfg, geo, x, op = _op64(oracle)
+    dims = cfg.dims
+    n = x.size
+    g = torch.Generator().manual_seed(0)
+    xv = torch.randn(n, dtype=torch.float64, generator=g).to(cuda).requires_grad_()
+    yv = torch.randn(op.rows, dtype=torch.float64, generator=g).to(cuda).requires_grad_()
+    assert torch.autograd.gradcheck(lambda t: AG.A(op, t), (xv,), eps=1e-6, atol=1e-8)
+    assert torch.autograd.gradcheck(lambda t: AG.At(op, t), (yv,), eps=1e-6, atol=1e-8)
+    assert torch.autograd.gradcheck(lambda t: AG.D(t, dims), (xv,), eps=1e-6, atol=1e-8)
+    v3 = torch.randn(3 * n, dtype=torch.float64, generator=g).to(cuda).requires_grad_()
+    assert torch.autograd.gradcheck(lambda t: AG.Dt(t, dims), (v3,), eps=1e-6, atol=1e-8)
+
+
+@pytest.mark.parametrize("iso", [True, False])
+def test_shrink_adjoint_gradcheck(cuda, iso):
+    import torch
+    from tval3_gb300 import autograd as AG
+    g = torch.Generator().manual_seed(1)
+    v = (torch.randn(3 * 50, dtype=torch.float64, generator=g) * 0.5).to(cuda)
+    # keep away from the kinks |v| = t, where the subgradient is not a derivative
+    t = torch.tensor(0.3, dtype=torch.float64, device=cuda, requires_grad=True)
+    if iso:
+        nv = v.reshape(3, -1).norm(dim=0)
+        keep = ((nv - 0.3).abs() > 0.05).repeat(3)
+    else:
+        keep = ((v.abs() - 0.3).abs() > 0.05)
+    v = torch.where(keep, v, torch.full_like(v, 0.9)).requires_grad_()
+    assert torch.autograd.gradcheck(lambda a, b: AG.shrink(a, b, iso), (v, t), eps=1e-7, atol=1e-7)
+
+
+def test_dot_product_adjoints(cuda, oracle):
+    import torch
+    from tval3_gb300 import autograd as AG
+    cfg, geo, x, op = _op64(oracle, 12, 8)
+    dims = cfg.dims
+    g = torch.Generator().manual_seed(2)
+    u = torch.randn(x.size, dtype=torch.float64, generator=g).to(cuda)
+    y = torch.randn(op.rows, dtype=torch.float64, generator=g).to(cuda)
+    p = torch.randn(3 * x.size, dtype=torch.float64, generator=g).to(cuda)
+    assert abs(float((AG.A(op, u) * y).sum() - (u * AG.At(op, y)).sum())) < 1e-10 * float(y.norm() * u.norm())
+    assert abs(float((AG.D(u, dims) * p).sum() - (u * AG.Dt(p, dims)).sum())) < 1e-10 * float(p.norm() * u.norm())
+
+
+def _loss_setup(oracle, n, ne, iters, cuda):
+    import torch
+    from tval3_gb300 import workloads as W
+    cfg, geo, x, op = _op64(oracle, n, ne, seed=3)
+    ptr, ind, val = oracle.siddon_csr(geo)
+    b = W.add_noise(oracle.spmv(ptr, ind, val, x), 0.01, 3).astype(np.float64)
+    # scale as the reference does (scaleb_gpu), so mu and beta have their usual meaning
+    bmin, bmax = b[np.argmin(np.abs(b))], b[np.argmax(np.abs(b))]
+    scl = 1.5 / abs(bmax - bmin)
+    bt = torch.tensor(b * scl, device=cuda)
+    xt = torch.tensor(x.reshape(-1) * scl, dtype=torch.float64, device=cuda)
+    return cfg, op, bt, xt
+
+
+@pytest.mark.parametrize("size,rays,iters", [(16, 12, 8), (96, 256, 20)])
+def test_unrolled_gradient_vs_finite_differences(cuda, oracle, size, rays, iters):
+    """loss = ||U_K - x_true||^2 through K unrolled iterations; gradients wrt
+    b (random direction), mu and beta vs central differences with h = 1e-3
+    (relative to mu and beta, absolute along the unit direction for b).  The
+    96^3, 256 x 256-ray, 20-iteration case is the differentiable workload."""
+    import torch
+    from tval3_gb300 import autograd as AG
+    cfg, op, b, xt = _loss_setup(oracle, size, rays, iters, cuda)
+    dims = cfg.dims
+    mu0, beta0 = 2.0 ** 9, 2.0 ** 6
+
+    def loss(bb, mu, beta):
+        U = AG.unrolled_tval3(op, bb, dims, mu, beta, iters=iters, iso=True)
+        return ((U - xt) ** 2).sum()
+
+    bb = b.clone().requires_grad_()
+    mu = torch.tensor(mu0, dtype=torch.float64, device=cuda, requires_grad=True)
+    beta = torch.tensor(beta0, dtype=torch.float64, device=cuda, requires_grad=True)
+    L = loss(bb, mu, beta)
+    L.backward()
+    g = torch.Generator().manual_seed(5)
+    v = torch.randn(b.numel(), dtype=torch.float64, generator=g).to(cuda)
+    v /= v.norm()
+    h = 1e-3
+    with torch.no_grad():
+        fd_b = (loss(b + h * v, mu0, beta0) - loss(b - h * v, mu0, beta0)) / (2 * h)
+        fd_mu = (loss(b, mu0 * (1 + h), beta0) - loss(b, mu0 * (1 - h), beta0)) / (2 * h * mu0)
+        fd_beta = (loss(b, mu0, beta0 * (1 + h)) - loss(b, mu0, beta0 * (1 - h))) / (2 * h * beta0)
+    an_b = float((bb.grad * v).sum())
+    for an, fd in ((an_b, float(fd_b)), (float(mu.grad), float(fd_mu)), (float(beta.grad), float(fd_beta))):
+        assert abs(an - fd) <= 2e-3 * max(abs(fd), 1e-8 * float(L)), (an, fd)
+
+
+def test_checkpointing_matches_plain(cuda, oracle):
+    import torch
+    from tval3_gb300 import autograd as AG
+    cfg, op, b, xt = _loss_setup(oracle, 12, 8, 6, cuda)
+    outs = []
+    for ck in (True, False):
+        bb = b.clone().requires_grad_()
+        U = AG.unrolled_tval3(op, bb, cfg.dims, 512.0, 64.0, iters=6, use_checkpoint=ck)
+        ((U - xt) ** 2).sum().backward()
+        outs.append((U.detach(), bb.grad))
+    assert torch.allclose(outs[0][0], outs[1][0], rtol=0, atol=0)
+    assert torch.allclose(outs[0][1], outs[1][1], rtol=1e-12, atol=1e-14)

@@ -480,6 +480,33 @@ tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, 
     });
 }
 
+tval3_status tval3_shrink_f32(int64_t n, const float* v, double t, int iso, float* W, void* stream) {
+    return guard([&] {
+        if (n < 0 || (n > 0 && (!v || !W))) arg_error(TVAL3_ERR_ARG, "Argument error: bad shrinkage arrays!");
+        shrink_fwd<float>((long)n, v, t, iso, W, (cudaStream_t)stream);
+    });
+}
+tval3_status tval3_shrink_f64(int64_t n, const double* v, double t, int iso, double* W, void* stream) {
+    return guard([&] {
+        if (n < 0 || (n > 0 && (!v || !W))) arg_error(TVAL3_ERR_ARG, "Argument error: bad shrinkage arrays!");
+        shrink_fwd<double>((long)n, v, t, iso, W, (cudaStream_t)stream);
+    });
+}
+tval3_status tval3_shrink_adjoint_f32(int64_t n, const float* v, double t, int iso, const float* gW, float* gv,
+                                      float* gt, void* stream) {
+    return guard([&] {
+        if (n < 0 || (n > 0 && (!v || !gW || !gv))) arg_error(TVAL3_ERR_ARG, "Argument error: bad shrinkage arrays!");
+        shrink_bwd<float>((long)n, v, t, iso, gW, gv, gt, (cudaStream_t)stream);
+    });
+}
+tval3_status tval3_shrink_adjoint_f64(int64_t n, const double* v, double t, int iso, const double* gW, double* gv,
+                                      double* gt, void* stream) {
+    return guard([&] {
+        if (n < 0 || (n > 0 && (!v || !gW || !gv))) arg_error(TVAL3_ERR_ARG, "Argument error: bad shrinkage arrays!");
+        shrink_bwd<double>((long)n, v, t, iso, gW, gv, gt, (cudaStream_t)stream);
+    });
+}
+
 tval3_status tval3_df64_from_f64(const double* d_in, void* d_pairs, int64_t n, void* stream) {
     return guard([&] {
         if (n < 0 || (n > 0 && (!d_in || !d_pairs))) arg_error(TVAL3_ERR_ARG, "Argument error: bad conversion!");

@@ -100,6 +100,11 @@ LinOp<df64>* make_df64_view(const LinOp<double>* base);
 void convert_to_df64(const double* in, void* out, long n, cudaStream_t s);
 void convert_from_df64(const void* in, double* out, long n, cudaStream_t s);
 
+// Differentiable shrinkage (shrink_ad.cu): W = shrink(v, t) and its adjoint.
+template <class T> void shrink_fwd(long n, const T* v, double t, int iso, T* W, cudaStream_t s);
+template <class T>
+void shrink_bwd(long n, const T* v, double t, int iso, const T* gW, T* gv, T* gt, cudaStream_t s);
+
 // Ray-geometry operators (ray.cu).
 struct RayList;  // compacted ray list and geometry on the device
 template <class T>
