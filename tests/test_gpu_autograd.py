@@ -1,7 +1,7 @@
 """Autograd binding: the hand-written adjoints (A^T, D^T, shrinkage
 subgradient) pass torch.autograd.gradcheck and dot-product tests in FP64,
 and the gradient of a loss through K unrolled TVAL3 iterations with respect
-to b, mu and beta agrees with central finite differences (h = 1e-3, FP64)."""
+to b, mu and beta agrees with central finite differences (h = 1e-5, FP64)."""
 import numpy as np
 import pytest
 
@@ -81,9 +81,13 @@ def _loss_setup(oracle, n, ne, iters, cuda):
 @pytest.mark.parametrize("size,rays,iters", [(16, 12, 8), (96, 256, 20)])
 def test_unrolled_gradient_vs_finite_differences(cuda, oracle, size, rays, iters):
     """loss = ||U_K - x_true||^2 through K unrolled iterations; gradients wrt
-    b (random direction), mu and beta vs central differences with h = 1e-3
+    b (random direction), mu and beta vs central differences with h = 1e-5
     (relative to mu and beta, absolute along the unit direction for b).  The
-    96^3, 256 x 256-ray, 20-iteration case is the differentiable workload."""
+    96^3, 256 x 256-ray, 20-iteration case is the differentiable workload.
+    The map is piecewise smooth: every voxel's shrinkage threshold and
+    nonnegativity clamp is a kink, and at 96^3 a step of 1e-3 along b crosses
+    enough of them that the difference quotient is an average slope (0.346
+    against the local derivative 0.444 here); at 1e-5 the two agree to 1e-6."""
     import torch
     from tval3_gb300 import autograd as AG
     cfg, op, b, xt = _loss_setup(oracle, size, rays, iters, cuda)
@@ -102,7 +106,7 @@ def test_unrolled_gradient_vs_finite_differences(cuda, oracle, size, rays, iters
     g = torch.Generator().manual_seed(5)
     v = torch.randn(b.numel(), dtype=torch.float64, generator=g).to(cuda)
     v /= v.norm()
-    h = 1e-3
+    h = 1e-5
     with torch.no_grad():
         fd_b = (loss(b + h * v, mu0, beta0) - loss(b - h * v, mu0, beta0)) / (2 * h)
         fd_mu = (loss(b, mu0 * (1 + h), beta0) - loss(b, mu0 * (1 - h), beta0)) / (2 * h * mu0)
