@@ -303,6 +303,23 @@ TVAL3_API tval3_status tval3_shrink_adjoint_f32(int64_t n, const float* d_v, dou
 TVAL3_API tval3_status tval3_shrink_adjoint_f64(int64_t n, const double* d_v, double t, int iso, const double* d_gW,
                                                 double* d_gv, double* d_gt, void* stream);
 
+/* ---------------------------------------------------------------------- *
+ * Dense A^T*y without any device allocation (no counterpart in the
+ * reference; same result as tval3_mat_vec_mul(trans = 1) on a dense FP32
+ * operator up to summation order).  For callers that must not allocate
+ * device memory while running (fixed memory budgets, their own pool
+ * allocator, no cudaMalloc inside a stream capture): A (rows x cols,
+ * row-major, one ray per row), y (rows) and x (cols) are the caller's device
+ * arrays; the slab partial sums live in one static device array of
+ * 1,048,576 floats, so cols must not exceed that (TVAL3_ERR_SHAPE
+ * otherwise).  The first call on a device looks up that array's address:
+ * make it before any stream capture.  Calls that overlap in time on one
+ * device share the array and race; order them.
+ * ---------------------------------------------------------------------- */
+#define TVAL3_NOALLOC_SCRATCH_FLOATS 1048576
+TVAL3_API tval3_status tval3_dense_rmatvec_f32_noalloc(int rows, int cols, const float* d_A, const float* d_y,
+                                                       float* d_x, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -213,6 +213,11 @@ void check_problem(const T* U, int dim_y, int dim_x, int dim_z, long A_rows, lon
 
 }  // namespace
 
+namespace tv3 {
+// noalloc.cu: dense A^T*y with its slab partials in a static device array
+void dense_rmatvec_noalloc_f32(long rows, long cols, const float* A, const float* y, float* x, cudaStream_t s);
+}  // namespace tv3
+
 extern "C" {
 
 void tval3_options_default(tval3_options* o) {
@@ -614,6 +619,11 @@ tval3_status tval3_Dt_f64(int dim_y, int dim_x, int dim_z, const double* V, doub
         launch_Dt_plain<double>(dim_y, dim_x, dim_z, V, out, (cudaStream_t)stream);
         TV3_CUDA(cudaGetLastError());
     });
+}
+
+tval3_status tval3_dense_rmatvec_f32_noalloc(int rows, int cols, const float* d_A, const float* d_y, float* d_x,
+                                             void* stream) {
+    return guard([&] { dense_rmatvec_noalloc_f32(rows, cols, d_A, d_y, d_x, (cudaStream_t)stream); });
 }
 
 }  // extern "C"

@@ -108,6 +108,7 @@ _SIG = {
     "tval3_Dt_f32": (_I, [_I, _I, _I, _P, _P, _P]),
     "tval3_D_f64": (_I, [_I, _I, _I, _P, _P, _P]),
     "tval3_Dt_f64": (_I, [_I, _I, _I, _P, _P, _P]),
+    "tval3_dense_rmatvec_f32_noalloc": (_I, [_I, _I, _P, _P, _P, _P]),
 }
 
 _lib = None
