@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-API measurement (profiling runs)")
     ap.add_argument("--only-spmv", default=None, choices=["fp32", "fp64vec", "df64", "bf16", "fp16"],
                     help="time only the CSR products of this precision (kernel profiling runs)")
+    ap.add_argument("--batch", type=int, default=64,
+                    help="slices of the batched-2D leg (0 skips it); printed under 'batched_2d'")
+    ap.add_argument("--only-batched", action="store_true", help="run only the batched-2D leg (development)")
     ap.add_argument("--solver-mode", type=int, default=1,
                     help="1: whole solve as one CUDA graph; 0: host-driven loop (same kernels; profilers "
                          "cannot see kernels inside graphs with conditional nodes)")
@@ -213,6 +216,8 @@ def run_ours(args):
     m, nnz = op32.rows, op32.nnz
     if args.only_spmv:
         return spmv_only(args, T, torch, geo, op32, n, m, nnz, dev)
+    if args.only_batched:
+        return {"batched_2d": batched_2d(args, T, torch, dev)}
     xd = torch.tensor(x_true.reshape(-1), device=dev)
     Ax = torch.empty(m, device=dev)
     op32.mat_vec_mul(0, xd, Ax, stream=torch.cuda.current_stream())
@@ -340,7 +345,7 @@ def run_ours(args):
     tf = ROOT / "profiles" / "spmv_traffic.json"
     if tf.exists():
         try:
-            traffic = json.loads(tf.read_text()).get(f"{dom[0]}_{args.size}")
+            traffic = json.loads(tf.read_text()).get(f"{dom[0]}_{head}_{args.size}")
         except Exception:
             traffic = None
     roofline = {"kernel": dom[0], "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
@@ -370,6 +375,8 @@ def run_ours(args):
                "d2h_bytes_per_step": int(d2h), "relerr_vs_oracle": relerr(Ue, xstar),
                "entry": ("tval3_gpu_3d_sparse_f64" if dtn == np.float64 else "tval3_gpu_3d_sparse_f32") +
                         f" (FP32 CSR+CSC values, host arrays, mode {head})"}
+
+    batched = batched_2d(args, T, torch, dev) if args.batch > 0 else None
 
     if rank != 0:
         return None
@@ -403,8 +410,69 @@ def run_ours(args):
         "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clocks,
+        "batched_2d": batched,
     }
     return line
+
+
+def batched_2d(args, T, torch, dev, reps=3):
+    """The batched-2D workload: args.batch ring slices (side ~ U[96, 256],
+    N_t ~ U[128, 512]) solved to the 2D options' tol/maxit in FP32, once as
+    ONE graph launch (tval3_batch_solve) and once slice after slice with a
+    plain FP32 solver each (one graph launch per slice); L2 flushed before
+    every repetition, CUDA events on the launching stream."""
+    from tval3_gb300.workloads import add_noise, config_batched_2d
+    sl = config_batched_2d(args.batch, seed=0)
+    stream = torch.cuda.Stream(device=dev)
+    ops, shapes, bs, Us = [], [], [], []
+    t0 = time.time()
+    for cfg, geo, x in sl:
+        op = T.Operator.from_geometry(geo, mode=0, precision=T.PREC_FP32)
+        xd = torch.tensor(x.reshape(-1), device=dev)
+        Ax = torch.empty(op.rows, device=dev)
+        op.mat_vec_mul(0, xd, Ax, stream=torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        b = add_noise(Ax.double().cpu().numpy(), cfg.noise, cfg.seed)
+        ops.append(op)
+        shapes.append(cfg.dims)
+        bs.append(torch.tensor(b, dtype=torch.float32, device=dev))
+        Us.append(torch.empty(int(np.prod(cfg.dims)), dtype=torch.float32, device=dev))
+    build_s = time.time() - t0
+    opts = sl[0][0].opts
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def timed(fn):
+        fn()  # warm-up (graph build)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                r = fn()
+                e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1000.0)
+        return float(np.median(ts)), r
+
+    bt = T.Batch(ops, shapes, opts)
+    t_batch, infos = timed(lambda: bt.solve(bs, Us, stream=stream))
+    Ub = [u.clone() for u in Us]
+    solvers = [T.Solver(op, sh, opts, mode=1) for op, sh in zip(ops, shapes)]
+    t_seq, infos_s = timed(lambda: [s.solve(b, u, stream=stream) for s, b, u in zip(solvers, bs, Us)])
+    same = all(torch.equal(a, b) for a, b in zip(Ub, Us))
+    for s in solvers:
+        s.close()
+    bt.close()
+    nnz = sum(op.nnz for op in ops)
+    return {"workload": f"{args.batch} ring slices, side U[96,256], N_t U[128,512], all pairs, Siddon CSR, FP32",
+            "voxels": int(sum(np.prod(sh) for sh in shapes)), "rays": int(sum(op.rows for op in ops)),
+            "nnz": int(nnz), "batch_s": round(t_batch, 5), "sequential_s": round(t_seq, 5),
+            "speedup_vs_sequential": round(t_seq / t_batch, 3), "slices_per_s": round(args.batch / t_batch, 2),
+            "iters_total": int(sum(i["total_iters"] for i in infos)),
+            "results_identical_to_sequential": bool(same), "device_build_s": round(build_s, 2)}
 
 
 def op_vectors(torch, pairs, dt, n, m, dev):

@@ -209,11 +209,16 @@ TVAL3_API tval3_status tval3_gpu_3d_geometry_sparse_f32(float* U, int dim_y, int
                                                         int Ut_len, int pagelocked, int mainGPU, int numGPUs,
                                                         const int* gpuArray, tval3_info* info);
 /* 2D: tval3_gpu(U, sparse_mat_host A, b, opts, Ut, pagelocked), 2d/tval3_gpu.h:9-13;
- * U is rows x cols (dim_y x dim_x), periodic D in 2D (2d/tval3.cu:202-331). */
+ * U is rows x cols (dim_y x dim_x), periodic D in 2D (2d/tval3.cu:202-331).
+ * layers = b_len / A.rows columns of b share A (2d/tval3.cu:1406-1426): U
+ * (and Ut) then hold rows*cols*layers values, one image per column, solved
+ * jointly (shared step sizes and penalties, D inside each image). */
 TVAL3_API tval3_status tval3_gpu_sparse(float* U, int rows, int cols, const tval3_sparse_host* A, const float* b,
                                         int b_len, const tval3_options* opts, const float* Ut, int Ut_len,
                                         int pagelocked, tval3_info* info);
-/* 2D dense: tval3_gpu(U, mat_host A, ...), 2d/tval3_gpu.h:15-19 */
+/* 2D dense: tval3_gpu(U, mat_host A, ...), 2d/tval3_gpu.h:15-19; layers as
+ * above.  opts->precision = TVAL3_PREC_BF16 stores A in BF16 with a per-row
+ * FP32 scale. */
 TVAL3_API tval3_status tval3_gpu_dense(float* U, int rows, int cols, const tval3_dense_host* A, const float* b,
                                        int b_len, const tval3_options* opts, const float* Ut, int Ut_len,
                                        int pagelocked, tval3_info* info);
@@ -267,6 +272,10 @@ TVAL3_API tval3_status tval3_df64_to_f64(const void* d_pairs, double* d_out, int
 typedef struct tval3_solver_s* tval3_solver;
 TVAL3_API tval3_status tval3_solver_create(tval3_solver* s, tval3_op A, int dim_y, int dim_x, int dim_z,
                                            const tval3_options* opts);
+/* The same with `layers` right-hand sides sharing A (the 2D entries' layers):
+ * d_b is rows(A) x layers and d_U cols(A) x layers, column-major. */
+TVAL3_API tval3_status tval3_solver_create_layers(tval3_solver* s, tval3_op A, int dim_y, int dim_x, int dim_z,
+                                                  int layers, const tval3_options* opts);
 /* mode 0: host-driven loop with device-resident scalars; mode 1: the whole
  * solve as one CUDA graph with conditional nodes (no host round trips). */
 TVAL3_API tval3_status tval3_solver_set_mode(tval3_solver s, int mode);
@@ -277,6 +286,40 @@ TVAL3_API tval3_status tval3_solver_solve(tval3_solver s, const void* d_b, void*
 TVAL3_API tval3_status tval3_solver_set_trace(tval3_solver s, const void* d_xstar);
 TVAL3_API tval3_status tval3_solver_trace(tval3_solver s, double* host_err, int len);
 TVAL3_API tval3_status tval3_solver_destroy(tval3_solver s);
+
+/* ---------------------------------------------------------------------- *
+ * Batched solves: many independent problems (the slices of a 2D stack, each
+ * with its own size and geometry) solved by ONE CUDA graph launch in which
+ * every problem is a parallel branch with its own loops.  The reference
+ * solves one image per tval3_gpu call (2d/tval3_gpu.h:9-19, 2d/tval3.cu:
+ * 1435-1513); these replace a host loop over that call.
+ * ---------------------------------------------------------------------- */
+typedef struct tval3_batch_s* tval3_batch;
+/* One solver per problem i over ops[i] (borrowed: keep the operators alive
+ * until the batch is destroyed) with volume dims[3i .. 3i+2] = (dim_y, dim_x,
+ * dim_z).  All operators must have the same vector type. */
+TVAL3_API tval3_status tval3_batch_create(tval3_batch* batch, const tval3_op* ops, const int* dims, int count,
+                                          const tval3_options* opts);
+/* d_b[i], d_U[i] and d_Ut[i] (d_Ut may be NULL, or hold NULL entries) are
+ * device vectors of the operators' vector type; infos (count entries, may be
+ * NULL) get each problem's counters, and secs = the time of the whole batch. */
+TVAL3_API tval3_status tval3_batch_solve(tval3_batch batch, const void* const* d_b, void* const* d_U,
+                                         const void* const* d_Ut, tval3_info* infos, void* stream);
+TVAL3_API tval3_status tval3_batch_destroy(tval3_batch batch);
+
+/* Host form: tval3_gpu(U, sparse A, b, opts, Ut) of every slice (FP32,
+ * U rows x cols), all slices in one launch. */
+typedef struct {
+    float* U;
+    int rows, cols;
+    const tval3_sparse_host* A;
+    const float* b;
+    int b_len;
+    const float* Ut;
+    int Ut_len;
+} tval3_slice_host;
+TVAL3_API tval3_status tval3_gpu_batched(const tval3_slice_host* slices, int count, const tval3_options* opts,
+                                         tval3_info* infos);
 
 /* ---------------------------------------------------------------------- *
  * Stencil operators on device arrays (D_gpu / Dt_gpu, 3d/tval3_gpu_3d.cpp:

@@ -74,6 +74,12 @@ def lib():
         L.oracle_tval3_dense.restype = C.c_int
         L.oracle_tval3_dense.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_long, P, P,
                                          C.POINTER(OracleOpts), P, P, C.POINTER(OracleInfo), P]
+        L.oracle_tval3_csr_layers.restype = C.c_int
+        L.oracle_tval3_csr_layers.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_long, P, P, P, P, P,
+                                              P, P, C.POINTER(OracleOpts), P, P, C.POINTER(OracleInfo)]
+        L.oracle_tval3_dense_layers.restype = C.c_int
+        L.oracle_tval3_dense_layers.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_long, P, P,
+                                                C.POINTER(OracleOpts), P, P, C.POINTER(OracleInfo)]
         L.oracle_num_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -219,6 +225,32 @@ def tval3_dense(dims, A, b, opts=None, prec=0, Ut=None):
     lib().oracle_tval3_dense(prec, p, q, r, A.shape[0], _p(A), _p(b), C.byref(o), _p(U), _p(Ut_a), C.byref(info),
                              None)
     return U.reshape(r, q, p), info.as_dict()
+
+
+def tval3_layers(dims, L, A, b, opts=None, prec=0, Ut=None):
+    """Joint solve of L layers sharing one matrix (the reference 2D entry with
+    b.len = A.rows * layers).  A: (ptr, ind, val) CSR or a dense row-major
+    array; b: m x L column-major (layer slowest).  Returns (U [L, z, x, y],
+    info)."""
+    p, q, r = dims
+    n = p * q * r
+    dt = np.float64 if prec == 0 else np.float32
+    b = np.ascontiguousarray(b, dt).reshape(-1)
+    U = np.zeros(n * L, dt)
+    Ut_a = None if Ut is None else np.ascontiguousarray(Ut, dt).reshape(-1)
+    o = opts if isinstance(opts, OracleOpts) else make_opts(**(opts or {}))
+    info = OracleInfo()
+    if isinstance(A, tuple):
+        ptr, ind, val = A
+        m = ptr.size - 1
+        tptr, tind, tval = transpose(m, n, ptr, ind, val)
+        lib().oracle_tval3_csr_layers(prec, p, q, r, L, m, _p(ptr), _p(ind), _p(val), _p(tptr), _p(tind), _p(tval),
+                                      _p(b), C.byref(o), _p(U), _p(Ut_a), C.byref(info))
+    else:
+        A = np.ascontiguousarray(A, np.float32)
+        lib().oracle_tval3_dense_layers(prec, p, q, r, L, A.shape[0], _p(A), _p(b), C.byref(o), _p(U), _p(Ut_a),
+                                        C.byref(info))
+    return U.reshape(L, r, q, p), info.as_dict()
 
 
 def num_threads() -> int:

@@ -72,9 +72,13 @@ void pfor(long n, F f) {
     for (long i = 0; i < n; ++i) f(i);
 }
 
+// L > 1: L independent volumes ("layers", the reference 2D entry's
+// b.len / A.rows, 2d/tval3.cu:1418-1425) stored one after the other; D acts
+// inside each layer and A on each layer's column.
 struct Dims {
     int p, q, r;  // dim_y (fastest), dim_x, dim_z
-    long n() const { return (long)p * q * r; }
+    int L = 1;
+    long n() const { return (long)p * q * r * L; }
 };
 
 // D: periodic forward differences.  Component 0 runs along the fastest axis
@@ -82,12 +86,13 @@ struct Dims {
 // 3d/tval3_gpu_3d.cpp:271-314 with 3d/tval3_gpu_3d_kernels.cu:170-215.
 template <class T>
 void D_op(const Dims& g, const T* U, T* D0, T* D1, T* D2) {
-    const long pq = (long)g.p * g.q;
-    pfor((long)g.q * g.r, [&](long xz) {
+    const long pq = (long)g.p * g.q, n1 = pq * g.r;
+    pfor((long)g.q * g.r * g.L, [&](long xzl) {
+        long xz = xzl % ((long)g.q * g.r), l0 = (xzl / ((long)g.q * g.r)) * n1;
         long x = xz % g.q, z = xz / g.q;
-        long base = x * g.p + z * pq;
-        long bx = (x + 1 < g.q) ? base + g.p : z * pq;               // x+1 wraps to 0
-        long bz = (z + 1 < g.r) ? base + pq : x * g.p;                // z+1 wraps to 0
+        long base = l0 + x * g.p + z * pq;
+        long bx = (x + 1 < g.q) ? base + g.p : l0 + z * pq;          // x+1 wraps to 0
+        long bz = (z + 1 < g.r) ? base + pq : l0 + x * g.p;           // z+1 wraps to 0
         for (long y = 0; y < g.p; ++y) {
             long i = base + y;
             T u = U[i];
@@ -102,10 +107,11 @@ void D_op(const Dims& g, const T* U, T* D0, T* D1, T* D2) {
 // D^T: 3d/tval3_gpu_3d_kernels.cu:479-510; res = (xp - X) + (yp - Y) + (zp - Z).
 template <class T>
 void Dt_op(const Dims& g, const T* V0, const T* V1, const T* V2, T* res) {
-    const long pq = (long)g.p * g.q;
-    pfor((long)g.q * g.r, [&](long xz) {
+    const long pq = (long)g.p * g.q, n1 = pq * g.r;
+    pfor((long)g.q * g.r * g.L, [&](long xzl) {
+        long xz = xzl % ((long)g.q * g.r), l0 = (xzl / ((long)g.q * g.r)) * n1;
         long x = xz % g.q, z = xz / g.q;
-        long base = x * g.p + z * pq;
+        long base = l0 + x * g.p + z * pq;
         long bx = (x > 0) ? base - g.p : base + (long)(g.q - 1) * g.p;
         long bz = (z > 0) ? base - pq : base + (long)(g.r - 1) * pq;
         for (long y = 0; y < g.p; ++y) {
@@ -173,6 +179,25 @@ struct DenseOp : Op<T> {
                 for (long c = c0; c < c1; ++c) x[c] += (T)row[c] * yr;
             }
         });
+    }
+};
+
+// The same operator on each of L layers (block diagonal): the reference's
+// multi-column products (csrmm / gemm with `layers` columns,
+// 2d/mat_vec_mul.h:65-71, :96-99).
+template <class T>
+struct LayerOp : Op<T> {
+    const Op<T>& A;
+    int L;
+    LayerOp(const Op<T>& a, int l) : A(a), L(l) {
+        this->m = a.m * l;
+        this->n = a.n * l;
+    }
+    void N(const T* x, T* y) const override {
+        for (int l = 0; l < L; ++l) A.N(x + l * A.n, y + l * A.m);
+    }
+    void Tr(const T* y, T* x) const override {
+        for (int l = 0; l < L; ++l) A.Tr(y + l * A.m, x + l * A.n);
     }
 };
 
@@ -786,6 +811,43 @@ int oracle_tval3_dense(int prec, int p, int q, int r, long m, const float* a, co
     DenseOp<float> A;
     A.m = m; A.n = g.n(); A.a = a;
     return solve<float>(g, A, (const float*)b, *o, (float*)U_out, (const float*)Ut, info, trace_f);
+}
+
+// TVAL3 over L layers sharing one CSR matrix: b is m x L and U n x L, both
+// column-major (layer slowest); one joint solve (shared step sizes and
+// penalties), D inside each layer.
+int oracle_tval3_csr_layers(int prec, int p, int q, int r, int L, long m, const int* ptr, const int* ind,
+                            const float* val, const int* tptr, const int* tind, const float* tval, const void* b,
+                            const oracle_opts* o, void* U_out, const void* Ut, oracle_info* info) {
+    Dims g{p, q, r, L};
+    const long n1 = (long)p * q * r;
+    if (prec == 0) {
+        CsrOp<double> A;
+        A.m = m; A.n = n1; A.ptr = ptr; A.ind = ind; A.val = val; A.tptr = tptr; A.tind = tind; A.tval = tval;
+        LayerOp<double> AL(A, L);
+        return solve<double>(g, AL, (const double*)b, *o, (double*)U_out, (const double*)Ut, info, nullptr);
+    }
+    CsrOp<float> A;
+    A.m = m; A.n = n1; A.ptr = ptr; A.ind = ind; A.val = val; A.tptr = tptr; A.tind = tind; A.tval = tval;
+    LayerOp<float> AL(A, L);
+    return solve<float>(g, AL, (const float*)b, *o, (float*)U_out, (const float*)Ut, info, nullptr);
+}
+
+// TVAL3 over L layers sharing one dense row-major m x n matrix.
+int oracle_tval3_dense_layers(int prec, int p, int q, int r, int L, long m, const float* a, const void* b,
+                              const oracle_opts* o, void* U_out, const void* Ut, oracle_info* info) {
+    Dims g{p, q, r, L};
+    const long n1 = (long)p * q * r;
+    if (prec == 0) {
+        DenseOp<double> A;
+        A.m = m; A.n = n1; A.a = a;
+        LayerOp<double> AL(A, L);
+        return solve<double>(g, AL, (const double*)b, *o, (double*)U_out, (const double*)Ut, info, nullptr);
+    }
+    DenseOp<float> A;
+    A.m = m; A.n = n1; A.a = a;
+    LayerOp<float> AL(A, L);
+    return solve<float>(g, AL, (const float*)b, *o, (float*)U_out, (const float*)Ut, info, nullptr);
 }
 
 int oracle_num_threads(void) {

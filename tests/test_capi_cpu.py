@@ -81,6 +81,25 @@ def test_null_arguments(lib):
     assert lib.tval3_last_error_message()
     assert lib.tval3_mat_vec_mul(None, 0, None, None, None) == 1
     assert lib.tval3_solver_solve(None, None, None, None, None, None) == 1
+    assert lib.tval3_batch_create(None, None, None, 0, None) == 1
+    assert lib.tval3_batch_solve(None, None, None, None, None, None) == 1
+    assert lib.tval3_gpu_batched(None, 0, None, None) == 1
+
+
+def test_batched_slice_errors(lib):
+    """tval3_gpu_batched validates every slice (like tval3_gpu) before any
+    device work: a slice whose b does not match its matrix is rejected."""
+    import ctypes as C
+    from tval3_gb300 import capi, default_options
+    A = _tiny()
+    st_A = A.struct()
+    U = np.zeros(2, np.float32)
+    b = np.ones(3, np.float32)
+    arr = (capi.SliceHost * 1)()
+    arr[0] = capi.SliceHost(U.ctypes.data, 2, 1, C.cast(C.pointer(st_A), C.c_void_p), b.ctypes.data, 3, None, 0)
+    o = default_options()
+    assert lib.tval3_gpu_batched(arr, 1, C.byref(o), None) == 2
+    assert b"b.len must be equal" in lib.tval3_last_error_message()
 
 
 def test_python_mirror_names():

@@ -272,3 +272,21 @@ def test_scale_b_rules(oracle):
     for b, scl in (([0.1, 0.2], 0.5 / 0.1), ([1.0, 3.0], 1.5 / 2.0), ([0.0, 1.0], 1.0), ([0.5, 0.5], 1.0)):
         _, info = oracle.tval3_csr((2, 1, 1), ptr, ind, val, np.array(b), dict(maxit=1, maxcnt=1), prec=0)
         assert abs(info["scl"] - scl) < 1e-12
+
+
+def test_oracle_layers_of_identical_columns_equal_single_solve(oracle):
+    """A joint solve of L identical layers takes the same steps as the single
+    solve (every inner product, f and the Armijo terms scale by L), so each
+    layer equals the single-layer solution."""
+    from tval3_gb300 import workloads as W
+    geo = W.ring_geometry(16, 24)
+    x = W.ellipse_phantom(16, 3, seed=1, axes=(2.0, 6.4))
+    ptr, ind, val = oracle.siddon_csr(geo)
+    b = W.add_noise(oracle.spmv(ptr, ind, val, x), 0.01, 1).astype(np.float64)
+    o = dict(mu=256., mu0=64., beta=32., beta0=8., tol=1e-4, maxit=60, tv_iso=0)
+    U1, i1 = oracle.tval3_csr((16, 16, 1), ptr, ind, val, b, o)
+    UL, iL = oracle.tval3_layers((16, 16, 1), 3, (ptr, ind, val), np.concatenate([b, b, b]), o)
+    assert (iL["total_iters"], iL["outer_iters"], iL["backtracks"]) == \
+        (i1["total_iters"], i1["outer_iters"], i1["backtracks"])
+    for l in range(3):
+        assert np.linalg.norm(UL[l].reshape(-1) - U1.reshape(-1)) <= 1e-9 * np.linalg.norm(U1)

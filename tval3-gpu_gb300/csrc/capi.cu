@@ -9,6 +9,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 #include "solver.h"
 #include "tval3/tval3_c.h"
@@ -25,6 +26,17 @@ struct tval3_op_s {
         delete q;
         delete f;
         delete d;
+    }
+};
+
+struct tval3_batch_s {
+    Batch<float>* f = nullptr;
+    Batch<double>* d = nullptr;
+    Batch<df64>* q = nullptr;
+    ~tval3_batch_s() {
+        delete f;
+        delete d;
+        delete q;
     }
 };
 
@@ -177,10 +189,10 @@ void check_vec(const T* v, long n, const char* what) {
 template <class T>
 void solve_host(LinOp<T>* op, Ext<T>* U, int dim_y, int dim_x, int dim_z, const Ext<T>* b, int b_len,
                 const tval3_options* opts, const Ext<T>* Ut, int Ut_len, tval3_info* info,
-                std::chrono::steady_clock::time_point t0) {
+                std::chrono::steady_clock::time_point t0, int layers = 1) {
     using E = Ext<T>;
     std::unique_ptr<LinOp<T>> hold(op);
-    const long n = (long)dim_y * dim_x * dim_z;
+    const long n = (long)dim_y * dim_x * dim_z * layers;
     DBuf<E> db, dU, dUt;
     db.alloc(std::max<long>(b_len, 1));
     dU.alloc(std::max<long>(n, 1));
@@ -190,7 +202,7 @@ void solve_host(LinOp<T>* op, Ext<T>* U, int dim_y, int dim_x, int dim_z, const 
         dUt.alloc(n);
         TV3_CUDA(cudaMemcpy(dUt.p, Ut, n * sizeof(E), cudaMemcpyHostToDevice));
     }
-    Solver<T> s(op, dim_y, dim_x, dim_z, *opts);
+    Solver<T> s(op, dim_y, dim_x, dim_z, *opts, layers);
     s.mode = 1;  // the whole solve as one graph launch
     tval3_info inf{};
     s.solve(db.p, dU.p, use_ut ? dUt.p : nullptr, &inf, 0);
@@ -209,6 +221,26 @@ void check_problem(const T* U, int dim_y, int dim_x, int dim_z, long A_rows, lon
     if (b_len != A_rows) arg_error(TVAL3_ERR_SHAPE, "Argument error: b.len must be equal to A.dim_y!");
     if (b_len > 0 && !b) arg_error(TVAL3_ERR_ARG, "Argument error: b is NULL!");
     check_vec(b, b_len, "measurement b");
+}
+
+// The 2D entries' form (2d/tval3.cu:1406-1426): layers = b.len / A.rows
+// columns of b share A; U holds A.cols * layers values (U and Ut column-major,
+// one image per column).  Returns the number of layers.
+template <class T>
+int check_problem_2d(const T* U, int rows, int cols, long A_rows, long A_cols, const T* b, int b_len, const T* Ut,
+                     int Ut_len) {
+    if (!U || rows <= 0 || cols <= 0) arg_error(TVAL3_ERR_ARG, "Argument error: U must be a non-empty image!");
+    const long n = (long)rows * cols;
+    if (n != A_cols) arg_error(TVAL3_ERR_SHAPE, "Argument error: the length of U must be equal to A.cols * layers!");
+    if (A_rows == 0 && b_len == 0) return 1;
+    if (A_rows <= 0 || b_len <= 0 || b_len % A_rows != 0)
+        arg_error(TVAL3_ERR_SHAPE, "Argument error: b.len must be equal to A.rows * layers!");
+    const int layers = (int)(b_len / A_rows);
+    if (Ut && Ut_len > 0 && Ut_len != n * layers)
+        arg_error(TVAL3_ERR_SHAPE, "Argument error: U and Ut must have the same size!");
+    if (!b) arg_error(TVAL3_ERR_ARG, "Argument error: b is NULL!");
+    check_vec(b, b_len, "measurement b");
+    return layers;
 }
 
 }  // namespace
@@ -269,9 +301,15 @@ tval3_status tval3_gpu_3d_sparse_f64(double* U, int dim_y, int dim_x, int dim_z,
 }
 
 tval3_status tval3_gpu_sparse(float* U, int rows, int cols, const tval3_sparse_host* A, const float* b, int b_len,
-                              const tval3_options* opts, const float* Ut, int Ut_len, int pagelocked,
-                              tval3_info* info) {
-    return tval3_gpu_3d_sparse_f32(U, rows, cols, 1, A, b, b_len, opts, Ut, Ut_len, pagelocked, -1, 0, nullptr, info);
+                              const tval3_options* opts, const float* Ut, int Ut_len, int, tval3_info* info) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_opts(opts);
+        if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+        const int layers = check_problem_2d(U, rows, cols, A->rows, A->cols, b, b_len, Ut, Ut_len);
+        solve_host<float>(sparse_op<float>(A, TVAL3_PREC_FP32), U, rows, cols, 1, b, b_len, opts, Ut, Ut_len, info,
+                          t0, layers);
+    });
 }
 
 tval3_status tval3_gpu_3d_dense_f32(float* U, int dim_y, int dim_x, int dim_z, const tval3_dense_host* A,
@@ -301,9 +339,16 @@ tval3_status tval3_gpu_3d_dense_f64(double* U, int dim_y, int dim_x, int dim_z, 
 }
 
 tval3_status tval3_gpu_dense(float* U, int rows, int cols, const tval3_dense_host* A, const float* b, int b_len,
-                             const tval3_options* opts, const float* Ut, int Ut_len, int pagelocked,
-                             tval3_info* info) {
-    return tval3_gpu_3d_dense_f32(U, rows, cols, 1, A, b, b_len, opts, Ut, Ut_len, pagelocked, -1, 0, nullptr, info);
+                             const tval3_options* opts, const float* Ut, int Ut_len, int, tval3_info* info) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_opts(opts);
+        if (!A || !A->data || A->rows < 0 || A->cols < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad dense matrix!");
+        const int layers = check_problem_2d(U, rows, cols, A->rows, A->cols, b, b_len, Ut, Ut_len);
+        const int prec = (opts->precision == TVAL3_PREC_BF16) ? TVAL3_PREC_BF16 : TVAL3_PREC_FP32;
+        solve_host<float>(make_dense_op<float>(A->rows, A->cols, A->data, A->row_major, A->val_type, prec, 0), U,
+                          rows, cols, 1, b, b_len, opts, Ut, Ut_len, info, t0, layers);
+    });
 }
 
 tval3_status tval3_gpu_3d_geometry_f32(float* U, int dim_y, int dim_x, int dim_z, const tval3_geometry_host* A,
@@ -552,6 +597,30 @@ tval3_status tval3_solver_create(tval3_solver* s, tval3_op A, int dim_y, int dim
     });
 }
 
+tval3_status tval3_solver_create_layers(tval3_solver* s, tval3_op A, int dim_y, int dim_x, int dim_z, int layers,
+                                        const tval3_options* opts) {
+    return guard([&] {
+        if (!s || !A) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver or operator!");
+        if (layers < 1) arg_error(TVAL3_ERR_ARG, "Argument error: layers must be positive!");
+        check_opts(opts);
+        const long n = (long)dim_y * dim_x * dim_z;
+        long cols = A->q ? A->q->n : (A->dbl ? A->d->n : A->f->n);
+        if (dim_y <= 0 || dim_x <= 0 || dim_z <= 0 || n != cols)
+            arg_error(TVAL3_ERR_SHAPE, "Argument error: the length of U must be equal to A.dim_x!");
+        auto* h = new tval3_solver_s();
+        try {
+            h->dbl = A->dbl;
+            if (A->q) h->q = new Solver<df64>(A->q, dim_y, dim_x, dim_z, *opts, layers);
+            else if (A->dbl) h->d = new Solver<double>(A->d, dim_y, dim_x, dim_z, *opts, layers);
+            else h->f = new Solver<float>(A->f, dim_y, dim_x, dim_z, *opts, layers);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *s = h;
+    });
+}
+
 tval3_status tval3_solver_set_mode(tval3_solver s, int mode) {
     return guard([&] {
         if (!s || mode < 0 || mode > 1) arg_error(TVAL3_ERR_ARG, "Argument error: bad solver mode!");
@@ -571,6 +640,7 @@ tval3_status tval3_solver_set_trace(tval3_solver s, const void* d_xstar) {
     return guard([&] {
         if (!s) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver!");
         with_solver(s, [&](auto& v) {
+            if (d_xstar && v.L > 1) arg_error(TVAL3_ERR_UNSUPPORTED, "error trace of a multi-layer solver");
             v.xstar = d_xstar;
             if (v.gexec) cudaGraphExecDestroy(v.gexec);
             v.gexec = nullptr;
@@ -618,6 +688,113 @@ tval3_status tval3_Dt_f64(int dim_y, int dim_x, int dim_z, const double* V, doub
         if (dim_y <= 0 || dim_x <= 0 || dim_z <= 0 || !V || !out) arg_error(TVAL3_ERR_ARG, "Argument error: bad volume!");
         launch_Dt_plain<double>(dim_y, dim_x, dim_z, V, out, (cudaStream_t)stream);
         TV3_CUDA(cudaGetLastError());
+    });
+}
+
+tval3_status tval3_batch_create(tval3_batch* batch, const tval3_op* ops, const int* dims, int count,
+                                const tval3_options* opts) {
+    return guard([&] {
+        if (!batch || !ops || !dims || count <= 0) arg_error(TVAL3_ERR_ARG, "Argument error: empty batch!");
+        check_opts(opts);
+        // 0: float vectors, 1: double, 2: double-float
+        auto kind = [](tval3_op op) { return op->q ? 2 : (op->dbl ? 1 : 0); };
+        for (int i = 0; i < count; ++i) {
+            if (!ops[i]) arg_error(TVAL3_ERR_ARG, "Argument error: NULL operator in batch!");
+            if (kind(ops[i]) != kind(ops[0]))
+                arg_error(TVAL3_ERR_ARG, "Argument error: all operators of a batch must have the same vector type!");
+            const int* d = dims + 3 * (long)i;
+            const long n = (long)d[0] * d[1] * d[2];
+            const long cols = ops[i]->q ? ops[i]->q->n : (ops[i]->dbl ? ops[i]->d->n : ops[i]->f->n);
+            if (d[0] <= 0 || d[1] <= 0 || d[2] <= 0 || n != cols)
+                arg_error(TVAL3_ERR_SHAPE, "Argument error: the length of U must be equal to A.dim_x!");
+        }
+        auto* h = new tval3_batch_s();
+        try {
+            auto fill = [&](auto*& bt, auto get) {
+                using BT = std::remove_reference_t<decltype(*bt)>;
+                using ST = std::remove_pointer_t<typename decltype(BT::s)::value_type>;
+                bt = new BT();
+                for (int i = 0; i < count; ++i) {
+                    const int* d = dims + 3 * (long)i;
+                    bt->s.push_back(nullptr);
+                    bt->s.back() = new ST(get(ops[i]), d[0], d[1], d[2], *opts);
+                }
+            };
+            if (kind(ops[0]) == 2) fill(h->q, [](tval3_op op) { return op->q; });
+            else if (kind(ops[0]) == 1) fill(h->d, [](tval3_op op) { return op->d; });
+            else fill(h->f, [](tval3_op op) { return op->f; });
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *batch = h;
+    });
+}
+
+tval3_status tval3_batch_solve(tval3_batch batch, const void* const* d_b, void* const* d_U, const void* const* d_Ut,
+                               tval3_info* infos, void* stream) {
+    return guard([&] {
+        if (!batch || !d_b || !d_U) arg_error(TVAL3_ERR_ARG, "Argument error: NULL batch or vector list!");
+        const size_t k = batch->q ? batch->q->s.size() : (batch->d ? batch->d->s.size() : batch->f->s.size());
+        for (size_t i = 0; i < k; ++i)
+            if (!d_b[i] || !d_U[i]) arg_error(TVAL3_ERR_ARG, "Argument error: NULL vector in batch!");
+        std::vector<const void*> ut(k, nullptr);
+        if (d_Ut) ut.assign(d_Ut, d_Ut + k);
+        cudaStream_t st = (cudaStream_t)stream;
+        if (batch->q) batch->q->solve(d_b, d_U, ut.data(), infos, st);
+        else if (batch->d) batch->d->solve(d_b, d_U, ut.data(), infos, st);
+        else batch->f->solve(d_b, d_U, ut.data(), infos, st);
+    });
+}
+
+tval3_status tval3_batch_destroy(tval3_batch batch) {
+    return guard([&] { delete batch; });
+}
+
+tval3_status tval3_gpu_batched(const tval3_slice_host* slices, int count, const tval3_options* opts,
+                               tval3_info* infos) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        if (!slices || count <= 0) arg_error(TVAL3_ERR_ARG, "Argument error: empty batch!");
+        check_opts(opts);
+        for (int i = 0; i < count; ++i) {
+            const tval3_slice_host& sl = slices[i];
+            if (!sl.A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+            check_sparse(sl.A);
+            check_problem(sl.U, sl.rows, sl.cols, 1, sl.A->rows, sl.A->cols, sl.b, sl.b_len, sl.Ut, sl.Ut_len);
+        }
+        std::vector<std::unique_ptr<LinOp<float>>> ops;
+        std::vector<DBuf<float>> db(count), dU(count), dUt(count);
+        std::vector<const void*> pb(count), put(count, nullptr);
+        std::vector<void*> pU(count);
+        Batch<float> bt;
+        for (int i = 0; i < count; ++i) {
+            const tval3_slice_host& sl = slices[i];
+            const long n = (long)sl.rows * sl.cols;
+            ops.emplace_back(sparse_op<float>(sl.A, TVAL3_PREC_FP32));
+            db[i].alloc(std::max(sl.b_len, 1));
+            dU[i].alloc(std::max<long>(n, 1));
+            if (sl.b_len) TV3_CUDA(cudaMemcpy(db[i].p, sl.b, sl.b_len * sizeof(float), cudaMemcpyHostToDevice));
+            if (sl.Ut && sl.Ut_len == n) {
+                dUt[i].alloc(n);
+                TV3_CUDA(cudaMemcpy(dUt[i].p, sl.Ut, n * sizeof(float), cudaMemcpyHostToDevice));
+                put[i] = dUt[i].p;
+            }
+            pb[i] = db[i].p;
+            pU[i] = dU[i].p;
+            bt.s.push_back(new Solver<float>(ops.back().get(), sl.rows, sl.cols, 1, *opts));
+        }
+        std::vector<tval3_info> inf(count);
+        bt.solve(pb.data(), pU.data(), put.data(), inf.data(), 0);
+        for (int i = 0; i < count; ++i) {
+            const tval3_slice_host& sl = slices[i];
+            TV3_CUDA(cudaMemcpy(sl.U, dU[i].p, (size_t)sl.rows * sl.cols * sizeof(float), cudaMemcpyDeviceToHost));
+        }
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        for (int i = 0; i < count; ++i) {
+            inf[i].outer_secs = secs;
+            if (infos) infos[i] = inf[i];
+        }
     });
 }
 

@@ -5,12 +5,20 @@
 // slab of rows and the slabs are added by a second pass (deterministic, no
 // atomics).  Replaces cublasSgemv.
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 #include "dbuf.h"
 #include "ops.h"
 #include "tval3/tval3_c.h"
 
 namespace tv3 {
+
+// tensor-core multi-RHS products of BF16 operators (dense_tc.cu)
+struct UmmaPlan;
+bool umma_supported(long m, long n, int L);
+UmmaPlan* umma_plan_create(long m, long n, int L, const __nv_bfloat16* Aq);
+void umma_plan_destroy(UmmaPlan* p);
+void umma_apply(const UmmaPlan* p, int trans, const MatIO<float>& io, int epi, const float* rs, cudaStream_t s);
 
 template <class T, class V, int EPI>
 __global__ void __launch_bounds__(256) k_dense_N(long m, long n, const V* __restrict__ A, const float* __restrict__ rs,
@@ -88,6 +96,100 @@ __global__ void k_dense_T_sum(long n, int slabs, const T* __restrict__ part, Mat
     }
 }
 
+// Multi-RHS forms (L > 1, vectors interleaved: element (row, layer) at
+// row * L + layer; the reference's cublasSgemm with `layers` columns,
+// 2d/mat_vec_mul.h:91-99).  A*X: one warp per row, each lane a strided part
+// of the row for up to 32 layers, then a warp reduction per layer.  A^T*Y:
+// one warp per (column, layer chunk of 32) over a slab of rows, lanes =
+// layers, slab partials added in a fixed order.
+template <class T, class V, int EPI>
+__global__ void __launch_bounds__(256) k_dense_NL(long m, long n, int L, const V* __restrict__ A,
+                                                  const float* __restrict__ rs, MatIO<T> io) {
+    count_launch(io.ctl);
+    const int lane = threadIdx.x & 31;
+    const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = ((long)gridDim.x * blockDim.x) >> 5;
+    const int sel = io.by_parity ? io.ctl->parity : 0;
+    const T* __restrict__ x = io.x[sel];
+    T* __restrict__ y = io.y[sel];
+    double acc0 = 0.0, acc1 = 0.0;
+    for (long r = w; r < m; r += nw) {
+        const V* row = A + r * n;
+        for (int l0 = 0; l0 < L; l0 += 32) {
+            const int nl = min(32, L - l0);
+            T s[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) s[j] = T(0);
+            for (long c = lane; c < n; c += 32) {
+                const T a = (T)Acc<T, V>::load(row + c);
+                const T* xc = x + c * L + l0;
+#pragma unroll
+                for (int j = 0; j < 32; ++j)
+                    if (j < nl) s[j] += a * xc[j];
+            }
+            // lane j ends with the row sum of layer l0 + j
+            T mine = T(0);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                T v = s[j];
+                for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+                if (lane == j) mine = v;
+            }
+            if (lane < nl) {
+                if (rs) mine *= (T)rs[r];
+                const long o = r * L + l0 + lane;
+                if (EPI == SPMV_PLAIN) y[o] = mine;
+                else if (EPI == SPMV_SUB) y[o] = mine - io.sub[o];
+                else if (EPI == SPMV_LAM35) {
+                    y[o] = mine;
+                    double t = (double)mine - (double)io.b[o];
+                    acc0 += t * t;
+                    acc1 += (double)io.delta[o] * t;
+                } else if (EPI == SPMV_NORM2) {
+                    acc0 += (double)mine * mine;
+                }
+            }
+        }
+    }
+    if (EPI == SPMV_LAM35 || EPI == SPMV_NORM2) {
+        double v[2] = {acc0, acc1}, tot[2];
+        if (grid_reduce<2>(v, io.part, io.ticket, tot) && threadIdx.x == 0) {
+            Ctl* c = io.ctl;
+            if (EPI == SPMV_LAM35) {
+                c->lam3 = tot[0];
+                c->lam5 = tot[1];
+            } else {
+                c->Add = tot[0];
+                c->tau = fabs(c->dd / (c->dDd + c->muDbeta * c->Add));
+            }
+        }
+    }
+}
+
+// part[slab][c * L + l] = sum over the slab's rows of A[r][c] * s_r * Y[r * L + l]
+template <class T, class V>
+__global__ void __launch_bounds__(256) k_dense_TL_part(long m, long n, int L, long rows_per_slab,
+                                                       const V* __restrict__ A, const float* __restrict__ rs,
+                                                       MatIO<T> io, T* __restrict__ part) {
+    count_launch(io.ctl);
+    const int sel = io.by_parity ? io.ctl->parity : 0;
+    const T* __restrict__ yv = io.x[sel];
+    const int lane = threadIdx.x & 31;
+    const long chunks = (L + 31) / 32;
+    const long wi = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // (column, chunk)
+    if (wi >= n * chunks) return;
+    const long c = wi / chunks, l = (wi % chunks) * 32 + lane;
+    const long slab = blockIdx.y;
+    const long r0 = slab * rows_per_slab, r1 = min(m, r0 + rows_per_slab);
+    if (l >= L) return;
+    T s = T(0);
+    for (long r = r0; r < r1; ++r) {
+        T yr = yv[r * L + l];
+        if (rs) yr *= (T)rs[r];
+        s += (T)Acc<T, V>::load(A + r * n + c) * yr;
+    }
+    part[slab * n * L + c * L + l] = s;
+}
+
 template <class T, class V>
 struct DenseOp : LinOp<T> {
     DBuf<V> a;
@@ -98,6 +200,10 @@ struct DenseOp : LinOp<T> {
 
     void apply(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const override {
         const long m = this->m, n = this->n;
+        if (io.L > 1) {
+            apply_layers(trans, io, epi, s);
+            return;
+        }
         if (!trans) {
             long g = std::min<long>((m * 32 + 255) / 256, (long)num_sms() * 8);
             int grid = (int)std::max<long>(g, 1);
@@ -114,6 +220,76 @@ struct DenseOp : LinOp<T> {
             k_dense_T_sum<T><<<(int)std::max<long>(g, 1), 256, 0, s>>>(n, slabs, part.p, io, epi == SPMV_SUB);
         }
         TV3_CUDA(cudaGetLastError());
+    }
+
+    void apply_layers(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const {
+        const long m = this->m, n = this->n;
+        const int L = io.L;
+        if constexpr (std::is_same<T, float>::value && std::is_same<V, __nv_bfloat16>::value) {
+            if (umma && umma_L == L) {
+                umma_apply(umma, trans, io, epi, rs.p, s);
+                return;
+            }
+        }
+        if (!trans) {
+            long g = std::min<long>((m * 32 + 255) / 256, (long)num_sms() * 8);
+            int grid = (int)std::max<long>(g, 1);
+            switch (epi) {
+                case SPMV_SUB: k_dense_NL<T, V, SPMV_SUB><<<grid, 256, 0, s>>>(m, n, L, a.p, rs.p, io); break;
+                case SPMV_LAM35: k_dense_NL<T, V, SPMV_LAM35><<<grid, 256, 0, s>>>(m, n, L, a.p, rs.p, io); break;
+                case SPMV_NORM2: k_dense_NL<T, V, SPMV_NORM2><<<grid, 256, 0, s>>>(m, n, L, a.p, rs.p, io); break;
+                default: k_dense_NL<T, V, SPMV_PLAIN><<<grid, 256, 0, s>>>(m, n, L, a.p, rs.p, io); break;
+            }
+        } else {
+            long tiles, slabs_l, rps;
+            layer_slabs(L, tiles, slabs_l, rps);
+            if (part_l.n < (size_t)slabs_l * n * L)
+                throw Error{1, "dense multi-RHS product used before prepare()"};
+            k_dense_TL_part<T, V><<<dim3((unsigned)tiles, (unsigned)slabs_l), 256, 0, s>>>(m, n, L, rps, a.p, rs.p,
+                                                                                          io, part_l.p);
+            long g = std::min<long>((n * L + 255) / 256, (long)num_sms() * 8);
+            k_dense_T_sum<T><<<(int)std::max<long>(g, 1), 256, 0, s>>>(n * L, (int)slabs_l, part_l.p, io,
+                                                                       epi == SPMV_SUB);
+        }
+        TV3_CUDA(cudaGetLastError());
+    }
+    // column-tile x row-slab split of the multi-RHS A^T*Y
+    void layer_slabs(int L, long& tiles, long& slabs_l, long& rps) const {
+        const long m = this->m, n = this->n;
+        const long chunks = (L + 31) / 32;
+        tiles = (n * chunks * 32 + 255) / 256;
+        slabs_l = std::max<long>(1, (long)num_sms() * 8 / std::max<long>(tiles, 1));
+        slabs_l = std::min<long>(slabs_l, std::max<long>(m, 1));
+        rps = std::max<long>(1, (m + slabs_l - 1) / slabs_l);
+        slabs_l = std::max<long>(1, (m + rps - 1) / rps);
+    }
+    void prepare(int L) const override {
+        if (L <= 1) return;
+        if constexpr (std::is_same<T, float>::value && std::is_same<V, __nv_bfloat16>::value) {
+            if (use_umma && umma_supported(this->m, this->n, L)) {
+                if (umma && umma_L != L) {
+                    umma_plan_destroy(umma);
+                    umma = nullptr;
+                }
+                if (!umma) {
+                    umma = umma_plan_create(this->m, this->n, L, a.p);
+                    umma_L = L;
+                }
+                return;
+            }
+        }
+        long tiles, slabs_l, rps;
+        layer_slabs(L, tiles, slabs_l, rps);
+        const size_t need = (size_t)slabs_l * this->n * L;
+        if (part_l.n < need) part_l.alloc(need);
+    }
+    mutable DBuf<T> part_l;  // slab partials of the multi-RHS A^T*Y
+    bool multi_rhs() const override { return true; }
+    mutable UmmaPlan* umma = nullptr;  // tensor-core plan of the multi-RHS products (BF16 only)
+    mutable int umma_L = 0;
+    int use_umma = 1;
+    ~DenseOp() override {
+        if (umma) umma_plan_destroy(umma);
     }
 };
 

@@ -40,6 +40,7 @@ struct SpmvArgs {
     Ctl* ctl;
     double* part;
     unsigned* ticket;
+    int L;           // > 1: multi-RHS, vectors interleaved (element (row, layer) at row * L + layer)
 };
 
 template <class T, class V>
@@ -50,7 +51,8 @@ void launch_spmv(const SpmvArgs<T, V>& a, int epi, int G, int grid, cudaStream_t
 template <class T>
 struct SolverBufs {
     int p, q, r;   // dim_y (fastest), dim_x, dim_z
-    long n, m;
+    int L;         // layers sharing A (>= 1); vectors interleaved, layer fastest
+    long n, m;     // vector lengths: voxels * L and rays * L
     T* U[2];
     T* g[2];
     T* g2[2];

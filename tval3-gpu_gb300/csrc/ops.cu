@@ -189,11 +189,13 @@ struct CsrOp : LinOp<T> {
         a.by_parity = io.by_parity;
         a.sub = io.sub; a.b = io.b; a.delta = io.delta;
         a.ctl = io.ctl; a.part = io.part; a.ticket = io.ticket;
+        a.L = io.L;
         launch_spmv<T, V>(a, epi, trans ? Gt : Gn, trans ? grid_t : grid_n, s);
         TV3_CUDA(cudaGetLastError());
     }
 
     void export_csr(int* hptr, int* hind, float* hval, int* htptr, int* htind, float* htval) const override;
+    bool multi_rhs() const override { return true; }
 };
 
 template <class T, class V>
@@ -488,5 +490,33 @@ LinOp<float>* make_csr_op_device<float>(long rows, long cols, long nnz, const in
     }
     return op;
 }
+
+// column-major (rows x k) <-> interleaved (row * k + column)
+template <class T>
+__global__ void k_interleave(long rows, int k, const T* __restrict__ in, T* __restrict__ out, int inverse) {
+    const long tot = rows * k;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long)gridDim.x * blockDim.x) {
+        const long r = t / k, j = t - r * k;  // t = interleaved index
+        if (inverse) out[j * rows + r] = in[t];
+        else out[t] = in[j * rows + r];
+    }
+}
+
+template <class T>
+void apply_interleaved(const LinOp<T>& op, int trans, int k, const T* X, T* Y, cudaStream_t s) {
+    const long lx = trans ? op.m : op.n, ly = trans ? op.n : op.m;
+    op.prepare(k);
+    DBuf<T> xi(std::max<long>(lx * k, 1)), yi(std::max<long>(ly * k, 1));
+    if (lx > 0) k_interleave<T><<<ew(lx * k), 256, 0, s>>>(lx, k, X, xi.p, 0);
+    MatIO<T> io = plain_io<T>(xi.p, yi.p);
+    io.L = k;
+    op.apply(trans, io, SPMV_PLAIN, s);
+    if (ly > 0) k_interleave<T><<<ew(ly * k), 256, 0, s>>>(ly, k, yi.p, Y, 1);
+    TV3_CUDA(cudaGetLastError());
+    TV3_CUDA(cudaStreamSynchronize(s));  // the scratch is freed on return
+}
+template void apply_interleaved<float>(const LinOp<float>&, int, int, const float*, float*, cudaStream_t);
+template void apply_interleaved<double>(const LinOp<double>&, int, int, const double*, double*, cudaStream_t);
+template void apply_interleaved<df64>(const LinOp<df64>&, int, int, const df64*, df64*, cudaStream_t);
 
 }  // namespace tv3

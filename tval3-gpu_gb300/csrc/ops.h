@@ -12,6 +12,11 @@
 
 namespace tv3 {
 
+template <class T> struct LinOp;
+// column-major k-column product through one interleaved multi-RHS apply (ops.cu)
+template <class T>
+void apply_interleaved(const LinOp<T>& op, int trans, int k, const T* X, T* Y, cudaStream_t s);
+
 // I/O of one product inside the solver.  x and y are ping-pong pairs selected
 // by ctl->parity when by_parity is set; epilogues as in SpmvEpi.
 template <class T>
@@ -25,6 +30,7 @@ struct MatIO {
     Ctl* ctl;
     double* part;
     unsigned* ticket;
+    int L;  // > 1: L right-hand sides, interleaved (element (row, layer) at row * L + layer)
 };
 
 template <class T>
@@ -55,9 +61,19 @@ struct LinOp {
     virtual ~LinOp() {}
     // trans 0: y[rows m] = A x ; trans 1: y[rows n] = A^T x
     virtual void apply(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const = 0;
-    // multi-RHS products: columns of length n (trans 0: X n x k -> Y m x k)
+    // allocate what products with L interleaved right-hand sides need (called
+    // before any product, outside stream capture)
+    virtual void prepare(int L) const { (void)L; }
+    // true when apply() takes L > 1 interleaved right-hand sides
+    virtual bool multi_rhs() const { return false; }
+    // multi-RHS products: columns of length n (trans 0: X n x k -> Y m x k),
+    // column-major; operators with multi_rhs() run one interleaved product
     virtual void apply_multi(int trans, int k, const T* X, T* Y, cudaStream_t s) const {
         const long lx = trans ? m : n, ly = trans ? n : m;
+        if (k > 1 && multi_rhs()) {
+            apply_interleaved(*this, trans, k, X, Y, s);
+            return;
+        }
         for (int j = 0; j < k; ++j) apply(trans, plain_io<T>(X + j * lx, Y + j * ly), SPMV_PLAIN, s);
     }
     // export the stored matrix as FP32 CSR (stored operators only)
@@ -80,6 +96,10 @@ struct SplitOp : LinOp<T> {
     }
     void apply(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const override {
         (trans ? top : nop)->apply(trans, io, epi, s);
+    }
+    void prepare(int L) const override {
+        nop->prepare(L);
+        top->prepare(L);
     }
 };
 

@@ -323,6 +323,7 @@ struct BresOp : LinOp<float> {
         return v;
     }
     void apply(int trans, const MatIO<float>& io, int epi, cudaStream_t s) const override {
+        if (io.L > 1) throw Error{7, "on-the-fly ray operators take one right-hand side"};
         const GeomView g = view();
         const int G = 32;
         const int grid = grid_for(g.nrays * G, 256);

@@ -20,8 +20,12 @@
 namespace tv3 {
 
 template <class T>
-Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_)
-    : A(A_), p(p_), q(q_), r(r_), n((long)p_ * q_ * r_), m(A_->m), o(o_) {
+Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_, int L_)
+    : A(A_), p(p_), q(q_), r(r_), L(std::max(L_, 1)), n((long)p_ * q_ * r_ * std::max(L_, 1)),
+      m(A_->m * std::max(L_, 1)), o(o_) {
+    if (n >= (1L << 31))
+        throw Error{TVAL3_ERR_UNSUPPORTED, "voxels x layers exceeds the 32-bit index range of the stencil kernels"};
+    A->prepare(L);
     const long nvec = 22, mvec = 4;
     nv.alloc(nvec * n);
     mv.alloc(mvec * std::max<long>(m, 1));
@@ -33,7 +37,7 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
     TV3_CUDA(cudaMallocHost(&hctl, sizeof(Ctl)));
     T* v = nv.p;
     auto take = [&](long k) { T* t = v; v += k * n; return t; };
-    B.p = p; B.q = q; B.r = r; B.n = n; B.m = m;
+    B.p = p; B.q = q; B.r = r; B.L = L; B.n = n; B.m = m;
     B.U[0] = take(1); B.U[1] = take(1);
     B.g[0] = take(1); B.g[1] = take(1);
     B.g2[0] = take(1); B.g2[1] = take(1);
@@ -45,8 +49,11 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
     const long mm = std::max<long>(m, 1);
     B.Au[0] = w; B.Au[1] = w + mm; B.b = w + 2 * mm; B.delta = w + 3 * mm;
     B.ctl = ctl.p; B.part = part.p; B.ticket = ticket.p;
-    // reduction grid: a fixed multiple of the SM count (partials fit in `part`)
-    B.grid = std::max(1, std::min(num_sms() * 4, 8192));
+    // vector/reduction grid: about 1024 elements per block for small problems
+    // (so that many small solves can share the GPU), at most four blocks per
+    // SM (partials fit in `part`)
+    const long cap = std::max(1, std::min(num_sms() * 4, 8192));
+    B.grid = (int)std::max<long>(1, std::min<long>(cap, (std::max<long>(n, m) + 1023) / 1024));
     B.trace = trace.p;
 }
 
@@ -64,6 +71,7 @@ MatIO<T> Solver<T>::io_AU() const {
     io.by_parity = 1;
     io.b = B.b; io.delta = B.delta;
     io.ctl = B.ctl; io.part = B.part; io.ticket = B.ticket;
+    io.L = L;
     return io;
 }
 template <class T>
@@ -74,6 +82,7 @@ MatIO<T> Solver<T>::io_AtAu() const {
     io.by_parity = 1;
     io.sub = B.Atb;
     io.ctl = B.ctl; io.part = B.part; io.ticket = B.ticket;
+    io.L = L;
     return io;
 }
 template <class T>
@@ -82,6 +91,7 @@ MatIO<T> Solver<T>::io_Ad() const {
     io.x[0] = io.x[1] = B.d;
     io.y[0] = io.y[1] = nullptr;
     io.ctl = B.ctl; io.part = B.part; io.ticket = B.ticket;
+    io.L = L;
     return io;
 }
 
@@ -138,6 +148,7 @@ void Solver<T>::setup(const void* d_b, cudaStream_t s) {
     launch_scale_b<T>(d_b, B, s);                                    // scaleb_gpu
     MatIO<T> io_atb = plain_io<T>(B.b, B.Atb);
     io_atb.ctl = B.ctl;
+    io_atb.L = L;
     A->apply(1, io_atb, SPMV_PLAIN, s);                              // Atb = A^T b
     TV3_CUDA(cudaMemcpyAsync(B.U[0], B.Atb, n * sizeof(T), cudaMemcpyDeviceToDevice, s));   // U = Atb
     TV3_CUDA(cudaMemcpyAsync(B.rcdU, B.Atb, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
@@ -233,28 +244,22 @@ struct Body {
 
 }  // namespace
 
+// Adds the whole solve to `top` as an independent branch (its first nodes are
+// roots of `top`), capturing through stream cs.  Several solvers can add
+// their branches to one graph; they share nothing on the device.
 template <class T>
-void Solver<T>::build_graph(const void* d_b, void* d_U, const void* d_Ut, cudaStream_t s) {
-    if (gexec) {
-        cudaGraphExecDestroy(gexec);
-        gexec = nullptr;
-    }
-    cudaGraph_t top;
-    TV3_CUDA(cudaGraphCreate(&top, 0));
-    cudaStream_t cs;
-    TV3_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const void* d_Ut, cudaStream_t cs) {
+    const unsigned run = (o.maxcnt > 0 && o.maxit > 0) ? 1u : 0u;
+    cudaGraphConditionalHandle h_outer, h_inner, h_fst, h_arm, h_restart, h_mlp;
+    TV3_CUDA(cudaGraphConditionalHandleCreate(&h_outer, top, run, cudaGraphCondAssignDefault));
+    TV3_CUDA(cudaGraphConditionalHandleCreate(&h_inner, top, 1, cudaGraphCondAssignDefault));
+    TV3_CUDA(cudaGraphConditionalHandleCreate(&h_fst, top, 1, cudaGraphCondAssignDefault));
+    TV3_CUDA(cudaGraphConditionalHandleCreate(&h_arm, top, 0, cudaGraphCondAssignDefault));
+    TV3_CUDA(cudaGraphConditionalHandleCreate(&h_restart, top, 0, cudaGraphCondAssignDefault));
+    TV3_CUDA(cudaGraphConditionalHandleCreate(&h_mlp, top, 0, cudaGraphCondAssignDefault));
+    B.use_graph = 1;
+    B.h_inner = h_inner; B.h_arm = h_arm; B.h_mlp = h_mlp;
     try {
-        const unsigned run = (o.maxcnt > 0 && o.maxit > 0) ? 1u : 0u;
-        cudaGraphConditionalHandle h_outer, h_inner, h_fst, h_arm, h_restart, h_mlp;
-        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_outer, top, run, cudaGraphCondAssignDefault));
-        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_inner, top, 1, cudaGraphCondAssignDefault));
-        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_fst, top, 1, cudaGraphCondAssignDefault));
-        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_arm, top, 0, cudaGraphCondAssignDefault));
-        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_restart, top, 0, cudaGraphCondAssignDefault));
-        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_mlp, top, 0, cudaGraphCondAssignDefault));
-        B.use_graph = 1;
-        B.h_inner = h_inner; B.h_arm = h_arm; B.h_mlp = h_mlp;
-
         Body tb{top, {}, cs};
         tb.begin();
         setup(d_b, cs);
@@ -315,10 +320,27 @@ void Solver<T>::build_graph(const void* d_b, void* d_U, const void* d_Ut, cudaSt
         tb.begin();
         launch_finalize<T>(B, d_U, d_Ut, cs);
         tb.end();
-        B.use_graph = 0;
-        TV3_CUDA(cudaGraphInstantiate(&gexec, top, 0));
     } catch (...) {
         B.use_graph = 0;
+        throw;
+    }
+    B.use_graph = 0;
+}
+
+template <class T>
+void Solver<T>::build_graph(const void* d_b, void* d_U, const void* d_Ut, cudaStream_t s) {
+    if (gexec) {
+        cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+    }
+    cudaGraph_t top;
+    TV3_CUDA(cudaGraphCreate(&top, 0));
+    cudaStream_t cs;
+    TV3_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    try {
+        add_to_graph(top, d_b, d_U, d_Ut, cs);
+        TV3_CUDA(cudaGraphInstantiate(&gexec, top, 0));
+    } catch (...) {
         cudaStreamDestroy(cs);
         cudaGraphDestroy(top);
         throw;
@@ -351,13 +373,23 @@ void Solver<T>::solve(const void* d_b, void* d_U, const void* d_Ut, tval3_info* 
     TV3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    fill_info(info, ms / 1000.0);
+}
+
+template <class T>
+void Solver<T>::fetch_ctl(cudaStream_t s) {
+    TV3_CUDA(cudaMemcpyAsync(hctl, ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+}
+
+template <class T>
+void Solver<T>::fill_info(tval3_info* info, double secs) const {
     if (hctl->err) throw Error{TVAL3_ERR_CUDA, "device-side error word set during the solve"};
     if (info) {
         info->total_iters = hctl->count_total;
         info->outer_iters = hctl->count_outer;
         info->rel_chg = hctl->relchgout;
         info->rel_error = hctl->rel_error;
-        info->secs = ms / 1000.0;
+        info->secs = secs;
         info->backtracks = hctl->backtracks;
         info->restarts = hctl->restarts;
         info->final_f = hctl->f;
@@ -371,8 +403,65 @@ void Solver<T>::read_trace(double* host, int len) {
     if (k > 0) TV3_CUDA(cudaMemcpy(host, trace.p, k * sizeof(double), cudaMemcpyDeviceToHost));
 }
 
+template <class T>
+Batch<T>::~Batch() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    for (auto* x : s) delete x;
+}
+
+template <class T>
+void Batch<T>::solve(const void* const* b, void* const* U, const void* const* Ut, tval3_info* infos,
+                     cudaStream_t st) {
+    const size_t k = s.size();
+    bool same = gexec && g_b.size() == k;
+    for (size_t i = 0; same && i < k; ++i) same = g_b[i] == b[i] && g_U[i] == U[i] && g_Ut[i] == Ut[i];
+    if (!same) {
+        if (gexec) {
+            cudaGraphExecDestroy(gexec);
+            gexec = nullptr;
+        }
+        cudaGraph_t top;
+        TV3_CUDA(cudaGraphCreate(&top, 0));
+        cudaStream_t cs;
+        TV3_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        try {
+            for (size_t i = 0; i < k; ++i) {
+                s[i]->xstar = nullptr;
+                s[i]->B.xstar = nullptr;
+                s[i]->add_to_graph(top, b[i], U[i], Ut[i], cs);
+            }
+            TV3_CUDA(cudaGraphInstantiate(&gexec, top, 0));
+        } catch (...) {
+            cudaStreamDestroy(cs);
+            cudaGraphDestroy(top);
+            throw;
+        }
+        cudaStreamDestroy(cs);
+        cudaGraphDestroy(top);
+        g_b.assign(b, b + k);
+        g_U.assign(U, U + k);
+        g_Ut.assign(Ut, Ut + k);
+    }
+    cudaEvent_t e0, e1;
+    TV3_CUDA(cudaEventCreate(&e0));
+    TV3_CUDA(cudaEventCreate(&e1));
+    TV3_CUDA(cudaEventRecord(e0, st));
+    TV3_CUDA(cudaGraphLaunch(gexec, st));
+    TV3_CUDA(cudaEventRecord(e1, st));
+    for (auto* x : s) x->fetch_ctl(st);
+    TV3_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    TV3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (size_t i = 0; i < k; ++i) s[i]->fill_info(infos ? infos + i : nullptr, ms / 1000.0);
+}
+
 template struct Solver<float>;
 template struct Solver<double>;
 template struct Solver<df64>;
+template struct Batch<float>;
+template struct Batch<double>;
+template struct Batch<df64>;
 
 }  // namespace tv3

@@ -1,6 +1,7 @@
 // TVAL3 solver workspace and loop driver (internal).
 #pragma once
 
+#include <vector>
 #include "dbuf.h"
 #include "ops.h"
 #include "tval3/tval3_c.h"
@@ -11,7 +12,8 @@ template <class T>
 struct Solver {
     const LinOp<T>* A;
     int p, q, r;
-    long n, m;
+    int L;         // layers sharing A (the 2D entry's b.len / A.rows)
+    long n, m;     // vector lengths (voxels * L, rays * L)
     tval3_options o;
     DBuf<T> nv, mv;
     DBuf<Ctl> ctl;
@@ -29,12 +31,18 @@ struct Solver {
     const void* g_Ut = nullptr;
     cudaStream_t g_stream = nullptr;
 
-    Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_);
+    Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_, int L_ = 1);
     ~Solver();
     // b, U and Ut are device arrays of the caller-facing type Ext<T>
     // (float for float vectors, double for double and double-float vectors)
     void solve(const void* d_b, void* d_U, const void* d_Ut, tval3_info* info, cudaStream_t s);
     void read_trace(double* host, int len);
+    // the whole solve as an independent branch of `top` (mode 1 form)
+    void add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const void* d_Ut, cudaStream_t cs);
+    // enqueue the copy of the control block to its pinned mirror; after the
+    // stream is synchronised, fill_info reports it
+    void fetch_ctl(cudaStream_t s);
+    void fill_info(tval3_info* info, double secs) const;
 
    private:
     void init_ctl(cudaStream_t s);
@@ -47,6 +55,23 @@ struct Solver {
     MatIO<T> io_AU() const;
     MatIO<T> io_AtAu() const;
     MatIO<T> io_Ad() const;
+};
+
+// Many independent solves (e.g. the slices of a 2D stack) as ONE CUDA graph:
+// every solver's whole-solve graph is a parallel branch, each with its own
+// conditional loops, so slices that converge early simply stop while the
+// others go on, and small slices fill the GPU together.
+template <class T>
+struct Batch {
+    std::vector<Solver<T>*> s;  // owned
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<const void*> g_b, g_Ut;
+    std::vector<void*> g_U;
+
+    ~Batch();
+    // b[i], U[i], Ut[i] (may be NULL): device arrays of the type Ext<T>;
+    // infos[i].secs is the time of the whole batch
+    void solve(const void* const* b, void* const* U, const void* const* Ut, tval3_info* infos, cudaStream_t st);
 };
 
 }  // namespace tv3

@@ -19,6 +19,7 @@
 // lam5 = <delta, Au - b> (3d/tval3_gpu_3d_kernels.cu:876-919), ||Ad||^2 for the
 // first-iteration step size (3d/tval3_gpu_3d.cpp:577-610), and g = A^T Au - Atb
 // (3d/tval3_gpu_3d.cpp:565).
+#include <algorithm>
 #include "tval3_internal.cuh"
 #include "launch.h"
 
@@ -162,6 +163,106 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs<T, V> a) {
     }
 }
 
+// Multi-RHS form (L > 1 right-hand sides, the reference's csrmm with `layers`
+// columns, 2d/mat_vec_mul.h:65-71): vectors are interleaved, element
+// (row, layer) at row * L + layer, so the L values one nonzero gathers are
+// contiguous.  One group of G lanes per row (G = L rounded up to a power of
+// two, at most 32; layers beyond 32 in further passes); lane l accumulates
+// layer l.  The row's indices and values are read once per pass for all its
+// layers (broadcast loads).  Same epilogues as k_spmv, summed over layers.
+template <class T, class V, int G, int EPI>
+__global__ void __launch_bounds__(256) k_spmm(SpmvArgs<T, V> a) {
+    count_launch(a.ctl);
+    using VV = typename VT<V>::type;
+    const long L = a.L;
+    const int lane = threadIdx.x % G;
+    const long grp = ((long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    const long ngrp = ((long)gridDim.x * blockDim.x) / G;
+    int sel = 0;
+    if (a.by_parity) sel = a.ctl->parity;
+    const T* __restrict__ x = a.x[sel];
+    T* __restrict__ y = a.y[sel];
+    const int* __restrict__ ind = a.ind;
+    const V* __restrict__ val = a.val;
+    const float* __restrict__ xs = a.xscale;
+    double acc0 = 0.0, acc1 = 0.0;
+    for (long r = grp; r < a.rows; r += ngrp) {
+        const int beg = __ldg(a.ptr + r), end = __ldg(a.ptr + r + 1);
+        for (long l0 = 0; l0 < L; l0 += G) {
+            const long l = l0 + lane;
+            const bool on = l < L;
+            RowAcc<T> acc;
+            int k = beg;
+            for (; k + 1 < end; k += 2) {
+                const int c0 = __ldg(ind + k), c1 = __ldg(ind + k + 1);
+                const VV v0 = (VV)Acc<VV, V>::load(val + k), v1 = (VV)Acc<VV, V>::load(val + k + 1);
+                if (on) {
+                    T x0 = x[(long)c0 * L + l], x1 = x[(long)c1 * L + l];
+                    if (xs) {
+                        x0 *= (T)__ldg(xs + c0);
+                        x1 *= (T)__ldg(xs + c1);
+                    }
+                    madd(acc, v0, x0);
+                    madd(acc, v1, x1);
+                }
+            }
+            if (k < end && on) {
+                const int c0 = __ldg(ind + k);
+                T x0 = x[(long)c0 * L + l];
+                if (xs) x0 *= (T)__ldg(xs + c0);
+                madd(acc, (VV)Acc<VV, V>::load(val + k), x0);
+            }
+            if (on) {
+                T s = acc.value();
+                if (a.rscale) s *= (T)__ldg(a.rscale + r);
+                const long o = r * L + l;
+                if (EPI == SPMV_PLAIN) {
+                    y[o] = s;
+                } else if (EPI == SPMV_SUB) {
+                    y[o] = s - a.sub[o];
+                } else if (EPI == SPMV_LAM35) {
+                    y[o] = s;
+                    double t = acc_d(to_acc(s) - to_acc(a.b[o]));
+                    acc0 += t * t;
+                    acc1 += acc_d(to_acc(a.delta[o])) * t;
+                } else if (EPI == SPMV_NORM2) {
+                    const double sd = acc_d(to_acc(s));
+                    acc0 += sd * sd;
+                }
+            }
+        }
+    }
+    if (EPI == SPMV_LAM35 || EPI == SPMV_NORM2) {
+        double v[2] = {acc0, acc1}, tot[2];
+        if (grid_reduce<2>(v, a.part, a.ticket, tot) && threadIdx.x == 0) {
+            Ctl* c = a.ctl;
+            if (EPI == SPMV_LAM35) {
+                c->lam3 = tot[0];
+                c->lam5 = tot[1];
+            } else {
+                c->Add = tot[0];
+                c->tau = fabs(c->dd / (c->dDd + c->muDbeta * c->Add));
+            }
+        }
+    }
+}
+
+template <class T, class V, int EPI>
+static void launch_mm(const SpmvArgs<T, V>& a, cudaStream_t s) {
+    int G = 1;
+    while (G < a.L && G < 32) G <<= 1;
+    long g = (a.rows * G + 255) / 256;
+    const long cap = (long)num_sms() * 16;
+    const int grid = (int)std::max<long>(1, std::min(g, cap));
+    switch (G) {
+        case 2: k_spmm<T, V, 2, EPI><<<grid, 256, 0, s>>>(a); break;
+        case 4: k_spmm<T, V, 4, EPI><<<grid, 256, 0, s>>>(a); break;
+        case 8: k_spmm<T, V, 8, EPI><<<grid, 256, 0, s>>>(a); break;
+        case 16: k_spmm<T, V, 16, EPI><<<grid, 256, 0, s>>>(a); break;
+        default: k_spmm<T, V, 32, EPI><<<grid, 256, 0, s>>>(a); break;
+    }
+}
+
 // lanes: the group size G (4, 8, 16, 32), plus SPMV_SCALAR for the scalar-lane variant
 template <class T, class V, int EPI, int VEC>
 static void launch_v(const SpmvArgs<T, V>& a, int G, int grid, cudaStream_t s) {
@@ -181,6 +282,15 @@ static void launch_g(const SpmvArgs<T, V>& a, int lanes, int grid, cudaStream_t 
 
 template <class T, class V>
 void launch_spmv(const SpmvArgs<T, V>& a, int epi, int lanes, int grid, cudaStream_t s) {
+    if (a.L > 1) {
+        switch (epi) {
+            case SPMV_SUB: launch_mm<T, V, SPMV_SUB>(a, s); break;
+            case SPMV_LAM35: launch_mm<T, V, SPMV_LAM35>(a, s); break;
+            case SPMV_NORM2: launch_mm<T, V, SPMV_NORM2>(a, s); break;
+            default: launch_mm<T, V, SPMV_PLAIN>(a, s); break;
+        }
+        return;
+    }
     switch (epi) {
         case SPMV_SUB: launch_g<T, V, SPMV_SUB>(a, lanes, grid, s); break;
         case SPMV_LAM35: launch_g<T, V, SPMV_LAM35>(a, lanes, grid, s); break;

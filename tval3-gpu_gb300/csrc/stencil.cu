@@ -43,9 +43,13 @@ __device__ __forceinline__ unsigned fdiv(unsigned i, const FastDiv& f) {
     return (unsigned)(((unsigned long long)__umulhi(i, f.M) + i) >> f.L);
 }
 
+// Volume geometry of the vectors: element i = voxel * L + layer, voxel =
+// y + x*p + z*p*q.  With L > 1 (layers sharing A) the differences stay inside
+// each layer.
 struct Geo {
     FastDiv p, q;
     int r;
+    FastDiv l;  // layers (d = 1: one volume)
 };
 
 struct Nb {
@@ -53,20 +57,25 @@ struct Nb {
 };
 
 __device__ __forceinline__ Nb neighbours(const Geo& g, long i) {
-    const unsigned ui = (unsigned)i;
-    const unsigned t = fdiv(ui, g.p);
-    const int y = (int)(ui - t * g.p.d);
+    unsigned v = (unsigned)i;
+    long u = 1;  // element stride of one voxel
+    if (g.l.d > 1) {
+        v = fdiv(v, g.l);
+        u = g.l.d;
+    }
+    const unsigned t = fdiv(v, g.p);
+    const int y = (int)(v - t * g.p.d);
     const unsigned zz = fdiv(t, g.q);
     const int x = (int)(t - zz * g.q.d);
     const int z = (int)zz;
     const long p = g.p.d, q = g.q.d, pq = p * q;
     Nb o;
-    o.yp = (y + 1 < (int)p) ? i + 1 : i - y;
-    o.ym = (y > 0) ? i - 1 : i + (p - 1);
-    o.xp = (x + 1 < (int)q) ? i + p : i - (long)x * p;
-    o.xm = (x > 0) ? i - p : i + (q - 1) * p;
-    o.zp = (z + 1 < g.r) ? i + pq : i - (long)z * pq;
-    o.zm = (z > 0) ? i - pq : i + (long)(g.r - 1) * pq;
+    o.yp = (y + 1 < (int)p) ? i + u : i - y * u;
+    o.ym = (y > 0) ? i - u : i + (p - 1) * u;
+    o.xp = (x + 1 < (int)q) ? i + p * u : i - (long)x * p * u;
+    o.xm = (x > 0) ? i - p * u : i + (q - 1) * p * u;
+    o.zp = (z + 1 < g.r) ? i + pq * u : i - (long)z * pq * u;
+    o.zm = (z > 0) ? i - pq * u : i + (long)(g.r - 1) * pq * u;
     return o;
 }
 
@@ -130,12 +139,17 @@ __global__ void __launch_bounds__(1024) k_scale_find(const E* __restrict__ b, lo
     }
 }
 
+// b_in is the caller's m x L column-major array; b is interleaved (ray * L + layer)
 template <class T>
-__global__ void k_scale_apply(const Ext<T>* __restrict__ b_in, T* __restrict__ b, long m, Ctl* ctl) {
+__global__ void k_scale_apply(const Ext<T>* __restrict__ b_in, T* __restrict__ b, long m, int L, Ctl* ctl) {
     count_launch(ctl);
     const double scl = ctl->scl;
     const Ext<T> s = (Ext<T>)scl;
-    GRID_STRIDE(i, m) b[i] = from_ext<T>((scl == 1.0) ? b_in[i] : b_in[i] * s);
+    const long m1 = m / L;
+    GRID_STRIDE(i, m) {
+        const long src = (L == 1) ? i : (i % L) * m1 + i / L;
+        b[i] = from_ext<T>((scl == 1.0) ? b_in[src] : b_in[src] * s);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -629,13 +643,16 @@ __global__ void k_finalize(SolverBufs<T> B, Ext<T>* __restrict__ out, const Ext<
     const double scl = ctl->scl;
     const T s = scal<T>(scl);
     double e = 0.0, t = 0.0;
+    const long L = B.L, n1 = B.n / B.L;
     GRID_STRIDE(i, B.n) {
+        // out and Ut are the caller's n x L column-major arrays
+        const long o = (L == 1) ? i : (i % L) * n1 + i / L;
         Ext<T> u = to_ext<T>((scl == 1.0) ? U[i] : U[i] / s);
-        out[i] = u;
+        out[o] = u;
         if (Ut) {
-            double dv = (double)Ut[i] - (double)u;
+            double dv = (double)Ut[o] - (double)u;
             e += dv * dv;
-            t += (double)Ut[i] * Ut[i];
+            t += (double)Ut[o] * Ut[o];
         }
     }
     double v[2] = {e, t}, tot[2];
@@ -685,19 +702,20 @@ static int ew_grid(long n) {
     return (int)g;
 }
 
-static Geo geo_of(int p, int q, int r) {
+static Geo geo_of(int p, int q, int r, int L = 1) {
     Geo g;
     g.p = make_div((unsigned)p);
     g.q = make_div((unsigned)q);
     g.r = r;
+    g.l = make_div((unsigned)(L > 1 ? L : 1));
     return g;
 }
-template <class T> static Geo geo_of(const SolverBufs<T>& B) { return geo_of(B.p, B.q, B.r); }
+template <class T> static Geo geo_of(const SolverBufs<T>& B) { return geo_of(B.p, B.q, B.r, B.L); }
 
 template <class T> void launch_scale_b(const void* b_in, SolverBufs<T>& B, cudaStream_t s) {
     const Ext<T>* b = static_cast<const Ext<T>*>(b_in);
     k_scale_find<Ext<T>><<<1, 1024, 0, s>>>(b, B.m, B.ctl);
-    k_scale_apply<T><<<ew_grid(B.m), 256, 0, s>>>(b, B.b, B.m, B.ctl);
+    k_scale_apply<T><<<ew_grid(B.m), 256, 0, s>>>(b, B.b, B.m, B.L, B.ctl);
 }
 template <class T> void launch_D_only(SolverBufs<T>& B, cudaStream_t s) {
     k_D_only<T><<<ew_grid(B.n), 256, 0, s>>>(B, geo_of(B));

@@ -230,11 +230,15 @@ def tval3_gpu_3d(shape, A, b, opts=None, Ut=None, *, dtype=np.float32, pagelocke
 
 
 def tval3_gpu(shape, A, b, opts=None, Ut=None, pagelocked=True):
-    """2D entry (2d/tval3_gpu.h:9-19): shape = (rows, cols); returns U [cols, rows]."""
+    """2D entry (2d/tval3_gpu.h:9-19): shape = (rows, cols); returns U [cols, rows].
+    b may hold `layers` columns (b.size = A.rows * layers, column-major), which
+    share A and are solved jointly; U is then [layers, cols, rows]."""
     lib = load()
     rows, cols = shape
     b = np.ascontiguousarray(b, dtype=np.float32)
-    U = np.zeros((cols, rows), dtype=np.float32)
+    nrows = A.rows
+    layers = b.size // nrows if nrows and b.size % nrows == 0 else 1
+    U = np.zeros((cols, rows) if layers == 1 else (layers, cols, rows), dtype=np.float32)
     Ut_a = None if Ut is None else np.ascontiguousarray(Ut, dtype=np.float32).reshape(-1)
     o = _opts(opts)
     info = Info()
@@ -317,13 +321,17 @@ class Operator:
 class Solver:
     """Device-resident workspace (tval3_solver) for repeated solves."""
 
-    def __init__(self, op: Operator, shape, opts=None, mode: int = 0):
+    def __init__(self, op: Operator, shape, opts=None, mode: int = 0, layers: int = 1):
         self.op = op
         self.shape = shape
+        self.layers = layers
         self._h = C.c_void_p()
         o = _opts(opts)
         self.maxit = o.maxit
-        check(load().tval3_solver_create(C.byref(self._h), op.handle, *shape, C.byref(o)))
+        if layers == 1:
+            check(load().tval3_solver_create(C.byref(self._h), op.handle, *shape, C.byref(o)))
+        else:
+            check(load().tval3_solver_create_layers(C.byref(self._h), op.handle, *shape, layers, C.byref(o)))
         self.set_mode(mode)
 
     def set_mode(self, mode: int):
@@ -353,6 +361,66 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+class Batch:
+    """Independent problems solved by one CUDA graph launch (tval3_batch_*):
+    ops[i] with volume shapes[i] = (dim_y, dim_x, dim_z).  The operators are
+    borrowed and kept alive by this object."""
+
+    def __init__(self, ops, shapes, opts=None):
+        self.ops = list(ops)
+        self.count = len(self.ops)
+        dims = (C.c_int * (3 * self.count))(*[int(v) for sh in shapes for v in sh])
+        handles = (C.c_void_p * self.count)(*[op.handle.value for op in self.ops])
+        self._h = C.c_void_p()
+        o = _opts(opts)
+        check(load().tval3_batch_create(C.byref(self._h), handles, dims, self.count, C.byref(o)))
+
+    def solve(self, b_devs, U_devs, Ut_devs=None, stream=None) -> list[dict]:
+        k = self.count
+        pb = (C.c_void_p * k)(*[_ptr(x) for x in b_devs])
+        pU = (C.c_void_p * k)(*[_ptr(x) for x in U_devs])
+        pUt = None if Ut_devs is None else (C.c_void_p * k)(*[_ptr(x) for x in Ut_devs])
+        infos = (Info * k)()
+        check(load().tval3_batch_solve(self._h, pb, pU, pUt, infos, _stream(stream)))
+        return [i.as_dict() for i in infos]
+
+    def close(self):
+        if self._h:
+            load().tval3_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tval3_gpu_batched(slices, opts=None):
+    """tval3_gpu for every slice in one launch.  slices: list of (shape
+    (rows, cols), SparseMatrix A, b[, Ut]).  Returns ([U [cols, rows]], [info])."""
+    lib = load()
+    k = len(slices)
+    arr = (capi.SliceHost * k)()
+    keep = []
+    outs = []
+    for i, sl in enumerate(slices):
+        (rows, cols), A, b = sl[0], sl[1], sl[2]
+        Ut = sl[3] if len(sl) > 3 else None
+        b = np.ascontiguousarray(b, dtype=np.float32)
+        U = np.zeros((cols, rows), dtype=np.float32)
+        Ut_a = None if Ut is None else np.ascontiguousarray(Ut, dtype=np.float32).reshape(-1)
+        st = A.struct()
+        keep += [b, Ut_a, st]
+        outs.append(U)
+        arr[i] = capi.SliceHost(_ptr(U), rows, cols, C.cast(C.pointer(st), C.c_void_p), _ptr(b), b.size,
+                                _ptr(Ut_a), 0 if Ut_a is None else Ut_a.size)
+    o = _opts(opts)
+    infos = (Info * k)()
+    check(lib.tval3_gpu_batched(arr, k, C.byref(o), infos))
+    return outs, [i.as_dict() for i in infos]
 
 
 def D(U_dev, shape, DU_dev, stream=None):

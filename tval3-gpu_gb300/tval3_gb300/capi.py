@@ -69,6 +69,11 @@ class GeometryHost(C.Structure):
                 ("xr_pos", C.c_void_p), ("yr_pos", C.c_void_p), ("zr_pos", C.c_void_p)]
 
 
+class SliceHost(C.Structure):
+    _fields_ = [("U", C.c_void_p), ("rows", C.c_int), ("cols", C.c_int), ("A", C.c_void_p), ("b", C.c_void_p),
+                ("b_len", C.c_int), ("Ut", C.c_void_p), ("Ut_len", C.c_int)]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _SIG = {
@@ -99,6 +104,7 @@ _SIG = {
     "tval3_df64_from_f64": (_I, [_P, _P, C.c_int64, _P]),
     "tval3_df64_to_f64": (_I, [_P, _P, C.c_int64, _P]),
     "tval3_solver_create": (_I, [_P, _P, _I, _I, _I, _P]),
+    "tval3_solver_create_layers": (_I, [_P, _P, _I, _I, _I, _I, _P]),
     "tval3_solver_set_mode": (_I, [_P, _I]),
     "tval3_solver_solve": (_I, [_P, _P, _P, _P, _P, _P]),
     "tval3_solver_set_trace": (_I, [_P, _P]),
@@ -108,6 +114,10 @@ _SIG = {
     "tval3_Dt_f32": (_I, [_I, _I, _I, _P, _P, _P]),
     "tval3_D_f64": (_I, [_I, _I, _I, _P, _P, _P]),
     "tval3_Dt_f64": (_I, [_I, _I, _I, _P, _P, _P]),
+    "tval3_batch_create": (_I, [_P, _P, _P, _I, _P]),
+    "tval3_batch_solve": (_I, [_P, _P, _P, _P, _P, _P]),
+    "tval3_batch_destroy": (_I, [_P]),
+    "tval3_gpu_batched": (_I, [_P, _I, _P, _P]),
     "tval3_dense_rmatvec_f32_noalloc": (_I, [_I, _I, _P, _P, _P, _P]),
 }
 

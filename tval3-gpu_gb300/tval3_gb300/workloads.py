@@ -159,3 +159,17 @@ def config_3d(n_vox=128, n_em=512, n_rc=512, seed=0) -> tuple[Config, Geometry, 
                  dict(mu=2.0 ** 9, mu0=2.0 ** 9, beta=2.0 ** 6, beta0=2.0 ** 6, tol=1e-4, maxit=200, tv_type=1),
                  0.005, seed)
     return cfg, geo, x
+
+
+def config_batched_2d(count: int = 64, seed: int = 0, side=(96, 256), n_trans=(128, 512)):
+    """The batched-2D workload: `count` independent slices, each with its own
+    side ~ U[96, 256] px and ring of N_t ~ U[128, 512] transducers (all
+    N_t (N_t - 1) / 2 pairs as rays), the 2D phantom, noise and options of
+    config_2d.  Returns a list of (Config, Geometry, phantom)."""
+    rng = np.random.default_rng(seed + 104729)
+    out = []
+    for i in range(count):
+        s = int(rng.integers(side[0], side[1] + 1))
+        nt = int(rng.integers(n_trans[0], n_trans[1] + 1))
+        out.append(config_2d(s, nt, seed + i))
+    return out
