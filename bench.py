@@ -67,6 +67,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=64,
                     help="slices of the batched-2D leg (0 skips it); printed under 'batched_2d'")
     ap.add_argument("--only-batched", action="store_true", help="run only the batched-2D leg (development)")
+    ap.add_argument("--dense-rhs", type=int, default=32,
+                    help="right-hand sides of the dense multi-RHS leg (0 skips it); printed under 'dense_multi_rhs'")
+    ap.add_argument("--only-dense", action="store_true", help="run only the dense multi-RHS products (development)")
     ap.add_argument("--solver-mode", type=int, default=1,
                     help="1: whole solve as one CUDA graph; 0: host-driven loop (same kernels; profilers "
                          "cannot see kernels inside graphs with conditional nodes)")
@@ -218,6 +221,8 @@ def run_ours(args):
         return spmv_only(args, T, torch, geo, op32, n, m, nnz, dev)
     if args.only_batched:
         return {"batched_2d": batched_2d(args, T, torch, dev)}
+    if args.only_dense:
+        return {"dense_multi_rhs": dense_multi_rhs(args, T, torch, dev)}
     xd = torch.tensor(x_true.reshape(-1), device=dev)
     Ax = torch.empty(m, device=dev)
     op32.mat_vec_mul(0, xd, Ax, stream=torch.cuda.current_stream())
@@ -377,6 +382,7 @@ def run_ours(args):
                         f" (FP32 CSR+CSC values, host arrays, mode {head})"}
 
     batched = batched_2d(args, T, torch, dev) if args.batch > 0 else None
+    dense = dense_multi_rhs(args, T, torch, dev) if args.dense_rhs > 0 else None
 
     if rank != 0:
         return None
@@ -411,6 +417,7 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clocks,
         "batched_2d": batched,
+        "dense_multi_rhs": dense,
     }
     return line
 
@@ -473,6 +480,94 @@ def batched_2d(args, T, torch, dev, reps=3):
             "speedup_vs_sequential": round(t_seq / t_batch, 3), "slices_per_s": round(args.batch / t_batch, 2),
             "iters_total": int(sum(i["total_iters"] for i in infos)),
             "results_identical_to_sequential": bool(same), "device_build_s": round(build_s, 2)}
+
+
+def dense_multi_rhs(args, T, torch, dev, reps=20):
+    """The dense multi-RHS workload: one 128^2 slice, a 256-transducer ring
+    (m = 32,640 rays), the ray matrix stored dense in BF16 with per-ray FP32
+    scales (1.07 GB), 32 noise realisations solved jointly (layers).  Times:
+    the two tensor-core products (CUDA events, L2 flushed), one joint solve
+    of the 32 right-hand sides to the 2D options' tol/maxit, and the
+    per-iteration time of a single-RHS solve on the same operator."""
+    from tval3_gb300.workloads import add_noise, config_2d
+    L = args.dense_rhs
+    cfg, geo, x = config_2d(128, 256, seed=0)
+    op32 = T.Operator.from_geometry(geo, mode=0, precision=T.PREC_FP32)
+    m, n = op32.rows, op32.cols
+    ptr, ind, val, _, _, _ = op32.export_csr()
+    A = np.zeros((m, n), np.float32)
+    rows = np.repeat(np.arange(m), np.diff(ptr))
+    A[rows, ind] = val
+    t0 = time.time()
+    op = T.Operator.from_dense(T.DenseMatrix(A), precision=T.PREC_BF16)
+    build_s = time.time() - t0
+    Ax = A.astype(np.float64) @ x.reshape(-1).astype(np.float64)
+    del A
+    b = np.concatenate([add_noise(Ax, cfg.noise, cfg.seed + l) for l in range(L)]).astype(np.float32)
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    g = torch.Generator().manual_seed(0)
+    X = torch.randn(n * L, generator=g).to(dev)
+    Y = torch.randn(m * L, generator=g).to(dev)
+    outm = torch.empty(m * L, device=dev)
+    outn = torch.empty(n * L, device=dev)
+
+    def time_prod(trans):
+        src, dst = (Y, outn) if trans else (X, outm)
+        for _ in range(3):
+            op.mat_mat_mul_interleaved(trans, L, src, dst, stream=stream)
+        torch.cuda.synchronize()
+        tot = 0.0
+        torch.cuda.nvtx.range_push("gemm_T" if trans else "gemm_N")
+        for _ in range(reps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                op.mat_mat_mul_interleaved(trans, L, src, dst, stream=stream)
+                e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1) / 1000.0
+        torch.cuda.nvtx.range_pop()
+        return tot / reps
+    tN, tT = time_prod(0), time_prod(1)
+    byts = 2 * m * n + 4 * (n + m) * L  # BF16 A once, FP32 right-hand sides in, FP32 results out
+    flops = 2.0 * m * n * L
+    out = {"workload": f"128^2 slice, 256-transducer ring (m={m}), dense BF16 A + FP32 row scales "
+                       f"({2 * m * n / 1e9:.2f} GB), {L} right-hand sides",
+           "gemm_N_us": round(tN * 1e6, 1), "gemm_T_us": round(tT * 1e6, 1),
+           "gemm_N_GBs": round(byts / tN / 1e9, 1), "gemm_T_GBs": round(byts / tT / 1e9, 1),
+           "gemm_N_TFLOPs": round(flops / tN / 1e12, 2), "gemm_T_TFLOPs": round(flops / tT / 1e12, 2),
+           "bytes_per_product": int(byts), "device_build_s": round(build_s, 2)}
+    if args.only_dense:
+        return out
+    # joint solve of the L right-hand sides, and single-RHS iterations for comparison
+    sj = T.Solver(op, cfg.dims, cfg.opts, mode=1, layers=L)
+    bd = torch.tensor(b, device=dev)
+    U = torch.empty(n * L, device=dev)
+    sj.solve(bd, U, stream=stream)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        flush.fill_(1.0)
+        info = sj.solve(bd, U, stream=stream)
+    torch.cuda.synchronize()
+    sj.close()
+    s1 = T.Solver(op, cfg.dims, cfg.opts, mode=1)
+    b1 = torch.tensor(b[:m], device=dev)
+    U1 = torch.empty(n, device=dev)
+    s1.solve(b1, U1, stream=stream)
+    torch.cuda.synchronize()
+    info1 = s1.solve(b1, U1, stream=stream)
+    torch.cuda.synchronize()
+    s1.close()
+    per_it_joint = info["secs"] / max(info["total_iters"], 1)
+    per_it_single = info1["secs"] / max(info1["total_iters"], 1)
+    out.update({"joint_solve_s": round(info["secs"], 4), "joint_iters": info["total_iters"],
+                "joint_ms_per_iter": round(per_it_joint * 1e3, 3),
+                "single_rhs_ms_per_iter": round(per_it_single * 1e3, 3),
+                "speedup_per_rhs_iter_vs_single": round(L * per_it_single / per_it_joint, 2)})
+    return out
 
 
 def op_vectors(torch, pairs, dt, n, m, dev):

@@ -259,6 +259,13 @@ TVAL3_API tval3_status tval3_op_export_csr(tval3_op op, int* ptr, int* ind, floa
  * `layers`, 2d/mat_vec_mul.h:65-71, :96-99). */
 TVAL3_API tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, void* stream);
 TVAL3_API tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, void* Y, void* stream);
+/* The same product on interleaved data: element (row, column j) at
+ * row * nrhs + j, the layout the multi-layer solver keeps.  One SpMM (CSR),
+ * tensor-core GEMM (BF16 dense) or SIMT GEMM (FP32/FP64 dense) launch
+ * sequence; the first call for a given nrhs sets up the operator's scratch
+ * (make it before any stream capture), later calls allocate nothing. */
+TVAL3_API tval3_status tval3_mat_mat_mul_interleaved(tval3_op op, int trans, int nrhs, const void* X, void* Y,
+                                                     void* stream);
 /* Device conversions between double and the double-float pairs used by
  * FP32_DF64 operators (hi = round(x), lo = round(x - hi)). */
 TVAL3_API tval3_status tval3_df64_from_f64(const double* d_in, void* d_pairs, int64_t n, void* stream);

@@ -109,3 +109,33 @@ def test_dense_bf16_layers_solve(cuda, oracle):
     assert Ug.shape == (L, n, n)
     assert ig["total_iters"] == io["total_iters"]
     assert np.linalg.norm(Ug.reshape(-1) - Uo.reshape(-1)) <= 1e-3 * np.linalg.norm(Uo)
+
+
+@pytest.mark.parametrize("prec", ["bf16", "csr32"])
+def test_interleaved_product_matches_column_major(cuda, oracle, prec):
+    import torch
+    from tval3_gb300 import PREC_BF16, PREC_FP32, DenseMatrix, Operator, SparseMatrix
+    from tval3_gb300 import workloads as W
+    geo = W.ring_geometry(32, 48)
+    ptr, ind, val = oracle.siddon_csr(geo)
+    m, n = ptr.size - 1, 32 * 32
+    if prec == "bf16":
+        A = np.zeros((m, n), np.float32)
+        for r in range(m):
+            A[r, ind[ptr[r]:ptr[r + 1]]] = val[ptr[r]:ptr[r + 1]]
+        op = Operator.from_dense(DenseMatrix(A), precision=PREC_BF16)
+    else:
+        op = Operator.from_sparse(SparseMatrix(m, n, ptr, ind, val), precision=PREC_FP32)
+    k = 32
+    g = torch.Generator().manual_seed(9)
+    for trans in (0, 1):
+        lx, ly = (m, n) if trans else (n, m)
+        Xc = torch.randn(k, lx, generator=g).to(cuda)
+        Yc = torch.empty(k, ly, device=cuda)
+        op.mat_mat_mul(trans, k, Xc, Yc)
+        Xi = Xc.t().contiguous()
+        Yi = torch.empty(ly, k, device=cuda)
+        for _ in range(2):  # second call: the plan set up by the first is reused
+            op.mat_mat_mul_interleaved(trans, k, Xi, Yi)
+            torch.cuda.synchronize()
+            assert torch.equal(Yi.t(), Yc)

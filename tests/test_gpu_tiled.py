@@ -1,0 +1,78 @@
+"""Tile-staged A^T*y (tiled.cu): operators built from a geometry know their
+volume and regroup A^T by voxel tiles, staging each tile's y values in
+shared memory; operators built from a bare sparse matrix use the plain CSR
+kernel.  Both must give the same products: FP64 and double-float to 1e-12,
+FP32 to 1e-5 (relative to sum |a||y| per voxel), BF16 exactly like the
+per-ray scaled plain kernel up to FP32 rounding."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _geo(kind):
+    from tval3_gb300 import workloads as W
+    if kind == "ring":
+        return W.ring_geometry(64, 96)
+    return W.hemisphere_geometry(40, 48, 48, seed=1)
+
+
+@pytest.mark.parametrize("kind", ["ring", "hemi"])
+@pytest.mark.parametrize("prec", ["fp32", "df64", "bf16"])
+def test_tiled_transpose_matches_plain_csr(cuda, kind, prec):
+    import torch
+    from tval3_gb300 import PREC_BF16, PREC_FP32, PREC_FP32_DF64, Operator, SparseMatrix
+    geo = _geo(kind)
+    p = {"fp32": PREC_FP32, "df64": PREC_FP32_DF64, "bf16": PREC_BF16}[prec]
+    tiled = Operator.from_geometry(geo, mode=0, precision=p)
+    ptr, ind, val, tptr, tind, tval = Operator.from_geometry(geo, mode=0, precision=PREC_FP32).export_csr()
+    m, n = ptr.size - 1, tptr.size - 1
+    plain = Operator.from_sparse(SparseMatrix(m, n, ptr, ind, val, tptr, tind, tval), precision=p)
+    g = torch.Generator().manual_seed(7)
+    yh = torch.randn(m, dtype=torch.float64, generator=g)
+    absA = np.zeros(n)
+    np.add.at(absA, np.repeat(np.arange(n), np.diff(tptr)), np.abs(tval.astype(np.float64)) * np.abs(yh.numpy()[tind]))
+    if prec == "df64":
+        from tval3_gb300 import capi
+        lib = capi.load()
+        yd = torch.empty(2 * m, dtype=torch.float32, device=cuda)
+        capi.check(lib.tval3_df64_from_f64(yh.to(cuda).data_ptr(), yd.data_ptr(), m, None))
+        outs = []
+        for op in (tiled, plain):
+            xd = torch.empty(2 * n, dtype=torch.float32, device=cuda)
+            op.mat_vec_mul(1, yd, xd)
+            xo = torch.empty(n, dtype=torch.float64, device=cuda)
+            capi.check(lib.tval3_df64_to_f64(xd.data_ptr(), xo.data_ptr(), n, None))
+            outs.append(xo.cpu().numpy())
+        tol = 1e-12
+    else:
+        yd = yh.float().to(cuda)
+        outs = []
+        for op in (tiled, plain):
+            xd = torch.empty(n, dtype=torch.float32, device=cuda)
+            op.mat_vec_mul(1, yd, xd)
+            outs.append(xd.cpu().numpy().astype(np.float64))
+        tol = 1e-5
+    torch.cuda.synchronize()
+    assert np.all(np.abs(outs[0] - outs[1]) <= tol * absA + 1e-30)
+
+
+def test_tiled_solve_matches_oracle_fp64(cuda, oracle):
+    """A full FP64 3D solve through a solver (which gives its operator the
+    volume, so A^T is tiled) keeps the oracle's control flow and result."""
+    import torch
+    from tval3_gb300 import PREC_FP64, Operator, Solver, SparseMatrix
+    from tval3_gb300 import workloads as W
+    cfg, geo, x = W.config_3d(24, 32, 32, seed=2)
+    ptr, ind, val = oracle.siddon_csr(geo)
+    b = W.add_noise(oracle.spmv(ptr, ind, val, x), cfg.noise, 2).astype(np.float64)
+    o = dict(cfg.opts, maxit=60)
+    Uo, io = oracle.tval3_csr(cfg.dims, ptr, ind, val, b, o)
+    op = Operator.from_sparse(SparseMatrix(ptr.size - 1, x.size, ptr, ind, val.astype(np.float64)),
+                              precision=PREC_FP64)
+    s = Solver(op, cfg.dims, o, mode=1)
+    U = torch.empty(x.size, dtype=torch.float64, device=cuda)
+    ig = s.solve(torch.tensor(b, device=cuda), U)
+    assert (ig["total_iters"], ig["outer_iters"], ig["backtracks"], ig["restarts"]) == \
+        (io["total_iters"], io["outer_iters"], io["backtracks"], io["restarts"])
+    assert np.linalg.norm(U.cpu().numpy() - Uo.reshape(-1)) <= 1e-7 * np.linalg.norm(Uo)

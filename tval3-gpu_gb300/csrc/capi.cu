@@ -457,6 +457,12 @@ tval3_status tval3_op_create_geometry(tval3_op* op, const tval3_geometry_host* G
             } else {
                 h->f = make_geometry_op<float>(G, mode, precision, 0);
             }
+            // the geometry fixes the volume: regroup A^T by voxel tiles now
+            if (G && mode == 0) {
+                if (h->q) h->q->set_volume(G->rv_y, G->rv_x, G->rv_z);
+                else if (h->d) h->d->set_volume(G->rv_y, G->rv_x, G->rv_z);
+                else h->f->set_volume(G->rv_y, G->rv_x, G->rv_z);
+            }
         } catch (...) {
             delete h;
             throw;
@@ -527,6 +533,25 @@ tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, 
         if (op->q) op->q->apply_multi(trans ? 1 : 0, nrhs, (const df64*)X, (df64*)Y, s);
         else if (op->dbl) op->d->apply_multi(trans ? 1 : 0, nrhs, (const double*)X, (double*)Y, s);
         else op->f->apply_multi(trans ? 1 : 0, nrhs, (const float*)X, (float*)Y, s);
+    });
+}
+
+tval3_status tval3_mat_mat_mul_interleaved(tval3_op op, int trans, int nrhs, const void* X, void* Y, void* stream) {
+    return guard([&] {
+        if (!op || !X || !Y || nrhs < 1) arg_error(TVAL3_ERR_ARG, "Argument error: bad multi-RHS product!");
+        cudaStream_t s = (cudaStream_t)stream;
+        auto run = [&](auto* A, auto* x, auto* y) {
+            using T = std::remove_const_t<std::remove_pointer_t<decltype(x)>>;
+            if (nrhs > 1 && !A->multi_rhs())
+                arg_error(TVAL3_ERR_UNSUPPORTED, "operator has no interleaved multi-RHS product");
+            A->prepare(nrhs);
+            MatIO<T> io = plain_io<T>(x, y);
+            io.L = nrhs;
+            A->apply(trans ? 1 : 0, io, SPMV_PLAIN, s);
+        };
+        if (op->q) run(op->q, (const df64*)X, (df64*)Y);
+        else if (op->dbl) run(op->d, (const double*)X, (double*)Y);
+        else run(op->f, (const float*)X, (float*)Y);
     });
 }
 

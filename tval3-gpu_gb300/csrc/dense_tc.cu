@@ -139,7 +139,7 @@ struct GemmArgs {
     Ctl* ctl;        // error word and launch counter (may be null)
 };
 
-__global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(128, 2) k_umma_gemm(const __grid_constant__ CUtensorMap tmA,
                                                        const __grid_constant__ CUtensorMap tmBh,
                                                        const __grid_constant__ CUtensorMap tmBl, GemmArgs g) {
     count_launch(g.ctl);
@@ -152,7 +152,10 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ CU
     const unsigned a_bytes = UM * 128, b_bytes = (unsigned)g.Npad * 128;
     const unsigned stage_bytes = a_bytes + 2 * b_bytes;
     const int warp = threadIdx.x >> 5;
-    const long mt = blockIdx.x, ks = blockIdx.y;
+    // splits of K vary fastest across the grid, so the CTAs resident at one
+    // time stream from many different column ranges of A (DRAM pages and
+    // channels) rather than from the same offset of every row
+    const long ks = blockIdx.x, mt = blockIdx.y;
     const long KB = (g.K + UK - 1) / UK;
     const long kb0 = ks * g.kb_per_split;
     const int nkb = (int)max(0L, min((long)g.kb_per_split, KB - kb0));
@@ -179,11 +182,14 @@ __global__ void __launch_bounds__(128, 1) k_umma_gemm(const __grid_constant__ CU
 
     if (threadIdx.x == 0 && nkb > 0) {
         const uint32_t idesc = idesc_bf16(UM, g.Npad);
-        auto load = [&](int j) {  // k-block j of this split into stage j % S
+        // this CTA's k-blocks in a rotated order (start differs per row tile)
+        const int rot = (int)((mt * 5) % nkb);
+        auto load = [&](int j) {  // the j-th k-block of this split into stage j % S
             const int s = j % S;
             unsigned char* st = sm + (size_t)s * stage_bytes;
             mbar_expect_tx(&full[s], stage_bytes);
-            const int kx = (int)((kb0 + j) * UK);
+            const int jj = (j + rot) % nkb;
+            const int kx = (int)((kb0 + jj) * UK);
             tma_load_2d(st, &tmA, kx, (int)(mt * UM), &full[s]);
             tma_load_2d(st + a_bytes, &tmBh, kx, 0, &full[s]);
             tma_load_2d(st + a_bytes + b_bytes, &tmBl, kx, 0, &full[s]);
@@ -421,7 +427,7 @@ UmmaPlan* umma_plan_create(long m, long n, int L, const __nv_bfloat16* Aq) {
         p->mapBTh = make_map(p->bT_h.p, m, p->Npad, p->mp, p->Npad);
         p->mapBTl = make_map(p->bT_l.p, m, p->Npad, p->mp, p->Npad);
         const size_t stage = (size_t)UM * 128 + 2 * (size_t)p->Npad * 128;
-        const size_t budget = 200 * 1024;
+        const size_t budget = 100 * 1024;  // two CTAs per SM
         const int st = (int)std::min<size_t>(MAX_STAGES, std::max<size_t>(2, budget / stage));
         p->stagesN = p->stagesT = st;
         p->smemN = p->smemT = st * stage + 1024;
@@ -450,7 +456,7 @@ void umma_apply(const UmmaPlan* p, int trans, const MatIO<float>& io, int epi, c
     g.part = p->part.p;
     g.ctl = io.ctl;
     const int splits = trans ? p->splitsT : p->splitsN;
-    dim3 grid((unsigned)((M + UM - 1) / UM), (unsigned)splits);
+    dim3 grid((unsigned)splits, (unsigned)((M + UM - 1) / UM));
     k_umma_gemm<<<grid, 128, trans ? p->smemT : p->smemN, s>>>(trans ? p->mapAt : p->mapA,
                                                                trans ? p->mapBTh : p->mapBNh,
                                                                trans ? p->mapBTl : p->mapBNl, g);

@@ -8,6 +8,7 @@
 #include <vector>
 #include "dbuf.h"
 #include "ops.h"
+#include "tiled.h"
 
 namespace tv3 {
 
@@ -176,8 +177,54 @@ struct CsrOp : LinOp<T> {
     DBuf<V> val, tval;
     DBuf<float> rs;  // per-ray scale (16-bit storage only)
     int Gn = 32, Gt = 8, grid_n = 1, grid_t = 1;
+    mutable TiledT<T, V> tiled;  // A^T regrouped by voxel tiles (when the volume is known)
+    mutable int vol[3] = {0, 0, 0};
+
+    void set_volume(int p, int q, int r) const override {
+        if (vol[0] == p && vol[1] == q && vol[2] == r) return;
+        vol[0] = p; vol[1] = q; vol[2] = r;
+        tiled.build(this->n, this->m, p, q, r, tptr.p, tind.p, tval.p, this->nnz, 96 * 1024, 0);
+        // keep the tile-staged A^T only where it beats the tuned CSR kernel
+        if (tiled.ok && this->nnz >= (1L << 22) && time_transpose(false) <= time_transpose(true)) tiled = TiledT<T, V>();
+    }
+
+    // milliseconds of three A^T*y launches (after one warm-up), plain or tiled
+    float time_transpose(bool use_tiled) const {
+        const bool keep = tiled.ok;
+        tiled.ok = use_tiled && keep;
+        DBuf<T> x(std::max<long>(this->m, 1)), y(std::max<long>(this->n, 1));
+        TV3_CUDA(cudaMemset(x.p, 0, std::max<long>(this->m, 1) * sizeof(T)));
+        cudaEvent_t e0, e1;
+        TV3_CUDA(cudaEventCreate(&e0));
+        TV3_CUDA(cudaEventCreate(&e1));
+        MatIO<T> io = plain_io<T>(x.p, y.p);
+        apply(1, io, SPMV_PLAIN, 0);
+        TV3_CUDA(cudaEventRecord(e0, 0));
+        for (int k = 0; k < 3; ++k) apply(1, io, SPMV_PLAIN, 0);
+        TV3_CUDA(cudaEventRecord(e1, 0));
+        TV3_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        TV3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        tiled.ok = keep;
+        return ms;
+    }
 
     void apply(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const override {
+        if (trans && io.L <= 1 && tiled.ok && (epi == SPMV_PLAIN || epi == SPMV_SUB)) {
+            TiledArgs<T, V> t{};
+            t.ntiles = tiled.ntiles; t.ray_off = tiled.ray_off.p; t.rays = tiled.rays.p;
+            t.tile_slice = tiled.tile_slice.p; t.slice_off = tiled.slice_off.p; t.row_voxel = tiled.row_voxel.p;
+            t.lidx = tiled.lidx.p; t.val = tiled.val.p;
+            t.tile_unit = tiled.tile_unit.p; t.slice_unit = tiled.slice_unit.p; t.unit_slice = tiled.unit_slice.p;
+            t.unit_k0 = tiled.unit_k0.p; t.max_rays = tiled.max_rays;
+            t.xscale = rs.p;
+            t.x[0] = io.x[0]; t.x[1] = io.x[1]; t.y[0] = io.y[0]; t.y[1] = io.y[1];
+            t.by_parity = io.by_parity; t.sub = io.sub; t.ctl = io.ctl;
+            tiled.apply(t, epi, s);
+            return;
+        }
         SpmvArgs<T, V> a{};
         if (!trans) {
             a.rows = this->m; a.ptr = ptr.p; a.ind = ind.p; a.val = val.p; a.rscale = rs.p; a.xscale = nullptr;

@@ -64,6 +64,13 @@ struct LinOp {
     // allocate what products with L interleaved right-hand sides need (called
     // before any product, outside stream capture)
     virtual void prepare(int L) const { (void)L; }
+    // the volume the columns form (dim_y fastest, dim_x, dim_z): lets stored
+    // operators regroup A^T by voxel tiles (tiled.cu); called outside capture
+    virtual void set_volume(int p, int q, int r) const {
+        (void)p;
+        (void)q;
+        (void)r;
+    }
     // true when apply() takes L > 1 interleaved right-hand sides
     virtual bool multi_rhs() const { return false; }
     // multi-RHS products: columns of length n (trans 0: X n x k -> Y m x k),
@@ -101,6 +108,7 @@ struct SplitOp : LinOp<T> {
         nop->prepare(L);
         top->prepare(L);
     }
+    void set_volume(int p, int q, int r) const override { top->set_volume(p, q, r); }
 };
 
 // CSR operator: A and the CSR of A^T on the device.

@@ -1,0 +1,397 @@
+// A^T*y with the gathered vector staged in shared memory per voxel tile.
+//
+// In the CSR of A^T (rows = voxels) every nonzero gathers one y value of a
+// ray.  A ray crosses a tile of voxels (16 x 16 x 8 in 3D, 32 x 32 in 2D) in
+// a run of about a dozen consecutive voxels, so the ~26,000 nonzeros of a
+// tile at 128^3 touch only ~2,000 distinct rays.  The tiled form stores, per
+// tile, the ascending list of those rays and, per nonzero, the ray's position
+// in that list (16 bits) instead of its index (32 bits).  One CTA per tile
+// gathers the tile's y values once into shared memory, then sums its voxel
+// rows from shared memory: global gathers drop by an order of magnitude, the
+// matrix stream drops from 8 to 6 bytes per FP32 nonzero, and the rows'
+// gathers cost shared-memory bandwidth instead of L1/L2 wavefronts.
+//
+// Inside a tile the voxel rows are sorted by length (longest first) and cut
+// into slices of 32 rows stored "sliced ELL" style: entry k of the slice's
+// lane l sits at slice_off + 32 k + l, so a warp (one row per lane) reads 32
+// entries with one coalesced load of positions and one of values, and the
+// slice is padded only to its first (longest) row.  Every row is summed by one
+// thread in its original nonzero order (deterministic).
+//
+// Built once on the device from the CSR of A^T with a radix sort of
+// (tile, ray) keys; used for A^T*y when the operator knows the volume's
+// dimensions and every tile's ray list fits the shared-memory budget.
+//
+// Work inside a tile is split into units of at most TILED_UNIT_K steps of
+// one slice (32 rows), so the warps of a CTA get near-equal work; each unit
+// leaves 32 partial sums in shared memory and every row adds its units'
+// partials in order after a barrier (deterministic).
+#include <cub/cub.cuh>
+#include <algorithm>
+#include <vector>
+#include "ops.h"
+#include "tiled.h"
+
+namespace tv3 {
+
+namespace {
+
+int ewt(long n) {
+    long g = (n + 255) / 256;
+    long cap = (long)num_sms() * 32;
+    return (int)std::max<long>(1, std::min(g, cap));
+}
+
+template <class V> struct TVT { using type = float; };
+template <> struct TVT<double> { using type = double; };
+
+__global__ void k_tile_of_voxel(long n, int p, int q, int ty, int tx, int tz, int nty, int ntx, int* __restrict__ tv,
+                                int* __restrict__ iota) {
+    for (long v = (long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (long)gridDim.x * blockDim.x) {
+        const long y = v % p, x = (v / p) % q, z = v / ((long)p * q);
+        tv[v] = (int)((z / tz) * ((long)nty * ntx) + (x / tx) * nty + y / ty);
+        iota[v] = (int)v;
+    }
+}
+
+__global__ void k_rows_of(long rows, const int* __restrict__ ptr, int* __restrict__ rowof) {
+    const int lane = threadIdx.x & 31;
+    for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += ((long)gridDim.x * blockDim.x) >> 5)
+        for (int k = ptr[r] + lane; k < ptr[r + 1]; k += 32) rowof[k] = (int)r;
+}
+
+__global__ void k_keys(long nnz, const int* __restrict__ rowof, const int* __restrict__ tind,
+                       const int* __restrict__ tile_of, unsigned long long* __restrict__ key, int* __restrict__ idx) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
+        key[k] = ((unsigned long long)(unsigned)tile_of[rowof[k]] << 32) | (unsigned)tind[k];
+        idx[k] = (int)k;
+    }
+}
+
+// first-of-(tile, ray) flags of the sorted keys, and each tile's first position
+__global__ void k_flags(long nnz, const unsigned long long* __restrict__ key, int* __restrict__ newray,
+                        int* __restrict__ tile_first) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
+        const unsigned long long c = key[k];
+        newray[k] = (k == 0 || key[k - 1] != c) ? 1 : 0;
+        if (k == 0 || (key[k - 1] >> 32) != (c >> 32)) tile_first[c >> 32] = (int)k;
+    }
+}
+
+// uniq[k] = number of distinct (tile, ray) pairs up to and including k
+__global__ void k_local(long nnz, const unsigned long long* __restrict__ key, const int* __restrict__ uniq,
+                        const int* __restrict__ idx, const int* __restrict__ tile_first, int* __restrict__ rays,
+                        unsigned short* __restrict__ local_of_entry) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
+        const unsigned long long c = key[k];
+        const int t = (int)(c >> 32);
+        const int u = uniq[k] - 1;                 // this (tile, ray) in the concatenated lists
+        const int base = uniq[tile_first[t]] - 1;  // the tile's first
+        if (k == 0 || key[k - 1] != c) rays[u] = (int)(unsigned)(c & 0xffffffffu);
+        local_of_entry[idx[k]] = (unsigned short)(u - base);
+    }
+}
+
+__global__ void k_tile_start(int ntiles, const int* __restrict__ tile_first, const int* __restrict__ uniq,
+                             int* __restrict__ start) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
+        start[t] = tile_first[t] >= 0 ? uniq[tile_first[t]] - 1 : -1;
+}
+
+// sorted-row keys: (tile, longest first, voxel order kept by the stable sort)
+__global__ void k_row_keys(long n, const int* __restrict__ tile_of, const int* __restrict__ tptr,
+                           unsigned long long* __restrict__ key, int* __restrict__ iota, int* __restrict__ too_long) {
+    for (long v = (long)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (long)gridDim.x * blockDim.x) {
+        int len = tptr[v + 1] - tptr[v];
+        if (len > 0xffff) {
+            *too_long = 1;
+            len = 0xffff;
+        }
+        key[v] = ((unsigned long long)(unsigned)tile_of[v] << 16) | (unsigned)(0xffff - len);
+        iota[v] = (int)v;
+    }
+}
+
+template <class V>
+__global__ void k_fill_slices(long n, const unsigned long long* __restrict__ key, const int* __restrict__ vox,
+                              const int* __restrict__ tile_row, const int* __restrict__ tile_slice,
+                              const long long* __restrict__ slice_off, const int* __restrict__ tptr,
+                              const unsigned short* __restrict__ local_of, const V* __restrict__ tval,
+                              unsigned short* __restrict__ lidx, V* __restrict__ val, int* __restrict__ row_voxel) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int t = (int)(key[i] >> 16);
+        const int j = (int)(i - tile_row[t]);
+        const int sl = tile_slice[t] + j / 32, lane = j % 32;
+        const int v = vox[i];
+        row_voxel[(long)sl * 32 + lane] = v;
+        const long long o = slice_off[sl] + lane;
+        const int s0 = tptr[v], len = tptr[v + 1] - s0;
+        for (int k = 0; k < len; ++k) {
+            lidx[o + 32LL * k] = local_of[s0 + k];
+            val[o + 32LL * k] = tval[s0 + k];
+        }
+    }
+}
+
+template <class T, class V, int EPI, int U>
+__global__ void __launch_bounds__(512) k_spmv_tiled(TiledArgs<T, V> a) {
+    count_launch(a.ctl);
+    using VV = typename TVT<V>::type;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T* ysm = reinterpret_cast<T*>(sm_raw);
+    T* psm = ysm + a.max_rays;  // partial sums: 32 per work unit
+    const int sel = a.by_parity ? a.ctl->parity : 0;
+    const T* __restrict__ y = a.x[sel];
+    T* __restrict__ out = a.y[sel];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const int r0 = __ldg(a.ray_off + t), nr = __ldg(a.ray_off + t + 1) - r0;
+        // stage the tile's y values: 8 independent index loads, then 8 gathers
+        for (int j0 = threadIdx.x; j0 < nr; j0 += 8 * blockDim.x) {
+            int ray[8];
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int j = j0 + u * blockDim.x;
+                ray[u] = (j < nr) ? __ldg(a.rays + r0 + j) : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = (ray[u] >= 0) ? y[ray[u]] : T(0);
+            if (a.xscale) {
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (ray[u] >= 0) v[u] *= (T)__ldg(a.xscale + ray[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (ray[u] >= 0) ysm[j0 + u * blockDim.x] = v[u];
+        }
+        __syncthreads();
+        // work units: at most UNIT_K steps of one slice, so warps get equal work
+        const int u0 = __ldg(a.tile_unit + t), u1 = __ldg(a.tile_unit + t + 1);
+        for (int w = u0 + warp; w < u1; w += nwarps) {
+            const int sl = __ldg(a.unit_slice + w);
+            const long long off = a.slice_off[sl];
+            const int len = (int)((a.slice_off[sl + 1] - off) >> 5);
+            const int k0 = __ldg(a.unit_k0 + w), k1 = min(len, k0 + TILED_UNIT_K);
+            const unsigned short* __restrict__ li = a.lidx + off + lane;
+            const V* __restrict__ va = a.val + off + lane;
+            RowAcc<T> acc;
+            int k = k0;
+            for (; k + U <= k1; k += U) {
+                unsigned short ii[U];
+                VV vv[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    ii[u] = __ldcs(li + 32 * (k + u));
+                    vv[u] = (VV)Acc<VV, V>::load(va + 32 * (k + u));
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) madd(acc, vv[u], ysm[ii[u]]);
+            }
+            for (; k < k1; ++k) madd(acc, (VV)Acc<VV, V>::load(va + 32 * k), ysm[__ldcs(li + 32 * k)]);
+            psm[(w - u0) * 32 + lane] = acc.value();
+        }
+        __syncthreads();
+        // every row: its units' partials in order
+        const int s0 = __ldg(a.tile_slice + t), s1 = __ldg(a.tile_slice + t + 1);
+        for (int i = threadIdx.x; i < (s1 - s0) * 32; i += blockDim.x) {
+            const int sl = s0 + (i >> 5), ln = i & 31;
+            const int v = __ldg(a.row_voxel + (long)sl * 32 + ln);
+            if (v < 0) continue;
+            const int e0 = __ldg(a.slice_unit + sl) - u0, e1 = __ldg(a.slice_unit + sl + 1) - u0;
+            T sum = T(0);
+            for (int e = e0; e < e1; ++e) sum += psm[e * 32 + ln];
+            if (EPI == SPMV_SUB) out[v] = sum - a.sub[v];
+            else out[v] = sum;
+        }
+        __syncthreads();
+    }
+}
+
+template <class T, class V>
+void set_smem_attr(size_t smem) {
+    const int b = (int)smem;
+    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiled<T, V, SPMV_PLAIN, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiled<T, V, SPMV_SUB, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+}
+
+}  // namespace
+
+template <class T, class V>
+void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, const int* tind, const V* tval,
+                         long nnz, size_t max_smem, cudaStream_t s) {
+    ok = false;
+    n = n_;
+    if (nnz <= 0 || n <= 0 || m <= 0 || (long)p * q * r != n || nnz >= (1L << 31)) return;
+    // tile shape: 8 x 8 x 8 voxels in 3D, 16 x 16 in 2D
+    const int ty = std::min(p, r > 1 ? 8 : 16), tx = std::min(q, r > 1 ? 8 : 16), tz = std::min(r, 8);
+    const int nty = (p + ty - 1) / ty, ntx = (q + tx - 1) / tx, ntz = (r + tz - 1) / tz;
+    const long nt = (long)nty * ntx * ntz;
+    if (nt >= (1L << 24)) return;
+    ntiles = (int)nt;
+
+    // ---- (tile, ray) keys of every nonzero, sorted: the tiles' ray lists
+    DBuf<int> tile_of(n), iota(n), tile_first(ntiles);
+    DBuf<unsigned short> local_of(nnz);
+    int nuniq = 0;
+    {
+        DBuf<int> rowof(nnz), idx(nnz), idx_s(nnz), newray(nnz), uniq(nnz);
+        DBuf<unsigned long long> key(nnz), key_s(nnz);
+        k_tile_of_voxel<<<ewt(n), 256, 0, s>>>(n, p, q, ty, tx, tz, nty, ntx, tile_of.p, iota.p);
+        k_rows_of<<<ewt(n * 32), 256, 0, s>>>(n, tptr, rowof.p);
+        k_keys<<<ewt(nnz), 256, 0, s>>>(nnz, rowof.p, tind, tile_of.p, key.p, idx.p);
+        TV3_CUDA(cudaGetLastError());
+        int end_bit = 33;
+        while (end_bit < 64 && (1LL << (end_bit - 32)) < ntiles) ++end_bit;
+        size_t tb = 0;
+        TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, key.p, key_s.p, idx.p, idx_s.p, (int)nnz, 0, end_bit, s));
+        {
+            DBuf<char> tmp(std::max<size_t>(tb, 1));
+            TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, key.p, key_s.p, idx.p, idx_s.p, (int)nnz, 0, end_bit,
+                                                     s));
+            TV3_CUDA(cudaStreamSynchronize(s));
+        }
+        TV3_CUDA(cudaMemsetAsync(tile_first.p, 0xff, ntiles * sizeof(int), s));
+        k_flags<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, newray.p, tile_first.p);
+        size_t sb = 0;
+        TV3_CUDA(cub::DeviceScan::InclusiveSum(nullptr, sb, newray.p, uniq.p, (int)nnz, s));
+        {
+            DBuf<char> tmp(std::max<size_t>(sb, 1));
+            TV3_CUDA(cub::DeviceScan::InclusiveSum(tmp.p, sb, newray.p, uniq.p, (int)nnz, s));
+            TV3_CUDA(cudaStreamSynchronize(s));
+        }
+        TV3_CUDA(cudaMemcpy(&nuniq, uniq.p + nnz - 1, sizeof(int), cudaMemcpyDeviceToHost));
+        rays.alloc(std::max(nuniq, 1));
+        k_local<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, uniq.p, idx_s.p, tile_first.p, rays.p, local_of.p);
+        TV3_CUDA(cudaGetLastError());
+        // per-tile ray offsets: start of tile t's list = uniq[tile_first[t]] - 1;
+        // a tile without nonzeros takes the next tile's start
+        std::vector<int> roff(ntiles + 1, 0);
+        DBuf<int> st(ntiles);
+        k_tile_start<<<ewt(ntiles), 256, 0, s>>>(ntiles, tile_first.p, uniq.p, st.p);
+        std::vector<int> start(ntiles);
+        TV3_CUDA(cudaMemcpyAsync(start.data(), st.p, ntiles * sizeof(int), cudaMemcpyDeviceToHost, s));
+        TV3_CUDA(cudaStreamSynchronize(s));
+        roff[ntiles] = nuniq;
+        for (int t = ntiles - 1; t >= 0; --t) roff[t] = (start[t] >= 0) ? start[t] : roff[t + 1];
+        max_rays = 0;
+        for (int t = 0; t < ntiles; ++t) max_rays = std::max(max_rays, roff[t + 1] - roff[t]);
+        if (max_rays > 65535 || (size_t)max_rays * sizeof(T) > max_smem) {
+            rays.release();
+            return;
+        }
+        ray_off.alloc(ntiles + 1);
+        TV3_CUDA(cudaMemcpy(ray_off.p, roff.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    }
+
+    // ---- rows sorted by (tile, length descending), cut into slices of 32
+    DBuf<unsigned long long> rkey(n), rkey_s(n);
+    DBuf<int> vox(n), too_long(1);
+    TV3_CUDA(cudaMemsetAsync(too_long.p, 0, sizeof(int), s));
+    k_row_keys<<<ewt(n), 256, 0, s>>>(n, tile_of.p, tptr, rkey.p, iota.p, too_long.p);
+    int rbits = 17;
+    while (rbits < 64 && (1LL << (rbits - 16)) < ntiles) ++rbits;
+    size_t rb = 0;
+    TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, rb, rkey.p, rkey_s.p, iota.p, vox.p, (int)n, 0, rbits, s));
+    {
+        DBuf<char> tmp(std::max<size_t>(rb, 1));
+        TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, rb, rkey.p, rkey_s.p, iota.p, vox.p, (int)n, 0, rbits, s));
+        TV3_CUDA(cudaStreamSynchronize(s));
+    }
+    int tl = 0;
+    TV3_CUDA(cudaMemcpy(&tl, too_long.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (tl) {
+        rays.release();
+        ray_off.release();
+        return;
+    }
+    std::vector<unsigned long long> hk(n);
+    TV3_CUDA(cudaMemcpy(hk.data(), rkey_s.p, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    std::vector<int> trow(ntiles + 1, (int)n), tsl(ntiles + 1, 0);
+    for (long i = n - 1; i >= 0; --i) trow[hk[i] >> 16] = (int)i;
+    for (int t = ntiles - 1; t >= 0; --t) trow[t] = std::min(trow[t], trow[t + 1]);
+    std::vector<long long> soff(1, 0);
+    for (int t = 0; t < ntiles; ++t) {
+        tsl[t] = (int)(soff.size() - 1);
+        for (long i = trow[t]; i < trow[t + 1]; i += 32) {
+            const long len = 0xffff - (long)(hk[i] & 0xffff);  // the slice's first row is its longest
+            soff.push_back(soff.back() + 32 * len);
+        }
+    }
+    tsl[ntiles] = (int)(soff.size() - 1);
+    nslices = tsl[ntiles];
+    // work units of at most TILED_UNIT_K steps per slice (a slice of length 0 still gets one)
+    std::vector<int> uslice, tunit(ntiles + 1, 0), sunit(nslices + 1, 0);
+    std::vector<unsigned short> uk0;
+    max_units = 0;
+    for (int t = 0; t < ntiles; ++t) {
+        tunit[t] = (int)uslice.size();
+        for (int sl = tsl[t]; sl < tsl[t + 1]; ++sl) {
+            sunit[sl] = (int)uslice.size();
+            const long len = (soff[sl + 1] - soff[sl]) / 32;
+            for (long k0 = 0; k0 < std::max(len, 1L); k0 += TILED_UNIT_K) {
+                uslice.push_back(sl);
+                uk0.push_back((unsigned short)k0);
+            }
+        }
+        max_units = std::max(max_units, (int)uslice.size() - tunit[t]);
+    }
+    tunit[ntiles] = (int)uslice.size();
+    sunit[nslices] = (int)uslice.size();
+    if ((size_t)max_rays * sizeof(T) + (size_t)max_units * 32 * sizeof(T) > max_smem) {
+        rays.release();
+        ray_off.release();
+        return;
+    }
+    nunits = (int)uslice.size();
+    tile_unit.alloc(ntiles + 1);
+    slice_unit.alloc(nslices + 1);
+    unit_slice.alloc(std::max(nunits, 1));
+    unit_k0.alloc(std::max(nunits, 1));
+    TV3_CUDA(cudaMemcpy(tile_unit.p, tunit.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    TV3_CUDA(cudaMemcpy(slice_unit.p, sunit.data(), (nslices + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    if (nunits) {
+        TV3_CUDA(cudaMemcpy(unit_slice.p, uslice.data(), nunits * sizeof(int), cudaMemcpyHostToDevice));
+        TV3_CUDA(cudaMemcpy(unit_k0.p, uk0.data(), nunits * sizeof(unsigned short), cudaMemcpyHostToDevice));
+    }
+    const long long padded = soff.back();
+    tile_slice.alloc(ntiles + 1);
+    slice_off.alloc(nslices + 1);
+    TV3_CUDA(cudaMemcpy(tile_slice.p, tsl.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    TV3_CUDA(cudaMemcpy(slice_off.p, soff.data(), (nslices + 1) * sizeof(long long), cudaMemcpyHostToDevice));
+    DBuf<int> trow_d(ntiles + 1);
+    TV3_CUDA(cudaMemcpy(trow_d.p, trow.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    lidx.alloc(std::max<long long>(padded, 1));
+    val.alloc(std::max<long long>(padded, 1));
+    row_voxel.alloc((size_t)std::max(nslices, 1) * 32);
+    TV3_CUDA(cudaMemsetAsync(lidx.p, 0, std::max<long long>(padded, 1) * sizeof(unsigned short), s));
+    TV3_CUDA(cudaMemsetAsync(val.p, 0, std::max<long long>(padded, 1) * sizeof(V), s));
+    TV3_CUDA(cudaMemsetAsync(row_voxel.p, 0xff, (size_t)std::max(nslices, 1) * 32 * sizeof(int), s));
+    k_fill_slices<V><<<ewt(n), 256, 0, s>>>(n, rkey_s.p, vox.p, trow_d.p, tile_slice.p, slice_off.p, tptr, local_of.p,
+                                            tval, lidx.p, val.p, row_voxel.p);
+    TV3_CUDA(cudaGetLastError());
+    padded_entries = padded;
+    // the attribute is per kernel, shared by every operator: always the full budget
+    set_smem_attr<T, V>(max_smem);
+    TV3_CUDA(cudaStreamSynchronize(s));
+    ok = true;
+}
+
+template <class T, class V>
+void TiledT<T, V>::apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) const {
+    const size_t smem = std::max<size_t>(((size_t)max_rays + (size_t)max_units * 32) * sizeof(T), 16);
+    const int grid = std::max(a.ntiles, 1);
+    if (epi == SPMV_SUB) k_spmv_tiled<T, V, SPMV_SUB, 8><<<grid, 512, smem, s>>>(a);
+    else k_spmv_tiled<T, V, SPMV_PLAIN, 8><<<grid, 512, smem, s>>>(a);
+    TV3_CUDA(cudaGetLastError());
+}
+
+template struct TiledT<float, float>;
+template struct TiledT<double, double>;
+template struct TiledT<double, float>;
+template struct TiledT<df64, float>;
+template struct TiledT<float, __nv_bfloat16>;
+template struct TiledT<float, __half>;
+
+}  // namespace tv3

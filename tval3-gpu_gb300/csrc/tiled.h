@@ -1,0 +1,57 @@
+// Tile-staged A^T*y (tiled.cu): the CSR of A^T regrouped by voxel tiles, with
+// per-tile ray lists so that a CTA can stage the tile's y values in shared
+// memory.
+#pragma once
+
+#include <cuda_runtime.h>
+#include "dbuf.h"
+#include "launch.h"
+#include "tval3_internal.cuh"
+
+namespace tv3 {
+
+constexpr int TILED_UNIT_K = 16;  // steps of one slice per work unit
+
+template <class T, class V>
+struct TiledArgs {
+    int ntiles;
+    const int* ray_off;          // ntiles + 1: the tile's rays are rays[ray_off[t] .. ray_off[t+1])
+    const int* rays;             // ray indices, ascending inside each tile
+    const int* tile_slice;       // ntiles + 1: the tile's slices of 32 rows
+    const long long* slice_off;  // nslices + 1: entry k of lane l of slice s at slice_off[s] + 32 k + l
+    const int* row_voxel;        // 32 per slice: the voxel of each lane's row (-1: padding)
+    const unsigned short* lidx;  // position of the nonzero's ray in its tile's list (0 in padding)
+    const V* val;                // value (0 in padding)
+    const int* tile_unit;        // ntiles + 1: the tile's work units
+    const int* slice_unit;       // nslices + 1: the slice's work units
+    const int* unit_slice;       // slice of each unit
+    const unsigned short* unit_k0;  // first step of each unit
+    int max_rays;                // shared memory: max_rays values of y, then 32 partials per unit
+    const float* xscale;       // per-ray scale of the gathered y (16-bit storage), or null
+    const T* x[2];             // y (the input of A^T), ping-pong by parity
+    T* y[2];                   // the output volume
+    int by_parity;
+    const T* sub;              // SPMV_SUB: out = A^T y - sub
+    Ctl* ctl;
+};
+
+template <class T, class V>
+struct TiledT {
+    bool ok = false;
+    long n = 0;
+    int ntiles = 0, nslices = 0, nunits = 0, max_rays = 0, max_units = 0;
+    long long padded_entries = 0;
+    DBuf<int> ray_off, rays, tile_slice, row_voxel, tile_unit, slice_unit, unit_slice;
+    DBuf<unsigned short> unit_k0;
+    DBuf<long long> slice_off;
+    DBuf<unsigned short> lidx;
+    DBuf<V> val;
+    // build from the CSR of A^T (n voxel rows, ray indices < m) of a p x q x r
+    // volume; leaves ok = false when some tile's ray list exceeds max_smem
+    // bytes of T or 65,535 entries
+    void build(long n, long m, int p, int q, int r, const int* tptr, const int* tind, const V* tval, long nnz,
+               size_t max_smem, cudaStream_t s);
+    void apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) const;
+};
+
+}  // namespace tv3

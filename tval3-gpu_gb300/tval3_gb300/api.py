@@ -297,6 +297,11 @@ class Operator:
     def mat_mat_mul(self, trans: int, nrhs: int, X, Y, stream=None) -> None:
         check(load().tval3_mat_mat_mul(self._h, int(trans), nrhs, _ptr(X), _ptr(Y), _stream(stream)))
 
+    def mat_mat_mul_interleaved(self, trans: int, nrhs: int, X, Y, stream=None) -> None:
+        """Y = A X (or A^T X) for nrhs right-hand sides stored interleaved
+        (element (row, j) at row * nrhs + j)."""
+        check(load().tval3_mat_mat_mul_interleaved(self._h, trans, nrhs, _ptr(X), _ptr(Y), _stream(stream)))
+
     def export_csr(self):
         m, n, z = self.rows, self.cols, self.nnz
         ptr, tptr = np.empty(m + 1, np.int32), np.empty(n + 1, np.int32)
