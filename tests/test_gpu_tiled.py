@@ -1,9 +1,10 @@
-"""Tile-staged A^T*y (tiled.cu): operators built from a geometry know their
-volume and regroup A^T by voxel tiles, staging each tile's y values in
-shared memory; operators built from a bare sparse matrix use the plain CSR
-kernel.  Both must give the same products: FP64 and double-float to 1e-12,
-FP32 to 1e-5 (relative to sum |a||y| per voxel), BF16 exactly like the
-per-ray scaled plain kernel up to FP32 rounding."""
+"""Tile-staged products (tiled.cu): operators built from a geometry know
+their volume and regroup A^T by voxel tiles (each tile's y values staged in
+shared memory) and A into per-tile ray segments (each tile's x values staged,
+per-ray partials added in tile order); operators built from a bare sparse
+matrix use the plain CSR kernels.  Both must give the same products:
+double-float to 1e-12, FP32 and BF16 to 1e-5 (relative to sum |a||v| per
+output)."""
 import numpy as np
 import pytest
 
@@ -19,7 +20,8 @@ def _geo(kind):
 
 @pytest.mark.parametrize("kind", ["ring", "hemi"])
 @pytest.mark.parametrize("prec", ["fp32", "df64", "bf16"])
-def test_tiled_transpose_matches_plain_csr(cuda, kind, prec):
+@pytest.mark.parametrize("trans", [1, 0])
+def test_tiled_products_match_plain_csr(cuda, kind, prec, trans):
     import torch
     from tval3_gb300 import PREC_BF16, PREC_FP32, PREC_FP32_DF64, Operator, SparseMatrix
     geo = _geo(kind)
@@ -28,29 +30,33 @@ def test_tiled_transpose_matches_plain_csr(cuda, kind, prec):
     ptr, ind, val, tptr, tind, tval = Operator.from_geometry(geo, mode=0, precision=PREC_FP32).export_csr()
     m, n = ptr.size - 1, tptr.size - 1
     plain = Operator.from_sparse(SparseMatrix(m, n, ptr, ind, val, tptr, tind, tval), precision=p)
-    g = torch.Generator().manual_seed(7)
-    yh = torch.randn(m, dtype=torch.float64, generator=g)
-    absA = np.zeros(n)
-    np.add.at(absA, np.repeat(np.arange(n), np.diff(tptr)), np.abs(tval.astype(np.float64)) * np.abs(yh.numpy()[tind]))
+    g = torch.Generator().manual_seed(7 + trans)
+    lin, lout = (m, n) if trans else (n, m)
+    yh = torch.randn(lin, dtype=torch.float64, generator=g)
+    absA = np.zeros(lout)
+    if trans:
+        np.add.at(absA, np.repeat(np.arange(n), np.diff(tptr)), np.abs(tval.astype(np.float64)) * np.abs(yh.numpy()[tind]))
+    else:
+        np.add.at(absA, np.repeat(np.arange(m), np.diff(ptr)), np.abs(val.astype(np.float64)) * np.abs(yh.numpy()[ind]))
     if prec == "df64":
         from tval3_gb300 import capi
         lib = capi.load()
-        yd = torch.empty(2 * m, dtype=torch.float32, device=cuda)
-        capi.check(lib.tval3_df64_from_f64(yh.to(cuda).data_ptr(), yd.data_ptr(), m, None))
+        yd = torch.empty(2 * lin, dtype=torch.float32, device=cuda)
+        capi.check(lib.tval3_df64_from_f64(yh.to(cuda).data_ptr(), yd.data_ptr(), lin, None))
         outs = []
         for op in (tiled, plain):
-            xd = torch.empty(2 * n, dtype=torch.float32, device=cuda)
-            op.mat_vec_mul(1, yd, xd)
-            xo = torch.empty(n, dtype=torch.float64, device=cuda)
-            capi.check(lib.tval3_df64_to_f64(xd.data_ptr(), xo.data_ptr(), n, None))
+            xd = torch.empty(2 * lout, dtype=torch.float32, device=cuda)
+            op.mat_vec_mul(trans, yd, xd)
+            xo = torch.empty(lout, dtype=torch.float64, device=cuda)
+            capi.check(lib.tval3_df64_to_f64(xd.data_ptr(), xo.data_ptr(), lout, None))
             outs.append(xo.cpu().numpy())
         tol = 1e-12
     else:
         yd = yh.float().to(cuda)
         outs = []
         for op in (tiled, plain):
-            xd = torch.empty(n, dtype=torch.float32, device=cuda)
-            op.mat_vec_mul(1, yd, xd)
+            xd = torch.empty(lout, dtype=torch.float32, device=cuda)
+            op.mat_vec_mul(trans, yd, xd)
             outs.append(xd.cpu().numpy().astype(np.float64))
         tol = 1e-5
     torch.cuda.synchronize()

@@ -177,41 +177,62 @@ struct CsrOp : LinOp<T> {
     DBuf<V> val, tval;
     DBuf<float> rs;  // per-ray scale (16-bit storage only)
     int Gn = 32, Gt = 8, grid_n = 1, grid_t = 1;
-    mutable TiledT<T, V> tiled;  // A^T regrouped by voxel tiles (when the volume is known)
+    mutable TiledT<T, V> tiled;   // A^T regrouped by voxel tiles (when the volume is known)
+    mutable TiledN<T, V> tiledN;  // A cut into per-tile ray segments (when the volume is known)
     mutable int vol[3] = {0, 0, 0};
 
     void set_volume(int p, int q, int r) const override {
         if (vol[0] == p && vol[1] == q && vol[2] == r) return;
         vol[0] = p; vol[1] = q; vol[2] = r;
         tiled.build(this->n, this->m, p, q, r, tptr.p, tind.p, tval.p, this->nnz, 96 * 1024, 0);
-        // keep the tile-staged A^T only where it beats the tuned CSR kernel
-        if (tiled.ok && this->nnz >= (1L << 22) && time_transpose(false) <= time_transpose(true)) tiled = TiledT<T, V>();
+        tiledN.build(this->m, p, q, r, ptr.p, ind.p, val.p, this->nnz, 0);
+        // keep the tile-staged products only where they beat the tuned CSR kernels
+        if (this->nnz >= (1L << 22)) {
+            if (tiled.ok && time_product(1, false) <= time_product(1, true)) tiled = TiledT<T, V>();
+            if (tiledN.ok && time_product(0, false) <= time_product(0, true)) tiledN = TiledN<T, V>();
+        }
     }
 
-    // milliseconds of three A^T*y launches (after one warm-up), plain or tiled
-    float time_transpose(bool use_tiled) const {
-        const bool keep = tiled.ok;
-        tiled.ok = use_tiled && keep;
-        DBuf<T> x(std::max<long>(this->m, 1)), y(std::max<long>(this->n, 1));
-        TV3_CUDA(cudaMemset(x.p, 0, std::max<long>(this->m, 1) * sizeof(T)));
+    // milliseconds of three products (after one warm-up), plain CSR or tile-staged
+    float time_product(int trans, bool use_tiled) const {
+        bool& flag = trans ? tiled.ok : tiledN.ok;
+        const bool keep = flag;
+        flag = use_tiled && keep;
+        const long lx = trans ? this->m : this->n, ly = trans ? this->n : this->m;
+        DBuf<T> x(std::max<long>(lx, 1)), y(std::max<long>(ly, 1));
+        TV3_CUDA(cudaMemset(x.p, 0, std::max<long>(lx, 1) * sizeof(T)));
         cudaEvent_t e0, e1;
         TV3_CUDA(cudaEventCreate(&e0));
         TV3_CUDA(cudaEventCreate(&e1));
         MatIO<T> io = plain_io<T>(x.p, y.p);
-        apply(1, io, SPMV_PLAIN, 0);
+        apply(trans, io, SPMV_PLAIN, 0);
         TV3_CUDA(cudaEventRecord(e0, 0));
-        for (int k = 0; k < 3; ++k) apply(1, io, SPMV_PLAIN, 0);
+        for (int k = 0; k < 3; ++k) apply(trans, io, SPMV_PLAIN, 0);
         TV3_CUDA(cudaEventRecord(e1, 0));
         TV3_CUDA(cudaEventSynchronize(e1));
         float ms = 0.f;
         TV3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        tiled.ok = keep;
+        flag = keep;
         return ms;
     }
 
     void apply(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const override {
+        if (!trans && io.L <= 1 && tiledN.ok) {
+            TiledNArgs<T, V> t{};
+            t.ntiles = tiledN.ntiles;
+            t.p = tiledN.p; t.q = tiledN.q; t.r = tiledN.r; t.ty = tiledN.ty; t.tx = tiledN.tx; t.tz = tiledN.tz;
+            t.nty = tiledN.nty; t.ntx = tiledN.ntx;
+            t.tile_slice = tiledN.tile_slice.p; t.slice_off = tiledN.slice_off.p; t.slot_dest = tiledN.slot_dest.p;
+            t.lidx = tiledN.lidx.p; t.val = tiledN.val.p; t.part = tiledN.part.p; t.rseg = tiledN.rseg.p;
+            t.m = this->m; t.rscale = rs.p;
+            t.x[0] = io.x[0]; t.x[1] = io.x[1]; t.y[0] = io.y[0]; t.y[1] = io.y[1];
+            t.by_parity = io.by_parity; t.sub = io.sub; t.b = io.b; t.delta = io.delta; t.ctl = io.ctl;
+            t.rpart = io.part; t.ticket = io.ticket;
+            tiledN.apply(t, epi, s);
+            return;
+        }
         if (trans && io.L <= 1 && tiled.ok && (epi == SPMV_PLAIN || epi == SPMV_SUB)) {
             TiledArgs<T, V> t{};
             t.ntiles = tiled.ntiles; t.ray_off = tiled.ray_off.p; t.rays = tiled.rays.p;

@@ -387,6 +387,322 @@ void TiledT<T, V>::apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) cons
     TV3_CUDA(cudaGetLastError());
 }
 
+// ---------------------------------------------------------------------------
+// tile-staged A*x
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void k_n_keys(long nnz, const int* __restrict__ rowof, const int* __restrict__ ind,
+                         const int* __restrict__ tile_of, unsigned long long* __restrict__ key, int* __restrict__ idx) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
+        key[k] = ((unsigned long long)(unsigned)tile_of[ind[k]] << 32) | (unsigned)rowof[k];
+        idx[k] = (int)k;
+    }
+}
+
+__global__ void k_n_newseg(long nnz, const unsigned long long* __restrict__ key, int* __restrict__ f) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x)
+        f[k] = (k == 0 || key[k - 1] != key[k]) ? 1 : 0;
+}
+
+// per segment: its (tile, ray) key and first position in the sorted entries
+__global__ void k_n_segs(long nnz, const unsigned long long* __restrict__ key, const int* __restrict__ segid,
+                         unsigned long long* __restrict__ seg_key, int* __restrict__ seg_start) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x)
+        if (k == 0 || key[k - 1] != key[k]) {
+            seg_key[segid[k] - 1] = key[k];
+            seg_start[segid[k] - 1] = (int)k;
+        }
+}
+
+// segment keys for the slicing sort (tile, longest first) and the ray-major sort (ray, tile)
+__global__ void k_n_segkeys(long nseg, const unsigned long long* __restrict__ seg_key, const int* __restrict__ seg_start,
+                            long nnz, unsigned long long* __restrict__ k_slice, unsigned long long* __restrict__ k_ray,
+                            int* __restrict__ iota, int* __restrict__ too_long) {
+    for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += (long)gridDim.x * blockDim.x) {
+        const unsigned long long c = seg_key[s];
+        const long end = (s + 1 < nseg) ? seg_start[s + 1] : nnz;
+        long len = end - seg_start[s];
+        if (len > 0xffff) {
+            *too_long = 1;
+            len = 0xffff;
+        }
+        const unsigned tile = (unsigned)(c >> 32), ray = (unsigned)(c & 0xffffffffu);
+        k_slice[s] = ((unsigned long long)tile << 16) | (unsigned)(0xffff - len);
+        k_ray[s] = ((unsigned long long)ray << 32) | tile;
+        iota[s] = (int)s;
+    }
+}
+
+__global__ void k_n_dest(long nseg, const int* __restrict__ by_ray, const unsigned long long* __restrict__ k_ray_s,
+                         int* __restrict__ dest, int* __restrict__ rcount) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nseg; i += (long)gridDim.x * blockDim.x) {
+        dest[by_ray[i]] = (int)i;
+        atomicAdd(rcount + (k_ray_s[i] >> 32), 1);
+    }
+}
+
+template <class V>
+__global__ void k_n_fill(long nseg, const int* __restrict__ order, const unsigned long long* __restrict__ k_slice_s,
+                         const int* __restrict__ tile_seg0, const int* __restrict__ tile_slice,
+                         const long long* __restrict__ slice_off, const int* __restrict__ seg_start, long nnz,
+                         const int* __restrict__ idx_s, const int* __restrict__ ind, const V* __restrict__ valin,
+                         const int* __restrict__ dest, int p, int q, int ty, int tx, int tz,
+                         unsigned short* __restrict__ lidx, V* __restrict__ val, int* __restrict__ slot_dest) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nseg; i += (long)gridDim.x * blockDim.x) {
+        const int sid = order[i];
+        const int t = (int)(k_slice_s[i] >> 16);
+        const int j = (int)(i - tile_seg0[t]);
+        const int sl = tile_slice[t] + j / 32, lane = j % 32;
+        slot_dest[(long)sl * 32 + lane] = dest[sid];
+        const long long o = slice_off[sl] + lane;
+        const long b0 = seg_start[sid], b1 = (sid + 1 < nseg) ? seg_start[sid + 1] : nnz;
+        for (long k = b0; k < b1; ++k) {
+            const int e = idx_s[k];
+            const long v = ind[e];
+            const long y = v % p, x = (v / p) % q, z = v / ((long)p * q);
+            lidx[o + 32LL * (k - b0)] = (unsigned short)((y % ty) + ty * ((x % tx) + tx * (z % tz)));
+            val[o + 32LL * (k - b0)] = valin[e];
+        }
+    }
+}
+
+template <class T, class V, int U>
+__global__ void __launch_bounds__(512) k_spmv_tiledN(TiledNArgs<T, V> a) {
+    count_launch(a.ctl);
+    using VV = typename TVT<V>::type;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T* xsm = reinterpret_cast<T*>(sm_raw);
+    const int sel = a.by_parity ? a.ctl->parity : 0;
+    const T* __restrict__ x = a.x[sel];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int tvox = a.ty * a.tx * a.tz;
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const int s0 = __ldg(a.tile_slice + t), s1 = __ldg(a.tile_slice + t + 1);
+        if (s0 == s1) continue;  // uniform across the CTA
+        const int tzi = t / (a.nty * a.ntx), rem = t - tzi * a.nty * a.ntx, txi = rem / a.nty, tyi = rem - txi * a.nty;
+        const long y0 = (long)tyi * a.ty, x0 = (long)txi * a.tx, z0 = (long)tzi * a.tz;
+        for (int j = threadIdx.x; j < tvox; j += blockDim.x) {
+            const int ly = j % a.ty, lx = (j / a.ty) % a.tx, lz = j / (a.ty * a.tx);
+            const long yy = y0 + ly, xx = x0 + lx, zz = z0 + lz;
+            xsm[j] = (yy < a.p && xx < a.q && zz < a.r) ? x[yy + (long)a.p * (xx + (long)a.q * zz)] : T(0);
+        }
+        __syncthreads();
+        for (int sl = s0 + warp; sl < s1; sl += nwarps) {
+            const long long off = a.slice_off[sl];
+            const int len = (int)((a.slice_off[sl + 1] - off) >> 5);
+            const unsigned short* __restrict__ li = a.lidx + off + lane;
+            const V* __restrict__ va = a.val + off + lane;
+            RowAcc<T> acc;
+            int k = 0;
+            for (; k + U <= len; k += U) {
+                unsigned short ii[U];
+                VV vv[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    ii[u] = __ldcs(li + 32 * (k + u));
+                    vv[u] = (VV)Acc<VV, V>::load(va + 32 * (k + u));
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) madd(acc, vv[u], xsm[ii[u]]);
+            }
+            for (; k < len; ++k) madd(acc, (VV)Acc<VV, V>::load(va + 32 * k), xsm[__ldcs(li + 32 * k)]);
+            const int d = __ldg(a.slot_dest + (long)sl * 32 + lane);
+            if (d >= 0) a.part[d] = acc.value();
+        }
+        __syncthreads();
+    }
+}
+
+template <class T, class V, int EPI>
+__global__ void __launch_bounds__(256) k_tiledN_reduce(TiledNArgs<T, V> a) {
+    count_launch(a.ctl);
+    const int sel = a.by_parity ? a.ctl->parity : 0;
+    T* __restrict__ y = a.y[sel];
+    double acc0 = 0.0, acc1 = 0.0;
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < a.m; r += (long)gridDim.x * blockDim.x) {
+        const int e0 = __ldg(a.rseg + r), e1 = __ldg(a.rseg + r + 1);
+        T s = T(0);
+        for (int e = e0; e < e1; ++e) s += a.part[e];
+        if (a.rscale) s *= (T)__ldg(a.rscale + r);
+        if (EPI == SPMV_PLAIN) {
+            y[r] = s;
+        } else if (EPI == SPMV_SUB) {
+            y[r] = s - a.sub[r];
+        } else if (EPI == SPMV_LAM35) {
+            y[r] = s;
+            double t = acc_d(to_acc(s) - to_acc(a.b[r]));
+            acc0 += t * t;
+            acc1 += acc_d(to_acc(a.delta[r])) * t;
+        } else if (EPI == SPMV_NORM2) {
+            const double sd = acc_d(to_acc(s));
+            acc0 += sd * sd;
+        }
+    }
+    if (EPI == SPMV_LAM35 || EPI == SPMV_NORM2) {
+        double v[2] = {acc0, acc1}, tot[2];
+        if (grid_reduce<2>(v, a.rpart, a.ticket, tot) && threadIdx.x == 0) {
+            Ctl* c = a.ctl;
+            if (EPI == SPMV_LAM35) {
+                c->lam3 = tot[0];
+                c->lam5 = tot[1];
+            } else {
+                c->Add = tot[0];
+                c->tau = fabs(c->dd / (c->dDd + c->muDbeta * c->Add));
+            }
+        }
+    }
+}
+
+}  // namespace
+
+template <class T, class V>
+void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const int* ind, const V* valin, long nnz,
+                         cudaStream_t s) {
+    ok = false;
+    m = m_; p = p_; q = q_; r = r_;
+    const long n = (long)p * q * r;
+    if (nnz <= 0 || n <= 0 || m <= 0 || nnz >= (1L << 31) || m >= (1L << 31)) return;
+    ty = std::min(p, r > 1 ? 8 : 16); tx = std::min(q, r > 1 ? 8 : 16); tz = std::min(r, 8);
+    nty = (p + ty - 1) / ty; ntx = (q + tx - 1) / tx;
+    const int ntz = (r + tz - 1) / tz;
+    const long nt = (long)nty * ntx * ntz;
+    if (nt >= (1L << 24) || (long)ty * tx * tz > 65535) return;
+    ntiles = (int)nt;
+
+    // entries sorted by (tile, ray), ray order kept inside each segment
+    DBuf<int> tile_of(n), iota_v(n), rowof(nnz), idx(nnz), idx_s(nnz), flag(nnz), segid(nnz);
+    DBuf<unsigned long long> key(nnz), key_s(nnz);
+    k_tile_of_voxel<<<ewt(n), 256, 0, s>>>(n, p, q, ty, tx, tz, nty, ntx, tile_of.p, iota_v.p);
+    k_rows_of<<<ewt(m * 32), 256, 0, s>>>(m, ptr, rowof.p);
+    k_n_keys<<<ewt(nnz), 256, 0, s>>>(nnz, rowof.p, ind, tile_of.p, key.p, idx.p);
+    TV3_CUDA(cudaGetLastError());
+    int end_bit = 33;
+    while (end_bit < 64 && (1LL << (end_bit - 32)) < ntiles) ++end_bit;
+    {
+        size_t tb = 0;
+        TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, key.p, key_s.p, idx.p, idx_s.p, (int)nnz, 0, end_bit, s));
+        DBuf<char> tmp(std::max<size_t>(tb, 1));
+        TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, key.p, key_s.p, idx.p, idx_s.p, (int)nnz, 0, end_bit, s));
+        TV3_CUDA(cudaStreamSynchronize(s));
+    }
+    key.release();
+    idx.release();
+    k_n_newseg<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, flag.p);
+    {
+        size_t sb = 0;
+        TV3_CUDA(cub::DeviceScan::InclusiveSum(nullptr, sb, flag.p, segid.p, (int)nnz, s));
+        DBuf<char> tmp(std::max<size_t>(sb, 1));
+        TV3_CUDA(cub::DeviceScan::InclusiveSum(tmp.p, sb, flag.p, segid.p, (int)nnz, s));
+        TV3_CUDA(cudaStreamSynchronize(s));
+    }
+    int ns = 0;
+    TV3_CUDA(cudaMemcpy(&ns, segid.p + nnz - 1, sizeof(int), cudaMemcpyDeviceToHost));
+    nseg = ns;
+    DBuf<unsigned long long> seg_key(nseg), k_slice(nseg), k_slice_s(nseg), k_ray(nseg), k_ray_s(nseg);
+    DBuf<int> seg_start(nseg), iota_s(nseg), order(nseg), by_ray(nseg), dest(nseg), too_long(1), rcount(m + 1);
+    k_n_segs<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, segid.p, seg_key.p, seg_start.p);
+    TV3_CUDA(cudaMemsetAsync(too_long.p, 0, sizeof(int), s));
+    k_n_segkeys<<<ewt(nseg), 256, 0, s>>>(nseg, seg_key.p, seg_start.p, nnz, k_slice.p, k_ray.p, iota_s.p, too_long.p);
+    // slicing order: (tile, longest first), stable
+    int sbits = 17;
+    while (sbits < 64 && (1LL << (sbits - 16)) < ntiles) ++sbits;
+    {
+        size_t tb = 0;
+        TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, k_slice.p, k_slice_s.p, iota_s.p, order.p, (int)nseg, 0,
+                                                 sbits, s));
+        DBuf<char> tmp(std::max<size_t>(tb, 1));
+        TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, k_slice.p, k_slice_s.p, iota_s.p, order.p, (int)nseg, 0,
+                                                 sbits, s));
+        TV3_CUDA(cudaStreamSynchronize(s));
+    }
+    // ray-major order of the partials: (ray, tile)
+    int rbits = 33;
+    while (rbits < 64 && (1LL << (rbits - 32)) < m) ++rbits;
+    {
+        size_t tb = 0;
+        TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, k_ray.p, k_ray_s.p, iota_s.p, by_ray.p, (int)nseg, 0,
+                                                 rbits, s));
+        DBuf<char> tmp(std::max<size_t>(tb, 1));
+        TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, k_ray.p, k_ray_s.p, iota_s.p, by_ray.p, (int)nseg, 0,
+                                                 rbits, s));
+        TV3_CUDA(cudaStreamSynchronize(s));
+    }
+    int tl = 0;
+    TV3_CUDA(cudaMemcpy(&tl, too_long.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (tl) return;
+    TV3_CUDA(cudaMemsetAsync(rcount.p, 0, (m + 1) * sizeof(int), s));
+    k_n_dest<<<ewt(nseg), 256, 0, s>>>(nseg, by_ray.p, k_ray_s.p, dest.p, rcount.p);
+    rseg.alloc(m + 1);
+    {
+        size_t sb = 0;
+        TV3_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, sb, rcount.p, rseg.p, (int)(m + 1), s));
+        DBuf<char> tmp(std::max<size_t>(sb, 1));
+        TV3_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, sb, rcount.p, rseg.p, (int)(m + 1), s));
+        TV3_CUDA(cudaStreamSynchronize(s));
+    }
+    // slices (host): tiles' segment ranges and 32-segment slices
+    std::vector<unsigned long long> hk(nseg);
+    TV3_CUDA(cudaMemcpy(hk.data(), k_slice_s.p, nseg * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    std::vector<int> tseg(ntiles + 1, (int)nseg), tsl(ntiles + 1, 0);
+    for (long i = nseg - 1; i >= 0; --i) tseg[hk[i] >> 16] = (int)i;
+    for (int t = ntiles - 1; t >= 0; --t) tseg[t] = std::min(tseg[t], tseg[t + 1]);
+    std::vector<long long> soff(1, 0);
+    for (int t = 0; t < ntiles; ++t) {
+        tsl[t] = (int)(soff.size() - 1);
+        for (long i = tseg[t]; i < tseg[t + 1]; i += 32) {
+            const long len = 0xffff - (long)(hk[i] & 0xffff);
+            soff.push_back(soff.back() + 32 * len);
+        }
+    }
+    tsl[ntiles] = (int)(soff.size() - 1);
+    nslices = tsl[ntiles];
+    const long long padded = soff.back();
+    tile_slice.alloc(ntiles + 1);
+    slice_off.alloc(nslices + 1);
+    DBuf<int> tseg_d(ntiles + 1);
+    TV3_CUDA(cudaMemcpy(tile_slice.p, tsl.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    TV3_CUDA(cudaMemcpy(slice_off.p, soff.data(), (nslices + 1) * sizeof(long long), cudaMemcpyHostToDevice));
+    TV3_CUDA(cudaMemcpy(tseg_d.p, tseg.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    lidx.alloc(std::max<long long>(padded, 1));
+    val.alloc(std::max<long long>(padded, 1));
+    slot_dest.alloc((size_t)std::max(nslices, 1) * 32);
+    part.alloc(std::max<long>(nseg, 1));
+    TV3_CUDA(cudaMemsetAsync(lidx.p, 0, std::max<long long>(padded, 1) * sizeof(unsigned short), s));
+    TV3_CUDA(cudaMemsetAsync(val.p, 0, std::max<long long>(padded, 1) * sizeof(V), s));
+    TV3_CUDA(cudaMemsetAsync(slot_dest.p, 0xff, (size_t)std::max(nslices, 1) * 32 * sizeof(int), s));
+    k_n_fill<V><<<ewt(nseg), 256, 0, s>>>(nseg, order.p, k_slice_s.p, tseg_d.p, tile_slice.p, slice_off.p,
+                                          seg_start.p, nnz, idx_s.p, ind, valin, dest.p, p, q, ty, tx, tz, lidx.p,
+                                          val.p, slot_dest.p);
+    TV3_CUDA(cudaGetLastError());
+    const int smem = (int)std::max<size_t>((size_t)ty * tx * tz * sizeof(T), 16);
+    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiledN<T, V, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  std::max(smem, 48 * 1024)));
+    TV3_CUDA(cudaStreamSynchronize(s));
+    ok = true;
+}
+
+template <class T, class V>
+void TiledN<T, V>::apply(const TiledNArgs<T, V>& a, int epi, cudaStream_t s) const {
+    const size_t smem = std::max<size_t>((size_t)ty * tx * tz * sizeof(T), 16);
+    k_spmv_tiledN<T, V, 8><<<std::max(a.ntiles, 1), 512, smem, s>>>(a);
+    const int g = (int)std::max<long>(1, std::min<long>((a.m + 255) / 256, (long)num_sms() * 4));
+    switch (epi) {
+        case SPMV_SUB: k_tiledN_reduce<T, V, SPMV_SUB><<<g, 256, 0, s>>>(a); break;
+        case SPMV_LAM35: k_tiledN_reduce<T, V, SPMV_LAM35><<<g, 256, 0, s>>>(a); break;
+        case SPMV_NORM2: k_tiledN_reduce<T, V, SPMV_NORM2><<<g, 256, 0, s>>>(a); break;
+        default: k_tiledN_reduce<T, V, SPMV_PLAIN><<<g, 256, 0, s>>>(a); break;
+    }
+    TV3_CUDA(cudaGetLastError());
+}
+
+template struct TiledN<float, float>;
+template struct TiledN<double, double>;
+template struct TiledN<double, float>;
+template struct TiledN<df64, float>;
+template struct TiledN<float, __nv_bfloat16>;
+template struct TiledN<float, __half>;
+
 template struct TiledT<float, float>;
 template struct TiledT<double, double>;
 template struct TiledT<double, float>;

@@ -54,4 +54,49 @@ struct TiledT {
     void apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) const;
 };
 
+// Tile-staged A*x: the rays' nonzeros cut into segments (the part of a ray
+// inside one voxel tile).  A CTA stages its tile's x values in shared memory
+// and sums every segment (sliced ELL, one lane per segment); the partial sums
+// land ray by ray in `part`, and a second kernel adds each ray's partials in
+// tile order and applies the epilogues.
+template <class T, class V>
+struct TiledNArgs {
+    int ntiles;
+    int p, q, r, ty, tx, tz, nty, ntx;  // volume and tile shape (for staging x)
+    const int* tile_slice;       // ntiles + 1
+    const long long* slice_off;  // nslices + 1
+    const int* slot_dest;        // 32 per slice: index of the segment's partial in `part` (-1: padding)
+    const unsigned short* lidx;  // local voxel of each nonzero in its tile (0 in padding)
+    const V* val;                // value (0 in padding)
+    T* part;                     // one partial per segment, ray-major
+    const int* rseg;             // m + 1: ray r's partials are part[rseg[r] .. rseg[r+1])
+    long m;
+    const float* rscale;         // per-ray scale of the row sum (16-bit storage), or null
+    const T* x[2];
+    T* y[2];
+    int by_parity;
+    const T* sub;
+    const T* b;
+    const T* delta;
+    Ctl* ctl;
+    double* rpart;               // grid-reduction scratch of the epilogues
+    unsigned* ticket;
+};
+
+template <class T, class V>
+struct TiledN {
+    bool ok = false;
+    int ntiles = 0, nslices = 0;
+    int p = 0, q = 0, r = 0, ty = 0, tx = 0, tz = 0, nty = 0, ntx = 0;
+    long m = 0, nseg = 0;
+    DBuf<int> tile_slice, slot_dest, rseg;
+    DBuf<long long> slice_off;
+    DBuf<unsigned short> lidx;
+    DBuf<V> val;
+    mutable DBuf<T> part;
+    // build from the CSR of A (m ray rows over the p x q x r volume)
+    void build(long m, int p, int q, int r, const int* ptr, const int* ind, const V* val, long nnz, cudaStream_t s);
+    void apply(const TiledNArgs<T, V>& a, int epi, cudaStream_t s) const;
+};
+
 }  // namespace tv3
