@@ -78,9 +78,10 @@ typedef struct tval3_options {
     double rate_gam;  /* shrink rate of gam after a failed backtracking */
     int isreal;       /* kept for interface compatibility (unused, as in the reference) */
     int nonneg;       /* project onto U >= 0 */
-    unsigned numInitIterations; /* skip heuristic: must be 0 / skipMulRatio 0 (exact products) */
-    double skipMulRatio;
-    double maxRelativeChange;
+    unsigned numInitIterations; /* skip-A^T heuristic (3d/tval3_gpu_3d.cpp:398-468): A^T Au is always */
+    double skipMulRatio;        /* formed during the first numInitIterations get_g calls, then skipped */
+    double maxRelativeChange;   /* by this ratio unless ||Au - last_Au|| / ||Au|| > maxRelativeChange;
+                                   skipMulRatio = 0 (the default) forms it every time */
     int tv_type;      /* tval3_tv; the reference is anisotropic */
     int precision;    /* internal arithmetic of the host entry points: -1 = the entry point's
                          type; TVAL3_PREC_FP32_DF64 with an _f64 entry and FP32 matrix values
@@ -100,6 +101,7 @@ typedef struct tval3_info {
     int restarts;
     double final_f;
     int launches;     /* kernels the solve ran on the device */
+    int products_T;   /* A^T products formed by get_g under the skip heuristic (-1: heuristic off) */
 } tval3_info;
 
 /* Sparse matrix in host memory (sparse_mat_host, 2d/container_host.h:78-127).

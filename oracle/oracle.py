@@ -29,13 +29,15 @@ class OracleOpts(C.Structure):
     _fields_ = [("mu", C.c_double), ("mu0", C.c_double), ("beta", C.c_double), ("beta0", C.c_double),
                 ("rate_cnt", C.c_double), ("tol", C.c_double), ("tol_inn", C.c_double), ("maxcnt", C.c_int),
                 ("maxit", C.c_int), ("c", C.c_double), ("gamma", C.c_double), ("gam", C.c_double),
-                ("rate_gam", C.c_double), ("nonneg", C.c_int), ("tv_iso", C.c_int)]
+                ("rate_gam", C.c_double), ("nonneg", C.c_int), ("tv_iso", C.c_int),
+                ("num_init_iterations", C.c_uint), ("skip_mul_ratio", C.c_double),
+                ("max_relative_change", C.c_double)]
 
 
 class OracleInfo(C.Structure):
     _fields_ = [("total_iters", C.c_int), ("outer_iters", C.c_int), ("rel_chg", C.c_double),
                 ("rel_error", C.c_double), ("backtracks", C.c_int), ("restarts", C.c_int),
-                ("final_f", C.c_double), ("scl", C.c_double)]
+                ("final_f", C.c_double), ("scl", C.c_double), ("products_T", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -175,9 +177,9 @@ def make_opts(**kw) -> OracleOpts:
     o = OracleOpts(mu=256.0, mu0=256.0, beta=32.0, beta0=32.0, rate_cnt=2.0, tol=1e-6, tol_inn=1e-3, maxcnt=10,
                    maxit=1025, c=1e-5, gamma=0.6, gam=0.9995, rate_gam=0.9, nonneg=1, tv_iso=0)
     for k, v in kw.items():
-        if k == "tv_type":
-            k = "tv_iso"
-        if k in ("isreal", "numInitIterations", "skipMulRatio", "maxRelativeChange"):
+        k = {"tv_type": "tv_iso", "numInitIterations": "num_init_iterations", "skipMulRatio": "skip_mul_ratio",
+             "maxRelativeChange": "max_relative_change"}.get(k, k)
+        if k in ("isreal", "precision"):
             continue
         setattr(o, k, v)
     return o

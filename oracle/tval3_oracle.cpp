@@ -211,6 +211,10 @@ struct oracle_opts {
     double c, gamma, gam, rate_gam;
     int nonneg;
     int tv_iso;  // 0: anisotropic (reference), 1: isotropic
+    // skip-A^T heuristic (3d/tval3_gpu_3d.cpp:194-197, :398-468); ratio 0 = always multiply
+    unsigned num_init_iterations;
+    double skip_mul_ratio;
+    double max_relative_change;
 };
 
 struct oracle_info {
@@ -219,6 +223,7 @@ struct oracle_info {
     int backtracks, restarts;
     double final_f;
     double scl;
+    int products_T;  // A^T products formed by get_g
 };
 
 }  // extern "C"
@@ -236,6 +241,11 @@ struct Solver {
     std::vector<T> delta, b, U, Up, dU, uup, Atb, Au, Aup, dAu, d, gv, gp, dg, g2, g2p, dg2, DtsAtd;
     std::vector<T> DU[3], DUp[3], dDU[3], W[3], sig[3], V[3];
     int backtracks = 0, restarts = 0;
+    // skip-A^T state (3d/tval3_gpu_3d.cpp:155-157)
+    std::vector<T> last_Au;
+    unsigned cur_init = 0;
+    double cur_skip = 0.0;
+    int products_T = 0;  // A^T products formed by get_g
 
     Solver(Dims g_, const Op<T>& A_, const oracle_opts& o_) : g(g_), n(g_.n()), m(A_.m), A(A_), o(o_) {
         auto N = [&](std::vector<T>& v) { v.assign(n, T(0)); };
@@ -268,13 +278,41 @@ struct Solver {
     }
     void fval() { f = lam1 + beta / 2 * lam2 + mu / 2 * lam3 - lam4 - lam5; }
 
-    // get_g_gpu, 3d/tval3_gpu_3d.cpp:366-572 (skipMulRatio == 0: always multiply)
-    void get_g() {
+    // get_g_gpu, 3d/tval3_gpu_3d.cpp:366-572.  With skipMulRatio != 0 the
+    // A^T product is skipped by the rule of :398-468 (forced at start-up and
+    // at a restart, always during the first numInitIterations calls, then
+    // whenever the skip budget is spent or ||Au - last_Au|| / ||Au|| exceeds
+    // maxRelativeChange); a skipped call keeps the current g.  (The reference
+    // also subtracts Atb from the kept g once more, :562-565, a defect not
+    // reproduced.)
+    void get_g(bool force) {
         A.N(U.data(), Au.data());
-        A.Tr(Au.data(), gv.data());
+        bool mult = true;
+        if (o.skip_mul_ratio != 0.0) {
+            if (last_Au.empty()) last_Au.assign(m, T(0));
+            const double dn = dsum(m, [&](long i) { double v = (double)Au[i] - last_Au[i]; return v * v; });
+            const double an = dsum(m, [&](long i) { return (double)Au[i] * Au[i]; });
+            const double rel = std::sqrt(dn) / std::sqrt(an);
+            if (force) {
+                cur_skip = 0.0;
+            } else if (cur_init < o.num_init_iterations) {
+                ++cur_init;
+                cur_skip = 0.0;
+            } else if (cur_skip < 1.0) {
+                cur_skip += o.skip_mul_ratio;
+            } else if (!(rel > o.max_relative_change)) {
+                cur_skip -= 1.0;
+                mult = false;
+            }
+            if (mult) last_Au = Au;
+        }
+        if (mult) {
+            A.Tr(Au.data(), gv.data());
+            pfor(n, [&](long i) { gv[i] = gv[i] - Atb[i]; });
+            ++products_T;
+        }
         lam35();
         lam24_g2();
-        pfor(n, [&](long i) { gv[i] = gv[i] - Atb[i]; });
         fval();
     }
 
@@ -298,7 +336,7 @@ struct Solver {
     }
 
     // descend_gpu, :671-701
-    void descend(double tau) {
+    void descend(double tau, bool force) {
         const T mt = (T)(-tau);
         pfor(n, [&](long i) {
             T v = U[i] + mt * d[i];
@@ -306,7 +344,7 @@ struct Solver {
             U[i] = v;
         });
         D(U, DU);
-        get_g();
+        get_g(force);
     }
 
     // update_g_gpu, :706-818
@@ -335,7 +373,7 @@ struct Solver {
         double tau = get_tau(fst);
         Up = U; gp = gv; g2p = g2; Aup = Au;
         for (int a = 0; a < 3; ++a) DUp[a] = DU[a];
-        descend(tau);
+        descend(tau, false);
         double alpha = 1;
         pfor(n, [&](long i) { dU[i] = U[i] - Up[i]; });
         double c_armij = dot(d, d) * tau * o.c * beta;
@@ -352,7 +390,7 @@ struct Solver {
                     gam *= o.rate_gam;
                     tau = get_tau(true);
                     U = Up;
-                    descend(tau);
+                    descend(tau, true);
                     ++restarts;
                     break;
                 }
@@ -467,7 +505,7 @@ int solve(Dims g, const Op<T>& A, const T* b_in, const oracle_opts& o, T* U_out,
     std::vector<T> rcdU = s.U;
     s.D(s.U, s.DU);
     s.shrinkage();
-    s.get_g();
+    s.get_g(true);
     s.get_gradient();
     double Q = 1, Qp, C = s.f;
     int count_outer = 0, count_total = 0;
@@ -520,6 +558,7 @@ int solve(Dims g, const Op<T>& A, const T* b_in, const oracle_opts& o, T* U_out,
         info->restarts = s.restarts;
         info->final_f = s.f;
         info->scl = scl;
+        info->products_T = s.products_T;
         info->rel_error = 0;
         if (Ut) {
             double num = dsum(n, [&](long i) { double v = (double)Ut[i] - U_out[i]; return v * v; });

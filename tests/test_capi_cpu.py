@@ -45,7 +45,7 @@ def _tiny():
     ("b_len", 2, "b.len must be equal to A.dim_y"),
     ("ut_len", 2, "U and Ut must have the same size"),
     ("nan_b", 6, "non-finite"),
-    ("skip", 7, "skipMulRatio"),
+    ("skip", 1, "skipMulRatio"),
     ("bad_ptr", 2, "pointer"),
     ("bad_ind", 2, "index out of range"),
 ])
@@ -62,7 +62,7 @@ def test_argument_errors(lib, case, status, text):
     elif case == "nan_b":
         b = np.array([1.0, np.nan])
     elif case == "skip":
-        opts = dict(skipMulRatio=0.5)
+        opts = dict(skipMulRatio=-0.5)
     elif case == "bad_ptr":
         A = SparseMatrix(2, 2, np.array([0, 2, 1], np.int32), np.array([0, 1], np.int32), np.ones(2, np.float32))
     elif case == "bad_ind":

@@ -186,3 +186,30 @@ def test_dense_entry_points(cuda, oracle):
     Uo, io = oracle.tval3_dense((16, 16, 1), A, b.astype(np.float64), o, prec=0)
     assert idn["total_iters"] == io["total_iters"]
     assert np.linalg.norm(Ud - Uo) <= 1e-3 * np.linalg.norm(Uo)
+
+
+@pytest.mark.parametrize("max_rel", [1e-3, 0.0])
+def test_skip_heuristic_matches_oracle(cuda, oracle, max_rel):
+    """The skip-A^T heuristic (skipMulRatio, numInitIterations,
+    maxRelativeChange; 3d/tval3_gpu_3d.cpp:398-468) decided on the device:
+    FP64 solves take the oracle's decisions (same number of A^T products,
+    iterations, backtracks) and land within 1e-7; host-driven and graph forms
+    agree bit for bit."""
+    import torch
+    from tval3_gb300 import PREC_FP64, Operator, Solver, SparseMatrix
+    geo, x, ptr, ind, val, b = _problem(oracle)
+    o = dict(OPTS, tv_type=0, maxit=80, skipMulRatio=0.5, numInitIterations=4, maxRelativeChange=max_rel)
+    Uo, io = oracle.tval3_csr((16, 16, 1), ptr, ind, val, b.astype(np.float64), o, prec=0)
+    op = Operator.from_sparse(SparseMatrix(ptr.size - 1, x.size, ptr, ind, val.astype(np.float64)),
+                              precision=PREC_FP64)
+    outs = []
+    for mode in (0, 1):
+        s = Solver(op, (16, 16, 1), o, mode=mode)
+        U = torch.empty(x.size, dtype=torch.float64, device=cuda)
+        ig = s.solve(torch.tensor(b, dtype=torch.float64, device=cuda), U)
+        assert (ig["total_iters"], ig["backtracks"], ig["restarts"], ig["products_T"]) == \
+            (io["total_iters"], io["backtracks"], io["restarts"], io["products_T"])
+        assert np.linalg.norm(U.cpu().numpy() - Uo.reshape(-1)) <= 1e-7 * np.linalg.norm(Uo)
+        outs.append(U.cpu().numpy())
+        s.close()
+    assert np.array_equal(outs[0], outs[1])

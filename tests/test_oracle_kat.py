@@ -290,3 +290,27 @@ def test_oracle_layers_of_identical_columns_equal_single_solve(oracle):
         (i1["total_iters"], i1["outer_iters"], i1["backtracks"])
     for l in range(3):
         assert np.linalg.norm(UL[l].reshape(-1) - U1.reshape(-1)) <= 1e-9 * np.linalg.norm(U1)
+
+
+def test_oracle_skip_heuristic(oracle):
+    """The skip-A^T rule of get_g_gpu (3d/tval3_gpu_3d.cpp:398-468):
+    ratio 0 forms A^T Au in every get_g (1 at start-up + one per iteration +
+    one per restart); maxRelativeChange 0 forces every product, so the solve
+    is identical to the exact one; a small maxRelativeChange lets the budget
+    skip a few products.  (Skipped products leave the Barzilai-Borwein step
+    without its A^T A curvature, so larger thresholds make the loop unstable
+    on this problem, in the reference's rule as here.)"""
+    from tval3_gb300 import workloads as W
+    geo = W.ring_geometry(16, 24)
+    x = W.ellipse_phantom(16, 3, seed=1, axes=(2.0, 6.4))
+    ptr, ind, val = oracle.siddon_csr(geo)
+    b = W.add_noise(oracle.spmv(ptr, ind, val, x), 0.01, 1).astype(np.float64)
+    o = dict(mu=256., mu0=64., beta=32., beta0=8., tol=1e-4, maxit=80, tv_iso=0)
+    U0, i0 = oracle.tval3_csr((16, 16, 1), ptr, ind, val, b, o)
+    assert i0["products_T"] == 1 + i0["total_iters"] + i0["restarts"]
+    U1, i1 = oracle.tval3_csr((16, 16, 1), ptr, ind, val, b, dict(o, skipMulRatio=0.5, maxRelativeChange=0.0))
+    assert np.array_equal(U1, U0) and i1["total_iters"] == i0["total_iters"]
+    U2, i2 = oracle.tval3_csr((16, 16, 1), ptr, ind, val, b,
+                              dict(o, skipMulRatio=0.5, numInitIterations=4, maxRelativeChange=1e-3))
+    assert i2["products_T"] < 1 + i2["total_iters"] + i2["restarts"]
+    assert np.linalg.norm(U2 - U0) < 0.3 * np.linalg.norm(U0)

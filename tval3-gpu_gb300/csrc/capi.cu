@@ -165,8 +165,8 @@ LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision) {
 
 void check_opts(const tval3_options* o) {
     if (!o) arg_error(TVAL3_ERR_ARG, "Argument error: opts is NULL!");
-    if (o->skipMulRatio != 0.0 || o->numInitIterations != 0)
-        arg_error(TVAL3_ERR_UNSUPPORTED, "skipMulRatio/numInitIterations: only exact products (0) are provided");
+    if (!(o->skipMulRatio >= 0.0) || !std::isfinite(o->skipMulRatio) || std::isnan(o->maxRelativeChange))
+        arg_error(TVAL3_ERR_ARG, "Argument error: skipMulRatio must be finite and >= 0!");
     if (!(o->beta > 0) || !(o->mu > 0) || !(o->beta0 > 0) || !(o->mu0 > 0))
         arg_error(TVAL3_ERR_ARG, "Argument error: mu, mu0, beta, beta0 must be positive!");
 }

@@ -79,6 +79,10 @@ struct SolverBufs {
     unsigned long long h_inner;  // WHILE: continue the inner loop
     unsigned long long h_arm;    // IF: Armijo test failed after the descent
     unsigned long long h_mlp;    // IF: outer loop continues (multiplier update)
+    // skip-A^T heuristic (skip_ratio != 0 only): A*U of the last A^T product,
+    // and the IF handles of "multiply" and "keep g"
+    T* last_Au;
+    unsigned long long h_mult, h_keep;
 };
 
 // Flags that the tiny condition kernel copies from the control block into a
@@ -101,6 +105,10 @@ template <class T> void launch_bt_apply(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_mlp(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_outer_grad(SolverBufs<T>& B, cudaStream_t s);
+// skip-A^T decision after A*U (force: start-up and restart calls) and the
+// copies of its two branches (0: last_Au = Au, 1: g = the previous g)
+template <class T> void launch_skip_decide(SolverBufs<T>& B, int force, cudaStream_t s);
+template <class T> void launch_skip_copy(SolverBufs<T>& B, int which, cudaStream_t s);
 template <class T> void launch_finalize(SolverBufs<T>& B, void* U_out, const void* Ut, cudaStream_t s);
 
 // Standalone operators (tval3_D / tval3_Dt entry points).

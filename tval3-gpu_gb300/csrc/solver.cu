@@ -19,6 +19,43 @@
 
 namespace tv3 {
 
+// A body graph being filled by stream capture.  Between captured sequences,
+// conditional nodes are appended with the current tail as dependencies.
+struct Body {
+    cudaGraph_t g;
+    std::vector<cudaGraphNode_t> deps;
+    cudaStream_t s;
+    bool capturing = false;
+    void begin() {
+        TV3_CUDA(cudaStreamBeginCaptureToGraph(s, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                               cudaStreamCaptureModeThreadLocal));
+        capturing = true;
+    }
+    void end() {
+        cudaStreamCaptureStatus st;
+        const cudaGraphNode_t* d = nullptr;
+        size_t nd = 0;
+        TV3_CUDA(cudaStreamGetCaptureInfo(s, &st, nullptr, nullptr, &d, nullptr, &nd));
+        std::vector<cudaGraphNode_t> tail(d, d + nd);
+        cudaGraph_t out = g;
+        TV3_CUDA(cudaStreamEndCapture(s, &out));
+        deps = tail;
+        capturing = false;
+    }
+    // append a conditional node; returns its body graphs
+    std::vector<cudaGraph_t> cond(cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, unsigned size) {
+        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+        np.conditional.handle = h;
+        np.conditional.type = type;
+        np.conditional.size = size;
+        cudaGraphNode_t node;
+        TV3_CUDA(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &np));
+        deps.assign(1, node);
+        return std::vector<cudaGraph_t>(np.conditional.phGraph_out, np.conditional.phGraph_out + size);
+    }
+};
+
+
 template <class T>
 Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_, int L_)
     : A(A_), p(p_), q(q_), r(r_), L(std::max(L_, 1)), n((long)p_ * q_ * r_ * std::max(L_, 1)),
@@ -50,6 +87,10 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
     const long mm = std::max<long>(m, 1);
     B.Au[0] = w; B.Au[1] = w + mm; B.b = w + 2 * mm; B.delta = w + 3 * mm;
     B.ctl = ctl.p; B.part = part.p; B.ticket = ticket.p;
+    if (o.skipMulRatio != 0.0) {
+        last_Au.alloc(std::max<long>(m, 1));
+        B.last_Au = last_Au.p;
+    }
     // vector/reduction grid: about 1024 elements per block for small problems
     // (so that many small solves can share the GPU), at most four blocks per
     // SM (partials fit in `part`)
@@ -113,6 +154,9 @@ void Solver<T>::init_ctl(cudaStream_t s) {
     c.Q = 1.0;
     c.fst = 1;
     c.scl = 1.0;
+    c.skip_ratio = o.skipMulRatio;
+    c.max_rel_change = o.maxRelativeChange;
+    c.num_init = o.numInitIterations;
     c.launches = 1;  // this kernel
     k_init_ctl<<<1, 1, 0, s>>>(ctl.p, c);
     TV3_CUDA(cudaGetLastError());
@@ -125,10 +169,50 @@ void Solver<T>::read_ctl(cudaStream_t s) {
 }
 
 // get_g_gpu (:366-572): Au = A U, g = A^T Au - Atb, g2 = D^T(DU - W), f.
+// With the skip-A^T heuristic the A^T product and its alternative (keep the
+// previous g) are two IF bodies of the whole-solve graph (body != null), or
+// a host branch on the decision in the host-driven form.
 template <class T>
-void Solver<T>::get_g(int epi, cudaStream_t s) {
+void Solver<T>::get_g(int epi, cudaStream_t s, Body* body) {
     A->apply(0, io_AU(), SPMV_LAM35, s);
-    A->apply(1, io_AtAu(), SPMV_SUB, s);
+    if (o.skipMulRatio != 0.0) {
+        if (body) {
+            // a conditional handle drives one conditional node: fresh pair per call site
+            cudaGraphConditionalHandle hm, hk;
+            TV3_CUDA(cudaGraphConditionalHandleCreate(&hm, g_top, 1, cudaGraphCondAssignDefault));
+            TV3_CUDA(cudaGraphConditionalHandleCreate(&hk, g_top, 0, cudaGraphCondAssignDefault));
+            B.h_mult = hm;
+            B.h_keep = hk;
+        }
+        launch_skip_decide<T>(B, epi != EPI_G2_DESCEND, s);
+        if (body) {
+            body->end();
+            {
+                Body mb{body->cond(B.h_mult, cudaGraphCondTypeIf, 1)[0], {}, s};
+                mb.begin();
+                launch_skip_copy<T>(B, 0, s);
+                A->apply(1, io_AtAu(), SPMV_SUB, s);
+                mb.end();
+            }
+            {
+                Body kb{body->cond(B.h_keep, cudaGraphCondTypeIf, 1)[0], {}, s};
+                kb.begin();
+                launch_skip_copy<T>(B, 1, s);
+                kb.end();
+            }
+            body->begin();
+        } else {
+            read_ctl(s);
+            if (hctl->do_mult) {
+                launch_skip_copy<T>(B, 0, s);
+                A->apply(1, io_AtAu(), SPMV_SUB, s);
+            } else {
+                launch_skip_copy<T>(B, 1, s);
+            }
+        }
+    } else {
+        A->apply(1, io_AtAu(), SPMV_SUB, s);
+    }
     launch_g2<T>(B, epi, s);
 }
 
@@ -141,8 +225,9 @@ void Solver<T>::tau_first(cudaStream_t s) {
 
 // start-up (:1115-1149)
 template <class T>
-void Solver<T>::setup(const void* d_b, cudaStream_t s) {
+void Solver<T>::setup(const void* d_b, cudaStream_t s, Body* body) {
     init_ctl(s);
+    if (B.last_Au) TV3_CUDA(cudaMemsetAsync(B.last_Au, 0, std::max<long>(m, 1) * sizeof(T), s));
     TV3_CUDA(cudaMemsetAsync(B.sig, 0, 3 * n * sizeof(T), s));
     TV3_CUDA(cudaMemsetAsync(B.DtsAtd, 0, n * sizeof(T), s));
     if (m > 0) TV3_CUDA(cudaMemsetAsync(B.delta, 0, m * sizeof(T), s));
@@ -155,7 +240,7 @@ void Solver<T>::setup(const void* d_b, cudaStream_t s) {
     TV3_CUDA(cudaMemcpyAsync(B.rcdU, B.Atb, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
     launch_D_only<T>(B, s);
     launch_shrink<T>(B, EPI_G2_INIT, s);
-    get_g(EPI_G2_INIT, s);
+    get_g(EPI_G2_INIT, s, body);
     launch_gradient<T>(B, 0, s);
     TV3_CUDA(cudaGetLastError());
 }
@@ -205,45 +290,6 @@ void Solver<T>::run_host(cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // whole-solve graph
 // ---------------------------------------------------------------------------
-namespace {
-
-// A body graph being filled by stream capture.  Between captured sequences,
-// conditional nodes are appended with the current tail as dependencies.
-struct Body {
-    cudaGraph_t g;
-    std::vector<cudaGraphNode_t> deps;
-    cudaStream_t s;
-    bool capturing = false;
-    void begin() {
-        TV3_CUDA(cudaStreamBeginCaptureToGraph(s, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
-                                               cudaStreamCaptureModeThreadLocal));
-        capturing = true;
-    }
-    void end() {
-        cudaStreamCaptureStatus st;
-        const cudaGraphNode_t* d = nullptr;
-        size_t nd = 0;
-        TV3_CUDA(cudaStreamGetCaptureInfo(s, &st, nullptr, nullptr, &d, nullptr, &nd));
-        std::vector<cudaGraphNode_t> tail(d, d + nd);
-        cudaGraph_t out = g;
-        TV3_CUDA(cudaStreamEndCapture(s, &out));
-        deps = tail;
-        capturing = false;
-    }
-    // append a conditional node; returns its body graphs
-    std::vector<cudaGraph_t> cond(cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, unsigned size) {
-        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
-        np.conditional.handle = h;
-        np.conditional.type = type;
-        np.conditional.size = size;
-        cudaGraphNode_t node;
-        TV3_CUDA(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &np));
-        deps.assign(1, node);
-        return std::vector<cudaGraph_t>(np.conditional.phGraph_out, np.conditional.phGraph_out + size);
-    }
-};
-
-}  // namespace
 
 // Adds the whole solve to `top` as an independent branch (its first nodes are
 // roots of `top`), capturing through stream cs.  Several solvers can add
@@ -258,12 +304,13 @@ void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const 
     TV3_CUDA(cudaGraphConditionalHandleCreate(&h_arm, top, 0, cudaGraphCondAssignDefault));
     TV3_CUDA(cudaGraphConditionalHandleCreate(&h_restart, top, 0, cudaGraphCondAssignDefault));
     TV3_CUDA(cudaGraphConditionalHandleCreate(&h_mlp, top, 0, cudaGraphCondAssignDefault));
+    g_top = top;
     B.use_graph = 1;
     B.h_inner = h_inner; B.h_arm = h_arm; B.h_mlp = h_mlp;
     try {
         Body tb{top, {}, cs};
         tb.begin();
-        setup(d_b, cs);
+        setup(d_b, cs, &tb);
         tb.end();
         // outer while
         Body ob{tb.cond(h_outer, cudaGraphCondTypeWhile, 1)[0], {}, cs};
@@ -281,7 +328,7 @@ void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const 
             }
             ib.begin();
             launch_descend<T>(B, 0, cs);
-            get_g(EPI_G2_DESCEND, cs);  // sets h_arm
+            get_g(EPI_G2_DESCEND, cs, &ib);  // sets h_arm
             ib.end();
             {
                 Body ab{ib.cond(h_arm, cudaGraphCondTypeIf, 1)[0], {}, cs};
@@ -295,7 +342,7 @@ void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const 
                     rb.begin();
                     tau_first(cs);
                     launch_descend<T>(B, 1, cs);
-                    get_g(EPI_G2_RESTART, cs);
+                    get_g(EPI_G2_RESTART, cs, &rb);
                     rb.end();
                 }
             }
@@ -395,6 +442,7 @@ void Solver<T>::fill_info(tval3_info* info, double secs) const {
         info->restarts = hctl->restarts;
         info->final_f = hctl->f;
         info->launches = (int)hctl->launches;
+        info->products_T = (o.skipMulRatio != 0.0) ? hctl->products_T : -1;
     }
 }
 

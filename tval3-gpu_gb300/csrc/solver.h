@@ -8,6 +8,8 @@
 
 namespace tv3 {
 
+struct Body;  // a graph body being filled by stream capture (solver.cu)
+
 template <class T>
 struct Solver {
     const LinOp<T>* A;
@@ -20,6 +22,7 @@ struct Solver {
     DBuf<double> part;
     DBuf<unsigned> ticket;
     DBuf<double> trace;
+    DBuf<T> last_Au;      // skip-A^T heuristic only
     Ctl* hctl = nullptr;  // pinned mirror of the control block
     SolverBufs<T> B{};
     int mode = 0;         // 0: host-driven loop, 1: CUDA graph with conditional nodes
@@ -30,6 +33,7 @@ struct Solver {
     void* g_U = nullptr;
     const void* g_Ut = nullptr;
     cudaStream_t g_stream = nullptr;
+    cudaGraph_t g_top = nullptr;  // the graph being built by add_to_graph
 
     Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_, int L_ = 1);
     ~Solver();
@@ -47,8 +51,8 @@ struct Solver {
    private:
     void init_ctl(cudaStream_t s);
     void read_ctl(cudaStream_t s);
-    void setup(const void* d_b, cudaStream_t s);
-    void get_g(int epi, cudaStream_t s);
+    void setup(const void* d_b, cudaStream_t s, Body* body = nullptr);
+    void get_g(int epi, cudaStream_t s, Body* body = nullptr);
     void tau_first(cudaStream_t s);
     void run_host(cudaStream_t s);
     void build_graph(const void* d_b, void* d_U, const void* d_Ut, cudaStream_t s);

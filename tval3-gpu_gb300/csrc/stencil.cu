@@ -242,30 +242,38 @@ __device__ __forceinline__ void armijo(Ctl* c) {
 // ---------------------------------------------------------------------------
 // g2 = D^T (DU - W) with lam2 = ||DU - W||^2 and lam4 = <sigma, DU - W>.
 // ---------------------------------------------------------------------------
-template <class T>
+// After a descent (and the restart's descent) only lam2 and lam4 are needed:
+// the g2 of that point is replaced by update_W's before anything reads it,
+// except on the backtracking path, which forms its own (k_bt_g2).  So those
+// calls (WITH_G2 = false) skip D^T and the g2 store.
+template <class T, bool WITH_G2>
 __global__ void k_g2(SolverBufs<T> B, Geo g, int mode) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
-    using A = acc_t<T>;
     const int cur = ctl->parity;
     const long n = B.n;
     const T* __restrict__ DU = B.DU[cur];
     const T* __restrict__ W = B.W;
     const T* __restrict__ S = B.sig;
     T* __restrict__ g2 = B.g2[cur];
-    A l2(0.f), l4(0.f);
+    ProdAcc<T> l2, l4;
     GRID_STRIDE(i, n) {
-        Nb nb = neighbours(g, i);
         T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
-        T v0m = DU[nb.ym] - W[nb.ym];
-        T v1m = DU[n + nb.xm] - W[n + nb.xm];
-        T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
-        g2[i] = v0m - v0 + v1m - v1 + v2m - v2;
-        A a0 = to_acc(v0), a1 = to_acc(v1), a2 = to_acc(v2);
-        l2 += a0 * a0 + a1 * a1 + a2 * a2;
-        l4 += a0 * to_acc(S[i]) + a1 * to_acc(S[n + i]) + a2 * to_acc(S[2 * n + i]);
+        if (WITH_G2) {
+            Nb nb = neighbours(g, i);
+            T v0m = DU[nb.ym] - W[nb.ym];
+            T v1m = DU[n + nb.xm] - W[n + nb.xm];
+            T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
+            g2[i] = v0m - v0 + v1m - v1 + v2m - v2;
+        }
+        l2.add(v0, v0);
+        l2.add(v1, v1);
+        l2.add(v2, v2);
+        l4.add(v0, S[i]);
+        l4.add(v1, S[n + i]);
+        l4.add(v2, S[2 * n + i]);
     }
-    double v[2] = {acc_d(l2), acc_d(l4)}, tot[2];
+    double v[2] = {l2.value(), l4.value()}, tot[2];
     if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->lam2 = tot[0];
         ctl->lam4 = tot[1];
@@ -362,29 +370,29 @@ __global__ void k_gradient(SolverBufs<T> B, int iter) {
     const Ext<T>* __restrict__ xs = static_cast<const Ext<T>*>(B.xstar);
     const double iscl = 1.0 / ctl->scl;
     T* __restrict__ d = B.d;
-    A s0(0.f), s1(0.f), s2(0.f), s4(0.f);
+    ProdAcc<A> s0, s1, s2, s4;
     double s3 = 0.0;
     GRID_STRIDE(i, B.n) {
         const T gi = g[i], g2i = g2[i];
         T di = mdb * gi + g2i + dts[i];
         d[i] = di;
-        A ad = to_acc(di);
-        s2 += ad * ad;
+        const A ad = to_acc(di);
+        s2.add(ad, ad);
         if (iter) {
             A u = to_acc(U[i]), up = to_acc(Up[i]);
             A du = u - up;
-            s0 += up * up;
-            s1 += du * du;
+            s0.add(up, up);
+            s1.add(du, du);
             A dg = to_acc(gi) - to_acc(gp[i]);
             A dg2 = to_acc(g2i) - to_acc(g2p[i]);
-            s4 += du * (dg2 + mdbA * dg);
+            s4.add(du, dg2 + mdbA * dg);
             if (xs) {
                 double e = acc_d(u) * iscl - (double)xs[i];
                 s3 += e * e;
             }
         }
     }
-    double v[5] = {acc_d(s0), acc_d(s1), acc_d(s2), s3, acc_d(s4)}, tot[5];
+    double v[5] = {s0.value(), s1.value(), s2.value(), s3, s4.value()}, tot[5];
     if (grid_reduce<5>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->dd = tot[2];
         if (!iter) {
@@ -485,9 +493,9 @@ __global__ void k_bt_apply(SolverBufs<T> B) {
     const int cur = ctl->parity, prv = 1 - cur;
     const long n = B.n, m = B.m;
     const T al = scal<T>(ctl->alpha);
-    T *__restrict__ U = B.U[cur], *__restrict__ g = B.g[cur], *__restrict__ g2 = B.g2[cur];
+    T *__restrict__ U = B.U[cur], *__restrict__ g = B.g[cur];
     T *__restrict__ DU = B.DU[cur], *__restrict__ Au = B.Au[cur];
-    const T *__restrict__ Up = B.U[prv], *__restrict__ gp = B.g[prv], *__restrict__ g2p = B.g2[prv];
+    const T *__restrict__ Up = B.U[prv], *__restrict__ gp = B.g[prv];
     const T *__restrict__ DUp = B.DU[prv], *__restrict__ Aup = B.Au[prv];
     const long N = n > m ? n : m;
     GRID_STRIDE(i, N) {
@@ -496,8 +504,6 @@ __global__ void k_bt_apply(SolverBufs<T> B) {
             U[i] = p + al * (U[i] - p);
             p = gp[i];
             g[i] = p + al * (g[i] - p);
-            p = g2p[i];
-            g2[i] = p + al * (g2[i] - p);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 p = DUp[c * n + i];
@@ -508,6 +514,29 @@ __global__ void k_bt_apply(SolverBufs<T> B) {
             T p = Aup[i];
             Au[i] = p + al * (Au[i] - p);
         }
+    }
+}
+
+// g2 at the accepted point of the backtracking: D^T (DU(a) - W) with
+// DU(a) = DUp + a (DU1 - DUp), before k_bt_apply overwrites DU1 (D^T is
+// linear, so this is the reference's g2p + a (g2 - g2p), :706-818).
+template <class T>
+__global__ void k_bt_g2(SolverBufs<T> B, Geo g) {
+    Ctl* ctl = B.ctl;
+    count_launch(ctl);
+    if (ctl->armijo_fail) return;  // restart path: the restart's get_g and update_W follow
+    const int cur = ctl->parity, prv = 1 - cur;
+    const long n = B.n;
+    const T al = scal<T>(ctl->alpha);
+    const T *__restrict__ DU = B.DU[cur], *__restrict__ DUp = B.DU[prv], *__restrict__ W = B.W;
+    T* __restrict__ g2 = B.g2[cur];
+    auto v = [&](long j) {
+        const T p = DUp[j];
+        return p + al * (DU[j] - p) - W[j];
+    };
+    GRID_STRIDE(i, n) {
+        Nb nb = neighbours(g, i);
+        g2[i] = v(nb.ym) - v(i) + v(n + nb.xm) - v(n + i) + v(2 * n + nb.zm) - v(2 * n + i);
     }
 }
 
@@ -552,6 +581,68 @@ __global__ void k_cond(Ctl* ctl, unsigned long long h, int src) {
 
 void launch_cond(Ctl* ctl, unsigned long long handle, int src, cudaStream_t s) {
     k_cond<<<1, 1, 0, s>>>(ctl, handle, src);
+}
+
+// ---------------------------------------------------------------------------
+// skip-A^T heuristic (get_g_gpu, 3d/tval3_gpu_3d.cpp:398-468): after A*U,
+// ||Au - last_Au|| / ||Au|| and the reference's rule decide whether this
+// get_g forms A^T Au (forced at start-up and at a restart; always during the
+// first numInitIterations calls; then while the skip budget allows, or when
+// Au moved more than maxRelativeChange).  A skipped call keeps the previous g
+// (the reference also subtracts Atb from it once more, :562-565: a defect
+// not reproduced).
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_skip_decide(SolverBufs<T> B, int force) {
+    Ctl* ctl = B.ctl;
+    count_launch(ctl);
+    const T* __restrict__ Au = B.Au[ctl->parity];
+    const T* __restrict__ la = B.last_Au;
+    double dn = 0.0, an = 0.0;
+    GRID_STRIDE(i, B.m) {
+        const double a = acc_d(to_acc(Au[i])), d = a - acc_d(to_acc(la[i]));
+        dn += d * d;
+        an += a * a;
+    }
+    double v[2] = {dn, an}, tot[2];
+    if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        const double rel = sqrt(tot[0]) / sqrt(tot[1]);
+        ctl->rel_change = rel;
+        int mult = 1;
+        if (force) {
+            ctl->cur_skip = 0.0;
+        } else if (ctl->cur_init < ctl->num_init) {
+            ctl->cur_init += 1;
+            ctl->cur_skip = 0.0;
+        } else if (ctl->cur_skip < 1.0) {
+            ctl->cur_skip += ctl->skip_ratio;
+        } else if (!(rel > ctl->max_rel_change)) {
+            ctl->cur_skip -= 1.0;
+            mult = 0;
+        }
+        ctl->do_mult = mult;
+        if (mult) ctl->products_T += 1;
+        if (B.use_graph) {
+            cudaGraphSetConditional(B.h_mult, mult ? 1u : 0u);
+            cudaGraphSetConditional(B.h_keep, mult ? 0u : 1u);
+        }
+    }
+}
+
+template <class T>
+__global__ void k_skip_copy(SolverBufs<T> B, int which) {
+    Ctl* ctl = B.ctl;
+    count_launch(ctl);
+    const int cur = ctl->parity;
+    if (which == 0) {
+        const T* __restrict__ Au = B.Au[cur];
+        T* __restrict__ la = B.last_Au;
+        GRID_STRIDE(i, B.m) la[i] = Au[i];
+    } else {
+        const T* __restrict__ gp = B.g[1 - cur];
+        T* __restrict__ g = B.g[cur];
+        GRID_STRIDE(i, B.n) g[i] = gp[i];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -727,7 +818,8 @@ template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s) {
     k_Dd_norm<T><<<B.grid, 256, 0, s>>>(B, geo_of(B));
 }
 template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s) {
-    k_g2<T><<<B.grid, 256, 0, s>>>(B, geo_of(B), mode);
+    if (mode == EPI_G2_DESCEND || mode == EPI_G2_RESTART) k_g2<T, false><<<B.grid, 256, 0, s>>>(B, geo_of(B), mode);
+    else k_g2<T, true><<<B.grid, 256, 0, s>>>(B, geo_of(B), mode);
 }
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s) {
     k_shrink<T><<<B.grid, 256, 0, s>>>(B, mode);
@@ -736,10 +828,19 @@ template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t
     k_gradient<T><<<B.grid, 256, 0, s>>>(B, mode);
 }
 template <class T> void launch_bt_coef(SolverBufs<T>& B, cudaStream_t s) { k_bt_coef<T><<<B.grid, 256, 0, s>>>(B); }
-template <class T> void launch_bt_apply(SolverBufs<T>& B, cudaStream_t s) { k_bt_apply<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_bt_apply(SolverBufs<T>& B, cudaStream_t s) {
+    k_bt_g2<T><<<B.grid, 256, 0, s>>>(B, geo_of(B));
+    k_bt_apply<T><<<B.grid, 256, 0, s>>>(B);
+}
 template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s) { k_outer_relchg<T><<<B.grid, 256, 0, s>>>(B); }
 template <class T> void launch_mlp(SolverBufs<T>& B, cudaStream_t s) { k_mlp<T><<<B.grid, 256, 0, s>>>(B); }
 template <class T> void launch_outer_grad(SolverBufs<T>& B, cudaStream_t s) { k_outer_grad<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_skip_decide(SolverBufs<T>& B, int force, cudaStream_t s) {
+    k_skip_decide<T><<<B.grid, 256, 0, s>>>(B, force);
+}
+template <class T> void launch_skip_copy(SolverBufs<T>& B, int which, cudaStream_t s) {
+    k_skip_copy<T><<<ew_grid(which == 0 ? B.m : B.n), 256, 0, s>>>(B, which);
+}
 template <class T> void launch_finalize(SolverBufs<T>& B, void* U_out, const void* Ut, cudaStream_t s) {
     k_finalize<T><<<B.grid, 256, 0, s>>>(B, static_cast<Ext<T>*>(U_out), static_cast<const Ext<T>*>(Ut));
 }
@@ -765,6 +866,8 @@ template <class T> void launch_Dt_plain(int p, int q, int r, const T* V3, T* out
     template void launch_outer_relchg<T>(SolverBufs<T>&, cudaStream_t);             \
     template void launch_mlp<T>(SolverBufs<T>&, cudaStream_t);                      \
     template void launch_outer_grad<T>(SolverBufs<T>&, cudaStream_t);               \
+    template void launch_skip_decide<T>(SolverBufs<T>&, int, cudaStream_t);                  \
+    template void launch_skip_copy<T>(SolverBufs<T>&, int, cudaStream_t);                    \
     template void launch_finalize<T>(SolverBufs<T>&, void*, const void*, cudaStream_t);
 INST(float)
 INST(double)

@@ -73,6 +73,28 @@ __device__ __forceinline__ void madd(RowAcc<df64>& a, float v, df64 x) {
     a.c = __fadd_rn(a.c, __fadd_rn(t.lo, pl));
 }
 
+// Sums of products a*b for the loop's reductions (lam2, lam4, ...): FP64 for
+// float and double vectors; for double-float vectors the exact high product
+// plus the cross terms, accumulated with a compensated (Dot2-style) float
+// pair, which costs about half the instructions of full double-float
+// arithmetic and keeps errors of order u^2 per term.
+template <class T> struct ProdAcc {
+    double s = 0.0;
+    __device__ __forceinline__ void add(T a, T b) { s = fma((double)a, (double)b, s); }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct ProdAcc<df64> {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(df64 a, df64 b) {
+        df64 p = two_prod(a.hi, b.hi);
+        const float pl = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo));
+        df64 t = two_sum(s, p.hi);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, pl));
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 __device__ __forceinline__ float shfl_down(unsigned mask, float v, int o, int w) { return __shfl_down_sync(mask, v, o, w); }
 __device__ __forceinline__ double shfl_down(unsigned mask, double v, int o, int w) { return __shfl_down_sync(mask, v, o, w); }
 __device__ __forceinline__ df64 shfl_down(unsigned mask, df64 v, int o, int w) {
@@ -108,6 +130,11 @@ struct Ctl {
     int backtracks, restarts;
     int err;           // device-side error word (0 = none)
     unsigned launches; // kernels of this solve that ran (each counts itself once)
+    // skip-A^T heuristic (3d/tval3_gpu_3d.cpp:155-157, :398-468)
+    double skip_ratio, max_rel_change, cur_skip, rel_change;
+    unsigned num_init, cur_init;
+    int do_mult;       // 1: this get_g forms A^T Au; 0: it keeps the current g
+    int products_T;    // A^T products formed by get_g
 };
 
 // every solver kernel counts itself once (block 0, thread 0)

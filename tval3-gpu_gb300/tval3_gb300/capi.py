@@ -42,7 +42,8 @@ class Options(C.Structure):
 class Info(C.Structure):
     _fields_ = [("total_iters", C.c_int), ("outer_iters", C.c_int), ("rel_chg", C.c_double),
                 ("rel_error", C.c_double), ("secs", C.c_double), ("outer_secs", C.c_double),
-                ("backtracks", C.c_int), ("restarts", C.c_int), ("final_f", C.c_double), ("launches", C.c_int)]
+                ("backtracks", C.c_int), ("restarts", C.c_int), ("final_f", C.c_double), ("launches", C.c_int),
+                ("products_T", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
