@@ -598,12 +598,13 @@ def spmv_only(args, T, torch, geo, op32, n, m, nnz, dev):
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
     res = {}
-    for trans, (src, dst) in ((0, (x, outm)), (1, (y, outn))):
+
+    def timed(trans, src, dst, tag):
         for _ in range(3):
             op.mat_vec_mul(trans, src, dst, stream=stream)
         tot = 0.0
         # an NVTX range per product, so a profiler can select exactly these launches
-        torch.cuda.nvtx.range_push("spmv_AT" if trans else "spmv_A")
+        torch.cuda.nvtx.range_push(tag)
         for _ in range(20):
             with torch.cuda.stream(stream):
                 flush.fill_(1.0)
@@ -615,9 +616,24 @@ def spmv_only(args, T, torch, geo, op32, n, m, nnz, dev):
             e1.synchronize()
             tot += e0.elapsed_time(e1) / 1000.0
         torch.cuda.nvtx.range_pop()
-        t = tot / 20
+        return tot / 20
+
+    for trans, (src, dst) in ((0, (x, outm)), (1, (y, outn))):
+        chosen = op.variant(trans)
         bts = spmv_bytes(nnz, m, n, sv, sx, bool(trans)) + (4 * m if sv == 2 else 0)
-        res["AT" if trans else "A"] = {"us": round(t * 1e6, 2), "GBs": round(bts / t / 1e9, 1), "bytes": bts}
+        t = timed(trans, src, dst, "spmv_AT" if trans else "spmv_A")
+        entry = {"us": round(t * 1e6, 2), "GBs": round(bts / t / 1e9, 1), "bytes": bts,
+                 "variant": ("tiled" if chosen else "csr")}
+        # the other kernel of the same product, for comparison
+        other = 1 - chosen
+        try:
+            op.set_variant(trans, other)
+            t2 = timed(trans, src, dst, ("spmv_AT_" if trans else "spmv_A_") + ("tiled" if other else "csr"))
+            entry["tiled_us" if other else "csr_us"] = round(t2 * 1e6, 2)
+            op.set_variant(trans, chosen)
+        except T.Tval3Error:
+            pass
+        res["AT" if trans else "A"] = entry
     peak, kind = peaks()
     return {"spmv_only": args.only_spmv, "nnz": nnz, "rows": m, "cols": n, "peak_GBs": peak, "peak_source": kind,
             **res}

@@ -261,6 +261,15 @@ TVAL3_API tval3_status tval3_op_export_csr(tval3_op op, int* ptr, int* ind, floa
  * `layers`, 2d/mat_vec_mul.h:65-71, :96-99). */
 TVAL3_API tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, void* stream);
 TVAL3_API tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, void* Y, void* stream);
+/* Kernel of the single-vector products of a stored operator whose volume is
+ * known (geometry operators, or any operator once a solver has been created
+ * on it): variant 0 = CSR kernels, 1 = tile-staged (the vector staged per
+ * voxel tile in shared memory).  The library picks the faster one by timing
+ * when it builds the tiled form; pinning a variant makes a program's results
+ * independent of that timing.  TVAL3_ERR_UNSUPPORTED if the variant is not
+ * available. */
+TVAL3_API tval3_status tval3_op_set_variant(tval3_op op, int trans, int variant);
+TVAL3_API tval3_status tval3_op_get_variant(tval3_op op, int trans, int* variant);
 /* The same product on interleaved data: element (row, column j) at
  * row * nrhs + j, the layout the multi-layer solver keeps.  One SpMM (CSR),
  * tensor-core GEMM (BF16 dense) or SIMT GEMM (FP32/FP64 dense) launch

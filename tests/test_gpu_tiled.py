@@ -30,6 +30,8 @@ def test_tiled_products_match_plain_csr(cuda, kind, prec, trans):
     ptr, ind, val, tptr, tind, tval = Operator.from_geometry(geo, mode=0, precision=PREC_FP32).export_csr()
     m, n = ptr.size - 1, tptr.size - 1
     plain = Operator.from_sparse(SparseMatrix(m, n, ptr, ind, val, tptr, tind, tval), precision=p)
+    # small operators keep the tile-staged form without a timing contest
+    assert tiled.variant(trans) == 1 and plain.variant(trans) == 0
     g = torch.Generator().manual_seed(7 + trans)
     lin, lout = (m, n) if trans else (n, m)
     yh = torch.randn(lin, dtype=torch.float64, generator=g)
@@ -82,3 +84,27 @@ def test_tiled_solve_matches_oracle_fp64(cuda, oracle):
     assert (ig["total_iters"], ig["outer_iters"], ig["backtracks"], ig["restarts"]) == \
         (io["total_iters"], io["outer_iters"], io["backtracks"], io["restarts"])
     assert np.linalg.norm(U.cpu().numpy() - Uo.reshape(-1)) <= 1e-7 * np.linalg.norm(Uo)
+
+
+def test_variant_pinning(cuda):
+    """tval3_op_set_variant pins the kernel of each product; the two kernels
+    of one operator agree, and an operator without a volume has no tiled form."""
+    import torch
+    from tval3_gb300 import PREC_FP32, Operator, SparseMatrix, Tval3Error
+    geo = _geo("hemi")
+    op = Operator.from_geometry(geo, mode=0, precision=PREC_FP32)
+    g = torch.Generator().manual_seed(3)
+    y = torch.randn(op.rows, generator=g).to(cuda)
+    outs = []
+    for v in (0, 1):
+        op.set_variant(1, v)
+        assert op.variant(1) == v
+        x = torch.empty(op.cols, device=cuda)
+        op.mat_vec_mul(1, y, x)
+        outs.append(x)
+    torch.cuda.synchronize()
+    assert torch.allclose(outs[0], outs[1], rtol=1e-5, atol=1e-5 * float(outs[0].abs().max()))
+    ptr, ind, val, tptr, tind, tval = op.export_csr()
+    bare = Operator.from_sparse(SparseMatrix(ptr.size - 1, tptr.size - 1, ptr, ind, val), precision=PREC_FP32)
+    with pytest.raises(Tval3Error):
+        bare.set_variant(0, 1)

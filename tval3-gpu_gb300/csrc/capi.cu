@@ -536,6 +536,23 @@ tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, 
     });
 }
 
+tval3_status tval3_op_set_variant(tval3_op op, int trans, int variant) {
+    return guard([&] {
+        if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
+        bool ok = op->q ? op->q->set_variant(trans ? 1 : 0, variant)
+                        : (op->dbl ? op->d->set_variant(trans ? 1 : 0, variant) : op->f->set_variant(trans ? 1 : 0, variant));
+        if (!ok) arg_error(TVAL3_ERR_UNSUPPORTED, "product variant not available for this operator");
+    });
+}
+
+tval3_status tval3_op_get_variant(tval3_op op, int trans, int* variant) {
+    return guard([&] {
+        if (!op || !variant) arg_error(TVAL3_ERR_ARG, "Argument error: NULL argument!");
+        *variant = op->q ? op->q->variant(trans ? 1 : 0)
+                         : (op->dbl ? op->d->variant(trans ? 1 : 0) : op->f->variant(trans ? 1 : 0));
+    });
+}
+
 tval3_status tval3_mat_mat_mul_interleaved(tval3_op op, int trans, int nrhs, const void* X, void* Y, void* stream) {
     return guard([&] {
         if (!op || !X || !Y || nrhs < 1) arg_error(TVAL3_ERR_ARG, "Argument error: bad multi-RHS product!");

@@ -99,6 +99,7 @@ template <class T> void launch_descend(SolverBufs<T>& B, int restart, cudaStream
 template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s);
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s);
+template <class T> void launch_g2_gradient(SolverBufs<T>& B, cudaStream_t s);  // g2 (update_W) + gradient, fused
 template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t s);
 template <class T> void launch_bt_coef(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_bt_apply(SolverBufs<T>& B, cudaStream_t s);

@@ -179,6 +179,7 @@ struct CsrOp : LinOp<T> {
     int Gn = 32, Gt = 8, grid_n = 1, grid_t = 1;
     mutable TiledT<T, V> tiled;   // A^T regrouped by voxel tiles (when the volume is known)
     mutable TiledN<T, V> tiledN;  // A cut into per-tile ray segments (when the volume is known)
+    mutable bool useT = false, useN = false;  // products run tile-staged
     mutable int vol[3] = {0, 0, 0};
 
     void set_volume(int p, int q, int r) const override {
@@ -186,18 +187,28 @@ struct CsrOp : LinOp<T> {
         vol[0] = p; vol[1] = q; vol[2] = r;
         tiled.build(this->n, this->m, p, q, r, tptr.p, tind.p, tval.p, this->nnz, 96 * 1024, 0);
         tiledN.build(this->m, p, q, r, ptr.p, ind.p, val.p, this->nnz, 0);
-        // keep the tile-staged products only where they beat the tuned CSR kernels
+        useT = tiled.ok;
+        useN = tiledN.ok;
+        // large operators: the tile-staged products only where they beat the tuned CSR kernels
         if (this->nnz >= (1L << 22)) {
-            if (tiled.ok && time_product(1, false) <= time_product(1, true)) tiled = TiledT<T, V>();
-            if (tiledN.ok && time_product(0, false) <= time_product(0, true)) tiledN = TiledN<T, V>();
+            if (useT && time_product(1, false) <= time_product(1, true)) useT = false;
+            if (useN && time_product(0, false) <= time_product(0, true)) useN = false;
         }
     }
 
+    bool set_variant(int trans, int v) const override {
+        if (v != 0 && v != 1) return false;
+        if (v == 1 && !(trans ? tiled.ok : tiledN.ok)) return false;
+        (trans ? useT : useN) = (v == 1);
+        return true;
+    }
+    int variant(int trans) const override { return (trans ? useT : useN) ? 1 : 0; }
+
     // milliseconds of three products (after one warm-up), plain CSR or tile-staged
     float time_product(int trans, bool use_tiled) const {
-        bool& flag = trans ? tiled.ok : tiledN.ok;
+        bool& flag = trans ? useT : useN;
         const bool keep = flag;
-        flag = use_tiled && keep;
+        flag = use_tiled;
         const long lx = trans ? this->m : this->n, ly = trans ? this->n : this->m;
         DBuf<T> x(std::max<long>(lx, 1)), y(std::max<long>(ly, 1));
         TV3_CUDA(cudaMemset(x.p, 0, std::max<long>(lx, 1) * sizeof(T)));
@@ -219,7 +230,7 @@ struct CsrOp : LinOp<T> {
     }
 
     void apply(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const override {
-        if (!trans && io.L <= 1 && tiledN.ok) {
+        if (!trans && io.L <= 1 && useN && tiledN.ok) {
             TiledNArgs<T, V> t{};
             t.ntiles = tiledN.ntiles;
             t.p = tiledN.p; t.q = tiledN.q; t.r = tiledN.r; t.ty = tiledN.ty; t.tx = tiledN.tx; t.tz = tiledN.tz;
@@ -233,7 +244,7 @@ struct CsrOp : LinOp<T> {
             tiledN.apply(t, epi, s);
             return;
         }
-        if (trans && io.L <= 1 && tiled.ok && (epi == SPMV_PLAIN || epi == SPMV_SUB)) {
+        if (trans && io.L <= 1 && useT && tiled.ok && (epi == SPMV_PLAIN || epi == SPMV_SUB)) {
             TiledArgs<T, V> t{};
             t.ntiles = tiled.ntiles; t.ray_off = tiled.ray_off.p; t.rays = tiled.rays.p;
             t.tile_slice = tiled.tile_slice.p; t.slice_off = tiled.slice_off.p; t.row_voxel = tiled.row_voxel.p;

@@ -73,6 +73,17 @@ struct LinOp {
     }
     // true when apply() takes L > 1 interleaved right-hand sides
     virtual bool multi_rhs() const { return false; }
+    // kernel of A*x (trans 0) or A^T*y (trans 1): 0 = CSR kernels, 1 =
+    // tile-staged (when built); the build-time timing picks one, the caller
+    // may pin it.  Returns false when the variant is not available.
+    virtual bool set_variant(int trans, int variant) const {
+        (void)trans;
+        return variant == 0;
+    }
+    virtual int variant(int trans) const {
+        (void)trans;
+        return 0;
+    }
     // multi-RHS products: columns of length n (trans 0: X n x k -> Y m x k),
     // column-major; operators with multi_rhs() run one interleaved product
     virtual void apply_multi(int trans, int k, const T* X, T* Y, cudaStream_t s) const {
@@ -109,6 +120,8 @@ struct SplitOp : LinOp<T> {
         top->prepare(L);
     }
     void set_volume(int p, int q, int r) const override { top->set_volume(p, q, r); }
+    bool set_variant(int trans, int v) const override { return (trans ? top : nop)->set_variant(trans, v); }
+    int variant(int trans) const override { return (trans ? top : nop)->variant(trans); }
 };
 
 // CSR operator: A and the CSR of A^T on the device.

@@ -270,8 +270,7 @@ void Solver<T>::run_host(cudaStream_t s) {
         }
         // ---- update_W (:965-1029), reference values, gradient, RelChg
         launch_shrink<T>(B, EPI_G2_UPDATE_W, s);
-        launch_g2<T>(B, EPI_G2_UPDATE_W, s);
-        launch_gradient<T>(B, 1, s);
+        launch_g2_gradient<T>(B, s);
         read_ctl(s);
         fst = false;
         if (hctl->inner_break) {
@@ -348,8 +347,7 @@ void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const 
             }
             ib.begin();
             launch_shrink<T>(B, EPI_G2_UPDATE_W, cs);
-            launch_g2<T>(B, EPI_G2_UPDATE_W, cs);
-            launch_gradient<T>(B, 1, cs);  // sets h_inner
+            launch_g2_gradient<T>(B, cs);  // sets h_inner
             ib.end();
         }
         ob.begin();

@@ -412,6 +412,87 @@ __global__ void k_gradient(SolverBufs<T> B, int iter) {
 }
 
 // ---------------------------------------------------------------------------
+// The end of an inner iteration in one pass: update_W's g2 = D^T (DU - W),
+// lam2, lam4 (k_g2, UPDATE_W) and get_gradient's d with the next step size
+// and the stopping test (k_gradient, iter 1).  g2[i] is formed and used by
+// the same thread, so the pass saves the store-and-reload of g2 and a launch.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_g2_gradient(SolverBufs<T> B, Geo geo) {
+    Ctl* ctl = B.ctl;
+    count_launch(ctl);
+    using A = acc_t<T>;
+    const int cur = ctl->parity, prv = 1 - cur;
+    const long n = B.n;
+    const T* __restrict__ DU = B.DU[cur];
+    const T* __restrict__ W = B.W;
+    const T* __restrict__ S = B.sig;
+    T* __restrict__ g2o = B.g2[cur];
+    const T mdb = scal<T>(ctl->muDbeta);
+    const A mdbA = scal<A>(ctl->muDbeta);
+    const T *__restrict__ g = B.g[cur], *__restrict__ dts = B.DtsAtd;
+    const T *__restrict__ gp = B.g[prv], *__restrict__ g2p = B.g2[prv];
+    const T *__restrict__ U = B.U[cur], *__restrict__ Up = B.U[prv];
+    const Ext<T>* __restrict__ xs = static_cast<const Ext<T>*>(B.xstar);
+    const double iscl = 1.0 / ctl->scl;
+    T* __restrict__ d = B.d;
+    ProdAcc<T> l2, l4;
+    ProdAcc<A> s0, s1, s2, s4;
+    double s3 = 0.0;
+    GRID_STRIDE(i, n) {
+        const Nb nb = neighbours(geo, i);
+        const T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
+        const T v0m = DU[nb.ym] - W[nb.ym];
+        const T v1m = DU[n + nb.xm] - W[n + nb.xm];
+        const T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
+        const T g2i = v0m - v0 + v1m - v1 + v2m - v2;
+        g2o[i] = g2i;
+        l2.add(v0, v0);
+        l2.add(v1, v1);
+        l2.add(v2, v2);
+        l4.add(v0, S[i]);
+        l4.add(v1, S[n + i]);
+        l4.add(v2, S[2 * n + i]);
+        const T gi = g[i];
+        const T di = mdb * gi + g2i + dts[i];
+        d[i] = di;
+        const A ad = to_acc(di);
+        s2.add(ad, ad);
+        const A u = to_acc(U[i]), up = to_acc(Up[i]);
+        const A du = u - up;
+        s0.add(up, up);
+        s1.add(du, du);
+        const A dg = to_acc(gi) - to_acc(gp[i]);
+        const A dg2 = to_acc(g2i) - to_acc(g2p[i]);
+        s4.add(du, dg2 + mdbA * dg);
+        if (xs) {
+            double e = acc_d(u) * iscl - (double)xs[i];
+            s3 += e * e;
+        }
+    }
+    double v[7] = {l2.value(), l4.value(), s0.value(), s1.value(), s2.value(), s3, s4.value()}, tot[7];
+    if (grid_reduce<7>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        // update_W (:1016-1029) and the nonmonotone reference values (:1176-1177)
+        ctl->lam2 = tot[0];
+        ctl->lam4 = tot[1];
+        ctl->f += ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
+        double Qp = ctl->Q;
+        ctl->Q = ctl->gam * Qp + 1.0;
+        ctl->C = (ctl->gam * Qp * ctl->C + ctl->f) / ctl->Q;
+        // get_gradient, the next BB step and the inner stopping test
+        ctl->dd = tot[4];
+        ctl->tau = fabs(tot[3] / tot[6]);
+        ctl->nrmup = sqrt(tot[2]);
+        ctl->relchg = sqrt(tot[3]) / ctl->nrmup;
+        if (B.trace && xs) B.trace[ctl->count_total] = sqrt(tot[5]);
+        ctl->count_total += 1;
+        ctl->inner_break = ((ctl->relchg < ctl->tol_inn) && !ctl->fst) || (ctl->count_total >= ctl->maxit);
+        ctl->fst = 0;
+        if (B.use_graph) cudaGraphSetConditional(B.h_inner, ctl->inner_break ? 0u : 1u);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Backtracking in closed form.  update_g_gpu (:706-818) moves every quantity
 // along X(a) = Xp + a (X1 - Xp) (X1 the rejected full step) and re-evaluates
 // f(a) = lam1 + beta/2 lam2 + mu/2 lam3 - lam4 - lam5 for a = gamma, gamma^2,
@@ -824,6 +905,9 @@ template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s) {
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s) {
     k_shrink<T><<<B.grid, 256, 0, s>>>(B, mode);
 }
+template <class T> void launch_g2_gradient(SolverBufs<T>& B, cudaStream_t s) {
+    k_g2_gradient<T><<<B.grid, 256, 0, s>>>(B, geo_of(B));
+}
 template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t s) {
     k_gradient<T><<<B.grid, 256, 0, s>>>(B, mode);
 }
@@ -861,6 +945,7 @@ template <class T> void launch_Dt_plain(int p, int q, int r, const T* V3, T* out
     template void launch_g2<T>(SolverBufs<T>&, int, cudaStream_t);                  \
     template void launch_shrink<T>(SolverBufs<T>&, int, cudaStream_t);              \
     template void launch_gradient<T>(SolverBufs<T>&, int, cudaStream_t);            \
+    template void launch_g2_gradient<T>(SolverBufs<T>&, cudaStream_t);              \
     template void launch_bt_coef<T>(SolverBufs<T>&, cudaStream_t);                  \
     template void launch_bt_apply<T>(SolverBufs<T>&, cudaStream_t);                 \
     template void launch_outer_relchg<T>(SolverBufs<T>&, cudaStream_t);             \

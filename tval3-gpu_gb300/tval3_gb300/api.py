@@ -297,6 +297,15 @@ class Operator:
     def mat_mat_mul(self, trans: int, nrhs: int, X, Y, stream=None) -> None:
         check(load().tval3_mat_mat_mul(self._h, int(trans), nrhs, _ptr(X), _ptr(Y), _stream(stream)))
 
+    def set_variant(self, trans: int, variant: int) -> None:
+        """Pin the kernel of A*x (trans 0) or A^T*y (trans 1): 0 CSR, 1 tile-staged."""
+        check(load().tval3_op_set_variant(self._h, int(trans), int(variant)))
+
+    def variant(self, trans: int) -> int:
+        v = C.c_int()
+        check(load().tval3_op_get_variant(self._h, int(trans), C.byref(v)))
+        return v.value
+
     def mat_mat_mul_interleaved(self, trans: int, nrhs: int, X, Y, stream=None) -> None:
         """Y = A X (or A^T X) for nrhs right-hand sides stored interleaved
         (element (row, j) at row * nrhs + j)."""
