@@ -299,6 +299,23 @@ TVAL3_API tval3_status tval3_solver_create_layers(tval3_solver* s, tval3_op A, i
 TVAL3_API tval3_status tval3_solver_set_mode(tval3_solver s, int mode);
 TVAL3_API tval3_status tval3_solver_solve(tval3_solver s, const void* d_b, void* d_U, const void* d_Ut,
                                           tval3_info* info, void* stream);
+/* Solver state (no counterpart in the reference; checkpoint/resume): the
+ * control block and every workspace vector of a finished solve, in a host
+ * buffer of tval3_solver_state_size bytes.  tval3_solver_resume loads such a
+ * state into a solver of the same operator shape, volume, layers and vector
+ * type and continues the loop from it under this solver's maxit/maxcnt and
+ * pause, writing U like tval3_solver_solve.  A state saved at a pause
+ * continues exactly as if the solve had not stopped; a state saved after a
+ * stop by maxit continues after that outer step (which the stop completed). */
+/* Pause: solves and resumes of this solver stop once the total iteration
+ * count reaches `iterations` (0 = never) without ending the outer iteration
+ * in progress, so that save_state + resume continue exactly as an
+ * uninterrupted solve would (U is written at the pause). */
+TVAL3_API tval3_status tval3_solver_set_pause(tval3_solver s, int iterations);
+TVAL3_API tval3_status tval3_solver_state_size(tval3_solver s, size_t* bytes);
+TVAL3_API tval3_status tval3_solver_save_state(tval3_solver s, void* host_state, void* stream);
+TVAL3_API tval3_status tval3_solver_resume(tval3_solver s, const void* host_state, void* d_U, const void* d_Ut,
+                                           tval3_info* info, void* stream);
 /* Record ||U_k/scl - xstar|| after every iteration k (xstar on device, length
  * n; NULL disables).  Read with tval3_solver_trace (host array of maxit). */
 TVAL3_API tval3_status tval3_solver_set_trace(tval3_solver s, const void* d_xstar);

@@ -213,3 +213,33 @@ def test_skip_heuristic_matches_oracle(cuda, oracle, max_rel):
         outs.append(U.cpu().numpy())
         s.close()
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("dims", [(15, 14, 1), (9, 7, 5), (16, 12, 6)])
+def test_fp64_odd_and_even_volumes(cuda, oracle, dims):
+    """The pass-per-vector kernels take two voxels per 16-byte access when the
+    fastest dimension (stencils) or the volume (plain streams) is even, one
+    voxel otherwise; FP64 solves of odd and even volumes keep the oracle's
+    control flow and result."""
+    from tval3_gb300 import SparseMatrix, tval3_gpu_3d
+    from tval3_gb300 import workloads as W
+    p, q, r = dims
+    rng = np.random.default_rng(p * 100 + q * 10 + r)
+    n = p * q * r
+    m = 3 * n // 2
+    rows = []
+    for _ in range(m):
+        k = rng.integers(3, 9)
+        rows.append(np.sort(rng.choice(n, size=k, replace=False)))
+    ptr = np.zeros(m + 1, np.int32)
+    ptr[1:] = np.cumsum([len(x) for x in rows])
+    ind = np.concatenate(rows).astype(np.int32)
+    val = rng.uniform(0.2, 1.0, ind.size).astype(np.float32)
+    x = rng.uniform(0.0, 1.0, n)
+    b = W.add_noise(oracle.spmv(ptr, ind, val, x), 0.01, 3).astype(np.float64)
+    o = dict(OPTS, tv_type=1, maxit=40)
+    Uo, io = oracle.tval3_csr(dims, ptr, ind, val, b, o)
+    Ug, ig = tval3_gpu_3d(dims, SparseMatrix(m, n, ptr, ind, val.astype(np.float64)), b, o, dtype=np.float64)
+    assert (ig["total_iters"], ig["outer_iters"], ig["backtracks"], ig["restarts"]) == \
+        (io["total_iters"], io["outer_iters"], io["backtracks"], io["restarts"])
+    assert np.linalg.norm(Ug.reshape(-1) - Uo.reshape(-1)) <= 1e-7 * np.linalg.norm(Uo)

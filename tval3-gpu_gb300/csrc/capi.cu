@@ -678,6 +678,42 @@ tval3_status tval3_solver_solve(tval3_solver s, const void* d_b, void* d_U, cons
     });
 }
 
+tval3_status tval3_solver_set_pause(tval3_solver s, int iterations) {
+    return guard([&] {
+        if (!s || iterations < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad pause!");
+        with_solver(s, [&](auto& v) {
+            v.pause_at = iterations;
+            // the limit is a graph parameter: rebuild on the next solve
+            if (v.gexec) cudaGraphExecDestroy(v.gexec);
+            v.gexec = nullptr;
+            if (v.rexec) cudaGraphExecDestroy(v.rexec);
+            v.rexec = nullptr;
+        });
+    });
+}
+
+tval3_status tval3_solver_state_size(tval3_solver s, size_t* bytes) {
+    return guard([&] {
+        if (!s || !bytes) arg_error(TVAL3_ERR_ARG, "Argument error: NULL argument!");
+        with_solver(s, [&](auto& v) { *bytes = v.state_bytes(); });
+    });
+}
+
+tval3_status tval3_solver_save_state(tval3_solver s, void* host_state, void* stream) {
+    return guard([&] {
+        if (!s || !host_state) arg_error(TVAL3_ERR_ARG, "Argument error: NULL argument!");
+        with_solver(s, [&](auto& v) { v.save_state(host_state, (cudaStream_t)stream); });
+    });
+}
+
+tval3_status tval3_solver_resume(tval3_solver s, const void* host_state, void* d_U, const void* d_Ut,
+                                 tval3_info* info, void* stream) {
+    return guard([&] {
+        if (!s || !host_state || !d_U) arg_error(TVAL3_ERR_ARG, "Argument error: NULL argument!");
+        with_solver(s, [&](auto& v) { v.resume(host_state, d_U, d_Ut, info, (cudaStream_t)stream); });
+    });
+}
+
 tval3_status tval3_solver_set_trace(tval3_solver s, const void* d_xstar) {
     return guard([&] {
         if (!s) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver!");

@@ -102,6 +102,7 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
 template <class T>
 Solver<T>::~Solver() {
     if (gexec) cudaGraphExecDestroy(gexec);
+    if (rexec) cudaGraphExecDestroy(rexec);
     if (hctl) cudaFreeHost(hctl);
 }
 
@@ -139,6 +140,18 @@ MatIO<T> Solver<T>::io_Ad() const {
 
 __global__ void k_init_ctl(Ctl* c, Ctl v) { *c = v; }
 
+// resuming a saved state: the iteration limits of this solver's options, and
+// the loop runs again
+__global__ void k_resume_ctl(Ctl* c, int maxit, int maxcnt, int pause_at) {
+    c->maxit = maxit;
+    c->maxcnt = maxcnt;
+    c->pause_at = pause_at;
+    c->paused = 0;
+    c->done = !(c->count_outer < maxcnt && c->count_total < maxit);
+    c->err = 0;
+    c->launches += 1;
+}
+
 template <class T>
 void Solver<T>::init_ctl(cudaStream_t s) {
     Ctl c;
@@ -154,6 +167,7 @@ void Solver<T>::init_ctl(cudaStream_t s) {
     c.Q = 1.0;
     c.fst = 1;
     c.scl = 1.0;
+    c.pause_at = pause_at > 0 ? pause_at : 0x7fffffff;
     c.skip_ratio = o.skipMulRatio;
     c.max_rel_change = o.maxRelativeChange;
     c.num_init = o.numInitIterations;
@@ -248,7 +262,8 @@ void Solver<T>::setup(const void* d_b, cudaStream_t s, Body* body) {
 template <class T>
 void Solver<T>::run_host(cudaStream_t s) {
     if (!(o.maxcnt > 0 && o.maxit > 0)) return;
-    bool fst = true;
+    read_ctl(s);
+    bool fst = hctl->fst != 0;  // 1 after set-up; a resumed state carries its own
     for (;;) {
         // ---- min_u (:823-891); a non-first step size was formed by the
         // previous iteration's gradient kernel
@@ -294,7 +309,8 @@ void Solver<T>::run_host(cudaStream_t s) {
 // roots of `top`), capturing through stream cs.  Several solvers can add
 // their branches to one graph; they share nothing on the device.
 template <class T>
-void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const void* d_Ut, cudaStream_t cs) {
+void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const void* d_Ut, cudaStream_t cs,
+                             bool resume) {
     const unsigned run = (o.maxcnt > 0 && o.maxit > 0) ? 1u : 0u;
     cudaGraphConditionalHandle h_outer, h_inner, h_fst, h_arm, h_restart, h_mlp;
     TV3_CUDA(cudaGraphConditionalHandleCreate(&h_outer, top, run, cudaGraphCondAssignDefault));
@@ -309,7 +325,12 @@ void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const 
     try {
         Body tb{top, {}, cs};
         tb.begin();
-        setup(d_b, cs, &tb);
+        if (resume) {
+            k_resume_ctl<<<1, 1, 0, cs>>>(B.ctl, o.maxit, o.maxcnt, pause_at > 0 ? pause_at : 0x7fffffff);
+            launch_cond(B.ctl, h_outer, COND_NOT_DONE, cs);
+        } else {
+            setup(d_b, cs, &tb);
+        }
         tb.end();
         // outer while
         Body ob{tb.cond(h_outer, cudaGraphCondTypeWhile, 1)[0], {}, cs};
@@ -410,6 +431,108 @@ void Solver<T>::solve(const void* d_b, void* d_U, const void* d_Ut, tval3_info* 
         B.use_graph = 0;
         setup(d_b, s);
         run_host(s);
+        launch_finalize<T>(B, d_U, d_Ut, s);
+    }
+    TV3_CUDA(cudaEventRecord(e1, s));
+    TV3_CUDA(cudaGetLastError());
+    read_ctl(s);
+    float ms = 0.f;
+    TV3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    fill_info(info, ms / 1000.0);
+}
+
+// ---------------------------------------------------------------------------
+// solver state: the control block and every workspace vector, so a solve
+// stopped at its iteration limit can be continued later (here or in another
+// process) exactly as if it had not stopped
+// ---------------------------------------------------------------------------
+namespace {
+struct StateHeader {
+    char magic[8];
+    unsigned version, elem_size;
+    long long n, m, nv_len, mv_len, last_len;
+    int p, q, r, L;
+};
+}  // namespace
+
+template <class T>
+size_t Solver<T>::state_bytes() const {
+    return sizeof(StateHeader) + sizeof(Ctl) + (nv.n + mv.n + last_Au.n) * sizeof(T);
+}
+
+template <class T>
+void Solver<T>::save_state(void* host, cudaStream_t s) {
+    StateHeader h{};
+    std::memcpy(h.magic, "TVAL3ST", 8);
+    h.version = 1;
+    h.elem_size = sizeof(T);
+    h.n = n; h.m = m; h.nv_len = (long long)nv.n; h.mv_len = (long long)mv.n; h.last_len = (long long)last_Au.n;
+    h.p = p; h.q = q; h.r = r; h.L = L;
+    char* c = static_cast<char*>(host);
+    std::memcpy(c, &h, sizeof(h));
+    c += sizeof(h);
+    TV3_CUDA(cudaMemcpyAsync(c, ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    c += sizeof(Ctl);
+    TV3_CUDA(cudaMemcpyAsync(c, nv.p, nv.n * sizeof(T), cudaMemcpyDeviceToHost, s));
+    c += nv.n * sizeof(T);
+    if (mv.n) TV3_CUDA(cudaMemcpyAsync(c, mv.p, mv.n * sizeof(T), cudaMemcpyDeviceToHost, s));
+    c += mv.n * sizeof(T);
+    if (last_Au.n) TV3_CUDA(cudaMemcpyAsync(c, last_Au.p, last_Au.n * sizeof(T), cudaMemcpyDeviceToHost, s));
+    TV3_CUDA(cudaStreamSynchronize(s));
+}
+
+template <class T>
+void Solver<T>::resume(const void* host, void* d_U, const void* d_Ut, tval3_info* info, cudaStream_t s) {
+    StateHeader h;
+    std::memcpy(&h, host, sizeof(h));
+    if (std::memcmp(h.magic, "TVAL3ST", 8) != 0 || h.version != 1)
+        throw Error{TVAL3_ERR_ARG, "Argument error: not a solver state!"};
+    if (h.elem_size != sizeof(T) || h.n != n || h.m != m || h.nv_len != (long long)nv.n ||
+        h.mv_len != (long long)mv.n || h.last_len != (long long)last_Au.n || h.p != p || h.q != q || h.r != r ||
+        h.L != L)
+        throw Error{TVAL3_ERR_SHAPE, "Argument error: the state belongs to a solver of another shape or type!"};
+    const char* c = static_cast<const char*>(host) + sizeof(h);
+    TV3_CUDA(cudaMemcpyAsync(ctl.p, c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    c += sizeof(Ctl);
+    TV3_CUDA(cudaMemcpyAsync(nv.p, c, nv.n * sizeof(T), cudaMemcpyHostToDevice, s));
+    c += nv.n * sizeof(T);
+    if (mv.n) TV3_CUDA(cudaMemcpyAsync(mv.p, c, mv.n * sizeof(T), cudaMemcpyHostToDevice, s));
+    c += mv.n * sizeof(T);
+    if (last_Au.n) TV3_CUDA(cudaMemcpyAsync(last_Au.p, c, last_Au.n * sizeof(T), cudaMemcpyHostToDevice, s));
+    B.xstar = nullptr;
+    cudaEvent_t e0, e1;
+    TV3_CUDA(cudaEventCreate(&e0));
+    TV3_CUDA(cudaEventCreate(&e1));
+    TV3_CUDA(cudaEventRecord(e0, s));
+    if (mode == 1) {
+        if (!rexec || r_U != d_U || r_Ut != d_Ut) {
+            if (rexec) cudaGraphExecDestroy(rexec);
+            rexec = nullptr;
+            cudaGraph_t top;
+            TV3_CUDA(cudaGraphCreate(&top, 0));
+            cudaStream_t cs;
+            TV3_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+            try {
+                add_to_graph(top, nullptr, d_U, d_Ut, cs, true);
+                TV3_CUDA(cudaGraphInstantiate(&rexec, top, 0));
+            } catch (...) {
+                cudaStreamDestroy(cs);
+                cudaGraphDestroy(top);
+                throw;
+            }
+            cudaStreamDestroy(cs);
+            cudaGraphDestroy(top);
+            r_U = d_U;
+            r_Ut = d_Ut;
+        }
+        TV3_CUDA(cudaGraphLaunch(rexec, s));
+    } else {
+        B.use_graph = 0;
+        k_resume_ctl<<<1, 1, 0, s>>>(B.ctl, o.maxit, o.maxcnt, pause_at > 0 ? pause_at : 0x7fffffff);
+        read_ctl(s);
+        if (!hctl->done) run_host(s);
         launch_finalize<T>(B, d_U, d_Ut, s);
     }
     TV3_CUDA(cudaEventRecord(e1, s));

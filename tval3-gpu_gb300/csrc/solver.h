@@ -26,6 +26,7 @@ struct Solver {
     Ctl* hctl = nullptr;  // pinned mirror of the control block
     SolverBufs<T> B{};
     int mode = 0;         // 0: host-driven loop, 1: CUDA graph with conditional nodes
+    int pause_at = 0;     // > 0: stop after this many total iterations, resumable
     const void* xstar = nullptr;  // caller-type reference solution for the error trace
     // graph of the whole solve (mode 1), rebuilt when its inputs change
     cudaGraphExec_t gexec = nullptr;
@@ -34,6 +35,9 @@ struct Solver {
     const void* g_Ut = nullptr;
     cudaStream_t g_stream = nullptr;
     cudaGraph_t g_top = nullptr;  // the graph being built by add_to_graph
+    cudaGraphExec_t rexec = nullptr;  // resume graph (mode 1)
+    void* r_U = nullptr;
+    const void* r_Ut = nullptr;
 
     Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_, int L_ = 1);
     ~Solver();
@@ -41,8 +45,14 @@ struct Solver {
     // (float for float vectors, double for double and double-float vectors)
     void solve(const void* d_b, void* d_U, const void* d_Ut, tval3_info* info, cudaStream_t s);
     void read_trace(double* host, int len);
-    // the whole solve as an independent branch of `top` (mode 1 form)
-    void add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const void* d_Ut, cudaStream_t cs);
+    // the whole solve as an independent branch of `top` (mode 1 form); with
+    // resume, the loop continues from the current state instead of set-up
+    void add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const void* d_Ut, cudaStream_t cs,
+                      bool resume = false);
+    // solver state (control block and workspace) to host memory and back
+    size_t state_bytes() const;
+    void save_state(void* host, cudaStream_t s);
+    void resume(const void* host, void* d_U, const void* d_Ut, tval3_info* info, cudaStream_t s);
     // enqueue the copy of the control block to its pinned mirror; after the
     // stream is synchronised, fill_info reports it
     void fetch_ctl(cudaStream_t s);

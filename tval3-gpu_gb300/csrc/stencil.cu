@@ -81,6 +81,31 @@ __device__ __forceinline__ Nb neighbours(const Geo& g, long i) {
 
 #define GRID_STRIDE(i, N) for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < (N); i += (long)gridDim.x * blockDim.x)
 
+// Two consecutive elements with one 16-byte (8-byte for float) load or store:
+// the pass-per-vector kernels move 150 MB-sized sets where wide, streaming
+// accesses reach ~1.5x the bandwidth of 8-byte ones.  Used when every vector
+// offset is even (n even), so all pair addresses are aligned.
+template <class T> struct Two { T a, b; };
+__device__ __forceinline__ Two<float> ld2(const float* p) {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    return {v.x, v.y};
+}
+__device__ __forceinline__ Two<double> ld2(const double* p) {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    return {v.x, v.y};
+}
+__device__ __forceinline__ Two<df64> ld2(const df64* p) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    return {df64(v.x, v.y), df64(v.z, v.w)};
+}
+__device__ __forceinline__ void st2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
+__device__ __forceinline__ void st2(double* p, double a, double b) { *reinterpret_cast<double2*>(p) = make_double2(a, b); }
+__device__ __forceinline__ void st2(df64* p, df64 a, df64 b) {
+    *reinterpret_cast<float4*>(p) = make_float4(a.hi, a.lo, b.hi, b.lo);
+}
+#define GRID_STRIDE_PAIRS(i, N) \
+    for (long i = 2 * ((long)blockIdx.x * blockDim.x + threadIdx.x); i < (N); i += 2 * (long)gridDim.x * blockDim.x)
+
 template <class T> __device__ __forceinline__ T proj(T v, int nonneg) { return (nonneg && v < T(0)) ? T(0) : v; }
 
 // x / beta: division as in the reference for float and double; for df64 the
@@ -189,16 +214,38 @@ __global__ void k_descend(SolverBufs<T> B, Geo g, int restart) {
     T* __restrict__ DU = B.DU[dst];
     const T mt = scal<T>(-ctl->tau);
     const int nn = ctl->nonneg;
-    GRID_STRIDE(i, B.n) {
-        Nb nb = neighbours(g, i);
-        T uc = proj(Up[i] + mt * d[i], nn);
-        T uy = proj(Up[nb.yp] + mt * d[nb.yp], nn);
-        T ux = proj(Up[nb.xp] + mt * d[nb.xp], nn);
-        T uz = proj(Up[nb.zp] + mt * d[nb.zp], nn);
-        U[i] = uc;
-        DU[i] = uy - uc;
-        DU[B.n + i] = ux - uc;
-        DU[2 * B.n + i] = uz - uc;
+    const long n = B.n;
+    if (g.l.d == 1 && (g.p.d % 2) == 0) {
+        // voxel pairs (i, i+1) with y even: they share x and z, so their +x
+        // and +z neighbours are pairs too and the +y neighbour of i is i+1
+        GRID_STRIDE_PAIRS(i, n) {
+            const Nb nb = neighbours(g, i);
+            const Two<T> u0 = ld2(Up + i), d0 = ld2(d + i);
+            const T uca = proj(u0.a + mt * d0.a, nn), ucb = proj(u0.b + mt * d0.b, nn);
+            const unsigned ya = (unsigned)i - fdiv((unsigned)i, g.p) * g.p.d;  // even, <= p - 2
+            const long yb = (ya + 2 < g.p.d) ? i + 2 : i + 2 - (long)g.p.d;     // +y neighbour of i+1
+            const T uyb = proj(Up[yb] + mt * d[yb], nn);
+            const Two<T> ux = ld2(Up + nb.xp), dx = ld2(d + nb.xp);
+            const Two<T> uz = ld2(Up + nb.zp), dz = ld2(d + nb.zp);
+            const T uxa = proj(ux.a + mt * dx.a, nn), uxb = proj(ux.b + mt * dx.b, nn);
+            const T uza = proj(uz.a + mt * dz.a, nn), uzb = proj(uz.b + mt * dz.b, nn);
+            st2(U + i, uca, ucb);
+            st2(DU + i, ucb - uca, uyb - ucb);
+            st2(DU + n + i, uxa - uca, uxb - ucb);
+            st2(DU + 2 * n + i, uza - uca, uzb - ucb);
+        }
+    } else {
+        GRID_STRIDE(i, n) {
+            Nb nb = neighbours(g, i);
+            T uc = proj(Up[i] + mt * d[i], nn);
+            T uy = proj(Up[nb.yp] + mt * d[nb.yp], nn);
+            T ux = proj(Up[nb.xp] + mt * d[nb.xp], nn);
+            T uz = proj(Up[nb.zp] + mt * d[nb.zp], nn);
+            U[i] = uc;
+            DU[i] = uy - uc;
+            DU[n + i] = ux - uc;
+            DU[2 * n + i] = uz - uc;
+        }
     }
     if (!restart) {
         double v[1] = {0.0}, tot[1];
@@ -257,21 +304,36 @@ __global__ void k_g2(SolverBufs<T> B, Geo g, int mode) {
     const T* __restrict__ S = B.sig;
     T* __restrict__ g2 = B.g2[cur];
     ProdAcc<T> l2, l4;
-    GRID_STRIDE(i, n) {
-        T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
-        if (WITH_G2) {
-            Nb nb = neighbours(g, i);
-            T v0m = DU[nb.ym] - W[nb.ym];
-            T v1m = DU[n + nb.xm] - W[n + nb.xm];
-            T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
-            g2[i] = v0m - v0 + v1m - v1 + v2m - v2;
+    if (!WITH_G2 && (n % 2) == 0) {
+        // lam2 and lam4 only: a pure stream, two voxels per 16-byte access
+        GRID_STRIDE_PAIRS(i, n) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const Two<T> du = ld2(DU + c * n + i), w = ld2(W + c * n + i), sg = ld2(S + c * n + i);
+                const T va = du.a - w.a, vb = du.b - w.b;
+                l2.add(va, va);
+                l2.add(vb, vb);
+                l4.add(va, sg.a);
+                l4.add(vb, sg.b);
+            }
         }
-        l2.add(v0, v0);
-        l2.add(v1, v1);
-        l2.add(v2, v2);
-        l4.add(v0, S[i]);
-        l4.add(v1, S[n + i]);
-        l4.add(v2, S[2 * n + i]);
+    } else {
+        GRID_STRIDE(i, n) {
+            T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
+            if (WITH_G2) {
+                Nb nb = neighbours(g, i);
+                T v0m = DU[nb.ym] - W[nb.ym];
+                T v1m = DU[n + nb.xm] - W[n + nb.xm];
+                T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
+                g2[i] = v0m - v0 + v1m - v1 + v2m - v2;
+            }
+            l2.add(v0, v0);
+            l2.add(v1, v1);
+            l2.add(v2, v2);
+            l4.add(v0, S[i]);
+            l4.add(v1, S[n + i]);
+            l4.add(v2, S[2 * n + i]);
+        }
     }
     double v[2] = {l2.value(), l4.value()}, tot[2];
     if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
@@ -303,7 +365,7 @@ __global__ void k_g2(SolverBufs<T> B, Geo g, int mode) {
 // ---------------------------------------------------------------------------
 // shrinkage: W = shrink(DU - sigma/beta, 1/beta), lam1 = TV(W)
 // ---------------------------------------------------------------------------
-template <class T>
+template <class T, bool PAIRS>
 __global__ void k_shrink(SolverBufs<T> B, int mode) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
@@ -316,29 +378,44 @@ __global__ void k_shrink(SolverBufs<T> B, int mode) {
     const T bt = scal<T>(ctl->beta), ib = scal<T>(1.0 / ctl->beta);
     const int iso = ctl->iso;
     A l1(0.f);
-    GRID_STRIDE(i, n) {
-        T u0 = DU[i] - div_beta(S[i], bt, ib);
-        T u1 = DU[n + i] - div_beta(S[n + i], bt, ib);
-        T u2 = DU[2 * n + i] - div_beta(S[2 * n + i], bt, ib);
+    // one voxel: v = DU - sigma/beta -> W, adding its TV term to l1
+    auto voxel = [&](T d0, T d1, T d2, T s0, T s1, T s2, T& w0, T& w1, T& w2) {
+        T u0 = d0 - div_beta(s0, bt, ib);
+        T u1 = d1 - div_beta(s1, bt, ib);
+        T u2 = d2 - div_beta(s2, bt, ib);
         if (!iso) {
             T t0 = fabs(u0) - ib, t1 = fabs(u1) - ib, t2 = fabs(u2) - ib;
             t0 = (t0 >= T(0)) ? t0 : T(0);
             t1 = (t1 >= T(0)) ? t1 : T(0);
             t2 = (t2 >= T(0)) ? t2 : T(0);
-            W[i] = (u0 >= T(0)) ? t0 : -t0;
-            W[n + i] = (u1 >= T(0)) ? t1 : -t1;
-            W[2 * n + i] = (u2 >= T(0)) ? t2 : -t2;
+            w0 = (u0 >= T(0)) ? t0 : -t0;
+            w1 = (u1 >= T(0)) ? t1 : -t1;
+            w2 = (u2 >= T(0)) ? t2 : -t2;
             l1 += to_acc(t0) + to_acc(t1) + to_acc(t2);
         } else {
             T nv = sqrt(u0 * u0 + u1 * u1 + u2 * u2);
             T t = nv - ib;
             t = (t > T(0)) ? t : T(0);
             T sc = (t > T(0)) ? t / nv : T(0);
-            W[i] = u0 * sc;
-            W[n + i] = u1 * sc;
-            W[2 * n + i] = u2 * sc;
+            w0 = u0 * sc;
+            w1 = u1 * sc;
+            w2 = u2 * sc;
             l1 += to_acc(t);
         }
+    };
+    if (PAIRS) {
+        GRID_STRIDE_PAIRS(i, n) {
+            const Two<T> d0 = ld2(DU + i), d1 = ld2(DU + n + i), d2 = ld2(DU + 2 * n + i);
+            const Two<T> s0 = ld2(S + i), s1 = ld2(S + n + i), s2 = ld2(S + 2 * n + i);
+            T a0, a1, a2, b0, b1, b2;
+            voxel(d0.a, d1.a, d2.a, s0.a, s1.a, s2.a, a0, a1, a2);
+            voxel(d0.b, d1.b, d2.b, s0.b, s1.b, s2.b, b0, b1, b2);
+            st2(W + i, a0, b0);
+            st2(W + n + i, a1, b1);
+            st2(W + 2 * n + i, a2, b2);
+        }
+    } else {
+        GRID_STRIDE(i, n) voxel(DU[i], DU[n + i], DU[2 * n + i], S[i], S[n + i], S[2 * n + i], W[i], W[n + i], W[2 * n + i]);
     }
     double v[1] = {acc_d(l1)}, tot[1];
     if (grid_reduce<1>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
@@ -439,7 +516,52 @@ __global__ void k_g2_gradient(SolverBufs<T> B, Geo geo) {
     ProdAcc<T> l2, l4;
     ProdAcc<A> s0, s1, s2, s4;
     double s3 = 0.0;
-    GRID_STRIDE(i, n) {
+    // the gradient part of one voxel, given its g2
+    auto grad = [&](long i, T g2i, T gi, T dtsi, T Ui, T Upi, T gpi, T g2pi, T& di) {
+        di = mdb * gi + g2i + dtsi;
+        const A ad = to_acc(di);
+        s2.add(ad, ad);
+        const A u = to_acc(Ui), up = to_acc(Upi);
+        const A du = u - up;
+        s0.add(up, up);
+        s1.add(du, du);
+        const A dg = to_acc(gi) - to_acc(gpi);
+        const A dg2 = to_acc(g2i) - to_acc(g2pi);
+        s4.add(du, dg2 + mdbA * dg);
+        if (xs) {
+            double e = acc_d(u) * iscl - (double)xs[i];
+            s3 += e * e;
+        }
+    };
+    if (geo.l.d == 1 && (geo.p.d % 2) == 0) {
+        // voxel pairs (i, i+1) with y even: -x and -z neighbours are pairs, the
+        // -y neighbour of i+1 is i
+        GRID_STRIDE_PAIRS(i, n) {
+            const Nb nb = neighbours(geo, i);
+            Two<T> va[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const Two<T> du = ld2(DU + c * n + i), w = ld2(W + c * n + i), sg = ld2(S + c * n + i);
+                va[c] = {du.a - w.a, du.b - w.b};
+                l2.add(va[c].a, va[c].a);
+                l2.add(va[c].b, va[c].b);
+                l4.add(va[c].a, sg.a);
+                l4.add(va[c].b, sg.b);
+            }
+            const T v0m = DU[nb.ym] - W[nb.ym];
+            const Two<T> dxm = ld2(DU + n + nb.xm), wxm = ld2(W + n + nb.xm);
+            const Two<T> dzm = ld2(DU + 2 * n + nb.zm), wzm = ld2(W + 2 * n + nb.zm);
+            const T g2a = v0m - va[0].a + (dxm.a - wxm.a) - va[1].a + (dzm.a - wzm.a) - va[2].a;
+            const T g2b = va[0].a - va[0].b + (dxm.b - wxm.b) - va[1].b + (dzm.b - wzm.b) - va[2].b;
+            st2(g2o + i, g2a, g2b);
+            const Two<T> gi = ld2(g + i), dt = ld2(dts + i), u = ld2(U + i), up = ld2(Up + i);
+            const Two<T> gpi = ld2(gp + i), g2pi = ld2(g2p + i);
+            T da, db;
+            grad(i, g2a, gi.a, dt.a, u.a, up.a, gpi.a, g2pi.a, da);
+            grad(i + 1, g2b, gi.b, dt.b, u.b, up.b, gpi.b, g2pi.b, db);
+            st2(d + i, da, db);
+        }
+    } else GRID_STRIDE(i, n) {
         const Nb nb = neighbours(geo, i);
         const T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
         const T v0m = DU[nb.ym] - W[nb.ym];
@@ -453,22 +575,9 @@ __global__ void k_g2_gradient(SolverBufs<T> B, Geo geo) {
         l4.add(v0, S[i]);
         l4.add(v1, S[n + i]);
         l4.add(v2, S[2 * n + i]);
-        const T gi = g[i];
-        const T di = mdb * gi + g2i + dts[i];
+        T di;
+        grad(i, g2i, g[i], dts[i], U[i], Up[i], gp[i], g2p[i], di);
         d[i] = di;
-        const A ad = to_acc(di);
-        s2.add(ad, ad);
-        const A u = to_acc(U[i]), up = to_acc(Up[i]);
-        const A du = u - up;
-        s0.add(up, up);
-        s1.add(du, du);
-        const A dg = to_acc(gi) - to_acc(gp[i]);
-        const A dg2 = to_acc(g2i) - to_acc(g2p[i]);
-        s4.add(du, dg2 + mdbA * dg);
-        if (xs) {
-            double e = acc_d(u) * iscl - (double)xs[i];
-            s3 += e * e;
-        }
     }
     double v[7] = {l2.value(), l4.value(), s0.value(), s1.value(), s2.value(), s3, s4.value()}, tot[7];
     if (grid_reduce<7>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
@@ -486,7 +595,9 @@ __global__ void k_g2_gradient(SolverBufs<T> B, Geo geo) {
         ctl->relchg = sqrt(tot[3]) / ctl->nrmup;
         if (B.trace && xs) B.trace[ctl->count_total] = sqrt(tot[5]);
         ctl->count_total += 1;
-        ctl->inner_break = ((ctl->relchg < ctl->tol_inn) && !ctl->fst) || (ctl->count_total >= ctl->maxit);
+        const int natural = ((ctl->relchg < ctl->tol_inn) && !ctl->fst) || (ctl->count_total >= ctl->maxit);
+        ctl->paused = !natural && (ctl->count_total >= ctl->pause_at);
+        ctl->inner_break = natural || ctl->paused;
         ctl->fst = 0;
         if (B.use_graph) cudaGraphSetConditional(B.h_inner, ctl->inner_break ? 0u : 1u);
     }
@@ -629,6 +740,15 @@ __global__ void k_outer_relchg(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     using A = acc_t<T>;
+    if (ctl->paused) {
+        // stopped by the pause limit in the middle of an outer iteration: the
+        // outer step is left for the resumed solve
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            ctl->done = 1;
+            if (B.use_graph) cudaGraphSetConditional(B.h_mlp, 0u);
+        }
+        return;
+    }
     const T* __restrict__ U = B.U[ctl->parity];
     T* __restrict__ R = B.rcdU;
     A s(0.f);
@@ -903,7 +1023,8 @@ template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s) {
     else k_g2<T, true><<<B.grid, 256, 0, s>>>(B, geo_of(B), mode);
 }
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s) {
-    k_shrink<T><<<B.grid, 256, 0, s>>>(B, mode);
+    if (B.n % 2 == 0) k_shrink<T, true><<<B.grid, 256, 0, s>>>(B, mode);
+    else k_shrink<T, false><<<B.grid, 256, 0, s>>>(B, mode);
 }
 template <class T> void launch_g2_gradient(SolverBufs<T>& B, cudaStream_t s) {
     k_g2_gradient<T><<<B.grid, 256, 0, s>>>(B, geo_of(B));

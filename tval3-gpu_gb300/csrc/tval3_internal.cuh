@@ -135,6 +135,9 @@ struct Ctl {
     unsigned num_init, cur_init;
     int do_mult;       // 1: this get_g forms A^T Au; 0: it keeps the current g
     int products_T;    // A^T products formed by get_g
+    // pausing: the solve stops after pause_at total iterations without ending
+    // the outer iteration, so a saved state resumes exactly
+    int pause_at, paused;
 };
 
 // every solver kernel counts itself once (block 0, thread 0)

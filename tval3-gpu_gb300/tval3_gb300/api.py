@@ -365,6 +365,25 @@ class Solver:
                                         _stream(stream)))
         return info.as_dict()
 
+    def set_pause(self, iterations: int):
+        """Stop solves (resumably) after this many total iterations; 0 = never."""
+        check(load().tval3_solver_set_pause(self._h, int(iterations)))
+
+    def save_state(self, stream=None) -> bytes:
+        """The solver's state after a solve (checkpoint), as bytes."""
+        size = C.c_size_t()
+        check(load().tval3_solver_state_size(self._h, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        check(load().tval3_solver_save_state(self._h, buf, _stream(stream)))
+        return buf.raw
+
+    def resume(self, state: bytes, U_dev, Ut_dev=None, stream=None) -> dict:
+        """Continue a saved state under this solver's iteration limits."""
+        info = Info()
+        buf = C.create_string_buffer(bytes(state), len(state))
+        check(load().tval3_solver_resume(self._h, buf, _ptr(U_dev), _ptr(Ut_dev), C.byref(info), _stream(stream)))
+        return info.as_dict()
+
     def close(self):
         if self._h:
             load().tval3_solver_destroy(self._h)

@@ -111,6 +111,10 @@ _SIG = {
     "tval3_solver_create_layers": (_I, [_P, _P, _I, _I, _I, _I, _P]),
     "tval3_solver_set_mode": (_I, [_P, _I]),
     "tval3_solver_solve": (_I, [_P, _P, _P, _P, _P, _P]),
+    "tval3_solver_set_pause": (_I, [_P, _I]),
+    "tval3_solver_state_size": (_I, [_P, _P]),
+    "tval3_solver_save_state": (_I, [_P, _P, _P]),
+    "tval3_solver_resume": (_I, [_P, _P, _P, _P, _P, _P]),
     "tval3_solver_set_trace": (_I, [_P, _P]),
     "tval3_solver_trace": (_I, [_P, _P, _I]),
     "tval3_solver_destroy": (_I, [_P]),
