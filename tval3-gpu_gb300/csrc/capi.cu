@@ -3,8 +3,10 @@
 // 1351-1380), converts internal errors to a status code plus a thread-local
 // message (the reference throws tval3_gpu_exception, :1439-1445), and runs on
 // the caller's current device.
+#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <thread>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -83,6 +85,34 @@ struct HostVec {
     T* p = nullptr;
 };
 
+// true when pred(k) holds for every k in [0, n); large ranges are split over
+// the host's cores (input validation of 10^7-10^8 nonzeros)
+template <class F>
+bool all_of_range(long n, F pred) {
+    const long chunk = 1L << 20;
+    if (n <= 4 * chunk) {
+        for (long k = 0; k < n; ++k)
+            if (!pred(k)) return false;
+        return true;
+    }
+    const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    std::atomic<bool> ok{true};
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < hw; ++t)
+        th.emplace_back([&, t] {
+            for (long k = (long)t * chunk; k < n && ok.load(std::memory_order_relaxed); k += (long)hw * chunk) {
+                const long e = std::min(n, k + chunk);
+                for (long j = k; j < e; ++j)
+                    if (!pred(j)) {
+                        ok = false;
+                        return;
+                    }
+            }
+        });
+    for (auto& x : th) x.join();
+    return ok;
+}
+
 void check_sparse(const tval3_sparse_host* A) {
     if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
     if (A->rows < 0 || A->cols < 0 || A->nnz < 0) arg_error(TVAL3_ERR_SHAPE, "Argument error: negative matrix size!");
@@ -94,20 +124,19 @@ void check_sparse(const tval3_sparse_host* A) {
             arg_error(TVAL3_ERR_ARG, std::string("Argument error: missing ") + what + " arrays!");
         if (ptr[0] != 0 || ptr[rows] != A->nnz)
             arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: inconsistent ") + what + " pointer array!");
-        for (long r = 0; r < rows; ++r)
-            if (ptr[r + 1] < ptr[r]) arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: decreasing ") + what + " pointers!");
-        for (long k = 0; k < A->nnz; ++k)
-            if (ind[k] < 0 || ind[k] >= cols)
-                arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: ") + what + " index out of range!");
+        if (!all_of_range(rows, [&](long r) { return ptr[r + 1] >= ptr[r]; }))
+            arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: decreasing ") + what + " pointers!");
+        if (!all_of_range(A->nnz, [&](long k) { return ind[k] >= 0 && ind[k] < cols; }))
+            arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: ") + what + " index out of range!");
+        bool fin;
         if (A->val_type == TVAL3_PREC_FP32) {
             const float* v = (const float*)val;
-            for (long k = 0; k < A->nnz; ++k)
-                if (!std::isfinite(v[k])) arg_error(TVAL3_ERR_NONFINITE, "Argument error: non-finite matrix value!");
+            fin = all_of_range(A->nnz, [&](long k) { return std::isfinite(v[k]); });
         } else {
             const double* v = (const double*)val;
-            for (long k = 0; k < A->nnz; ++k)
-                if (!std::isfinite(v[k])) arg_error(TVAL3_ERR_NONFINITE, "Argument error: non-finite matrix value!");
+            fin = all_of_range(A->nnz, [&](long k) { return std::isfinite(v[k]); });
         }
+        if (!fin) arg_error(TVAL3_ERR_NONFINITE, "Argument error: non-finite matrix value!");
     };
     if (A->format & TVAL3_SPARSE_CSR) chk(A->csr_ptr, A->csr_ind, A->csr_val, A->rows, A->cols, "CSR");
     if (A->format & TVAL3_SPARSE_CSC) chk(A->csc_ptr, A->csc_ind, A->csc_val, A->cols, A->rows, "CSC");
@@ -130,11 +159,43 @@ void to_device(DBuf<T>& d, const void* h, long n, int src_type) {
     }
 }
 
-// device operator from a host sparse matrix
+// device operator from a host sparse matrix.  FP32 values under FP64 vectors
+// (TVAL3_PREC_FP32_F64VEC) go up as FP32 and stay FP32.  tune = false skips
+// the lane timing (an operator that only backs a double-float view).
 template <class T>
-LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision) {
+LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision, bool tune = true) {
     check_sparse(A);
     const long m = A->rows, n = A->cols, nnz = A->nnz;
+    if constexpr (std::is_same<T, double>::value) {
+        if (precision == TVAL3_PREC_FP32_F64VEC && A->val_type == TVAL3_PREC_FP32) {
+            DBuf<int> ptr, ind, tptr, tind;
+            DBuf<float> val, tval;
+            if (A->format & TVAL3_SPARSE_CSR) {
+                ptr.alloc(m + 1);
+                ind.alloc(std::max<long>(nnz, 1));
+                val.alloc(std::max<long>(nnz, 1));
+                TV3_CUDA(cudaMemcpy(ptr.p, A->csr_ptr, (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
+                if (nnz) TV3_CUDA(cudaMemcpy(ind.p, A->csr_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
+                if (nnz) TV3_CUDA(cudaMemcpy(val.p, A->csr_val, nnz * sizeof(float), cudaMemcpyHostToDevice));
+            }
+            if (A->format & TVAL3_SPARSE_CSC) {
+                tptr.alloc(n + 1);
+                tind.alloc(std::max<long>(nnz, 1));
+                tval.alloc(std::max<long>(nnz, 1));
+                TV3_CUDA(cudaMemcpy(tptr.p, A->csc_ptr, (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+                if (nnz) TV3_CUDA(cudaMemcpy(tind.p, A->csc_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
+                if (nnz) TV3_CUDA(cudaMemcpy(tval.p, A->csc_val, nnz * sizeof(float), cudaMemcpyHostToDevice));
+            }
+            if (!(A->format & TVAL3_SPARSE_CSR)) {
+                ptr.alloc(m + 1);
+                ind.alloc(std::max<long>(nnz, 1));
+                val.alloc(std::max<long>(nnz, 1));
+                csr_transpose_device<float>(n, m, nnz, tptr.p, tind.p, tval.p, ptr.p, ind.p, val.p, 0);
+            }
+            return make_csr_op_f64vec(m, n, nnz, ptr.p, ind.p, val.p, tptr.p, tptr.p ? tind.p : nullptr,
+                                      tptr.p ? tval.p : nullptr, 0, tune);
+        }
+    }
     DBuf<int> ptr, ind, tptr, tind;
     DBuf<T> val, tval;
     cudaStream_t s = 0;
@@ -291,7 +352,7 @@ tval3_status tval3_gpu_3d_sparse_f64(double* U, int dim_y, int dim_x, int dim_z,
         const int prec = (A->val_type == TVAL3_PREC_FP32) ? TVAL3_PREC_FP32_F64VEC : TVAL3_PREC_FP64;
         if (prec == TVAL3_PREC_FP32_F64VEC && opts->precision == TVAL3_PREC_FP32_DF64) {
             // double-float solve over the FP32 matrix; FP64 at the interface
-            std::unique_ptr<LinOp<double>> base(sparse_op<double>(A, prec));
+            std::unique_ptr<LinOp<double>> base(sparse_op<double>(A, prec, false));
             solve_host<df64>(make_df64_view(base.get()), U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len, info,
                              t0);
             return;
@@ -403,7 +464,7 @@ tval3_status tval3_op_create_sparse(tval3_op* op, const tval3_sparse_host* A, in
             h->precision = precision;
             if (precision == TVAL3_PREC_FP32_DF64) {
                 h->dbl = 1;
-                h->d = sparse_op<double>(A, TVAL3_PREC_FP32_F64VEC);
+                h->d = sparse_op<double>(A, TVAL3_PREC_FP32_F64VEC, false);
                 h->q = make_df64_view(h->d);
             } else if (precision == TVAL3_PREC_FP64 || precision == TVAL3_PREC_FP32_F64VEC) {
                 h->dbl = 1;
@@ -452,7 +513,7 @@ tval3_status tval3_op_create_geometry(tval3_op* op, const tval3_geometry_host* G
             h->precision = precision;
             if (precision == TVAL3_PREC_FP32_F64VEC || precision == TVAL3_PREC_FP32_DF64) {
                 h->dbl = 1;
-                h->d = make_geometry_op<double>(G, mode, TVAL3_PREC_FP32_F64VEC, 0);
+                h->d = make_geometry_op<double>(G, mode, precision, 0);
                 if (precision == TVAL3_PREC_FP32_DF64) h->q = make_df64_view(h->d);
             } else {
                 h->f = make_geometry_op<float>(G, mode, precision, 0);

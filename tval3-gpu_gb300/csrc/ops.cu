@@ -374,12 +374,12 @@ static void tune_lanes(CsrOp<T, V>* op) {
 }
 
 template <class T, class V>
-static void finish_layout(CsrOp<T, V>* op) {
+static void finish_layout(CsrOp<T, V>* op, bool tune = true) {
     op->Gn = pick_lanes(op->m ? (double)op->nnz / op->m : 0.0);
     op->Gt = pick_lanes(op->n ? (double)op->nnz / op->n : 0.0);
     op->grid_n = spmv_grid(op->m, op->Gn);
     op->grid_t = spmv_grid(op->n, op->Gt);
-    if (op->nnz >= (1L << 22)) tune_lanes(op);
+    if (tune && op->nnz >= (1L << 22)) tune_lanes(op);
 }
 
 // Build from device arrays (FP32 values for the FP32/BF16/FP16 precisions,
@@ -411,7 +411,7 @@ void export_vals<double, float>(const CsrOp<double, float>& op, float* hval, flo
 // operator, the products, vectors and reductions are FP64.
 LinOp<double>* make_csr_op_f64vec(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind,
                                   const float* d_val, const int* d_tptr, const int* d_tind, const float* d_tval,
-                                  cudaStream_t s) {
+                                  cudaStream_t s, bool tune) {
     auto* op = new CsrOp<double, float>();
     try {
         copy_structure<double>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
@@ -428,7 +428,7 @@ LinOp<double>* make_csr_op_f64vec(long rows, long cols, long nnz, const int* d_p
             csr_transpose_device<float>(rows, cols, nnz, op->ptr.p, op->ind.p, op->val.p, op->tptr.p, op->tind.p,
                                         op->tval.p, s);
         }
-        finish_layout(op);
+        finish_layout(op, tune);
     } catch (...) {
         delete op;
         throw;
@@ -491,7 +491,7 @@ LinOp<double>* make_csr_op_device<double>(long rows, long cols, long nnz, const 
         if (nnz && d_tptr) k_convert<double, float><<<ew(nnz), 256, 0, s>>>(nnz, d_tval, tv.p);
         TV3_CUDA(cudaGetLastError());
         TV3_CUDA(cudaStreamSynchronize(s));
-        return make_csr_op_f64vec(rows, cols, nnz, d_ptr, d_ind, v.p, d_tptr, d_tind, d_tptr ? tv.p : nullptr, s);
+        return make_csr_op_f64vec(rows, cols, nnz, d_ptr, d_ind, v.p, d_tptr, d_tind, d_tptr ? tv.p : nullptr, s, true);
     }
     auto* op = new CsrOp<double, double>();
     try {

@@ -133,7 +133,7 @@ LinOp<T>* make_csr_op_device(long rows, long cols, long nnz, const int* d_ptr, c
 // FP32 stored values, FP64 vectors (precision TVAL3_PREC_FP32_F64VEC).
 LinOp<double>* make_csr_op_f64vec(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind,
                                   const float* d_val, const int* d_tptr, const int* d_tind, const float* d_tval,
-                                  cudaStream_t s);
+                                  cudaStream_t s, bool tune = true);
 
 // Double-float products over the arrays of an FP32-value / FP64-vector CSR
 // operator (precision TVAL3_PREC_FP32_DF64); the view does not own the arrays.

@@ -491,10 +491,13 @@ LinOp<float>* make_geometry_op<float>(const void* gh, int mode, int precision, c
 
 template <>
 LinOp<double>* make_geometry_op<double>(const void* gh, int mode, int precision, cudaStream_t s) {
-    if (mode != 0 || precision != 4)
+    // precision 4: FP64-vector products; 5: the storage behind a double-float
+    // view, which runs no products of its own (so no lane timing)
+    if (mode != 0 || (precision != 4 && precision != 5))
         throw Error{7, "FP64-vector geometry operators are stored (mode 0) with FP32 values"};
     RayCsr c = build_ray_csr(static_cast<const tval3_geometry_host*>(gh), s);
-    return make_csr_op_f64vec(c.m, c.n, c.nnz, c.ptr.p, c.ind.p, c.val.p, nullptr, nullptr, nullptr, s);
+    return make_csr_op_f64vec(c.m, c.n, c.nnz, c.ptr.p, c.ind.p, c.val.p, nullptr, nullptr, nullptr, s,
+                              precision == 4);
 }
 
 }  // namespace tv3
