@@ -354,10 +354,10 @@ static void tune_lanes(CsrOp<T, V>* op) {
             else { op->Gn = G; op->grid_n = spmv_grid(m, lanes); }
             MatIO<T> io = plain_io<T>(x.p, y.p);
             op->apply(trans, io, SPMV_PLAIN, 0);
-            float ms = 1e30f;  // best of three rounds of three launches
-            for (int round = 0; round < 3; ++round) {
+            float ms = 1e30f;  // best of two rounds of two launches
+            for (int round = 0; round < 2; ++round) {
                 TV3_CUDA(cudaEventRecord(e0, 0));
-                for (int r = 0; r < 3; ++r) op->apply(trans, io, SPMV_PLAIN, 0);
+                for (int r = 0; r < 2; ++r) op->apply(trans, io, SPMV_PLAIN, 0);
                 TV3_CUDA(cudaEventRecord(e1, 0));
                 TV3_CUDA(cudaEventSynchronize(e1));
                 float t = 0.f;
