@@ -92,9 +92,11 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
         B.last_Au = last_Au.p;
     }
     // vector/reduction grid: about 1024 elements per block for small problems
-    // (so that many small solves can share the GPU), at most four blocks per
-    // SM (partials fit in `part`)
-    const long cap = std::max(1, std::min(num_sms() * 4, 8192));
+    // (so that many small solves can share the GPU), at most eight blocks of
+    // 256 threads per SM (a full SM); each launcher trims it further to the
+    // blocks its kernel can keep resident.  Partials of the widest reduction
+    // (10 values) fit in `part` up to 6,553 blocks.
+    const long cap = std::max(1, std::min(num_sms() * 8, 6553));
     B.grid = (int)std::max<long>(1, std::min<long>(cap, (std::max<long>(n, m) + 1023) / 1024));
     B.trace = trace.p;
 }

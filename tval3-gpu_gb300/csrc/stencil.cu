@@ -7,7 +7,9 @@
 // pipes); per-thread sums use acc_t<T>.
 //
 // Reference counterparts (3d/tval3_gpu_3d.cpp unless noted):
-//   k_D_only / k_descend   D_gpu :271-314 (+ axpy and nonneg_kernel, :671-701)
+//   k_D_only / k_descend   D_gpu :271-314 (+ axpy and nonneg_kernel, :671-701;
+//                          k_descend also lam2_4_kernel's sums at the new point)
+//   k_armijo               f and the Armijo test, min_u_gpu :848-858
 //   k_Dd_norm              get_tau_gpu first iteration :583-600
 //   k_gradient (BB step)   get_tau_kernel, 3d/tval3_gpu_3d_kernels.cu:1017-1067
 //   k_g2                   V = DU - W, lam2_4_kernel, Dt_gpu (get_g_gpu :484-571)
@@ -18,6 +20,9 @@
 //   k_mlp                  update_mlp_gpu :1034-1083 and continuation :1222-1237
 //   k_outer_grad           DtsAtd and get_gradient :1238-1249
 #include <math.h>
+#include <algorithm>
+#include <map>
+#include <mutex>
 #include "tval3_internal.cuh"
 #include "launch.h"
 
@@ -195,15 +200,18 @@ __global__ void k_D_only(SolverBufs<T> B, Geo g) {
 }
 
 // ---------------------------------------------------------------------------
-// descent step fused with D: U = P(Up - tau d), DU = D U.  U at the forward
-// neighbours is recomputed from Up and d (same expression, so bit-identical
-// to the stored value).  Normal mode reads the current slot, writes the other
+// descent step fused with D: U = P(Up - tau d), DU = D U, and the two terms
+// of the new point's Lagrangian that need DU: lam2 = ||DU - W||^2 and
+// lam4 = <sigma, DU - W> (get_g_gpu's lam2_4 pass, :528-547, done here while
+// DU is in registers instead of by a second pass over DU, W and sigma).  U at
+// the forward neighbours is recomputed from Up and d (same expression, so
+// bit-identical to the stored value).  Normal mode reads the current slot, writes the other
 // one and flips the parity (the previous values become Up, gp, g2p, Aup, DUp
 // without copies, :831-833); restart mode reads the previous slot (U = Up,
 // :878) and writes the current one.
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void k_descend(SolverBufs<T> B, Geo g, int restart) {
+__global__ void __launch_bounds__(256, 6) k_descend(SolverBufs<T> B, Geo g, int restart) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     const int cur = ctl->parity;
@@ -212,9 +220,12 @@ __global__ void k_descend(SolverBufs<T> B, Geo g, int restart) {
     const T* __restrict__ d = B.d;
     T* __restrict__ U = B.U[dst];
     T* __restrict__ DU = B.DU[dst];
+    const T* __restrict__ W = B.W;
+    const T* __restrict__ S = B.sig;
     const T mt = scal<T>(-ctl->tau);
     const int nn = ctl->nonneg;
     const long n = B.n;
+    ProdAcc<T> l2, l4;
     if (g.l.d == 1 && (g.p.d % 2) == 0) {
         // voxel pairs (i, i+1) with y even: they share x and z, so their +x
         // and +z neighbours are pairs too and the +y neighbour of i is i+1
@@ -229,10 +240,18 @@ __global__ void k_descend(SolverBufs<T> B, Geo g, int restart) {
             const Two<T> uz = ld2(Up + nb.zp), dz = ld2(d + nb.zp);
             const T uxa = proj(ux.a + mt * dx.a, nn), uxb = proj(ux.b + mt * dx.b, nn);
             const T uza = proj(uz.a + mt * dz.a, nn), uzb = proj(uz.b + mt * dz.b, nn);
+            const Two<T> dv[3] = {{ucb - uca, uyb - ucb}, {uxa - uca, uxb - ucb}, {uza - uca, uzb - ucb}};
             st2(U + i, uca, ucb);
-            st2(DU + i, ucb - uca, uyb - ucb);
-            st2(DU + n + i, uxa - uca, uxb - ucb);
-            st2(DU + 2 * n + i, uza - uca, uzb - ucb);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                st2(DU + c * n + i, dv[c].a, dv[c].b);
+                const Two<T> w = ld2(W + c * n + i), sg = ld2(S + c * n + i);
+                const T va = dv[c].a - w.a, vb = dv[c].b - w.b;
+                l2.add(va, va);
+                l2.add(vb, vb);
+                l4.add(va, sg.a);
+                l4.add(vb, sg.b);
+            }
         }
     } else {
         GRID_STRIDE(i, n) {
@@ -241,15 +260,22 @@ __global__ void k_descend(SolverBufs<T> B, Geo g, int restart) {
             T uy = proj(Up[nb.yp] + mt * d[nb.yp], nn);
             T ux = proj(Up[nb.xp] + mt * d[nb.xp], nn);
             T uz = proj(Up[nb.zp] + mt * d[nb.zp], nn);
+            const T dv[3] = {uy - uc, ux - uc, uz - uc};
             U[i] = uc;
-            DU[i] = uy - uc;
-            DU[n + i] = ux - uc;
-            DU[2 * n + i] = uz - uc;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                DU[c * n + i] = dv[c];
+                const T v = dv[c] - W[c * n + i];
+                l2.add(v, v);
+                l4.add(v, S[c * n + i]);
+            }
         }
     }
-    if (!restart) {
-        double v[1] = {0.0}, tot[1];
-        if (grid_reduce<1>(v, B.part, B.ticket, tot) && threadIdx.x == 0) ctl->parity = 1 - cur;
+    double v[2] = {l2.value(), l4.value()}, tot[2];
+    if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        ctl->lam2 = tot[0];
+        ctl->lam4 = tot[1];
+        if (!restart) ctl->parity = 1 - cur;
     }
 }
 
@@ -287,14 +313,13 @@ __device__ __forceinline__ void armijo(Ctl* c) {
 }
 
 // ---------------------------------------------------------------------------
-// g2 = D^T (DU - W) with lam2 = ||DU - W||^2 and lam4 = <sigma, DU - W>.
+// g2 = D^T (DU - W) with lam2 = ||DU - W||^2 and lam4 = <sigma, DU - W>
+// (start-up get_g; after a descent lam2 and lam4 come from k_descend and the
+// g2 of that point is replaced by update_W's before anything reads it, except
+// on the backtracking path, which forms its own with k_bt_g2).
 // ---------------------------------------------------------------------------
-// After a descent (and the restart's descent) only lam2 and lam4 are needed:
-// the g2 of that point is replaced by update_W's before anything reads it,
-// except on the backtracking path, which forms its own (k_bt_g2).  So those
-// calls (WITH_G2 = false) skip D^T and the g2 store.
-template <class T, bool WITH_G2>
-__global__ void k_g2(SolverBufs<T> B, Geo g, int mode) {
+template <class T>
+__global__ void k_g2(SolverBufs<T> B, Geo g) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     const int cur = ctl->parity;
@@ -304,61 +329,50 @@ __global__ void k_g2(SolverBufs<T> B, Geo g, int mode) {
     const T* __restrict__ S = B.sig;
     T* __restrict__ g2 = B.g2[cur];
     ProdAcc<T> l2, l4;
-    if (!WITH_G2 && (n % 2) == 0) {
-        // lam2 and lam4 only: a pure stream, two voxels per 16-byte access
-        GRID_STRIDE_PAIRS(i, n) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const Two<T> du = ld2(DU + c * n + i), w = ld2(W + c * n + i), sg = ld2(S + c * n + i);
-                const T va = du.a - w.a, vb = du.b - w.b;
-                l2.add(va, va);
-                l2.add(vb, vb);
-                l4.add(va, sg.a);
-                l4.add(vb, sg.b);
-            }
-        }
-    } else {
-        GRID_STRIDE(i, n) {
-            T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
-            if (WITH_G2) {
-                Nb nb = neighbours(g, i);
-                T v0m = DU[nb.ym] - W[nb.ym];
-                T v1m = DU[n + nb.xm] - W[n + nb.xm];
-                T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
-                g2[i] = v0m - v0 + v1m - v1 + v2m - v2;
-            }
-            l2.add(v0, v0);
-            l2.add(v1, v1);
-            l2.add(v2, v2);
-            l4.add(v0, S[i]);
-            l4.add(v1, S[n + i]);
-            l4.add(v2, S[2 * n + i]);
-        }
+    GRID_STRIDE(i, n) {
+        T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
+        Nb nb = neighbours(g, i);
+        T v0m = DU[nb.ym] - W[nb.ym];
+        T v1m = DU[n + nb.xm] - W[n + nb.xm];
+        T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
+        g2[i] = v0m - v0 + v1m - v1 + v2m - v2;
+        l2.add(v0, v0);
+        l2.add(v1, v1);
+        l2.add(v2, v2);
+        l4.add(v0, S[i]);
+        l4.add(v1, S[n + i]);
+        l4.add(v2, S[2 * n + i]);
     }
     double v[2] = {l2.value(), l4.value()}, tot[2];
     if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->lam2 = tot[0];
         ctl->lam4 = tot[1];
-        if (mode == EPI_G2_UPDATE_W) {
-            ctl->f += ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
-            // nonmonotone reference values (:1176-1177)
-            double Qp = ctl->Q;
-            ctl->Q = ctl->gam * Qp + 1.0;
-            ctl->C = (ctl->gam * Qp * ctl->C + ctl->f) / ctl->Q;
-        } else {
-            ctl->f = fval(ctl);
-            if (mode == EPI_G2_DESCEND) {
-                ctl->alpha = 1.0;
-                ctl->cnt = 0;
-                ctl->c_armij = ctl->dd * ctl->tau * ctl->c_arm * ctl->beta;
-                armijo(ctl);
-                if (ctl->armijo_fail) ctl->alpha *= ctl->gamma;
-                if (B.use_graph) cudaGraphSetConditional(B.h_arm, ctl->armijo_fail ? 1u : 0u);
-            } else {
-                ctl->armijo_fail = 0;
-                if (mode == EPI_G2_RESTART) ctl->restarts += 1;
-            }
-        }
+        ctl->f = fval(ctl);
+        ctl->armijo_fail = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The Lagrangian at a new point and, after a descent, the Armijo test
+// (:848-858): one thread, once A*U has supplied lam3 and lam5 (k_descend
+// supplied lam2 and lam4).  Sets the graph's Armijo IF condition.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_armijo(SolverBufs<T> B, int mode) {
+    Ctl* ctl = B.ctl;
+    count_launch(ctl);
+    if (threadIdx.x != 0) return;
+    ctl->f = fval(ctl);
+    if (mode == EPI_G2_DESCEND) {
+        ctl->alpha = 1.0;
+        ctl->cnt = 0;
+        ctl->c_armij = ctl->dd * ctl->tau * ctl->c_arm * ctl->beta;
+        armijo(ctl);
+        if (ctl->armijo_fail) ctl->alpha *= ctl->gamma;
+        if (B.use_graph) cudaGraphSetConditional(B.h_arm, ctl->armijo_fail ? 1u : 0u);
+    } else {
+        ctl->armijo_fail = 0;
+        if (mode == EPI_G2_RESTART) ctl->restarts += 1;
     }
 }
 
@@ -366,7 +380,7 @@ __global__ void k_g2(SolverBufs<T> B, Geo g, int mode) {
 // shrinkage: W = shrink(DU - sigma/beta, 1/beta), lam1 = TV(W)
 // ---------------------------------------------------------------------------
 template <class T, bool PAIRS>
-__global__ void k_shrink(SolverBufs<T> B, int mode) {
+__global__ void __launch_bounds__(256, 5) k_shrink(SolverBufs<T> B, int mode) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     using A = acc_t<T>;
@@ -495,7 +509,7 @@ __global__ void k_gradient(SolverBufs<T> B, int iter) {
 // the same thread, so the pass saves the store-and-reload of g2 and a launch.
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void k_g2_gradient(SolverBufs<T> B, Geo geo) {
+__global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     using A = acc_t<T>;
@@ -615,7 +629,7 @@ __global__ void k_g2_gradient(SolverBufs<T> B, Geo geo) {
 // :876-882).  k_bt_apply materialises the accepted point once.
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void k_bt_coef(SolverBufs<T> B) {
+__global__ void __launch_bounds__(256, 4) k_bt_coef(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     using A = acc_t<T>;
@@ -986,6 +1000,28 @@ int num_sms() {
     return g_sms;
 }
 
+// Blocks of a grid-stride reducing kernel (256 threads): `want` (about one per
+// 1,024 elements, so that small solves leave room for others), but never
+// more than can be resident at once.  A grid one wave larger than the GPU
+// holds runs its last partial wave at a fraction of the occupancy (608 blocks
+// of a kernel that fits 3 per SM took two full waves' time).
+static int resident_grid(const void* kernel, int want) {
+    static std::mutex mu;
+    static std::map<const void*, int> cap;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cap.find(kernel);
+    if (it == cap.end()) {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, 256, 0) != cudaSuccess || nb < 1) nb = 1;
+        it = cap.emplace(kernel, nb * num_sms()).first;
+    }
+    return std::max(1, std::min(want, it->second));
+}
+template <class... P, class... A>
+static void rlaunch(void (*kernel)(P...), int want, cudaStream_t s, A... args) {
+    kernel<<<resident_grid(reinterpret_cast<const void*>(kernel), want), 256, 0, s>>>(args...);
+}
+
 static int ew_grid(long n) {
     long g = (n + 255) / 256;
     long cap = (long)num_sms() * 16;
@@ -1013,41 +1049,41 @@ template <class T> void launch_D_only(SolverBufs<T>& B, cudaStream_t s) {
     k_D_only<T><<<ew_grid(B.n), 256, 0, s>>>(B, geo_of(B));
 }
 template <class T> void launch_descend(SolverBufs<T>& B, int restart, cudaStream_t s) {
-    k_descend<T><<<B.grid, 256, 0, s>>>(B, geo_of(B), restart);
+    rlaunch(k_descend<T>, B.grid, s, B, geo_of(B), restart);
 }
 template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s) {
-    k_Dd_norm<T><<<B.grid, 256, 0, s>>>(B, geo_of(B));
+    rlaunch(k_Dd_norm<T>, B.grid, s, B, geo_of(B));
 }
 template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s) {
-    if (mode == EPI_G2_DESCEND || mode == EPI_G2_RESTART) k_g2<T, false><<<B.grid, 256, 0, s>>>(B, geo_of(B), mode);
-    else k_g2<T, true><<<B.grid, 256, 0, s>>>(B, geo_of(B), mode);
+    if (mode == EPI_G2_DESCEND || mode == EPI_G2_RESTART) k_armijo<T><<<1, 32, 0, s>>>(B, mode);
+    else rlaunch(k_g2<T>, B.grid, s, B, geo_of(B));
 }
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s) {
-    if (B.n % 2 == 0) k_shrink<T, true><<<B.grid, 256, 0, s>>>(B, mode);
-    else k_shrink<T, false><<<B.grid, 256, 0, s>>>(B, mode);
+    if (B.n % 2 == 0) rlaunch(k_shrink<T, true>, B.grid, s, B, mode);
+    else rlaunch(k_shrink<T, false>, B.grid, s, B, mode);
 }
 template <class T> void launch_g2_gradient(SolverBufs<T>& B, cudaStream_t s) {
-    k_g2_gradient<T><<<B.grid, 256, 0, s>>>(B, geo_of(B));
+    rlaunch(k_g2_gradient<T>, B.grid, s, B, geo_of(B));
 }
 template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t s) {
-    k_gradient<T><<<B.grid, 256, 0, s>>>(B, mode);
+    rlaunch(k_gradient<T>, B.grid, s, B, mode);
 }
-template <class T> void launch_bt_coef(SolverBufs<T>& B, cudaStream_t s) { k_bt_coef<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_bt_coef(SolverBufs<T>& B, cudaStream_t s) { rlaunch(k_bt_coef<T>, B.grid, s, B); }
 template <class T> void launch_bt_apply(SolverBufs<T>& B, cudaStream_t s) {
-    k_bt_g2<T><<<B.grid, 256, 0, s>>>(B, geo_of(B));
-    k_bt_apply<T><<<B.grid, 256, 0, s>>>(B);
+    rlaunch(k_bt_g2<T>, B.grid, s, B, geo_of(B));
+    rlaunch(k_bt_apply<T>, B.grid, s, B);
 }
-template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s) { k_outer_relchg<T><<<B.grid, 256, 0, s>>>(B); }
-template <class T> void launch_mlp(SolverBufs<T>& B, cudaStream_t s) { k_mlp<T><<<B.grid, 256, 0, s>>>(B); }
-template <class T> void launch_outer_grad(SolverBufs<T>& B, cudaStream_t s) { k_outer_grad<T><<<B.grid, 256, 0, s>>>(B); }
+template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s) { rlaunch(k_outer_relchg<T>, B.grid, s, B); }
+template <class T> void launch_mlp(SolverBufs<T>& B, cudaStream_t s) { rlaunch(k_mlp<T>, B.grid, s, B); }
+template <class T> void launch_outer_grad(SolverBufs<T>& B, cudaStream_t s) { rlaunch(k_outer_grad<T>, B.grid, s, B); }
 template <class T> void launch_skip_decide(SolverBufs<T>& B, int force, cudaStream_t s) {
-    k_skip_decide<T><<<B.grid, 256, 0, s>>>(B, force);
+    rlaunch(k_skip_decide<T>, B.grid, s, B, force);
 }
 template <class T> void launch_skip_copy(SolverBufs<T>& B, int which, cudaStream_t s) {
     k_skip_copy<T><<<ew_grid(which == 0 ? B.m : B.n), 256, 0, s>>>(B, which);
 }
 template <class T> void launch_finalize(SolverBufs<T>& B, void* U_out, const void* Ut, cudaStream_t s) {
-    k_finalize<T><<<B.grid, 256, 0, s>>>(B, static_cast<Ext<T>*>(U_out), static_cast<const Ext<T>*>(Ut));
+    rlaunch(k_finalize<T>, B.grid, s, B, static_cast<Ext<T>*>(U_out), static_cast<const Ext<T>*>(Ut));
 }
 template <class T> void launch_D_plain(int p, int q, int r, const T* U, T* DU3, cudaStream_t s) {
     long n = (long)p * q * r;
