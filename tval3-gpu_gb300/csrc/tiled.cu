@@ -123,9 +123,10 @@ __global__ void k_fill_slices(long n, const unsigned long long* __restrict__ key
         const int j = (int)(i - tile_row[t]);
         const int sl = tile_slice[t] + j / 32, lane = j % 32;
         const int v = vox[i];
+        const int s0 = tptr[v], len = tptr[v + 1] - s0;
+        if (len == 0) continue;  // rows without nonzeros sort last and sit in the zero-row list
         row_voxel[(long)sl * 32 + lane] = v;
         const long long o = slice_off[sl] + lane;
-        const int s0 = tptr[v], len = tptr[v + 1] - s0;
         for (int k = 0; k < len; ++k) {
             lidx[o + 32LL * k] = local_of[s0 + k];
             val[o + 32LL * k] = tval[s0 + k];
@@ -144,68 +145,82 @@ __global__ void __launch_bounds__(512) k_spmv_tiled(TiledArgs<T, V> a) {
     const T* __restrict__ y = a.x[sel];
     T* __restrict__ out = a.y[sel];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const int r0 = __ldg(a.ray_off + t), nr = __ldg(a.ray_off + t + 1) - r0;
-        // stage the tile's y values: 8 independent index loads, then 8 gathers
-        for (int j0 = threadIdx.x; j0 < nr; j0 += 8 * blockDim.x) {
-            int ray[8];
-            T v[8];
+    if ((int)blockIdx.x >= a.nwork) {
+        // rows without nonzeros: (A^T y)_v = 0
+        const long z = (long)(blockIdx.x - a.nwork) * blockDim.x + threadIdx.x;
+        if (z < a.nzero) {
+            const int v = __ldg(a.zrows + z);
+            out[v] = (EPI == SPMV_SUB) ? T(0) - a.sub[v] : T(0);
+        }
+        return;
+    }
+    const int t = __ldg(a.tile_order + blockIdx.x);
+    const int r0 = __ldg(a.ray_off + t), nr = __ldg(a.ray_off + t + 1) - r0;
+    const int u0 = __ldg(a.tile_unit + t), u1 = __ldg(a.tile_unit + t + 1);
+    const int s0 = __ldg(a.tile_slice + t), s1 = __ldg(a.tile_slice + t + 1);
+    // this thread's row of the final sums (a tile has at most 512 rows): its
+    // voxel, unit range and subtrahend, loaded now so their latency hides
+    // behind the staging and the products
+    int rv = -1, re0 = 0, re1 = 0;
+    T rsub = T(0);
+    if ((int)threadIdx.x < (s1 - s0) * 32) {
+        const int sl = s0 + warp;
+        rv = __ldg(a.row_voxel + (long)sl * 32 + lane);
+        re0 = __ldg(a.slice_unit + sl) - u0;
+        re1 = __ldg(a.slice_unit + sl + 1) - u0;
+        if (EPI == SPMV_SUB && rv >= 0) rsub = a.sub[rv];
+    }
+    // stage the tile's y values: 8 independent index loads, then 8 gathers
+    for (int j0 = threadIdx.x; j0 < nr; j0 += 8 * blockDim.x) {
+        int ray[8];
+        T v[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int j = j0 + u * blockDim.x;
-                ray[u] = (j < nr) ? __ldg(a.rays + r0 + j) : -1;
-            }
+        for (int u = 0; u < 8; ++u) {
+            const int j = j0 + u * blockDim.x;
+            ray[u] = (j < nr) ? __ldg(a.rays + r0 + j) : -1;
+        }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = (ray[u] >= 0) ? y[ray[u]] : T(0);
-            if (a.xscale) {
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (ray[u] >= 0) v[u] *= (T)__ldg(a.xscale + ray[u]);
-            }
+        for (int u = 0; u < 8; ++u) v[u] = (ray[u] >= 0) ? y[ray[u]] : T(0);
+        if (a.xscale) {
 #pragma unroll
             for (int u = 0; u < 8; ++u)
-                if (ray[u] >= 0) ysm[j0 + u * blockDim.x] = v[u];
+                if (ray[u] >= 0) v[u] *= (T)__ldg(a.xscale + ray[u]);
         }
-        __syncthreads();
-        // work units: at most UNIT_K steps of one slice, so warps get equal work
-        const int u0 = __ldg(a.tile_unit + t), u1 = __ldg(a.tile_unit + t + 1);
-        for (int w = u0 + warp; w < u1; w += nwarps) {
-            const int sl = __ldg(a.unit_slice + w);
-            const long long off = a.slice_off[sl];
-            const int len = (int)((a.slice_off[sl + 1] - off) >> 5);
-            const int k0 = __ldg(a.unit_k0 + w), k1 = min(len, k0 + TILED_UNIT_K);
-            const unsigned short* __restrict__ li = a.lidx + off + lane;
-            const V* __restrict__ va = a.val + off + lane;
-            RowAcc<T> acc;
-            int k = k0;
-            for (; k + U <= k1; k += U) {
-                unsigned short ii[U];
-                VV vv[U];
 #pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    ii[u] = __ldcs(li + 32 * (k + u));
-                    vv[u] = (VV)Acc<VV, V>::load(va + 32 * (k + u));
-                }
+        for (int u = 0; u < 8; ++u)
+            if (ray[u] >= 0) ysm[j0 + u * blockDim.x] = v[u];
+    }
+    __syncthreads();
+    // work units: at most UNIT_K steps of one slice, so warps get equal work
+    for (int w = u0 + warp; w < u1; w += nwarps) {
+        const int sl = __ldg(a.unit_slice + w);
+        const long long off = a.slice_off[sl];
+        const int len = (int)((a.slice_off[sl + 1] - off) >> 5);
+        const int k0 = __ldg(a.unit_k0 + w), k1 = min(len, k0 + TILED_UNIT_K);
+        const unsigned short* __restrict__ li = a.lidx + off + lane;
+        const V* __restrict__ va = a.val + off + lane;
+        RowAcc<T> acc;
+        int k = k0;
+        for (; k + U <= k1; k += U) {
+            unsigned short ii[U];
+            VV vv[U];
 #pragma unroll
-                for (int u = 0; u < U; ++u) madd(acc, vv[u], ysm[ii[u]]);
+            for (int u = 0; u < U; ++u) {
+                ii[u] = __ldcs(li + 32 * (k + u));
+                vv[u] = (VV)Acc<VV, V>::load(va + 32 * (k + u));
             }
-            for (; k < k1; ++k) madd(acc, (VV)Acc<VV, V>::load(va + 32 * k), ysm[__ldcs(li + 32 * k)]);
-            psm[(w - u0) * 32 + lane] = acc.value();
+#pragma unroll
+            for (int u = 0; u < U; ++u) madd(acc, vv[u], ysm[ii[u]]);
         }
-        __syncthreads();
-        // every row: its units' partials in order
-        const int s0 = __ldg(a.tile_slice + t), s1 = __ldg(a.tile_slice + t + 1);
-        for (int i = threadIdx.x; i < (s1 - s0) * 32; i += blockDim.x) {
-            const int sl = s0 + (i >> 5), ln = i & 31;
-            const int v = __ldg(a.row_voxel + (long)sl * 32 + ln);
-            if (v < 0) continue;
-            const int e0 = __ldg(a.slice_unit + sl) - u0, e1 = __ldg(a.slice_unit + sl + 1) - u0;
-            T sum = T(0);
-            for (int e = e0; e < e1; ++e) sum += psm[e * 32 + ln];
-            if (EPI == SPMV_SUB) out[v] = sum - a.sub[v];
-            else out[v] = sum;
-        }
-        __syncthreads();
+        for (; k < k1; ++k) madd(acc, (VV)Acc<VV, V>::load(va + 32 * k), ysm[__ldcs(li + 32 * k)]);
+        psm[(w - u0) * 32 + lane] = acc.value();
+    }
+    __syncthreads();
+    // every row: its units' partials in order
+    if (rv >= 0) {
+        T sum = T(0);
+        for (int e = re0; e < re1; ++e) sum += psm[e * 32 + lane];
+        out[rv] = (EPI == SPMV_SUB) ? sum - rsub : sum;
     }
 }
 
@@ -228,7 +243,7 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
     const int ty = std::min(p, r > 1 ? 8 : 16), tx = std::min(q, r > 1 ? 8 : 16), tz = std::min(r, 8);
     const int nty = (p + ty - 1) / ty, ntx = (q + tx - 1) / tx, ntz = (r + tz - 1) / tz;
     const long nt = (long)nty * ntx * ntz;
-    if (nt >= (1L << 24)) return;
+    if (nt >= (1L << 24) || (long)ty * tx * tz > 512) return;  // the kernel gives each row of a tile one thread
     ntiles = (int)nt;
 
     // ---- (tile, ray) keys of every nonzero, sorted: the tiles' ray lists
@@ -311,16 +326,41 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
     std::vector<int> trow(ntiles + 1, (int)n), tsl(ntiles + 1, 0);
     for (long i = n - 1; i >= 0; --i) trow[hk[i] >> 16] = (int)i;
     for (int t = ntiles - 1; t >= 0; --t) trow[t] = std::min(trow[t], trow[t + 1]);
+    // rows are sorted longest first inside each tile, so the rows without
+    // nonzeros are a suffix of the tile's rows; they leave the slices and go
+    // to one list of voxels whose result is 0 (or -sub)
+    std::vector<int> hvox(n);
+    TV3_CUDA(cudaMemcpy(hvox.data(), vox.p, n * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<int> zlist;
     std::vector<long long> soff(1, 0);
     for (int t = 0; t < ntiles; ++t) {
         tsl[t] = (int)(soff.size() - 1);
-        for (long i = trow[t]; i < trow[t + 1]; i += 32) {
+        long nz_end = trow[t];
+        while (nz_end < trow[t + 1] && (hk[nz_end] & 0xffff) != 0xffff) ++nz_end;
+        for (long i = trow[t]; i < nz_end; i += 32) {
             const long len = 0xffff - (long)(hk[i] & 0xffff);  // the slice's first row is its longest
             soff.push_back(soff.back() + 32 * len);
         }
+        for (long i = nz_end; i < trow[t + 1]; ++i) zlist.push_back(hvox[i]);
     }
     tsl[ntiles] = (int)(soff.size() - 1);
     nslices = tsl[ntiles];
+    // tiles with work, largest first: the longest tiles start in the first
+    // wave and the last wave is made of the smallest ones
+    {
+        std::vector<std::pair<long long, int>> w;
+        for (int t = 0; t < ntiles; ++t)
+            if (tsl[t + 1] > tsl[t]) w.push_back({-(soff[tsl[t + 1]] - soff[tsl[t]]), t});
+        std::sort(w.begin(), w.end());
+        std::vector<int> o(w.size());
+        for (size_t i = 0; i < w.size(); ++i) o[i] = w[i].second;
+        nwork = (int)o.size();
+        tile_order.alloc(std::max(nwork, 1));
+        if (nwork) TV3_CUDA(cudaMemcpy(tile_order.p, o.data(), nwork * sizeof(int), cudaMemcpyHostToDevice));
+        nzero = (long)zlist.size();
+        zrows.alloc(std::max<long>(nzero, 1));
+        if (nzero) TV3_CUDA(cudaMemcpy(zrows.p, zlist.data(), nzero * sizeof(int), cudaMemcpyHostToDevice));
+    }
     // work units of at most TILED_UNIT_K steps per slice (a slice of length 0 still gets one)
     std::vector<int> uslice, tunit(ntiles + 1, 0), sunit(nslices + 1, 0);
     std::vector<unsigned short> uk0;
@@ -381,9 +421,14 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
 template <class T, class V>
 void TiledT<T, V>::apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) const {
     const size_t smem = std::max<size_t>(((size_t)max_rays + (size_t)max_units * 32) * sizeof(T), 16);
-    const int grid = std::max(a.ntiles, 1);
-    if (epi == SPMV_SUB) k_spmv_tiled<T, V, SPMV_SUB, 8><<<grid, 512, smem, s>>>(a);
-    else k_spmv_tiled<T, V, SPMV_PLAIN, 8><<<grid, 512, smem, s>>>(a);
+    TiledArgs<T, V> b = a;
+    b.tile_order = tile_order.p;
+    b.nwork = nwork;
+    b.zrows = zrows.p;
+    b.nzero = nzero;
+    const long grid = std::max<long>((long)nwork + (nzero + 511) / 512, 1);
+    if (epi == SPMV_SUB) k_spmv_tiled<T, V, SPMV_SUB, 8><<<(unsigned)grid, 512, smem, s>>>(b);
+    else k_spmv_tiled<T, V, SPMV_PLAIN, 8><<<(unsigned)grid, 512, smem, s>>>(b);
     TV3_CUDA(cudaGetLastError());
 }
 
@@ -477,9 +522,9 @@ __global__ void __launch_bounds__(512) k_spmv_tiledN(TiledNArgs<T, V> a) {
     const T* __restrict__ x = a.x[sel];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int tvox = a.ty * a.tx * a.tz;
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+    {
+        const int t = __ldg(a.tile_order + blockIdx.x);  // tiles with segments, largest first
         const int s0 = __ldg(a.tile_slice + t), s1 = __ldg(a.tile_slice + t + 1);
-        if (s0 == s1) continue;  // uniform across the CTA
         const int tzi = t / (a.nty * a.ntx), rem = t - tzi * a.nty * a.ntx, txi = rem / a.nty, tyi = rem - txi * a.nty;
         const long y0 = (long)tyi * a.ty, x0 = (long)txi * a.tx, z0 = (long)tzi * a.tz;
         for (int j = threadIdx.x; j < tvox; j += blockDim.x) {
@@ -510,7 +555,6 @@ __global__ void __launch_bounds__(512) k_spmv_tiledN(TiledNArgs<T, V> a) {
             const int d = __ldg(a.slot_dest + (long)sl * 32 + lane);
             if (d >= 0) a.part[d] = acc.value();
         }
-        __syncthreads();
     }
 }
 
@@ -657,6 +701,17 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     }
     tsl[ntiles] = (int)(soff.size() - 1);
     nslices = tsl[ntiles];
+    {
+        std::vector<std::pair<long long, int>> w;
+        for (int t = 0; t < ntiles; ++t)
+            if (tsl[t + 1] > tsl[t]) w.push_back({-(soff[tsl[t + 1]] - soff[tsl[t]]), t});
+        std::sort(w.begin(), w.end());
+        std::vector<int> o(w.size());
+        for (size_t i = 0; i < w.size(); ++i) o[i] = w[i].second;
+        nwork = (int)o.size();
+        tile_order.alloc(std::max(nwork, 1));
+        if (nwork) TV3_CUDA(cudaMemcpy(tile_order.p, o.data(), nwork * sizeof(int), cudaMemcpyHostToDevice));
+    }
     const long long padded = soff.back();
     tile_slice.alloc(ntiles + 1);
     slice_off.alloc(nslices + 1);
@@ -685,13 +740,15 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
 template <class T, class V>
 void TiledN<T, V>::apply(const TiledNArgs<T, V>& a, int epi, cudaStream_t s) const {
     const size_t smem = std::max<size_t>((size_t)ty * tx * tz * sizeof(T), 16);
-    k_spmv_tiledN<T, V, 8><<<std::max(a.ntiles, 1), 512, smem, s>>>(a);
+    TiledNArgs<T, V> b = a;
+    b.tile_order = tile_order.p;
+    if (nwork > 0) k_spmv_tiledN<T, V, 8><<<nwork, 512, smem, s>>>(b);
     const int g = (int)std::max<long>(1, std::min<long>((a.m + 255) / 256, (long)num_sms() * 4));
     switch (epi) {
-        case SPMV_SUB: k_tiledN_reduce<T, V, SPMV_SUB><<<g, 256, 0, s>>>(a); break;
-        case SPMV_LAM35: k_tiledN_reduce<T, V, SPMV_LAM35><<<g, 256, 0, s>>>(a); break;
-        case SPMV_NORM2: k_tiledN_reduce<T, V, SPMV_NORM2><<<g, 256, 0, s>>>(a); break;
-        default: k_tiledN_reduce<T, V, SPMV_PLAIN><<<g, 256, 0, s>>>(a); break;
+        case SPMV_SUB: k_tiledN_reduce<T, V, SPMV_SUB><<<g, 256, 0, s>>>(b); break;
+        case SPMV_LAM35: k_tiledN_reduce<T, V, SPMV_LAM35><<<g, 256, 0, s>>>(b); break;
+        case SPMV_NORM2: k_tiledN_reduce<T, V, SPMV_NORM2><<<g, 256, 0, s>>>(b); break;
+        default: k_tiledN_reduce<T, V, SPMV_PLAIN><<<g, 256, 0, s>>>(b); break;
     }
     TV3_CUDA(cudaGetLastError());
 }

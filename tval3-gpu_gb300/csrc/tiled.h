@@ -33,13 +33,19 @@ struct TiledArgs {
     int by_parity;
     const T* sub;              // SPMV_SUB: out = A^T y - sub
     Ctl* ctl;
+    const int* tile_order;     // tiles with nonzeros, largest first (one per CTA)
+    int nwork;
+    const int* zrows;          // voxels whose row of A^T is empty (result 0 or -sub)
+    long nzero;
 };
 
 template <class T, class V>
 struct TiledT {
     bool ok = false;
     long n = 0;
-    int ntiles = 0, nslices = 0, nunits = 0, max_rays = 0, max_units = 0;
+    int ntiles = 0, nslices = 0, nunits = 0, max_rays = 0, max_units = 0, nwork = 0;
+    long nzero = 0;
+    DBuf<int> tile_order, zrows;
     long long padded_entries = 0;
     DBuf<int> ray_off, rays, tile_slice, row_voxel, tile_unit, slice_unit, unit_slice;
     DBuf<unsigned short> unit_k0;
@@ -81,12 +87,14 @@ struct TiledNArgs {
     Ctl* ctl;
     double* rpart;               // grid-reduction scratch of the epilogues
     unsigned* ticket;
+    const int* tile_order;       // tiles with segments, largest first (one per CTA)
 };
 
 template <class T, class V>
 struct TiledN {
     bool ok = false;
-    int ntiles = 0, nslices = 0;
+    int ntiles = 0, nslices = 0, nwork = 0;
+    DBuf<int> tile_order;
     int p = 0, q = 0, r = 0, ty = 0, tx = 0, tz = 0, nty = 0, ntx = 0;
     long m = 0, nseg = 0;
     DBuf<int> tile_slice, slot_dest, rseg;
