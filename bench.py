@@ -618,21 +618,23 @@ def spmv_only(args, T, torch, geo, op32, n, m, nnz, dev):
         torch.cuda.nvtx.range_pop()
         return tot / 20
 
+    names = {0: "csr", 1: "tiled", 2: "tiled_pipe"}
     for trans, (src, dst) in ((0, (x, outm)), (1, (y, outn))):
         chosen = op.variant(trans)
         bts = spmv_bytes(nnz, m, n, sv, sx, bool(trans)) + (4 * m if sv == 2 else 0)
         t = timed(trans, src, dst, "spmv_AT" if trans else "spmv_A")
-        entry = {"us": round(t * 1e6, 2), "GBs": round(bts / t / 1e9, 1), "bytes": bts,
-                 "variant": ("tiled" if chosen else "csr")}
-        # the other kernel of the same product, for comparison
-        other = 1 - chosen
-        try:
-            op.set_variant(trans, other)
-            t2 = timed(trans, src, dst, ("spmv_AT_" if trans else "spmv_A_") + ("tiled" if other else "csr"))
-            entry["tiled_us" if other else "csr_us"] = round(t2 * 1e6, 2)
-            op.set_variant(trans, chosen)
-        except T.Tval3Error:
-            pass
+        entry = {"us": round(t * 1e6, 2), "GBs": round(bts / t / 1e9, 1), "bytes": bts, "variant": names[chosen]}
+        # the other kernels of the same product, for comparison
+        for other in names:
+            if other == chosen:
+                continue
+            try:
+                op.set_variant(trans, other)
+            except T.Tval3Error:
+                continue
+            t2 = timed(trans, src, dst, ("spmv_AT_" if trans else "spmv_A_") + names[other])
+            entry[names[other] + "_us"] = round(t2 * 1e6, 2)
+        op.set_variant(trans, chosen)
         res["AT" if trans else "A"] = entry
     peak, kind = peaks()
     return {"spmv_only": args.only_spmv, "nnz": nnz, "rows": m, "cols": n, "peak_GBs": peak, "peak_source": kind,

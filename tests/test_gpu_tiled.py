@@ -86,6 +86,62 @@ def test_tiled_solve_matches_oracle_fp64(cuda, oracle):
     assert np.linalg.norm(U.cpu().numpy() - Uo.reshape(-1)) <= 1e-7 * np.linalg.norm(Uo)
 
 
+@pytest.mark.parametrize("kind", ["ring", "hemi"])
+@pytest.mark.parametrize("prec", ["fp32", "df64", "fp64vec"])
+def test_pipelined_AT_is_bit_identical_to_tiled(cuda, kind, prec):
+    """Variant 2 of A^T*y (producer warp streaming the units through a
+    shared-memory ring) forms exactly the sums of variant 1, in the same
+    order: the outputs agree bit for bit, rows without nonzeros included."""
+    import torch
+    from tval3_gb300 import PREC_FP32, PREC_FP32_DF64, PREC_FP32_F64VEC, Operator
+    geo = _geo(kind)
+    p = {"fp32": PREC_FP32, "df64": PREC_FP32_DF64, "fp64vec": PREC_FP32_F64VEC}[prec]
+    op = Operator.from_geometry(geo, mode=0, precision=p)
+    g = torch.Generator().manual_seed(11)
+    words = 2 if prec == "df64" else 1
+    dt = torch.float64 if prec == "fp64vec" else torch.float32
+    y = torch.randn(words * op.rows, generator=g, dtype=torch.float64).to(dt).to(cuda)
+    if prec == "df64":
+        y[1::2] = y[0::2] * 1e-8  # a nonzero low word in every element
+    outs = []
+    for v in (1, 2):
+        op.set_variant(1, v)
+        assert op.variant(1) == v
+        x = torch.full((words * op.cols,), float("nan"), dtype=dt, device=cuda)
+        for _ in range(2):  # twice: the second launch starts from a used ring
+            op.mat_vec_mul(1, y, x)
+        outs.append(x.cpu())
+    torch.cuda.synchronize()
+    assert not torch.isnan(outs[1]).any()
+    assert torch.equal(outs[0], outs[1])
+
+
+def test_pipelined_AT_in_a_solve(cuda, oracle):
+    """A double-float 3D solve with A^T pinned to the pipelined kernel (its
+    SUB epilogue, g = A^T Au - Atb) takes the same path to the same result,
+    bit for bit, as with the tile-staged kernel."""
+    import torch
+    from tval3_gb300 import PREC_FP32_DF64, Operator, Solver
+    from tval3_gb300 import workloads as W
+    cfg, geo, x = W.config_3d(24, 32, 32, seed=4)
+    ptr, ind, val = oracle.siddon_csr(geo)
+    b = W.add_noise(oracle.spmv(ptr, ind, val, x), cfg.noise, 4).astype(np.float64)
+    o = dict(cfg.opts, maxit=40)
+    res = []
+    for v in (1, 2):
+        op = Operator.from_geometry(geo, mode=0, precision=PREC_FP32_DF64)
+        op.set_variant(1, v)
+        s = Solver(op, cfg.dims, o, mode=1)
+        U = torch.empty(x.size, dtype=torch.float64, device=cuda)
+        info = s.solve(torch.tensor(b, device=cuda), U)
+        torch.cuda.synchronize()
+        assert op.variant(1) == v
+        res.append((info["total_iters"], info["backtracks"], info["restarts"], U.cpu()))
+        s.close()
+    assert res[0][:3] == res[1][:3]
+    assert torch.equal(res[0][3], res[1][3])
+
+
 def test_variant_pinning(cuda):
     """tval3_op_set_variant pins the kernel of each product; the two kernels
     of one operator agree, and an operator without a volume has no tiled form."""
@@ -96,7 +152,7 @@ def test_variant_pinning(cuda):
     g = torch.Generator().manual_seed(3)
     y = torch.randn(op.rows, generator=g).to(cuda)
     outs = []
-    for v in (0, 1):
+    for v in (0, 1, 2):
         op.set_variant(1, v)
         assert op.variant(1) == v
         x = torch.empty(op.cols, device=cuda)
@@ -104,6 +160,9 @@ def test_variant_pinning(cuda):
         outs.append(x)
     torch.cuda.synchronize()
     assert torch.allclose(outs[0], outs[1], rtol=1e-5, atol=1e-5 * float(outs[0].abs().max()))
+    assert torch.equal(outs[1], outs[2])
+    with pytest.raises(Tval3Error):
+        op.set_variant(0, 2)  # A*x has no pipelined form
     ptr, ind, val, tptr, tind, tval = op.export_csr()
     bare = Operator.from_sparse(SparseMatrix(ptr.size - 1, tptr.size - 1, ptr, ind, val), precision=PREC_FP32)
     with pytest.raises(Tval3Error):

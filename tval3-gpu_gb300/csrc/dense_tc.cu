@@ -35,6 +35,7 @@
 #include <algorithm>
 #include <mutex>
 #include "dbuf.h"
+#include "mbar.cuh"
 #include "ops.h"
 #include "tval3/tval3_c.h"
 
@@ -45,33 +46,6 @@ namespace {
 constexpr int UM = 128;          // tile rows (TMEM lanes)
 constexpr int UK = 64;           // K per stage: one 128-byte swizzle row of BF16
 constexpr int MAX_STAGES = 6;
-constexpr long long WAIT_CYCLES = 4000000000LL;  // about 2 s at 2 GHz
-constexpr unsigned ERR_UMMA_TIMEOUT = 0x10u;
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-// bounded wait for the completion of phase `parity`; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
-    const unsigned a = smem_u32(b);
-    const long long t0 = clock64();
-    for (;;) {
-        unsigned ok;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (ok) return true;
-        if (clock64() - t0 > WAIT_CYCLES) return false;
-    }
-}
-
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(

@@ -179,7 +179,8 @@ struct CsrOp : LinOp<T> {
     int Gn = 32, Gt = 8, grid_n = 1, grid_t = 1;
     mutable TiledT<T, V> tiled;   // A^T regrouped by voxel tiles (when the volume is known)
     mutable TiledN<T, V> tiledN;  // A cut into per-tile ray segments (when the volume is known)
-    mutable bool useT = false, useN = false;  // products run tile-staged
+    // kernel of each product: 0 CSR, 1 tile-staged, 2 (A^T only) tile-staged and pipelined
+    mutable int varT = 0, varN = 0;
     mutable int vol[3] = {0, 0, 0};
 
     void set_volume(int p, int q, int r) const override {
@@ -187,28 +188,39 @@ struct CsrOp : LinOp<T> {
         vol[0] = p; vol[1] = q; vol[2] = r;
         tiled.build(this->n, this->m, p, q, r, tptr.p, tind.p, tval.p, this->nnz, 96 * 1024, 0);
         tiledN.build(this->m, p, q, r, ptr.p, ind.p, val.p, this->nnz, 0);
-        useT = tiled.ok;
-        useN = tiledN.ok;
-        // large operators: the tile-staged products only where they beat the tuned CSR kernels
+        varT = tiled.ok ? 1 : 0;
+        varN = tiledN.ok ? 1 : 0;
+        // large operators: the fastest kernel of each product, timed here
         if (this->nnz >= (1L << 22)) {
-            if (useT && time_product(1, false) <= time_product(1, true)) useT = false;
-            if (useN && time_product(0, false) <= time_product(0, true)) useN = false;
+            const int nT = tiled.pipe_ok ? 3 : (tiled.ok ? 2 : 1), nN = tiledN.ok ? 2 : 1;
+            for (int trans = 0; trans < 2; ++trans) {
+                const int nv = trans ? nT : nN;
+                if (nv < 2) continue;
+                int best = 0;
+                float tbest = time_product(trans, 0);
+                for (int v = 1; v < nv; ++v) {
+                    const float tv = time_product(trans, v);
+                    if (tv < tbest) tbest = tv, best = v;
+                }
+                (trans ? varT : varN) = best;
+            }
         }
     }
 
     bool set_variant(int trans, int v) const override {
-        if (v != 0 && v != 1) return false;
+        if (v < 0 || v > (trans ? 2 : 1)) return false;
         if (v == 1 && !(trans ? tiled.ok : tiledN.ok)) return false;
-        (trans ? useT : useN) = (v == 1);
+        if (v == 2 && !tiled.pipe_ok) return false;
+        (trans ? varT : varN) = v;
         return true;
     }
-    int variant(int trans) const override { return (trans ? useT : useN) ? 1 : 0; }
+    int variant(int trans) const override { return trans ? varT : varN; }
 
-    // milliseconds of three products (after one warm-up), plain CSR or tile-staged
-    float time_product(int trans, bool use_tiled) const {
-        bool& flag = trans ? useT : useN;
-        const bool keep = flag;
-        flag = use_tiled;
+    // milliseconds of three products (after one warm-up) with kernel variant use_variant
+    float time_product(int trans, int use_variant) const {
+        int& flag = trans ? varT : varN;
+        const int keep = flag;
+        flag = use_variant;
         const long lx = trans ? this->m : this->n, ly = trans ? this->n : this->m;
         DBuf<T> x(std::max<long>(lx, 1)), y(std::max<long>(ly, 1));
         TV3_CUDA(cudaMemset(x.p, 0, std::max<long>(lx, 1) * sizeof(T)));
@@ -235,7 +247,7 @@ struct CsrOp : LinOp<T> {
     }
 
     void apply(int trans, const MatIO<T>& io, int epi, cudaStream_t s) const override {
-        if (!trans && io.L <= 1 && useN && tiledN.ok) {
+        if (!trans && io.L <= 1 && varN == 1 && tiledN.ok) {
             TiledNArgs<T, V> t{};
             t.ntiles = tiledN.ntiles;
             t.p = tiledN.p; t.q = tiledN.q; t.r = tiledN.r; t.ty = tiledN.ty; t.tx = tiledN.tx; t.tz = tiledN.tz;
@@ -249,7 +261,7 @@ struct CsrOp : LinOp<T> {
             tiledN.apply(t, epi, s);
             return;
         }
-        if (trans && io.L <= 1 && useT && tiled.ok && (epi == SPMV_PLAIN || epi == SPMV_SUB)) {
+        if (trans && io.L <= 1 && varT >= 1 && tiled.ok && (epi == SPMV_PLAIN || epi == SPMV_SUB)) {
             TiledArgs<T, V> t{};
             t.ntiles = tiled.ntiles; t.ray_off = tiled.ray_off.p; t.rays = tiled.rays.p;
             t.tile_slice = tiled.tile_slice.p; t.slice_off = tiled.slice_off.p; t.row_voxel = tiled.row_voxel.p;
@@ -259,7 +271,8 @@ struct CsrOp : LinOp<T> {
             t.xscale = rs.p;
             t.x[0] = io.x[0]; t.x[1] = io.x[1]; t.y[0] = io.y[0]; t.y[1] = io.y[1];
             t.by_parity = io.by_parity; t.sub = io.sub; t.ctl = io.ctl;
-            tiled.apply(t, epi, s);
+            if (varT == 2) tiled.apply_pipe(t, epi, s);
+            else tiled.apply(t, epi, s);
             return;
         }
         SpmvArgs<T, V> a{};

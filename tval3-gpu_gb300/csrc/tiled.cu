@@ -28,9 +28,11 @@
 // partials in order after a barrier (deterministic).
 #include <cub/cub.cuh>
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 #include "ops.h"
 #include "tiled.h"
+#include "mbar.cuh"
 
 namespace tv3 {
 
@@ -224,6 +226,208 @@ __global__ void __launch_bounds__(512) k_spmv_tiled(TiledArgs<T, V> a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined A^T*y.  One persistent CTA per SM takes the tiles with work in
+// largest-first order, snaking over the CTAs (tile k*G + b for even k,
+// k*G + G-1-b for odd k).  Two producer warps:
+//   - warp PIPE_CONSUMERS, per chunk of work units, bulk-copies the units'
+//     descriptors, positions and values into the next stage of a
+//     shared-memory ring;
+//   - warp PIPE_CONSUMERS + 1, per tile, bulk-copies the tile's ray list into
+//     shared memory and gathers the tile's y values with 4/8-byte
+//     asynchronous copies into one of two y buffers (the next tile's gather
+//     overlaps this tile's sums).
+// The consumer warps sum units straight from shared memory (unit j of a
+// tile belongs to warp j mod 16, so the sums, and the row sums in unit
+// order, are those of k_spmv_tiled bit for bit).  Stages are released
+// through "empty" barriers, y buffers through "yempty" barriers.
+//
+// Every mbarrier wait is bounded.  On a timeout the warp records
+// ERR_TILED_TIMEOUT, stops computing, keeps taking part in the consumers'
+// named barriers so no warp is left waiting, and the producer waits (bounded)
+// for its own copies in flight before it returns.
+// ---------------------------------------------------------------------------
+template <class T, class V, int EPI>
+__global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 2), 1) k_spmv_tiled_pipe(TiledArgs<T, V> a, PipeArgs pa) {
+    count_launch(a.ctl);
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    const int NS = pa.stages;
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm_raw);
+    uint64_t* empty = full + NS;
+    uint64_t* yfull = empty + NS;  // 2
+    uint64_t* yempty = yfull + 2;  // 2
+    uint64_t* rbar = yempty + 2;   // 1
+    unsigned char* ring = sm_raw + PIPE_BAR_BYTES;
+    T* ybuf = reinterpret_cast<T*>(ring + (size_t)NS * pa.stage_bytes);
+    int* ridx = reinterpret_cast<int*>(ybuf + 2 * (size_t)pa.ybuf_elems);
+    T* psm = reinterpret_cast<T*>(ridx + pa.ybuf_elems);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NS; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], PIPE_CONSUMERS);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&yfull[i], 32);
+            mbar_init(&yempty[i], PIPE_CONSUMERS);
+        }
+        mbar_init(rbar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const int sel = a.by_parity ? a.ctl->parity : 0;
+    const T* __restrict__ y = a.x[sel];
+    T* __restrict__ out = a.y[sel];
+    const int G = gridDim.x, b = blockIdx.x;
+    auto tile_at = [&](int i) {  // this CTA's i-th tile (position in the largest-first order)
+        return i * G + ((i & 1) ? G - 1 - b : b);
+    };
+    bool ok = true;
+    auto sched_of = [&](int i, int4& s0, int4& s1) {  // this CTA's i-th tile record (or none)
+        const int k = tile_at(i);
+        if (k < a.nwork) {
+            s0 = __ldg(pa.sched + 2 * k);
+            s1 = __ldg(pa.sched + 2 * k + 1);
+        } else {
+            s0 = make_int4(-1, 0, 0, 0);
+            s1 = make_int4(0, 0, 0, 0);
+        }
+    };
+    if (warp == PIPE_CONSUMERS + 1) {
+        // ---------------------------------------------------- y producer: per
+        // tile, the ray list by one bulk copy, then the tile's y values by
+        // 4/8-byte asynchronous copies into the free y buffer (a tile ahead)
+        int rpend = -1;  // parity of a ray-list copy not yet seen complete
+        int4 ta, tb, na, nb4;
+        sched_of(0, ta, tb);
+        for (int i = 0; ok && ta.x >= 0; ++i, ta = na, tb = nb4) {
+            sched_of(i + 1, na, nb4);  // the next record loads while this tile is served
+            const int yb = i & 1, nr = tb.z;
+            if (i >= 2) ok = __all_sync(FULL, mbar_wait(&yempty[yb], (unsigned)(((i - 2) >> 1) & 1)));
+            if (!ok) break;
+            const unsigned nbytes = (unsigned)((nr + 3) & ~3) * 4u;
+            if (lane == 0) {
+                mbar_expect_tx(rbar, nbytes);
+                bulk_g2s(ridx, pa.rays_pad + tb.w, nbytes, rbar);
+            }
+            rpend = i & 1;
+            ok = __all_sync(FULL, mbar_wait(rbar, (unsigned)rpend));
+            if (!ok) break;
+            rpend = -1;
+            T* ys = ybuf + (size_t)yb * pa.ybuf_elems;
+            for (int j = lane; j < nr; j += 32) cp_async<(int)sizeof(T)>(ys + j, y + ridx[j]);
+            cp_async_arrive(&yfull[yb]);
+            __syncwarp();  // every lane has read ridx before the next list overwrites it
+        }
+        if (!ok && lane == 0 && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
+        cp_async_wait_all();  // the gathers land before the CTA may exit
+        if (lane == 0 && rpend >= 0) mbar_wait(rbar, (unsigned)rpend);
+        return;
+    }
+    if (warp == PIPE_CONSUMERS) {
+        // ------------------------------------------------ chunk producer: the
+        // units of every tile, chunk by chunk, into the ring.  The chunk
+        // records of 32 chunks are loaded at once (one per lane) and handed
+        // to lane 0 by shuffles, so no global load sits between two copies.
+        long g = 0;  // chunks issued
+        int4 ta, tb, na, nb4;
+        sched_of(0, ta, tb);
+        for (int i = 0; ok && ta.x >= 0; ++i, ta = na, tb = nb4) {
+            sched_of(i + 1, na, nb4);
+            for (int cb = tb.x; ok && cb < tb.y; cb += 32) {
+                const int4 ci = (cb + lane < tb.y) ? __ldg(pa.cinfo + cb + lane) : make_int4(0, 0, 0, 0);
+                const int nc = min(32, tb.y - cb);
+                for (int q = 0; q < nc; ++q, ++g) {
+                    const int e32 = __shfl_sync(FULL, ci.x, q), ne = __shfl_sync(FULL, ci.y, q);
+                    const int d0 = __shfl_sync(FULL, ci.z, q), jn = __shfl_sync(FULL, ci.w, q);
+                    const int st = (int)(g % NS);
+                    if (g >= NS) ok = __all_sync(FULL, mbar_wait(&empty[st], (unsigned)(((g / NS) - 1) & 1)));
+                    if (!ok) break;
+                    if (lane == 0) {
+                        unsigned char* sp = ring + (size_t)st * pa.stage_bytes;
+                        const int nu = jn & 0xff;
+                        const long long e0 = 32LL * (unsigned)e32;
+                        int* hdr = reinterpret_cast<int*>(sp);
+                        hdr[0] = jn >> 8;
+                        hdr[1] = nu;
+                        const unsigned db = (unsigned)((nu + 3) & ~3) * 4u, lb = (unsigned)ne * 2u,
+                                       vb = (unsigned)ne * (unsigned)sizeof(V);
+                        mbar_expect_tx(&full[st], db + lb + vb);
+                        bulk_g2s(sp + 16, pa.udesc + d0, db, &full[st]);
+                        bulk_g2s(sp + 16 + 4 * PIPE_CHUNK_U, a.lidx + e0, lb, &full[st]);
+                        bulk_g2s(sp + 16 + 4 * PIPE_CHUNK_U + 2 * PIPE_CHUNK_E, a.val + e0, vb, &full[st]);
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+        if (!ok && lane == 0 && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
+        // copies still in flight land before the CTA may exit
+        if (lane == 0)
+            for (long q = (g > NS ? g - NS : 0); q < g; ++q) mbar_wait(&full[q % NS], (unsigned)((q / NS) & 1));
+        return;
+    }
+    // ---------------------------------------------------------------- consumers
+    long g = 0;
+    int4 ta, tb, na, nb4;
+    sched_of(0, ta, tb);
+    for (int i = 0; ta.x >= 0; ++i, ta = na, tb = nb4) {
+        sched_of(i + 1, na, nb4);
+        const int yb = i & 1;
+        const int u0 = ta.y, s0 = ta.z, s1 = ta.w, c0 = tb.x, c1 = tb.y;
+        int rv = -1, re0 = 0, re1 = 0;
+        T rsub = T(0);
+        if ((int)threadIdx.x < (s1 - s0) * 32) {
+            const int sl = s0 + warp;
+            rv = __ldg(a.row_voxel + (long)sl * 32 + lane);
+            re0 = __ldg(a.slice_unit + sl) - u0;
+            re1 = __ldg(a.slice_unit + sl + 1) - u0;
+            if (EPI == SPMV_SUB && rv >= 0) rsub = a.sub[rv];
+        }
+        if (ok) ok = __all_sync(FULL, mbar_wait(&yfull[yb], (unsigned)((i >> 1) & 1)));
+        const T* ysm = ybuf + (size_t)yb * pa.ybuf_elems;
+        for (int c = c0; c < c1; ++c, ++g) {
+            const int st = (int)(g % NS);
+            if (ok) ok = __all_sync(FULL, mbar_wait(&full[st], (unsigned)((g / NS) & 1)));
+            if (ok) {
+                const unsigned char* sp = ring + (size_t)st * pa.stage_bytes;
+                const int j0 = reinterpret_cast<const int*>(sp)[0], nu = reinterpret_cast<const int*>(sp)[1];
+                const unsigned* sd = reinterpret_cast<const unsigned*>(sp + 16);
+                const unsigned short* sl = reinterpret_cast<const unsigned short*>(sp + 16 + 4 * PIPE_CHUNK_U);
+                const V* sv = reinterpret_cast<const V*>(sp + 16 + 4 * PIPE_CHUNK_U + 2 * PIPE_CHUNK_E);
+                for (int j = j0 + ((warp - j0) % PIPE_CONSUMERS + PIPE_CONSUMERS) % PIPE_CONSUMERS; j < j0 + nu;
+                     j += PIPE_CONSUMERS) {
+                    const unsigned d = sd[j - j0];
+                    const int rel = (int)(d >> 8), steps = (int)(d & 0xffu);
+                    const unsigned short* li = sl + rel * 32 + lane;
+                    const V* va = sv + rel * 32 + lane;
+                    RowAcc<T> acc;
+#pragma unroll 4
+                    for (int q = 0; q < steps; ++q) madd(acc, (typename TVT<V>::type)va[32 * q], ysm[li[32 * q]]);
+                    psm[j * 32 + lane] = acc.value();
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&yempty[yb]);
+        named_sync(1, 32 * PIPE_CONSUMERS);  // every unit's partials are in psm
+        if (rv >= 0) {
+            T sum = T(0);
+            for (int e = re0; e < re1; ++e) sum += psm[e * 32 + lane];
+            out[rv] = (EPI == SPMV_SUB) ? sum - rsub : sum;
+        }
+        named_sync(1, 32 * PIPE_CONSUMERS);  // psm is free for the next tile
+    }
+    if (!ok && lane == 0 && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
+    // rows without nonzeros, spread over the CTAs
+    for (long z = (long)b * (32 * PIPE_CONSUMERS) + threadIdx.x; z < a.nzero; z += (long)G * (32 * PIPE_CONSUMERS)) {
+        const int v = __ldg(a.zrows + z);
+        out[v] = (EPI == SPMV_SUB) ? T(0) - a.sub[v] : T(0);
+    }
+}
+
 template <class T, class V>
 void set_smem_attr(size_t smem) {
     const int b = (int)smem;
@@ -414,8 +618,116 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
     padded_entries = padded;
     // the attribute is per kernel, shared by every operator: always the full budget
     set_smem_attr<T, V>(max_smem);
+    build_pipe(soff, tsl, tunit, uslice, uk0, s);
     TV3_CUDA(cudaStreamSynchronize(s));
     ok = true;
+}
+
+// Chunk tables and padded ray lists of the pipelined form, when its shared
+// memory (ring of at least two stages, two y buffers, the ray list and the
+// unit partials) fits one CTA.
+template <class T, class V>
+void TiledT<T, V>::build_pipe(const std::vector<long long>& soff, const std::vector<int>& tsl,
+                              const std::vector<int>& tunit, const std::vector<int>& uslice,
+                              const std::vector<unsigned short>& uk0, cudaStream_t s) {
+    pipe_ok = false;
+    if (!(std::is_same<V, float>::value || std::is_same<V, double>::value) || ntiles <= 0) return;
+    int dev = 0, optin = 0;
+    TV3_CUDA(cudaGetDevice(&dev));
+    TV3_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const int sb = (16 + 4 * PIPE_CHUNK_U + 2 * PIPE_CHUNK_E + (int)sizeof(V) * PIPE_CHUNK_E + 127) / 128 * 128;
+    const int ybe = (max_rays + 3) & ~3;
+    const size_t fixed = PIPE_BAR_BYTES + 2 * (size_t)ybe * sizeof(T) + (size_t)ybe * 4 + (size_t)max_units * 32 * sizeof(T);
+    int ns = PIPE_MAX_STAGES;
+    while (ns >= 2 && fixed + (size_t)ns * sb > (size_t)optin) --ns;
+    if (ns < 2) return;
+    TV3_CUDA(cudaStreamSynchronize(s));  // ray lists were built on s
+    // chunks: consecutive units of one tile, their entries contiguous
+    std::vector<int> tch(ntiles + 1);
+    std::vector<int4> ci;
+    std::vector<unsigned> ud;
+    for (int t = 0; t < ntiles; ++t) {
+        tch[t] = (int)ci.size();
+        int u = tunit[t];
+        while (u < tunit[t + 1]) {
+            const long long e0 = soff[uslice[u]] + 32LL * uk0[u];
+            const int d0 = (int)ud.size(), j0 = u - tunit[t];
+            int ne = 0, nu = 0;
+            while (u < tunit[t + 1] && nu < PIPE_CHUNK_U) {
+                const int sl = uslice[u];
+                const long len = (long)((soff[sl + 1] - soff[sl]) / 32);
+                const int steps = (int)std::min<long>(len - uk0[u], TILED_UNIT_K);
+                if (nu > 0 && ne + 32 * steps > PIPE_CHUNK_E) break;
+                ud.push_back(((unsigned)(ne / 32) << 8) | (unsigned)steps);
+                ne += 32 * steps;
+                ++nu;
+                ++u;
+            }
+            while (ud.size() % 4) ud.push_back(0u);
+            if (e0 / 32 > 0x7fffffffLL || j0 >= (1 << 23)) return;  // beyond the packed record
+            ci.push_back(make_int4((int)(e0 / 32), ne, d0, (j0 << 8) | nu));
+        }
+    }
+    tch[ntiles] = (int)ci.size();
+    nchunks = (int)ci.size();
+    // ray lists starting at multiples of four entries (16-byte bulk copies)
+    std::vector<int> roff(ntiles + 1);
+    TV3_CUDA(cudaMemcpy(roff.data(), ray_off.p, (ntiles + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<int> hr(std::max(roff[ntiles], 1));
+    if (roff[ntiles] > 0)
+        TV3_CUDA(cudaMemcpy(hr.data(), rays.p, roff[ntiles] * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<int> rpo(ntiles), rp;
+    for (int t = 0; t < ntiles; ++t) {
+        rpo[t] = (int)rp.size();
+        for (int j = roff[t]; j < roff[t + 1]; ++j) rp.push_back(hr[j]);
+        while (rp.size() % 4) rp.push_back(0);
+    }
+    if (rp.empty()) rp.assign(4, 0);
+    // per position of the largest-first order: the tile's two records
+    std::vector<int> ord(std::max(nwork, 1));
+    if (nwork) TV3_CUDA(cudaMemcpy(ord.data(), tile_order.p, nwork * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<int4> sc(2 * (size_t)std::max(nwork, 1), make_int4(0, 0, 0, 0));
+    for (int k = 0; k < nwork; ++k) {
+        const int t = ord[k];
+        sc[2 * k] = make_int4(t, tunit[t], tsl[t], tsl[t + 1]);
+        sc[2 * k + 1] = make_int4(tch[t], tch[t + 1], roff[t + 1] - roff[t], rpo[t]);
+    }
+    auto up = [&](auto& d, const auto& h) {
+        d.alloc(std::max<size_t>(h.size(), 1));
+        if (!h.empty()) TV3_CUDA(cudaMemcpy(d.p, h.data(), h.size() * sizeof(h[0]), cudaMemcpyHostToDevice));
+    };
+    up(sched, sc);
+    up(cinfo, ci);
+    up(udesc, ud);
+    up(rays_pad, rp);
+    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiled_pipe<T, V, SPMV_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  optin));
+    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiled_pipe<T, V, SPMV_SUB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  optin));
+    pipe_stages = ns;
+    pipe_stage_bytes = sb;
+    pipe_ybe = ybe;
+    pipe_smem = fixed + (size_t)ns * sb;
+    pipe_ok = true;
+}
+
+template <class T, class V>
+void TiledT<T, V>::apply_pipe(const TiledArgs<T, V>& a, int epi, cudaStream_t s) const {
+    if (!pipe_ok || a.xscale) {
+        apply(a, epi, s);
+        return;
+    }
+    TiledArgs<T, V> b = a;
+    b.tile_order = tile_order.p;
+    b.nwork = nwork;
+    b.zrows = zrows.p;
+    b.nzero = nzero;
+    PipeArgs pa{sched.p, cinfo.p, udesc.p, rays_pad.p, pipe_stages, pipe_stage_bytes, pipe_ybe};
+    const int grid = std::max(1, num_sms());
+    const int threads = 32 * (PIPE_CONSUMERS + 2);
+    if (epi == SPMV_SUB) k_spmv_tiled_pipe<T, V, SPMV_SUB><<<grid, threads, pipe_smem, s>>>(b, pa);
+    else k_spmv_tiled_pipe<T, V, SPMV_PLAIN><<<grid, threads, pipe_smem, s>>>(b, pa);
+    TV3_CUDA(cudaGetLastError());
 }
 
 template <class T, class V>
