@@ -377,10 +377,12 @@ __global__ void k_armijo(SolverBufs<T> B, int mode) {
 }
 
 // ---------------------------------------------------------------------------
-// shrinkage: W = shrink(DU - sigma/beta, 1/beta), lam1 = TV(W)
+// shrinkage: W = shrink(DU - sigma/beta, 1/beta), lam1 = TV(W), and the
+// terms of update_W that need only the voxel itself: lam2 = ||DU - W||^2,
+// lam4 = <sigma, DU - W>
 // ---------------------------------------------------------------------------
 template <class T, bool PAIRS>
-__global__ void __launch_bounds__(256, 5) k_shrink(SolverBufs<T> B, int mode) {
+__global__ void __launch_bounds__(256, 4) k_shrink(SolverBufs<T> B, int mode) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     using A = acc_t<T>;
@@ -392,7 +394,9 @@ __global__ void __launch_bounds__(256, 5) k_shrink(SolverBufs<T> B, int mode) {
     const T bt = scal<T>(ctl->beta), ib = scal<T>(1.0 / ctl->beta);
     const int iso = ctl->iso;
     A l1(0.f);
-    // one voxel: v = DU - sigma/beta -> W, adding its TV term to l1
+    ProdAcc<T> l2, l4;
+    // one voxel: v = DU - sigma/beta -> W, adding its TV term to l1 and
+    // (DU - W)^2, sigma (DU - W) to l2, l4
     auto voxel = [&](T d0, T d1, T d2, T s0, T s1, T s2, T& w0, T& w1, T& w2) {
         T u0 = d0 - div_beta(s0, bt, ib);
         T u1 = d1 - div_beta(s1, bt, ib);
@@ -416,6 +420,13 @@ __global__ void __launch_bounds__(256, 5) k_shrink(SolverBufs<T> B, int mode) {
             w2 = u2 * sc;
             l1 += to_acc(t);
         }
+        const T v0 = d0 - w0, v1 = d1 - w1, v2 = d2 - w2;
+        l2.add(v0, v0);
+        l2.add(v1, v1);
+        l2.add(v2, v2);
+        l4.add(v0, s0);
+        l4.add(v1, s1);
+        l4.add(v2, s2);
     };
     if (PAIRS) {
         GRID_STRIDE_PAIRS(i, n) {
@@ -431,10 +442,22 @@ __global__ void __launch_bounds__(256, 5) k_shrink(SolverBufs<T> B, int mode) {
     } else {
         GRID_STRIDE(i, n) voxel(DU[i], DU[n + i], DU[2 * n + i], S[i], S[n + i], S[2 * n + i], W[i], W[n + i], W[2 * n + i]);
     }
-    double v[1] = {acc_d(l1)}, tot[1];
-    if (grid_reduce<1>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
-        if (mode == EPI_G2_UPDATE_W) ctl->f -= ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
-        ctl->lam1 = tot[0];
+    double v[3] = {acc_d(l1), l2.value(), l4.value()}, tot[3];
+    if (grid_reduce<3>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        if (mode == EPI_G2_UPDATE_W) {
+            // update_W (:1016-1029): f takes the new lam1, lam2, lam4; then the
+            // nonmonotone reference values (:1176-1177)
+            ctl->f -= ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
+            ctl->lam1 = tot[0];
+            ctl->lam2 = tot[1];
+            ctl->lam4 = tot[2];
+            ctl->f += ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
+            const double Qp = ctl->Q;
+            ctl->Q = ctl->gam * Qp + 1.0;
+            ctl->C = (ctl->gam * Qp * ctl->C + ctl->f) / ctl->Q;
+        } else {
+            ctl->lam1 = tot[0];  // start-up: k_g2 forms lam2, lam4 and f next
+        }
     }
 }
 
@@ -503,10 +526,11 @@ __global__ void k_gradient(SolverBufs<T> B, int iter) {
 }
 
 // ---------------------------------------------------------------------------
-// The end of an inner iteration in one pass: update_W's g2 = D^T (DU - W),
-// lam2, lam4 (k_g2, UPDATE_W) and get_gradient's d with the next step size
-// and the stopping test (k_gradient, iter 1).  g2[i] is formed and used by
-// the same thread, so the pass saves the store-and-reload of g2 and a launch.
+// The end of an inner iteration in one pass: update_W's g2 = D^T (DU - W)
+// (its lam2 and lam4 come from k_shrink) and get_gradient's d with the next
+// step size and the stopping test (k_gradient, iter 1).  g2[i] is formed and
+// used by the same thread, so the pass saves the store-and-reload of g2 and a
+// launch.
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo) {
@@ -517,7 +541,6 @@ __global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo
     const long n = B.n;
     const T* __restrict__ DU = B.DU[cur];
     const T* __restrict__ W = B.W;
-    const T* __restrict__ S = B.sig;
     T* __restrict__ g2o = B.g2[cur];
     const T mdb = scal<T>(ctl->muDbeta);
     const A mdbA = scal<A>(ctl->muDbeta);
@@ -527,7 +550,6 @@ __global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo
     const Ext<T>* __restrict__ xs = static_cast<const Ext<T>*>(B.xstar);
     const double iscl = 1.0 / ctl->scl;
     T* __restrict__ d = B.d;
-    ProdAcc<T> l2, l4;
     ProdAcc<A> s0, s1, s2, s4;
     double s3 = 0.0;
     // the gradient part of one voxel, given its g2
@@ -555,12 +577,8 @@ __global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo
             Two<T> va[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const Two<T> du = ld2(DU + c * n + i), w = ld2(W + c * n + i), sg = ld2(S + c * n + i);
+                const Two<T> du = ld2(DU + c * n + i), w = ld2(W + c * n + i);
                 va[c] = {du.a - w.a, du.b - w.b};
-                l2.add(va[c].a, va[c].a);
-                l2.add(va[c].b, va[c].b);
-                l4.add(va[c].a, sg.a);
-                l4.add(va[c].b, sg.b);
             }
             const T v0m = DU[nb.ym] - W[nb.ym];
             const Two<T> dxm = ld2(DU + n + nb.xm), wxm = ld2(W + n + nb.xm);
@@ -583,31 +601,18 @@ __global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo
         const T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
         const T g2i = v0m - v0 + v1m - v1 + v2m - v2;
         g2o[i] = g2i;
-        l2.add(v0, v0);
-        l2.add(v1, v1);
-        l2.add(v2, v2);
-        l4.add(v0, S[i]);
-        l4.add(v1, S[n + i]);
-        l4.add(v2, S[2 * n + i]);
         T di;
         grad(i, g2i, g[i], dts[i], U[i], Up[i], gp[i], g2p[i], di);
         d[i] = di;
     }
-    double v[7] = {l2.value(), l4.value(), s0.value(), s1.value(), s2.value(), s3, s4.value()}, tot[7];
-    if (grid_reduce<7>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
-        // update_W (:1016-1029) and the nonmonotone reference values (:1176-1177)
-        ctl->lam2 = tot[0];
-        ctl->lam4 = tot[1];
-        ctl->f += ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
-        double Qp = ctl->Q;
-        ctl->Q = ctl->gam * Qp + 1.0;
-        ctl->C = (ctl->gam * Qp * ctl->C + ctl->f) / ctl->Q;
+    double v[5] = {s0.value(), s1.value(), s2.value(), s3, s4.value()}, tot[5];
+    if (grid_reduce<5>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         // get_gradient, the next BB step and the inner stopping test
-        ctl->dd = tot[4];
-        ctl->tau = fabs(tot[3] / tot[6]);
-        ctl->nrmup = sqrt(tot[2]);
-        ctl->relchg = sqrt(tot[3]) / ctl->nrmup;
-        if (B.trace && xs) B.trace[ctl->count_total] = sqrt(tot[5]);
+        ctl->dd = tot[2];
+        ctl->tau = fabs(tot[1] / tot[4]);
+        ctl->nrmup = sqrt(tot[0]);
+        ctl->relchg = sqrt(tot[1]) / ctl->nrmup;
+        if (B.trace && xs) B.trace[ctl->count_total] = sqrt(tot[3]);
         ctl->count_total += 1;
         const int natural = ((ctl->relchg < ctl->tol_inn) && !ctl->fst) || (ctl->count_total >= ctl->maxit);
         ctl->paused = !natural && (ctl->count_total >= ctl->pause_at);
