@@ -10,6 +10,29 @@ namespace tv3 {
 
 struct Ctl;
 
+void throw_cuda(cudaError_t e, const char* what);
+
+// Launch with programmatic stream serialization: inside a stream (and in a
+// captured graph) the kernel's blocks may be scheduled while the previous
+// kernel drains, hiding most of the launch gap.  The kernel must call
+// pdl_wait() (count_launch does) before touching memory the previous kernel
+// writes.
+template <class... P, class... A>
+void launch_k(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, args...);
+    if (e != cudaSuccess) throw_cuda(e, "cudaLaunchKernelEx");
+}
+
 enum SpmvEpi : int { SPMV_PLAIN = 0, SPMV_SUB = 1, SPMV_LAM35 = 2, SPMV_NORM2 = 3 };
 
 // Slack (elements) behind the index and value arrays of a CSR operator: the

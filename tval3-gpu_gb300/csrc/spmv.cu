@@ -267,10 +267,10 @@ static void launch_mm(const SpmvArgs<T, V>& a, cudaStream_t s) {
 template <class T, class V, int EPI, int VEC>
 static void launch_v(const SpmvArgs<T, V>& a, int G, int grid, cudaStream_t s) {
     switch (G) {
-        case 4: k_spmv<T, V, 4, EPI, VEC><<<grid, 256, 0, s>>>(a); break;
-        case 8: k_spmv<T, V, 8, EPI, VEC><<<grid, 256, 0, s>>>(a); break;
-        case 16: k_spmv<T, V, 16, EPI, VEC><<<grid, 256, 0, s>>>(a); break;
-        default: k_spmv<T, V, 32, EPI, VEC><<<grid, 256, 0, s>>>(a); break;
+        case 4: launch_k(k_spmv<T, V, 4, EPI, VEC>, dim3(grid), dim3(256), 0, s, a); break;
+        case 8: launch_k(k_spmv<T, V, 8, EPI, VEC>, dim3(grid), dim3(256), 0, s, a); break;
+        case 16: launch_k(k_spmv<T, V, 16, EPI, VEC>, dim3(grid), dim3(256), 0, s, a); break;
+        default: launch_k(k_spmv<T, V, 32, EPI, VEC>, dim3(grid), dim3(256), 0, s, a); break;
     }
 }
 

@@ -643,7 +643,8 @@ __global__ void __launch_bounds__(256, 4) k_bt_coef(SolverBufs<T> B) {
     const T *__restrict__ DU = B.DU[cur], *__restrict__ DUp = B.DU[prv];
     const T *__restrict__ Au = B.Au[cur], *__restrict__ Aup = B.Au[prv];
     const T *__restrict__ W = B.W, *__restrict__ S = B.sig, *__restrict__ bb = B.b, *__restrict__ dl = B.delta;
-    A a2(0.f), b2(0.f), c2(0.f), a4(0.f), b4(0.f), a3(0.f), b3(0.f), c3(0.f), a5(0.f), b5(0.f);
+    // compensated product sums (ProdAcc), as in the other reductions
+    ProdAcc<A> a2, b2, c2, a4, b4, a3, b3, c3, a5, b5;
     const long N = n > m ? n : m;
     GRID_STRIDE(i, N) {
         if (i < n) {
@@ -652,25 +653,25 @@ __global__ void __launch_bounds__(256, 4) k_bt_coef(SolverBufs<T> B) {
                 const long k = c * n + i;
                 const T dp = DUp[k];
                 const A v0 = to_acc(dp - W[k]), dv = to_acc(DU[k] - dp), s = to_acc(S[k]);
-                a2 += v0 * v0;
-                b2 += v0 * dv;
-                c2 += dv * dv;
-                a4 += s * v0;
-                b4 += s * dv;
+                a2.add(v0, v0);
+                b2.add(v0, dv);
+                c2.add(dv, dv);
+                a4.add(s, v0);
+                b4.add(s, dv);
             }
         }
         if (i < m) {
             const T ap = Aup[i];
             const A r0 = to_acc(ap) - to_acc(bb[i]), dr = to_acc(Au[i]) - to_acc(ap), d = to_acc(dl[i]);
-            a3 += r0 * r0;
-            b3 += r0 * dr;
-            c3 += dr * dr;
-            a5 += d * r0;
-            b5 += d * dr;
+            a3.add(r0, r0);
+            b3.add(r0, dr);
+            c3.add(dr, dr);
+            a5.add(d, r0);
+            b5.add(d, dr);
         }
     }
-    double v[10] = {acc_d(a2), acc_d(b2), acc_d(c2), acc_d(a4), acc_d(b4),
-                    acc_d(a3), acc_d(b3), acc_d(c3), acc_d(a5), acc_d(b5)},
+    double v[10] = {a2.value(), b2.value(), c2.value(), a4.value(), b4.value(),
+                    a3.value(), b3.value(), c3.value(), a5.value(), b5.value()},
            tot[10];
     if (grid_reduce<10>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         // alpha was already multiplied by gamma once by the Armijo epilogue of k_g2
@@ -1024,7 +1025,7 @@ static int resident_grid(const void* kernel, int want) {
 }
 template <class... P, class... A>
 static void rlaunch(void (*kernel)(P...), int want, cudaStream_t s, A... args) {
-    kernel<<<resident_grid(reinterpret_cast<const void*>(kernel), want), 256, 0, s>>>(args...);
+    launch_k(kernel, dim3(resident_grid(reinterpret_cast<const void*>(kernel), want)), dim3(256), 0, s, args...);
 }
 
 static int ew_grid(long n) {
@@ -1060,7 +1061,7 @@ template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s) {
     rlaunch(k_Dd_norm<T>, B.grid, s, B, geo_of(B));
 }
 template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s) {
-    if (mode == EPI_G2_DESCEND || mode == EPI_G2_RESTART) k_armijo<T><<<1, 32, 0, s>>>(B, mode);
+    if (mode == EPI_G2_DESCEND || mode == EPI_G2_RESTART) launch_k(k_armijo<T>, dim3(1), dim3(32), 0, s, B, mode);
     else rlaunch(k_g2<T>, B.grid, s, B, geo_of(B));
 }
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s) {

@@ -739,8 +739,8 @@ void TiledT<T, V>::apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) cons
     b.zrows = zrows.p;
     b.nzero = nzero;
     const long grid = std::max<long>((long)nwork + (nzero + 511) / 512, 1);
-    if (epi == SPMV_SUB) k_spmv_tiled<T, V, SPMV_SUB, 8><<<(unsigned)grid, 512, smem, s>>>(b);
-    else k_spmv_tiled<T, V, SPMV_PLAIN, 8><<<(unsigned)grid, 512, smem, s>>>(b);
+    if (epi == SPMV_SUB) launch_k(k_spmv_tiled<T, V, SPMV_SUB, 8>, dim3((unsigned)grid), dim3(512), smem, s, b);
+    else launch_k(k_spmv_tiled<T, V, SPMV_PLAIN, 8>, dim3((unsigned)grid), dim3(512), smem, s, b);
     TV3_CUDA(cudaGetLastError());
 }
 
@@ -1054,13 +1054,13 @@ void TiledN<T, V>::apply(const TiledNArgs<T, V>& a, int epi, cudaStream_t s) con
     const size_t smem = std::max<size_t>((size_t)ty * tx * tz * sizeof(T), 16);
     TiledNArgs<T, V> b = a;
     b.tile_order = tile_order.p;
-    if (nwork > 0) k_spmv_tiledN<T, V, 8><<<nwork, 512, smem, s>>>(b);
+    if (nwork > 0) launch_k(k_spmv_tiledN<T, V, 8>, dim3(nwork), dim3(512), smem, s, b);
     const int g = (int)std::max<long>(1, std::min<long>((a.m + 255) / 256, (long)num_sms() * 4));
     switch (epi) {
-        case SPMV_SUB: k_tiledN_reduce<T, V, SPMV_SUB><<<g, 256, 0, s>>>(b); break;
-        case SPMV_LAM35: k_tiledN_reduce<T, V, SPMV_LAM35><<<g, 256, 0, s>>>(b); break;
-        case SPMV_NORM2: k_tiledN_reduce<T, V, SPMV_NORM2><<<g, 256, 0, s>>>(b); break;
-        default: k_tiledN_reduce<T, V, SPMV_PLAIN><<<g, 256, 0, s>>>(b); break;
+        case SPMV_SUB: launch_k(k_tiledN_reduce<T, V, SPMV_SUB>, dim3(g), dim3(256), 0, s, b); break;
+        case SPMV_LAM35: launch_k(k_tiledN_reduce<T, V, SPMV_LAM35>, dim3(g), dim3(256), 0, s, b); break;
+        case SPMV_NORM2: launch_k(k_tiledN_reduce<T, V, SPMV_NORM2>, dim3(g), dim3(256), 0, s, b); break;
+        default: launch_k(k_tiledN_reduce<T, V, SPMV_PLAIN>, dim3(g), dim3(256), 0, s, b); break;
     }
     TV3_CUDA(cudaGetLastError());
 }

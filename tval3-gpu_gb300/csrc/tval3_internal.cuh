@@ -140,8 +140,17 @@ struct Ctl {
     int pause_at, paused;
 };
 
-// every solver kernel counts itself once (block 0, thread 0)
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization (launch_k) may have its blocks scheduled while the kernel
+// before it drains; griddepcontrol.wait holds every thread until that kernel
+// has completed and its memory writes are visible.  For a kernel launched
+// without the attribute it returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Entry of every solver kernel, before its first global-memory access: the
+// dependent-launch wait, then the kernel counts itself once (block 0, thread 0).
 __device__ __forceinline__ void count_launch(Ctl* c) {
+    pdl_wait();
     if (c && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c->launches, 1u);
 }
 
