@@ -84,7 +84,7 @@ struct SolverBufs {
     T* d;
     T* DtsAtd;
     T* Atb;
-    T* W;          // 3n
+    T* W[2];       // 3n each; slot ctl->wsel is current, the other takes the next W
     T* sig;        // 3n
     T* b;          // m, scaled
     T* delta;      // m

@@ -64,7 +64,7 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
         throw Error{TVAL3_ERR_UNSUPPORTED, "voxels x layers exceeds the 32-bit index range of the stencil kernels"};
     A->prepare(L);
     if (L == 1) A->set_volume(p_, q_, r_);
-    const long nvec = 22, mvec = 4;
+    const long nvec = 25, mvec = 4;
     nv.alloc(nvec * n);
     mv.alloc(mvec * std::max<long>(m, 1));
     ctl.alloc(1);
@@ -81,7 +81,7 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
     B.g2[0] = take(1); B.g2[1] = take(1);
     B.DU[0] = take(3); B.DU[1] = take(3);
     B.d = take(1); B.DtsAtd = take(1); B.Atb = take(1);
-    B.W = take(3); B.sig = take(3);
+    B.W[0] = take(3); B.W[1] = take(3); B.sig = take(3);
     B.rcdU = take(1);
     T* w = mv.p;
     const long mm = std::max<long>(m, 1);
@@ -284,9 +284,11 @@ void Solver<T>::run_host(cudaStream_t s) {
                 launch_descend<T>(B, 1, s);
                 get_g(EPI_G2_RESTART, s);
             }
+            // update_W at the point taken (an accepted full step committed the
+            // descent's W in the Armijo kernel instead)
+            launch_shrink<T>(B, EPI_G2_UPDATE_W, s);
         }
-        // ---- update_W (:965-1029), reference values, gradient, RelChg
-        launch_shrink<T>(B, EPI_G2_UPDATE_W, s);
+        // ---- g2 of update_W (:965-1029), gradient, RelChg
         launch_g2_gradient<T>(B, s);
         read_ctl(s);
         fst = false;
@@ -367,9 +369,13 @@ void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const 
                     get_g(EPI_G2_RESTART, cs, &rb);
                     rb.end();
                 }
+                // update_W at the point taken (an accepted full step committed
+                // the descent's W in the Armijo kernel instead)
+                ab.begin();
+                launch_shrink<T>(B, EPI_G2_UPDATE_W, cs);
+                ab.end();
             }
             ib.begin();
-            launch_shrink<T>(B, EPI_G2_UPDATE_W, cs);
             launch_g2_gradient<T>(B, cs);  // sets h_inner
             ib.end();
         }

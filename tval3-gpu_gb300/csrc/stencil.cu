@@ -16,6 +16,8 @@
 //   k_shrink               shrinkage_kernel, 3d/tval3_gpu_3d_kernels.cu:1249-1300
 //   k_gradient             get_gradient_gpu :896-919 and the RelChg test :1178-1200
 //   k_bt_coef / k_bt_apply min_u_gpu Armijo branch :848-890 with update_g_gpu :706-818
+//                          (g2 at the accepted point is not formed: update_W's
+//                          g2 replaces it before anything reads it)
 //   k_outer_relchg         :1204-1220
 //   k_mlp                  update_mlp_gpu :1034-1083 and continuation :1222-1237
 //   k_outer_grad           DtsAtd and get_gradient :1238-1249
@@ -200,32 +202,80 @@ __global__ void k_D_only(SolverBufs<T> B, Geo g) {
 }
 
 // ---------------------------------------------------------------------------
+// Shrinkage of one voxel (shrinkage_kernel, 3d/tval3_gpu_3d_kernels.cu:1249-1300,
+// plus the isotropic form): u = DU - sigma/beta, W = shrink(u, 1/beta); adds
+// the voxel's TV term to l1 and (DU - W)^2, sigma (DU - W) to l2, l4 (the
+// sums update_W needs).  Used by k_shrink and, speculatively for the full
+// step, by k_descend.
+// ---------------------------------------------------------------------------
+template <class T, class A>
+__device__ __forceinline__ void shrink_voxel(T d0, T d1, T d2, T s0, T s1, T s2, T bt, T ib, int iso, T& w0, T& w1,
+                                             T& w2, A& l1, ProdAcc<T>& l2, ProdAcc<T>& l4) {
+    T u0 = d0 - div_beta(s0, bt, ib);
+    T u1 = d1 - div_beta(s1, bt, ib);
+    T u2 = d2 - div_beta(s2, bt, ib);
+    if (!iso) {
+        T t0 = fabs(u0) - ib, t1 = fabs(u1) - ib, t2 = fabs(u2) - ib;
+        t0 = (t0 >= T(0)) ? t0 : T(0);
+        t1 = (t1 >= T(0)) ? t1 : T(0);
+        t2 = (t2 >= T(0)) ? t2 : T(0);
+        w0 = (u0 >= T(0)) ? t0 : -t0;
+        w1 = (u1 >= T(0)) ? t1 : -t1;
+        w2 = (u2 >= T(0)) ? t2 : -t2;
+        l1 += to_acc(t0) + to_acc(t1) + to_acc(t2);
+    } else {
+        T nv = sqrt(u0 * u0 + u1 * u1 + u2 * u2);
+        T t = nv - ib;
+        t = (t > T(0)) ? t : T(0);
+        T sc = (t > T(0)) ? t / nv : T(0);
+        w0 = u0 * sc;
+        w1 = u1 * sc;
+        w2 = u2 * sc;
+        l1 += to_acc(t);
+    }
+    const T v0 = d0 - w0, v1 = d1 - w1, v2 = d2 - w2;
+    l2.add(v0, v0);
+    l2.add(v1, v1);
+    l2.add(v2, v2);
+    l4.add(v0, s0);
+    l4.add(v1, s1);
+    l4.add(v2, s2);
+}
+
+// ---------------------------------------------------------------------------
 // descent step fused with D: U = P(Up - tau d), DU = D U, and the two terms
 // of the new point's Lagrangian that need DU: lam2 = ||DU - W||^2 and
 // lam4 = <sigma, DU - W> (get_g_gpu's lam2_4 pass, :528-547, done here while
-// DU is in registers instead of by a second pass over DU, W and sigma).  U at
-// the forward neighbours is recomputed from Up and d (same expression, so
-// bit-identical to the stored value).  Normal mode reads the current slot, writes the other
+// DU is in registers instead of by a second pass over DU, W and sigma).  The
+// same pass forms update_W's shrinkage of the full step into the free W slot
+// with its lam1, lam2, lam4: most steps pass the Armijo test, which then
+// commits it (k_armijo) and no shrinkage pass runs.  U at the forward
+// neighbours is recomputed from Up and d (same expression, so bit-identical
+// to the stored value).  Normal mode reads the current slot, writes the other
 // one and flips the parity (the previous values become Up, gp, g2p, Aup, DUp
 // without copies, :831-833); restart mode reads the previous slot (U = Up,
 // :878) and writes the current one.
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void __launch_bounds__(256, 6) k_descend(SolverBufs<T> B, Geo g, int restart) {
+__global__ void __launch_bounds__(256, 4) k_descend(SolverBufs<T> B, Geo g, int restart) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
-    const int cur = ctl->parity;
+    using A = acc_t<T>;
+    const int cur = ctl->parity, ws = ctl->wsel;
     const int src = restart ? 1 - cur : cur, dst = restart ? cur : 1 - cur;
     const T* __restrict__ Up = B.U[src];
     const T* __restrict__ d = B.d;
     T* __restrict__ U = B.U[dst];
     T* __restrict__ DU = B.DU[dst];
-    const T* __restrict__ W = B.W;
+    const T* __restrict__ W = B.W[ws];
+    T* __restrict__ Wn = B.W[1 - ws];  // speculative update_W of the full step
     const T* __restrict__ S = B.sig;
     const T mt = scal<T>(-ctl->tau);
-    const int nn = ctl->nonneg;
+    const T bt = scal<T>(ctl->beta), ib = scal<T>(1.0 / ctl->beta);
+    const int nn = ctl->nonneg, iso = ctl->iso;
     const long n = B.n;
-    ProdAcc<T> l2, l4;
+    ProdAcc<T> l2, l4, l2s, l4s;
+    A l1s(0.f);
     if (g.l.d == 1 && (g.p.d % 2) == 0) {
         // voxel pairs (i, i+1) with y even: they share x and z, so their +x
         // and +z neighbours are pairs too and the +y neighbour of i is i+1
@@ -242,16 +292,24 @@ __global__ void __launch_bounds__(256, 6) k_descend(SolverBufs<T> B, Geo g, int 
             const T uza = proj(uz.a + mt * dz.a, nn), uzb = proj(uz.b + mt * dz.b, nn);
             const Two<T> dv[3] = {{ucb - uca, uyb - ucb}, {uxa - uca, uxb - ucb}, {uza - uca, uzb - ucb}};
             st2(U + i, uca, ucb);
+            Two<T> sg[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 st2(DU + c * n + i, dv[c].a, dv[c].b);
-                const Two<T> w = ld2(W + c * n + i), sg = ld2(S + c * n + i);
+                const Two<T> w = ld2(W + c * n + i);
+                sg[c] = ld2(S + c * n + i);
                 const T va = dv[c].a - w.a, vb = dv[c].b - w.b;
                 l2.add(va, va);
                 l2.add(vb, vb);
-                l4.add(va, sg.a);
-                l4.add(vb, sg.b);
+                l4.add(va, sg[c].a);
+                l4.add(vb, sg[c].b);
             }
+            T a0, a1, a2, b0, b1, b2;
+            shrink_voxel(dv[0].a, dv[1].a, dv[2].a, sg[0].a, sg[1].a, sg[2].a, bt, ib, iso, a0, a1, a2, l1s, l2s, l4s);
+            shrink_voxel(dv[0].b, dv[1].b, dv[2].b, sg[0].b, sg[1].b, sg[2].b, bt, ib, iso, b0, b1, b2, l1s, l2s, l4s);
+            st2(Wn + i, a0, b0);
+            st2(Wn + n + i, a1, b1);
+            st2(Wn + 2 * n + i, a2, b2);
         }
     } else {
         GRID_STRIDE(i, n) {
@@ -262,19 +320,29 @@ __global__ void __launch_bounds__(256, 6) k_descend(SolverBufs<T> B, Geo g, int 
             T uz = proj(Up[nb.zp] + mt * d[nb.zp], nn);
             const T dv[3] = {uy - uc, ux - uc, uz - uc};
             U[i] = uc;
+            T sg[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 DU[c * n + i] = dv[c];
+                sg[c] = S[c * n + i];
                 const T v = dv[c] - W[c * n + i];
                 l2.add(v, v);
-                l4.add(v, S[c * n + i]);
+                l4.add(v, sg[c]);
             }
+            T w0, w1, w2;
+            shrink_voxel(dv[0], dv[1], dv[2], sg[0], sg[1], sg[2], bt, ib, iso, w0, w1, w2, l1s, l2s, l4s);
+            Wn[i] = w0;
+            Wn[n + i] = w1;
+            Wn[2 * n + i] = w2;
         }
     }
-    double v[2] = {l2.value(), l4.value()}, tot[2];
-    if (grid_reduce<2>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+    double v[5] = {l2.value(), l4.value(), acc_d(l1s), l2s.value(), l4s.value()}, tot[5];
+    if (grid_reduce<5>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
         ctl->lam2 = tot[0];
         ctl->lam4 = tot[1];
+        ctl->lam1s = tot[2];
+        ctl->lam2s = tot[3];
+        ctl->lam4s = tot[4];
         if (!restart) ctl->parity = 1 - cur;
     }
 }
@@ -314,9 +382,8 @@ __device__ __forceinline__ void armijo(Ctl* c) {
 
 // ---------------------------------------------------------------------------
 // g2 = D^T (DU - W) with lam2 = ||DU - W||^2 and lam4 = <sigma, DU - W>
-// (start-up get_g; after a descent lam2 and lam4 come from k_descend and the
-// g2 of that point is replaced by update_W's before anything reads it, except
-// on the backtracking path, which forms its own with k_bt_g2).
+// (start-up get_g; after a descent lam2 and lam4 come from k_descend, and the
+// g2 of the new point is replaced by update_W's before anything reads it).
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void k_g2(SolverBufs<T> B, Geo g) {
@@ -325,7 +392,7 @@ __global__ void k_g2(SolverBufs<T> B, Geo g) {
     const int cur = ctl->parity;
     const long n = B.n;
     const T* __restrict__ DU = B.DU[cur];
-    const T* __restrict__ W = B.W;
+    const T* __restrict__ W = B.W[ctl->wsel];
     const T* __restrict__ S = B.sig;
     T* __restrict__ g2 = B.g2[cur];
     ProdAcc<T> l2, l4;
@@ -368,7 +435,21 @@ __global__ void k_armijo(SolverBufs<T> B, int mode) {
         ctl->cnt = 0;
         ctl->c_armij = ctl->dd * ctl->tau * ctl->c_arm * ctl->beta;
         armijo(ctl);
-        if (ctl->armijo_fail) ctl->alpha *= ctl->gamma;
+        if (ctl->armijo_fail) {
+            ctl->alpha *= ctl->gamma;
+        } else {
+            // full step accepted: update_W is the descent's speculative one
+            // (:1016-1029), then the nonmonotone reference values (:1176-1177)
+            ctl->wsel = 1 - ctl->wsel;
+            ctl->f -= ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
+            ctl->lam1 = ctl->lam1s;
+            ctl->lam2 = ctl->lam2s;
+            ctl->lam4 = ctl->lam4s;
+            ctl->f += ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
+            const double Qp = ctl->Q;
+            ctl->Q = ctl->gam * Qp + 1.0;
+            ctl->C = (ctl->gam * Qp * ctl->C + ctl->f) / ctl->Q;
+        }
         if (B.use_graph) cudaGraphSetConditional(B.h_arm, ctl->armijo_fail ? 1u : 0u);
     } else {
         ctl->armijo_fail = 0;
@@ -386,64 +467,33 @@ __global__ void __launch_bounds__(256, 4) k_shrink(SolverBufs<T> B, int mode) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     using A = acc_t<T>;
-    const int cur = ctl->parity;
+    const int cur = ctl->parity, ws = ctl->wsel;
     const long n = B.n;
     const T* __restrict__ DU = B.DU[cur];
     const T* __restrict__ S = B.sig;
-    T* __restrict__ W = B.W;
+    T* __restrict__ W = B.W[1 - ws];  // the new W goes to the free slot
     const T bt = scal<T>(ctl->beta), ib = scal<T>(1.0 / ctl->beta);
     const int iso = ctl->iso;
     A l1(0.f);
     ProdAcc<T> l2, l4;
-    // one voxel: v = DU - sigma/beta -> W, adding its TV term to l1 and
-    // (DU - W)^2, sigma (DU - W) to l2, l4
-    auto voxel = [&](T d0, T d1, T d2, T s0, T s1, T s2, T& w0, T& w1, T& w2) {
-        T u0 = d0 - div_beta(s0, bt, ib);
-        T u1 = d1 - div_beta(s1, bt, ib);
-        T u2 = d2 - div_beta(s2, bt, ib);
-        if (!iso) {
-            T t0 = fabs(u0) - ib, t1 = fabs(u1) - ib, t2 = fabs(u2) - ib;
-            t0 = (t0 >= T(0)) ? t0 : T(0);
-            t1 = (t1 >= T(0)) ? t1 : T(0);
-            t2 = (t2 >= T(0)) ? t2 : T(0);
-            w0 = (u0 >= T(0)) ? t0 : -t0;
-            w1 = (u1 >= T(0)) ? t1 : -t1;
-            w2 = (u2 >= T(0)) ? t2 : -t2;
-            l1 += to_acc(t0) + to_acc(t1) + to_acc(t2);
-        } else {
-            T nv = sqrt(u0 * u0 + u1 * u1 + u2 * u2);
-            T t = nv - ib;
-            t = (t > T(0)) ? t : T(0);
-            T sc = (t > T(0)) ? t / nv : T(0);
-            w0 = u0 * sc;
-            w1 = u1 * sc;
-            w2 = u2 * sc;
-            l1 += to_acc(t);
-        }
-        const T v0 = d0 - w0, v1 = d1 - w1, v2 = d2 - w2;
-        l2.add(v0, v0);
-        l2.add(v1, v1);
-        l2.add(v2, v2);
-        l4.add(v0, s0);
-        l4.add(v1, s1);
-        l4.add(v2, s2);
-    };
     if (PAIRS) {
         GRID_STRIDE_PAIRS(i, n) {
             const Two<T> d0 = ld2(DU + i), d1 = ld2(DU + n + i), d2 = ld2(DU + 2 * n + i);
             const Two<T> s0 = ld2(S + i), s1 = ld2(S + n + i), s2 = ld2(S + 2 * n + i);
             T a0, a1, a2, b0, b1, b2;
-            voxel(d0.a, d1.a, d2.a, s0.a, s1.a, s2.a, a0, a1, a2);
-            voxel(d0.b, d1.b, d2.b, s0.b, s1.b, s2.b, b0, b1, b2);
+            shrink_voxel(d0.a, d1.a, d2.a, s0.a, s1.a, s2.a, bt, ib, iso, a0, a1, a2, l1, l2, l4);
+            shrink_voxel(d0.b, d1.b, d2.b, s0.b, s1.b, s2.b, bt, ib, iso, b0, b1, b2, l1, l2, l4);
             st2(W + i, a0, b0);
             st2(W + n + i, a1, b1);
             st2(W + 2 * n + i, a2, b2);
         }
     } else {
-        GRID_STRIDE(i, n) voxel(DU[i], DU[n + i], DU[2 * n + i], S[i], S[n + i], S[2 * n + i], W[i], W[n + i], W[2 * n + i]);
+        GRID_STRIDE(i, n) shrink_voxel(DU[i], DU[n + i], DU[2 * n + i], S[i], S[n + i], S[2 * n + i], bt, ib, iso, W[i],
+                                       W[n + i], W[2 * n + i], l1, l2, l4);
     }
     double v[3] = {acc_d(l1), l2.value(), l4.value()}, tot[3];
     if (grid_reduce<3>(v, B.part, B.ticket, tot) && threadIdx.x == 0) {
+        ctl->wsel = 1 - ws;
         if (mode == EPI_G2_UPDATE_W) {
             // update_W (:1016-1029): f takes the new lam1, lam2, lam4; then the
             // nonmonotone reference values (:1176-1177)
@@ -540,7 +590,7 @@ __global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo
     const int cur = ctl->parity, prv = 1 - cur;
     const long n = B.n;
     const T* __restrict__ DU = B.DU[cur];
-    const T* __restrict__ W = B.W;
+    const T* __restrict__ W = B.W[ctl->wsel];
     T* __restrict__ g2o = B.g2[cur];
     const T mdb = scal<T>(ctl->muDbeta);
     const A mdbA = scal<A>(ctl->muDbeta);
@@ -642,7 +692,7 @@ __global__ void __launch_bounds__(256, 4) k_bt_coef(SolverBufs<T> B) {
     const long n = B.n, m = B.m;
     const T *__restrict__ DU = B.DU[cur], *__restrict__ DUp = B.DU[prv];
     const T *__restrict__ Au = B.Au[cur], *__restrict__ Aup = B.Au[prv];
-    const T *__restrict__ W = B.W, *__restrict__ S = B.sig, *__restrict__ bb = B.b, *__restrict__ dl = B.delta;
+    const T *__restrict__ W = B.W[ctl->wsel], *__restrict__ S = B.sig, *__restrict__ bb = B.b, *__restrict__ dl = B.delta;
     // compensated product sums (ProdAcc), as in the other reductions
     ProdAcc<A> a2, b2, c2, a4, b4, a3, b3, c3, a5, b5;
     const long N = n > m ? n : m;
@@ -726,29 +776,6 @@ __global__ void k_bt_apply(SolverBufs<T> B) {
             T p = Aup[i];
             Au[i] = p + al * (Au[i] - p);
         }
-    }
-}
-
-// g2 at the accepted point of the backtracking: D^T (DU(a) - W) with
-// DU(a) = DUp + a (DU1 - DUp), before k_bt_apply overwrites DU1 (D^T is
-// linear, so this is the reference's g2p + a (g2 - g2p), :706-818).
-template <class T>
-__global__ void k_bt_g2(SolverBufs<T> B, Geo g) {
-    Ctl* ctl = B.ctl;
-    count_launch(ctl);
-    if (ctl->armijo_fail) return;  // restart path: the restart's get_g and update_W follow
-    const int cur = ctl->parity, prv = 1 - cur;
-    const long n = B.n;
-    const T al = scal<T>(ctl->alpha);
-    const T *__restrict__ DU = B.DU[cur], *__restrict__ DUp = B.DU[prv], *__restrict__ W = B.W;
-    T* __restrict__ g2 = B.g2[cur];
-    auto v = [&](long j) {
-        const T p = DUp[j];
-        return p + al * (DU[j] - p) - W[j];
-    };
-    GRID_STRIDE(i, n) {
-        Nb nb = neighbours(g, i);
-        g2[i] = v(nb.ym) - v(i) + v(n + nb.xm) - v(n + i) + v(2 * n + nb.zm) - v(2 * n + i);
     }
 }
 
@@ -877,7 +904,7 @@ __global__ void k_mlp(SolverBufs<T> B) {
     const int cur = ctl->parity;
     const long n = B.n, m = B.m;
     const T bt = scal<T>(ctl->beta), mut = scal<T>(ctl->mu);
-    const T *__restrict__ DU = B.DU[cur], *__restrict__ W = B.W, *__restrict__ Au = B.Au[cur], *__restrict__ bb = B.b;
+    const T *__restrict__ DU = B.DU[cur], *__restrict__ W = B.W[ctl->wsel], *__restrict__ Au = B.Au[cur], *__restrict__ bb = B.b;
     T *__restrict__ S = B.sig, *__restrict__ dl = B.delta;
     A l4(0.f), l5(0.f);
     const long N = n > m ? n : m;
@@ -1076,7 +1103,6 @@ template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t
 }
 template <class T> void launch_bt_coef(SolverBufs<T>& B, cudaStream_t s) { rlaunch(k_bt_coef<T>, B.grid, s, B); }
 template <class T> void launch_bt_apply(SolverBufs<T>& B, cudaStream_t s) {
-    rlaunch(k_bt_g2<T>, B.grid, s, B, geo_of(B));
     rlaunch(k_bt_apply<T>, B.grid, s, B);
 }
 template <class T> void launch_outer_relchg(SolverBufs<T>& B, cudaStream_t s) { rlaunch(k_outer_relchg<T>, B.grid, s, B); }

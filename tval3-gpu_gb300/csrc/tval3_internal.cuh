@@ -138,6 +138,11 @@ struct Ctl {
     // pausing: the solve stops after pause_at total iterations without ending
     // the outer iteration, so a saved state resumes exactly
     int pause_at, paused;
+    // W slot in use; the descent writes a speculative update_W result (W of
+    // the full step, its lam1, lam2, lam4) into the other slot, committed by
+    // the Armijo test when the full step is accepted
+    int wsel;
+    double lam1s, lam2s, lam4s;
 };
 
 // Programmatic dependent launch: a kernel launched with programmatic stream
