@@ -316,16 +316,67 @@ template <class T>
 void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const void* d_Ut, cudaStream_t cs,
                              bool resume) {
     const unsigned run = (o.maxcnt > 0 && o.maxit > 0) ? 1u : 0u;
-    cudaGraphConditionalHandle h_outer, h_inner, h_fst, h_arm, h_restart, h_mlp;
+    // a conditional handle drives one conditional node: the unrolled first
+    // inner iteration has its own Armijo and restart handles
+    cudaGraphConditionalHandle h_outer, h_inner, h_fst = 0, h_arm, h_restart, h_arm1, h_restart1, h_mlp;
     TV3_CUDA(cudaGraphConditionalHandleCreate(&h_outer, top, run, cudaGraphCondAssignDefault));
     TV3_CUDA(cudaGraphConditionalHandleCreate(&h_inner, top, 1, cudaGraphCondAssignDefault));
-    TV3_CUDA(cudaGraphConditionalHandleCreate(&h_fst, top, 1, cudaGraphCondAssignDefault));
+    if (resume) TV3_CUDA(cudaGraphConditionalHandleCreate(&h_fst, top, 1, cudaGraphCondAssignDefault));
     TV3_CUDA(cudaGraphConditionalHandleCreate(&h_arm, top, 0, cudaGraphCondAssignDefault));
     TV3_CUDA(cudaGraphConditionalHandleCreate(&h_restart, top, 0, cudaGraphCondAssignDefault));
+    if (!resume) {
+        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_arm1, top, 0, cudaGraphCondAssignDefault));
+        TV3_CUDA(cudaGraphConditionalHandleCreate(&h_restart1, top, 0, cudaGraphCondAssignDefault));
+    }
     TV3_CUDA(cudaGraphConditionalHandleCreate(&h_mlp, top, 0, cudaGraphCondAssignDefault));
     g_top = top;
     B.use_graph = 1;
-    B.h_inner = h_inner; B.h_arm = h_arm; B.h_mlp = h_mlp;
+    B.h_inner = h_inner; B.h_mlp = h_mlp;
+    // one inner iteration (:1150-1200) appended to body `ib` (not capturing on
+    // entry or exit).  first: 0 = no first-step size, 1 = the first-step size
+    // unconditionally (the unrolled first iteration of an outer iteration),
+    // 2 = an IF node on the control block's fst (a resumed state).
+    auto iteration = [&](Body& ib, int first, cudaGraphConditionalHandle harm, cudaGraphConditionalHandle hrs) {
+        if (first == 2) {
+            ib.begin();
+            launch_cond(B.ctl, h_fst, COND_FST, cs);
+            ib.end();
+            Body t{ib.cond(h_fst, cudaGraphCondTypeIf, 1)[0], {}, cs};
+            t.begin();
+            tau_first(cs);
+            t.end();
+        }
+        ib.begin();
+        if (first == 1) tau_first(cs);
+        B.h_arm = harm;
+        launch_descend<T>(B, 0, cs);
+        get_g(EPI_G2_DESCEND, cs, &ib);  // sets harm
+        ib.end();
+        {
+            Body ab{ib.cond(harm, cudaGraphCondTypeIf, 1)[0], {}, cs};
+            ab.begin();
+            launch_bt_coef<T>(B, cs);
+            launch_bt_apply<T>(B, cs);
+            launch_cond(B.ctl, hrs, COND_RESTART, cs);
+            ab.end();
+            {
+                Body rb{ab.cond(hrs, cudaGraphCondTypeIf, 1)[0], {}, cs};
+                rb.begin();
+                tau_first(cs);
+                launch_descend<T>(B, 1, cs);
+                get_g(EPI_G2_RESTART, cs, &rb);
+                rb.end();
+            }
+            // update_W at the point taken (an accepted full step committed
+            // the descent's W in the Armijo kernel instead)
+            ab.begin();
+            launch_shrink<T>(B, EPI_G2_UPDATE_W, cs);
+            ab.end();
+        }
+        ib.begin();
+        launch_g2_gradient<T>(B, cs);  // sets h_inner
+        ib.end();
+    };
     try {
         Body tb{top, {}, cs};
         tb.begin();
@@ -338,46 +389,21 @@ void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const 
         tb.end();
         // outer while
         Body ob{tb.cond(h_outer, cudaGraphCondTypeWhile, 1)[0], {}, cs};
-        ob.begin();
-        launch_cond(B.ctl, h_inner, COND_ONE, cs);
-        ob.end();
-        {
+        if (resume) {
+            // the resumed state may stop inside an outer iteration: the inner
+            // loop starts at once and asks fst on the device
+            ob.begin();
+            launch_cond(B.ctl, h_inner, COND_ONE, cs);
+            ob.end();
             Body ib{ob.cond(h_inner, cudaGraphCondTypeWhile, 1)[0], {}, cs};
-            ib.begin();
-            launch_cond(B.ctl, h_fst, COND_FST, cs);
-            ib.end();
-            {
-                Body t{ib.cond(h_fst, cudaGraphCondTypeIf, 1)[0], {}, cs};
-                t.begin(); tau_first(cs); t.end();
-            }
-            ib.begin();
-            launch_descend<T>(B, 0, cs);
-            get_g(EPI_G2_DESCEND, cs, &ib);  // sets h_arm
-            ib.end();
-            {
-                Body ab{ib.cond(h_arm, cudaGraphCondTypeIf, 1)[0], {}, cs};
-                ab.begin();
-                launch_bt_coef<T>(B, cs);
-                launch_bt_apply<T>(B, cs);
-                launch_cond(B.ctl, h_restart, COND_RESTART, cs);
-                ab.end();
-                {
-                    Body rb{ab.cond(h_restart, cudaGraphCondTypeIf, 1)[0], {}, cs};
-                    rb.begin();
-                    tau_first(cs);
-                    launch_descend<T>(B, 1, cs);
-                    get_g(EPI_G2_RESTART, cs, &rb);
-                    rb.end();
-                }
-                // update_W at the point taken (an accepted full step committed
-                // the descent's W in the Armijo kernel instead)
-                ab.begin();
-                launch_shrink<T>(B, EPI_G2_UPDATE_W, cs);
-                ab.end();
-            }
-            ib.begin();
-            launch_g2_gradient<T>(B, cs);  // sets h_inner
-            ib.end();
+            iteration(ib, 2, h_arm, h_restart);
+        } else {
+            // every outer iteration starts with fst set (start-up, k_mlp): its
+            // first inner iteration is unrolled in front of the inner loop, so
+            // the loop carries no first-step branch
+            iteration(ob, 1, h_arm1, h_restart1);
+            Body ib{ob.cond(h_inner, cudaGraphCondTypeWhile, 1)[0], {}, cs};
+            iteration(ib, 0, h_arm, h_restart);
         }
         ob.begin();
         launch_outer_relchg<T>(B, cs);  // sets h_mlp
