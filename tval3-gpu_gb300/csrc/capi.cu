@@ -113,7 +113,12 @@ bool all_of_range(long n, F pred) {
     return ok;
 }
 
-void check_sparse(const tval3_sparse_host* A) {
+// Matrices above this many nonzeros are scanned on the device (one pass over
+// the uploaded arrays) instead of by host threads; smaller ones, and values
+// narrowed from FP64 to FP32 on the way up, are scanned on the host.
+constexpr long DEVICE_CHECK_NNZ = 1L << 22;
+
+void check_sparse(const tval3_sparse_host* A, bool host_scan = true) {
     if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
     if (A->rows < 0 || A->cols < 0 || A->nnz < 0) arg_error(TVAL3_ERR_SHAPE, "Argument error: negative matrix size!");
     if (A->format < 1 || A->format > 3) arg_error(TVAL3_ERR_ARG, "Argument error: unknown sparse format!");
@@ -124,6 +129,7 @@ void check_sparse(const tval3_sparse_host* A) {
             arg_error(TVAL3_ERR_ARG, std::string("Argument error: missing ") + what + " arrays!");
         if (ptr[0] != 0 || ptr[rows] != A->nnz)
             arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: inconsistent ") + what + " pointer array!");
+        if (!host_scan) return;
         if (!all_of_range(rows, [&](long r) { return ptr[r + 1] >= ptr[r]; }))
             arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: decreasing ") + what + " pointers!");
         if (!all_of_range(A->nnz, [&](long k) { return ind[k] >= 0 && ind[k] < cols; }))
@@ -140,6 +146,42 @@ void check_sparse(const tval3_sparse_host* A) {
     };
     if (A->format & TVAL3_SPARSE_CSR) chk(A->csr_ptr, A->csr_ind, A->csr_val, A->rows, A->cols, "CSR");
     if (A->format & TVAL3_SPARSE_CSC) chk(A->csc_ptr, A->csc_ind, A->csc_val, A->cols, A->rows, "CSC");
+}
+
+// One pass over a device CSR (or CSC) triple: bit 0 decreasing pointers,
+// bit 1 an index outside [0, cols), bit 2 a non-finite value.
+template <class V>
+__global__ void k_validate_sparse(const int* __restrict__ ptr, long rows, const int* __restrict__ ind,
+                                  const V* __restrict__ val, long nnz, long cols, unsigned* __restrict__ flags) {
+    unsigned f = 0u;
+    const long N = rows > nnz ? rows : nnz;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+        if (i < rows && ptr[i + 1] < ptr[i]) f |= 1u;
+        if (i < nnz) {
+            const int c = ind[i];
+            if (c < 0 || c >= cols) f |= 2u;
+            if (!isfinite(val[i])) f |= 4u;
+        }
+    }
+    f = __reduce_or_sync(0xffffffffu, f);
+    if (f && (threadIdx.x & 31) == 0) atomicOr(flags, f);
+}
+
+// the checks of check_sparse's host scan, on uploaded arrays, with the same
+// errors in the same order
+template <class V>
+void validate_device(const int* ptr, long rows, const int* ind, const V* val, long nnz, long cols, const char* what) {
+    DBuf<unsigned> flags(1);
+    TV3_CUDA(cudaMemset(flags.p, 0, sizeof(unsigned)));
+    const long N = std::max(rows, nnz);
+    const long grid = std::max<long>(1, std::min<long>((N + 255) / 256, (long)num_sms() * 16));
+    k_validate_sparse<V><<<(unsigned)grid, 256>>>(ptr, rows, ind, val, nnz, cols, flags.p);
+    TV3_CUDA(cudaGetLastError());
+    unsigned f = 0;
+    TV3_CUDA(cudaMemcpy(&f, flags.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (f & 1u) arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: decreasing ") + what + " pointers!");
+    if (f & 2u) arg_error(TVAL3_ERR_SHAPE, std::string("Argument error: ") + what + " index out of range!");
+    if (f & 4u) arg_error(TVAL3_ERR_NONFINITE, "Argument error: non-finite matrix value!");
 }
 
 template <class T>
@@ -164,7 +206,10 @@ void to_device(DBuf<T>& d, const void* h, long n, int src_type) {
 // the lane timing (an operator that only backs a double-float view).
 template <class T>
 LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision, bool tune = true) {
-    check_sparse(A);
+    if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+    const bool narrowed = std::is_same<T, float>::value && A->val_type == TVAL3_PREC_FP64;
+    const bool dev_check = A->nnz > DEVICE_CHECK_NNZ && !narrowed;
+    check_sparse(A, !dev_check);
     const long m = A->rows, n = A->cols, nnz = A->nnz;
     if constexpr (std::is_same<T, double>::value) {
         if (precision == TVAL3_PREC_FP32_F64VEC && A->val_type == TVAL3_PREC_FP32) {
@@ -185,6 +230,10 @@ LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision, bool tune = true)
                 TV3_CUDA(cudaMemcpy(tptr.p, A->csc_ptr, (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
                 if (nnz) TV3_CUDA(cudaMemcpy(tind.p, A->csc_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
                 if (nnz) TV3_CUDA(cudaMemcpy(tval.p, A->csc_val, nnz * sizeof(float), cudaMemcpyHostToDevice));
+            }
+            if (dev_check) {
+                if (A->format & TVAL3_SPARSE_CSR) validate_device<float>(ptr.p, m, ind.p, val.p, nnz, n, "CSR");
+                if (A->format & TVAL3_SPARSE_CSC) validate_device<float>(tptr.p, n, tind.p, tval.p, nnz, m, "CSC");
             }
             if (!(A->format & TVAL3_SPARSE_CSR)) {
                 ptr.alloc(m + 1);
@@ -212,6 +261,10 @@ LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision, bool tune = true)
         TV3_CUDA(cudaMemcpy(tptr.p, A->csc_ptr, (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
         if (nnz) TV3_CUDA(cudaMemcpy(tind.p, A->csc_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
         to_device(tval, A->csc_val, nnz, A->val_type);
+    }
+    if (dev_check) {
+        if (A->format & TVAL3_SPARSE_CSR) validate_device<T>(ptr.p, m, ind.p, val.p, nnz, n, "CSR");
+        if (A->format & TVAL3_SPARSE_CSC) validate_device<T>(tptr.p, n, tind.p, tval.p, nnz, m, "CSC");
     }
     if (!(A->format & TVAL3_SPARSE_CSR)) {
         // only CSC given: its transpose is the CSR of A
@@ -899,7 +952,7 @@ tval3_status tval3_gpu_batched(const tval3_slice_host* slices, int count, const 
         for (int i = 0; i < count; ++i) {
             const tval3_slice_host& sl = slices[i];
             if (!sl.A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
-            check_sparse(sl.A);
+            check_sparse(sl.A, false);  // O(nnz) checks run in sparse_op
             check_problem(sl.U, sl.rows, sl.cols, 1, sl.A->rows, sl.A->cols, sl.b, sl.b_len, sl.Ut, sl.Ut_len);
         }
         std::vector<std::unique_ptr<LinOp<float>>> ops;

@@ -192,7 +192,9 @@ struct CsrOp : LinOp<T> {
         varN = tiledN.ok ? 1 : 0;
         // large operators: the fastest kernel of each product, timed here
         if (this->nnz >= (1L << 22)) {
-            const int nT = tiled.pipe_ok ? 3 : (tiled.ok ? 2 : 1), nN = tiledN.ok ? 2 : 1;
+            // the pipelined A^T (variant 2) takes part only when pinned: it lost
+            // every measured contest and its tables cost build time
+            const int nT = tiled.ok ? 2 : 1, nN = tiledN.ok ? 2 : 1;
             for (int trans = 0; trans < 2; ++trans) {
                 const int nv = trans ? nT : nN;
                 if (nv < 2) continue;
@@ -210,7 +212,7 @@ struct CsrOp : LinOp<T> {
     bool set_variant(int trans, int v) const override {
         if (v < 0 || v > (trans ? 2 : 1)) return false;
         if (v == 1 && !(trans ? tiled.ok : tiledN.ok)) return false;
-        if (v == 2 && !tiled.pipe_ok) return false;
+        if (v == 2 && !tiled.ensure_pipe()) return false;
         (trans ? varT : varN) = v;
         return true;
     }

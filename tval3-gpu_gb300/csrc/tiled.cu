@@ -618,7 +618,14 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
     padded_entries = padded;
     // the attribute is per kernel, shared by every operator: always the full budget
     set_smem_attr<T, V>(max_smem);
-    build_pipe(soff, tsl, tunit, uslice, uk0, s);
+    // kept for the pipelined form, built on first use
+    h_soff = std::move(soff);
+    h_tsl = std::move(tsl);
+    h_tunit = std::move(tunit);
+    h_uslice = std::move(uslice);
+    h_uk0 = std::move(uk0);
+    pipe_tried = false;
+    pipe_ok = false;
     TV3_CUDA(cudaStreamSynchronize(s));
     ok = true;
 }
@@ -627,9 +634,22 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
 // memory (ring of at least two stages, two y buffers, the ray list and the
 // unit partials) fits one CTA.
 template <class T, class V>
-void TiledT<T, V>::build_pipe(const std::vector<long long>& soff, const std::vector<int>& tsl,
-                              const std::vector<int>& tunit, const std::vector<int>& uslice,
-                              const std::vector<unsigned short>& uk0, cudaStream_t s) {
+bool TiledT<T, V>::ensure_pipe() const {
+    if (!pipe_tried) {
+        pipe_tried = true;
+        if (ok) const_cast<TiledT*>(this)->build_pipe();
+    }
+    return pipe_ok;
+}
+
+template <class T, class V>
+void TiledT<T, V>::build_pipe() {
+    const std::vector<long long>& soff = h_soff;
+    const std::vector<int>& tsl = h_tsl;
+    const std::vector<int>& tunit = h_tunit;
+    const std::vector<int>& uslice = h_uslice;
+    const std::vector<unsigned short>& uk0 = h_uk0;
+    const cudaStream_t s = 0;
     pipe_ok = false;
     if (!(std::is_same<V, float>::value || std::is_same<V, double>::value) || ntiles <= 0) return;
     int dev = 0, optin = 0;

@@ -86,15 +86,21 @@ struct TiledT {
     // pipelined form: one CTA per SM, a producer warp streams the units in
     // chunks through a shared-memory ring (bulk copies) and gathers the next
     // tile's y values with asynchronous copies; FP32/FP64 values only
-    bool pipe_ok = false;
-    int nchunks = 0, pipe_stages = 0, pipe_stage_bytes = 0, pipe_ybe = 0;
-    size_t pipe_smem = 0;
-    DBuf<int4> sched, cinfo;
-    DBuf<int> rays_pad;
-    DBuf<unsigned> udesc;
+    mutable bool pipe_ok = false;
+    mutable int nchunks = 0, pipe_stages = 0, pipe_stage_bytes = 0, pipe_ybe = 0;
+    mutable size_t pipe_smem = 0;
+    mutable DBuf<int4> sched, cinfo;
+    mutable DBuf<int> rays_pad;
+    mutable DBuf<unsigned> udesc;
     void apply_pipe(const TiledArgs<T, V>& a, int epi, cudaStream_t s) const;
-    void build_pipe(const std::vector<long long>& soff, const std::vector<int>& tsl, const std::vector<int>& tunit,
-                    const std::vector<int>& uslice, const std::vector<unsigned short>& uk0, cudaStream_t s);
+    // the pipelined form's tables are built on first use (a caller pinning
+    // variant 2); the slice and unit layout they need is kept from build()
+    bool ensure_pipe() const;
+    mutable bool pipe_tried = false;
+    std::vector<long long> h_soff;
+    std::vector<int> h_tsl, h_tunit, h_uslice;
+    std::vector<unsigned short> h_uk0;
+    void build_pipe();
 };
 
 // Tile-staged A*x: the rays' nonzeros cut into segments (the part of a ray
