@@ -55,4 +55,37 @@ struct DBuf {
     }
 };
 
+// Scratch buffer of a build step (sort keys, index maps, cub workspace):
+// stream-ordered allocation on the legacy stream from the device's default
+// memory pool, which keeps up to 4 GB of freed memory for the next request,
+// so the temporaries of an operator build cost no driver mapping after the
+// first build.  Only for buffers used by work on the legacy stream (or on
+// streams that synchronise with it) and freed in the same scope.
+void tmp_pool_init();
+template <class T>
+struct TmpBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    TmpBuf() {}
+    explicit TmpBuf(size_t n_) { alloc(n_); }
+    void alloc(size_t n_) {
+        release();
+        if (n_) {
+            tmp_pool_init();
+            void* q = nullptr;
+            TV3_CUDA(cudaMallocAsync(&q, n_ * sizeof(T), 0));
+            p = static_cast<T*>(q);
+            n = n_;
+        }
+    }
+    void release() {
+        if (p) cudaFreeAsync(p, 0);
+        p = nullptr;
+        n = 0;
+    }
+    ~TmpBuf() { release(); }
+    TmpBuf(const TmpBuf&) = delete;
+    TmpBuf& operator=(const TmpBuf&) = delete;
+};
+
 }  // namespace tv3

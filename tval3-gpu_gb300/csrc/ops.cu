@@ -12,6 +12,18 @@
 
 namespace tv3 {
 
+void tmp_pool_init() {
+    static bool done[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long keep = 4ull << 30;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    done[dev] = true;
+}
+
 void throw_cuda(cudaError_t e, const char* what) {
     int st = (e == cudaErrorMemoryAllocation) ? 4 : 3;
     cudaGetLastError();  // clear a sticky launch error where possible

@@ -451,12 +451,12 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
     ntiles = (int)nt;
 
     // ---- (tile, ray) keys of every nonzero, sorted: the tiles' ray lists
-    DBuf<int> tile_of(n), iota(n), tile_first(ntiles);
-    DBuf<unsigned short> local_of(nnz);
+    TmpBuf<int> tile_of(n), iota(n), tile_first(ntiles);
+    TmpBuf<unsigned short> local_of(nnz);
     int nuniq = 0;
     {
-        DBuf<int> rowof(nnz), idx(nnz), idx_s(nnz), newray(nnz), uniq(nnz);
-        DBuf<unsigned long long> key(nnz), key_s(nnz);
+        TmpBuf<int> rowof(nnz), idx(nnz), idx_s(nnz), newray(nnz), uniq(nnz);
+        TmpBuf<unsigned long long> key(nnz), key_s(nnz);
         k_tile_of_voxel<<<ewt(n), 256, 0, s>>>(n, p, q, ty, tx, tz, nty, ntx, tile_of.p, iota.p);
         k_rows_of<<<ewt(n * 32), 256, 0, s>>>(n, tptr, rowof.p);
         k_keys<<<ewt(nnz), 256, 0, s>>>(nnz, rowof.p, tind, tile_of.p, key.p, idx.p);
@@ -466,7 +466,7 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
         size_t tb = 0;
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, key.p, key_s.p, idx.p, idx_s.p, (int)nnz, 0, end_bit, s));
         {
-            DBuf<char> tmp(std::max<size_t>(tb, 1));
+            TmpBuf<char> tmp(std::max<size_t>(tb, 1));
             TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, key.p, key_s.p, idx.p, idx_s.p, (int)nnz, 0, end_bit,
                                                      s));
             TV3_CUDA(cudaStreamSynchronize(s));
@@ -476,7 +476,7 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
         size_t sb = 0;
         TV3_CUDA(cub::DeviceScan::InclusiveSum(nullptr, sb, newray.p, uniq.p, (int)nnz, s));
         {
-            DBuf<char> tmp(std::max<size_t>(sb, 1));
+            TmpBuf<char> tmp(std::max<size_t>(sb, 1));
             TV3_CUDA(cub::DeviceScan::InclusiveSum(tmp.p, sb, newray.p, uniq.p, (int)nnz, s));
             TV3_CUDA(cudaStreamSynchronize(s));
         }
@@ -487,7 +487,7 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
         // per-tile ray offsets: start of tile t's list = uniq[tile_first[t]] - 1;
         // a tile without nonzeros takes the next tile's start
         std::vector<int> roff(ntiles + 1, 0);
-        DBuf<int> st(ntiles);
+        TmpBuf<int> st(ntiles);
         k_tile_start<<<ewt(ntiles), 256, 0, s>>>(ntiles, tile_first.p, uniq.p, st.p);
         std::vector<int> start(ntiles);
         TV3_CUDA(cudaMemcpyAsync(start.data(), st.p, ntiles * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -505,8 +505,8 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
     }
 
     // ---- rows sorted by (tile, length descending), cut into slices of 32
-    DBuf<unsigned long long> rkey(n), rkey_s(n);
-    DBuf<int> vox(n), too_long(1);
+    TmpBuf<unsigned long long> rkey(n), rkey_s(n);
+    TmpBuf<int> vox(n), too_long(1);
     TV3_CUDA(cudaMemsetAsync(too_long.p, 0, sizeof(int), s));
     k_row_keys<<<ewt(n), 256, 0, s>>>(n, tile_of.p, tptr, rkey.p, iota.p, too_long.p);
     int rbits = 17;
@@ -514,7 +514,7 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
     size_t rb = 0;
     TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, rb, rkey.p, rkey_s.p, iota.p, vox.p, (int)n, 0, rbits, s));
     {
-        DBuf<char> tmp(std::max<size_t>(rb, 1));
+        TmpBuf<char> tmp(std::max<size_t>(rb, 1));
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, rb, rkey.p, rkey_s.p, iota.p, vox.p, (int)n, 0, rbits, s));
         TV3_CUDA(cudaStreamSynchronize(s));
     }
@@ -604,7 +604,7 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
     slice_off.alloc(nslices + 1);
     TV3_CUDA(cudaMemcpy(tile_slice.p, tsl.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
     TV3_CUDA(cudaMemcpy(slice_off.p, soff.data(), (nslices + 1) * sizeof(long long), cudaMemcpyHostToDevice));
-    DBuf<int> trow_d(ntiles + 1);
+    TmpBuf<int> trow_d(ntiles + 1);
     TV3_CUDA(cudaMemcpy(trow_d.p, trow.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
     lidx.alloc(std::max<long long>(padded, 1));
     val.alloc(std::max<long long>(padded, 1));
@@ -947,8 +947,8 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     ntiles = (int)nt;
 
     // entries sorted by (tile, ray), ray order kept inside each segment
-    DBuf<int> tile_of(n), iota_v(n), rowof(nnz), idx(nnz), idx_s(nnz), flag(nnz), segid(nnz);
-    DBuf<unsigned long long> key(nnz), key_s(nnz);
+    TmpBuf<int> tile_of(n), iota_v(n), rowof(nnz), idx(nnz), idx_s(nnz), flag(nnz), segid(nnz);
+    TmpBuf<unsigned long long> key(nnz), key_s(nnz);
     k_tile_of_voxel<<<ewt(n), 256, 0, s>>>(n, p, q, ty, tx, tz, nty, ntx, tile_of.p, iota_v.p);
     k_rows_of<<<ewt(m * 32), 256, 0, s>>>(m, ptr, rowof.p);
     k_n_keys<<<ewt(nnz), 256, 0, s>>>(nnz, rowof.p, ind, tile_of.p, key.p, idx.p);
@@ -958,7 +958,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     {
         size_t tb = 0;
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, key.p, key_s.p, idx.p, idx_s.p, (int)nnz, 0, end_bit, s));
-        DBuf<char> tmp(std::max<size_t>(tb, 1));
+        TmpBuf<char> tmp(std::max<size_t>(tb, 1));
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, key.p, key_s.p, idx.p, idx_s.p, (int)nnz, 0, end_bit, s));
         TV3_CUDA(cudaStreamSynchronize(s));
     }
@@ -968,15 +968,15 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     {
         size_t sb = 0;
         TV3_CUDA(cub::DeviceScan::InclusiveSum(nullptr, sb, flag.p, segid.p, (int)nnz, s));
-        DBuf<char> tmp(std::max<size_t>(sb, 1));
+        TmpBuf<char> tmp(std::max<size_t>(sb, 1));
         TV3_CUDA(cub::DeviceScan::InclusiveSum(tmp.p, sb, flag.p, segid.p, (int)nnz, s));
         TV3_CUDA(cudaStreamSynchronize(s));
     }
     int ns = 0;
     TV3_CUDA(cudaMemcpy(&ns, segid.p + nnz - 1, sizeof(int), cudaMemcpyDeviceToHost));
     nseg = ns;
-    DBuf<unsigned long long> seg_key(nseg), k_slice(nseg), k_slice_s(nseg), k_ray(nseg), k_ray_s(nseg);
-    DBuf<int> seg_start(nseg), iota_s(nseg), order(nseg), by_ray(nseg), dest(nseg), too_long(1), rcount(m + 1);
+    TmpBuf<unsigned long long> seg_key(nseg), k_slice(nseg), k_slice_s(nseg), k_ray(nseg), k_ray_s(nseg);
+    TmpBuf<int> seg_start(nseg), iota_s(nseg), order(nseg), by_ray(nseg), dest(nseg), too_long(1), rcount(m + 1);
     k_n_segs<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, segid.p, seg_key.p, seg_start.p);
     TV3_CUDA(cudaMemsetAsync(too_long.p, 0, sizeof(int), s));
     k_n_segkeys<<<ewt(nseg), 256, 0, s>>>(nseg, seg_key.p, seg_start.p, nnz, k_slice.p, k_ray.p, iota_s.p, too_long.p);
@@ -987,7 +987,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
         size_t tb = 0;
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, k_slice.p, k_slice_s.p, iota_s.p, order.p, (int)nseg, 0,
                                                  sbits, s));
-        DBuf<char> tmp(std::max<size_t>(tb, 1));
+        TmpBuf<char> tmp(std::max<size_t>(tb, 1));
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, k_slice.p, k_slice_s.p, iota_s.p, order.p, (int)nseg, 0,
                                                  sbits, s));
         TV3_CUDA(cudaStreamSynchronize(s));
@@ -999,7 +999,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
         size_t tb = 0;
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, k_ray.p, k_ray_s.p, iota_s.p, by_ray.p, (int)nseg, 0,
                                                  rbits, s));
-        DBuf<char> tmp(std::max<size_t>(tb, 1));
+        TmpBuf<char> tmp(std::max<size_t>(tb, 1));
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, k_ray.p, k_ray_s.p, iota_s.p, by_ray.p, (int)nseg, 0,
                                                  rbits, s));
         TV3_CUDA(cudaStreamSynchronize(s));
@@ -1013,7 +1013,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     {
         size_t sb = 0;
         TV3_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, sb, rcount.p, rseg.p, (int)(m + 1), s));
-        DBuf<char> tmp(std::max<size_t>(sb, 1));
+        TmpBuf<char> tmp(std::max<size_t>(sb, 1));
         TV3_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, sb, rcount.p, rseg.p, (int)(m + 1), s));
         TV3_CUDA(cudaStreamSynchronize(s));
     }
@@ -1047,7 +1047,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     const long long padded = soff.back();
     tile_slice.alloc(ntiles + 1);
     slice_off.alloc(nslices + 1);
-    DBuf<int> tseg_d(ntiles + 1);
+    TmpBuf<int> tseg_d(ntiles + 1);
     TV3_CUDA(cudaMemcpy(tile_slice.p, tsl.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
     TV3_CUDA(cudaMemcpy(slice_off.p, soff.data(), (nslices + 1) * sizeof(long long), cudaMemcpyHostToDevice));
     TV3_CUDA(cudaMemcpy(tseg_d.p, tseg.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
