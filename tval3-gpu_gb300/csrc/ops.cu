@@ -183,12 +183,28 @@ template void csr_transpose_device<double>(long, long, long, const int*, const i
 // ---------------------------------------------------------------------------
 // the operator
 // ---------------------------------------------------------------------------
+template <class T, class V> struct CsrOp;
+template <class T, class V> static void tune_lanes(CsrOp<T, V>* op, int mask);
+
 template <class T, class V>
 struct CsrOp : LinOp<T> {
     DBuf<int> ptr, ind, tptr, tind, rowof_t;
     DBuf<V> val, tval;
     DBuf<float> rs;  // per-ray scale (16-bit storage only)
-    int Gn = 32, Gt = 8, grid_n = 1, grid_t = 1;
+    mutable int Gn = 32, Gt = 8, grid_n = 1, grid_t = 1;
+    // products whose CSR lane count is still the untimed default (bit trans):
+    // timed on their first CSR use outside stream capture, or never when a
+    // tile-staged kernel runs them
+    mutable unsigned pend = 0;
+    void tune_pending(int trans) const {
+        if (!((pend >> trans) & 1u)) return;
+        pend &= ~(1u << trans);
+        tune_lanes(const_cast<CsrOp*>(this), 1 << trans);
+    }
+    void ready() const override {
+        for (int trans = 0; trans < 2; ++trans)
+            if ((trans ? varT : varN) == 0) tune_pending(trans);
+    }
     mutable TiledT<T, V> tiled;   // A^T regrouped by voxel tiles (when the volume is known)
     mutable TiledN<T, V> tiledN;  // A cut into per-tile ray segments (when the volume is known)
     // kernel of each product: 0 CSR, 1 tile-staged, 2 (A^T only) tile-staged and pipelined
@@ -202,21 +218,24 @@ struct CsrOp : LinOp<T> {
         tiledN.build(this->m, p, q, r, ptr.p, ind.p, val.p, this->nnz, 0);
         varT = tiled.ok ? 1 : 0;
         varN = tiledN.ok ? 1 : 0;
-        // large operators: the fastest kernel of each product, timed here
+        // large operators: the faster kernel of each product, timed here.  The
+        // pipelined A^T (variant 2) takes part only when pinned: it lost every
+        // measured contest and its tables cost build time.  CSR runs first with
+        // its default lanes; its lanes are timed only when it comes within
+        // 1.5x of the tile-staged kernel.
         if (this->nnz >= (1L << 22)) {
-            // the pipelined A^T (variant 2) takes part only when pinned: it lost
-            // every measured contest and its tables cost build time
-            const int nT = tiled.ok ? 2 : 1, nN = tiledN.ok ? 2 : 1;
             for (int trans = 0; trans < 2; ++trans) {
-                const int nv = trans ? nT : nN;
-                if (nv < 2) continue;
-                int best = 0;
-                float tbest = time_product(trans, 0);
-                for (int v = 1; v < nv; ++v) {
-                    const float tv = time_product(trans, v);
-                    if (tv < tbest) tbest = tv, best = v;
+                if (!(trans ? tiled.ok : tiledN.ok)) continue;
+                const float t1 = time_product(trans, 1);
+                const unsigned keep = pend;
+                pend &= ~(1u << trans);
+                float t0 = time_product(trans, 0);
+                pend = keep;
+                if (t0 < 1.5f * t1 && ((pend >> trans) & 1u)) {
+                    tune_pending(trans);
+                    t0 = time_product(trans, 0);
                 }
-                (trans ? varT : varN) = best;
+                (trans ? varT : varN) = (t0 < t1) ? 0 : 1;
             }
         }
     }
@@ -301,6 +320,10 @@ struct CsrOp : LinOp<T> {
         a.sub = io.sub; a.b = io.b; a.delta = io.delta;
         a.ctl = io.ctl; a.part = io.part; a.ticket = io.ticket;
         a.L = io.L;
+        if ((pend >> trans) & 1u) {
+            cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+            if (cudaStreamIsCapturing(s, &st) == cudaSuccess && st == cudaStreamCaptureStatusNone) tune_pending(trans);
+        }
         launch_spmv<T, V>(a, epi, trans ? Gt : Gn, trans ? grid_t : grid_n, s);
         TV3_CUDA(cudaGetLastError());
     }
@@ -364,7 +387,7 @@ void CsrOp<T, V>::export_csr(int* hptr, int* hind, float* hval, int* htptr, int*
 // three launches each after one warm-up) and keep the fastest; small matrices
 // use the nonzeros-per-row heuristic.
 template <class T, class V>
-static void tune_lanes(CsrOp<T, V>* op) {
+static void tune_lanes(CsrOp<T, V>* op, int mask) {
     const long m = op->m, n = op->n;
     DBuf<T> x(std::max(m, n) + 1), y(std::max(m, n) + 1);
     TV3_CUDA(cudaMemset(x.p, 0, (std::max(m, n) + 1) * sizeof(T)));
@@ -373,6 +396,7 @@ static void tune_lanes(CsrOp<T, V>* op) {
     TV3_CUDA(cudaEventCreate(&e1));
     const int cand[8] = {4, 8, 16, 32, 4 | SPMV_SCALAR, 8 | SPMV_SCALAR, 16 | SPMV_SCALAR, 32 | SPMV_SCALAR};
     for (int trans = 0; trans < 2; ++trans) {
+        if (!((mask >> trans) & 1)) continue;
         float best = 1e30f;
         int bestG = trans ? op->Gt : op->Gn;
         for (int G : cand) {
@@ -406,7 +430,7 @@ static void finish_layout(CsrOp<T, V>* op, bool tune = true) {
     op->Gt = pick_lanes(op->n ? (double)op->nnz / op->n : 0.0);
     op->grid_n = spmv_grid(op->m, op->Gn);
     op->grid_t = spmv_grid(op->n, op->Gt);
-    if (tune && op->nnz >= (1L << 22)) tune_lanes(op);
+    op->pend = (tune && op->nnz >= (1L << 22)) ? 3u : 0u;  // lane timing on first CSR use
 }
 
 // Build from device arrays (FP32 values for the FP32/BF16/FP16 precisions,

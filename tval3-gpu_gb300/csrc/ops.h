@@ -71,6 +71,10 @@ struct LinOp {
         (void)q;
         (void)r;
     }
+    // settle what the chosen kernels still need before use, e.g. the lane
+    // timing of a CSR product the build-time contest did not need (called by
+    // a solver after set_volume, outside capture)
+    virtual void ready() const {}
     // true when apply() takes L > 1 interleaved right-hand sides
     virtual bool multi_rhs() const { return false; }
     // kernel of A*x (trans 0) or A^T*y (trans 1): 0 = CSR kernels, 1 =
@@ -120,6 +124,10 @@ struct SplitOp : LinOp<T> {
         top->prepare(L);
     }
     void set_volume(int p, int q, int r) const override { top->set_volume(p, q, r); }
+    void ready() const override {
+        nop->ready();
+        top->ready();
+    }
     bool set_variant(int trans, int v) const override { return (trans ? top : nop)->set_variant(trans, v); }
     int variant(int trans) const override { return (trans ? top : nop)->variant(trans); }
 };

@@ -63,7 +63,10 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
     if (n >= (1L << 31))
         throw Error{TVAL3_ERR_UNSUPPORTED, "voxels x layers exceeds the 32-bit index range of the stencil kernels"};
     A->prepare(L);
-    if (L == 1) A->set_volume(p_, q_, r_);
+    if (L == 1) {
+        A->set_volume(p_, q_, r_);
+        A->ready();
+    }
     const long nvec = 25, mvec = 4;
     nv.alloc(nvec * n);
     mv.alloc(mvec * std::max<long>(m, 1));
