@@ -1,4 +1,9 @@
-// Owning device buffer (cudaMalloc / cudaFree), move-only.
+// Owning device buffer, move-only.  Memory comes from the device's default
+// stream-ordered pool (see tmp_pool_init: freed memory is kept for the next
+// request, so repeated operator and solver set-ups cost no driver mapping).
+// It keeps cudaMalloc/cudaFree's guarantees: an allocation is complete before
+// alloc() returns (usable from any stream), and release() waits for the
+// device before handing the memory back to the pool.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -6,6 +11,8 @@
 #include "ops.h"
 
 namespace tv3 {
+
+void tmp_pool_init();
 
 template <class T>
 struct DBuf {
@@ -17,8 +24,10 @@ struct DBuf {
     void alloc(size_t n_) {
         release();
         if (n_) {
+            tmp_pool_init();
             void* q = nullptr;
-            TV3_CUDA(cudaMalloc(&q, n_ * sizeof(T)));
+            TV3_CUDA(cudaMallocAsync(&q, n_ * sizeof(T), 0));
+            TV3_CUDA(cudaStreamSynchronize(0));
             p = static_cast<T*>(q);
             n = n_;
         }
@@ -30,7 +39,10 @@ struct DBuf {
         own = false;
     }
     void release() {
-        if (p && own) cudaFree(p);
+        if (p && own) {
+            cudaDeviceSynchronize();
+            cudaFreeAsync(p, 0);
+        }
         p = nullptr;
         n = 0;
         own = true;
@@ -56,12 +68,9 @@ struct DBuf {
 };
 
 // Scratch buffer of a build step (sort keys, index maps, cub workspace):
-// stream-ordered allocation on the legacy stream from the device's default
-// memory pool, which keeps up to 4 GB of freed memory for the next request,
-// so the temporaries of an operator build cost no driver mapping after the
-// first build.  Only for buffers used by work on the legacy stream (or on
+// stream-ordered allocation and free on the legacy stream, with no device
+// synchronisation.  Only for buffers used by work on the legacy stream (or on
 // streams that synchronise with it) and freed in the same scope.
-void tmp_pool_init();
 template <class T>
 struct TmpBuf {
     T* p = nullptr;
