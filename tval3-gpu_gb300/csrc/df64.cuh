@@ -105,4 +105,30 @@ __device__ __forceinline__ df64 sqrt(df64 a) {
     return fast_two_sum(x, c);
 }
 
+// a^2 + b^2 + c^2 with the squares' rounding errors and cross terms kept in
+// a compensated float (the Dot2 idea, as ProdAcc): all terms are
+// non-negative, so the result is accurate to the double-float level.
+__device__ __forceinline__ df64 sum_sq3(df64 a, df64 b, df64 c) {
+    df64 pa = two_prod(a.hi, a.hi), pb = two_prod(b.hi, b.hi), pc = two_prod(c.hi, c.hi);
+    df64 s = two_sum(pa.hi, pb.hi);
+    df64 t = two_sum(s.hi, pc.hi);
+    float e = __fadd_rn(s.lo, t.lo);
+    e = __fadd_rn(e, __fadd_rn(__fadd_rn(pa.lo, pb.lo), pc.lo));
+    e = __fmaf_rn(2.f * a.hi, a.lo, e);
+    e = __fmaf_rn(2.f * b.hi, b.lo, e);
+    e = __fmaf_rn(2.f * c.hi, c.lo, e);
+    return fast_two_sum(t.hi, e);
+}
+
+// 1/sqrt(s) for s > 0: the correctly rounded FP32 reciprocal square root of
+// s.hi, then one Newton step y = y0 + y0 (1 - s y0^2) / 2 with the residual
+// formed in double-float (Karp & Markstein, "High-precision division and
+// square root", ACM TOMS 1997): the error of y0 (~2^-24) squares to ~2^-48.
+__device__ __forceinline__ df64 rsqrt_df(df64 s) {
+    const float y0 = __frsqrt_rn(s.hi);
+    const df64 y2 = two_prod(y0, y0);
+    const df64 r = df64(1.f) - s * y2;  // ~2^-24, exact enough in its high part
+    return fast_two_sum(y0, __fmul_rn(__fmul_rn(0.5f, y0), r.hi));
+}
+
 }  // namespace tv3

@@ -22,6 +22,7 @@
 //   k_mlp                  update_mlp_gpu :1034-1083 and continuation :1222-1237
 //   k_outer_grad           DtsAtd and get_gradient :1238-1249
 #include <math.h>
+#include <type_traits>
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -223,6 +224,21 @@ __device__ __forceinline__ void shrink_voxel(T d0, T d1, T d2, T s0, T s1, T s2,
         w1 = (u1 >= T(0)) ? t1 : -t1;
         w2 = (u2 >= T(0)) ? t2 : -t2;
         l1 += to_acc(t0) + to_acc(t1) + to_acc(t2);
+    } else if constexpr (std::is_same<T, df64>::value) {
+        // |u| and 1/|u| from one reciprocal square root: t = |u| - 1/beta and
+        // t/|u| = 1 - (1/beta)(1/|u|), so no double-float division runs
+        const df64 ss = sum_sq3(u0, u1, u2);
+        T t = T(0), sc = T(0);
+        if (ss.hi > 0.f) {
+            const df64 y = rsqrt_df(ss);
+            t = ss * y - ib;
+            if (t > T(0)) sc = df64(1.f) - ib * y;
+            else t = T(0);
+        }
+        w0 = u0 * sc;
+        w1 = u1 * sc;
+        w2 = u2 * sc;
+        l1 += to_acc(t);
     } else {
         T nv = sqrt(u0 * u0 + u1 * u1 + u2 * u2);
         T t = nv - ib;
