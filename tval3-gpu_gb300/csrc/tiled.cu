@@ -147,19 +147,13 @@ __global__ void __launch_bounds__(512) k_spmv_tiled(TiledArgs<T, V> a) {
     const T* __restrict__ y = a.x[sel];
     T* __restrict__ out = a.y[sel];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    if ((int)blockIdx.x >= a.nwork) {
-        // rows without nonzeros: (A^T y)_v = 0
-        const long z = (long)(blockIdx.x - a.nwork) * blockDim.x + threadIdx.x;
-        if (z < a.nzero) {
-            const int v = __ldg(a.zrows + z);
-            out[v] = (EPI == SPMV_SUB) ? T(0) - a.sub[v] : T(0);
-        }
-        return;
-    }
-    const int t = __ldg(a.tile_order + blockIdx.x);
-    const int r0 = __ldg(a.ray_off + t), nr = __ldg(a.ray_off + t + 1) - r0;
-    const int u0 = __ldg(a.tile_unit + t), u1 = __ldg(a.tile_unit + t + 1);
-    const int s0 = __ldg(a.tile_slice + t), s1 = __ldg(a.tile_slice + t + 1);
+    // one tile per CTA (no tile at all when no row has nonzeros: grid of one
+    // CTA that only writes the empty rows)
+    const bool has_tile = (int)blockIdx.x < a.nwork;
+    const int t = has_tile ? __ldg(a.tile_order + blockIdx.x) : 0;
+    const int r0 = __ldg(a.ray_off + t), nr = has_tile ? __ldg(a.ray_off + t + 1) - r0 : 0;
+    const int u0 = __ldg(a.tile_unit + t), u1 = has_tile ? __ldg(a.tile_unit + t + 1) : u0;
+    const int s0 = __ldg(a.tile_slice + t), s1 = has_tile ? __ldg(a.tile_slice + t + 1) : s0;
     // this thread's row of the final sums (a tile has at most 512 rows): its
     // voxel, unit range and subtrahend, loaded now so their latency hides
     // behind the staging and the products
@@ -223,6 +217,12 @@ __global__ void __launch_bounds__(512) k_spmv_tiled(TiledArgs<T, V> a) {
         T sum = T(0);
         for (int e = re0; e < re1; ++e) sum += psm[e * 32 + lane];
         out[rv] = (EPI == SPMV_SUB) ? sum - rsub : sum;
+    }
+    // rows without nonzeros, (A^T y)_v = 0, shared out over the tile CTAs (a
+    // CTA of their own would hold a tile's shared memory for a few stores)
+    for (long z = (long)blockIdx.x * blockDim.x + threadIdx.x; z < a.nzero; z += (long)gridDim.x * blockDim.x) {
+        const int v = __ldg(a.zrows + z);
+        out[v] = (EPI == SPMV_SUB) ? T(0) - a.sub[v] : T(0);
     }
 }
 
@@ -758,7 +758,7 @@ void TiledT<T, V>::apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) cons
     b.nwork = nwork;
     b.zrows = zrows.p;
     b.nzero = nzero;
-    const long grid = std::max<long>((long)nwork + (nzero + 511) / 512, 1);
+    const long grid = std::max<long>((long)nwork, 1);
     if (epi == SPMV_SUB) launch_k(k_spmv_tiled<T, V, SPMV_SUB, 8>, dim3((unsigned)grid), dim3(512), smem, s, b);
     else launch_k(k_spmv_tiled<T, V, SPMV_PLAIN, 8>, dim3((unsigned)grid), dim3(512), smem, s, b);
     TV3_CUDA(cudaGetLastError());
