@@ -229,44 +229,33 @@ __global__ void __launch_bounds__(512) k_spmv_tiled(TiledArgs<T, V> a) {
 // ---------------------------------------------------------------------------
 // Pipelined A^T*y.  One persistent CTA per SM takes the tiles with work in
 // largest-first order, snaking over the CTAs (tile k*G + b for even k,
-// k*G + G-1-b for odd k).  Two producer warps:
-//   - warp PIPE_CONSUMERS, per chunk of work units, bulk-copies the units'
-//     descriptors, positions and values into the next stage of a
-//     shared-memory ring;
-//   - warp PIPE_CONSUMERS + 1, per tile, bulk-copies the tile's ray list into
-//     shared memory and gathers the tile's y values with 4/8-byte
-//     asynchronous copies into one of two y buffers (the next tile's gather
-//     overlaps this tile's sums).
-// The consumer warps sum units straight from shared memory (unit j of a
-// tile belongs to warp j mod 16, so the sums, and the row sums in unit
-// order, are those of k_spmv_tiled bit for bit).  Stages are released
-// through "empty" barriers, y buffers through "yempty" barriers.
+// k*G + G-1-b for odd k).  Warp PIPE_CONSUMERS is a producer: per tile it
+// bulk-copies the tile's ray list into shared memory and gathers the tile's y
+// values with 4/8-byte asynchronous copies into one of two y buffers, so the
+// gather of the next tile runs while the PIPE_CONSUMERS consumer warps sum
+// the current one (the staging phase of k_spmv_tiled, which no streaming
+// overlaps inside its CTA).  The consumers stream the units from global
+// memory exactly as k_spmv_tiled does (unit j of a tile to warp j mod 31; the
+// sums and the row sums in unit order are the same, bit for bit).
 //
 // Every mbarrier wait is bounded.  On a timeout the warp records
 // ERR_TILED_TIMEOUT, stops computing, keeps taking part in the consumers'
 // named barriers so no warp is left waiting, and the producer waits (bounded)
 // for its own copies in flight before it returns.
 // ---------------------------------------------------------------------------
-template <class T, class V, int EPI>
-__global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 2), 1) k_spmv_tiled_pipe(TiledArgs<T, V> a, PipeArgs pa) {
+template <class T, class V, int EPI, int U>
+__global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 1), 1) k_spmv_tiled_pipe(TiledArgs<T, V> a, PipeArgs pa) {
     count_launch(a.ctl);
+    using VV = typename TVT<V>::type;
     extern __shared__ __align__(16) unsigned char sm_raw[];
-    const int NS = pa.stages;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm_raw);
-    uint64_t* empty = full + NS;
-    uint64_t* yfull = empty + NS;  // 2
-    uint64_t* yempty = yfull + 2;  // 2
-    uint64_t* rbar = yempty + 2;   // 1
-    unsigned char* ring = sm_raw + PIPE_BAR_BYTES;
-    T* ybuf = reinterpret_cast<T*>(ring + (size_t)NS * pa.stage_bytes);
+    uint64_t* yfull = reinterpret_cast<uint64_t*>(sm_raw);  // 2
+    uint64_t* yempty = yfull + 2;                             // 2
+    uint64_t* rbar = yempty + 2;                              // 1
+    T* ybuf = reinterpret_cast<T*>(sm_raw + 64);
     int* ridx = reinterpret_cast<int*>(ybuf + 2 * (size_t)pa.ybuf_elems);
     T* psm = reinterpret_cast<T*>(ridx + pa.ybuf_elems);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
-        for (int i = 0; i < NS; ++i) {
-            mbar_init(&full[i], 1);
-            mbar_init(&empty[i], PIPE_CONSUMERS);
-        }
         for (int i = 0; i < 2; ++i) {
             mbar_init(&yfull[i], 32);
             mbar_init(&yempty[i], PIPE_CONSUMERS);
@@ -282,7 +271,6 @@ __global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 2), 1) k_spmv_tiled_pip
     auto tile_at = [&](int i) {  // this CTA's i-th tile (position in the largest-first order)
         return i * G + ((i & 1) ? G - 1 - b : b);
     };
-    bool ok = true;
     auto sched_of = [&](int i, int4& s0, int4& s1) {  // this CTA's i-th tile record (or none)
         const int k = tile_at(i);
         if (k < a.nwork) {
@@ -293,8 +281,9 @@ __global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 2), 1) k_spmv_tiled_pip
             s1 = make_int4(0, 0, 0, 0);
         }
     };
-    if (warp == PIPE_CONSUMERS + 1) {
-        // ---------------------------------------------------- y producer: per
+    bool ok = true;
+    if (warp == PIPE_CONSUMERS) {
+        // ------------------------------------------------------- producer: per
         // tile, the ray list by one bulk copy, then the tile's y values by
         // 4/8-byte asynchronous copies into the free y buffer (a tile ahead)
         int rpend = -1;  // parity of a ray-list copy not yet seen complete
@@ -324,57 +313,14 @@ __global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 2), 1) k_spmv_tiled_pip
         if (lane == 0 && rpend >= 0) mbar_wait(rbar, (unsigned)rpend);
         return;
     }
-    if (warp == PIPE_CONSUMERS) {
-        // ------------------------------------------------ chunk producer: the
-        // units of every tile, chunk by chunk, into the ring.  The chunk
-        // records of 32 chunks are loaded at once (one per lane) and handed
-        // to lane 0 by shuffles, so no global load sits between two copies.
-        long g = 0;  // chunks issued
-        int4 ta, tb, na, nb4;
-        sched_of(0, ta, tb);
-        for (int i = 0; ok && ta.x >= 0; ++i, ta = na, tb = nb4) {
-            sched_of(i + 1, na, nb4);
-            for (int cb = tb.x; ok && cb < tb.y; cb += 32) {
-                const int4 ci = (cb + lane < tb.y) ? __ldg(pa.cinfo + cb + lane) : make_int4(0, 0, 0, 0);
-                const int nc = min(32, tb.y - cb);
-                for (int q = 0; q < nc; ++q, ++g) {
-                    const int e32 = __shfl_sync(FULL, ci.x, q), ne = __shfl_sync(FULL, ci.y, q);
-                    const int d0 = __shfl_sync(FULL, ci.z, q), jn = __shfl_sync(FULL, ci.w, q);
-                    const int st = (int)(g % NS);
-                    if (g >= NS) ok = __all_sync(FULL, mbar_wait(&empty[st], (unsigned)(((g / NS) - 1) & 1)));
-                    if (!ok) break;
-                    if (lane == 0) {
-                        unsigned char* sp = ring + (size_t)st * pa.stage_bytes;
-                        const int nu = jn & 0xff;
-                        const long long e0 = 32LL * (unsigned)e32;
-                        int* hdr = reinterpret_cast<int*>(sp);
-                        hdr[0] = jn >> 8;
-                        hdr[1] = nu;
-                        const unsigned db = (unsigned)((nu + 3) & ~3) * 4u, lb = (unsigned)ne * 2u,
-                                       vb = (unsigned)ne * (unsigned)sizeof(V);
-                        mbar_expect_tx(&full[st], db + lb + vb);
-                        bulk_g2s(sp + 16, pa.udesc + d0, db, &full[st]);
-                        bulk_g2s(sp + 16 + 4 * PIPE_CHUNK_U, a.lidx + e0, lb, &full[st]);
-                        bulk_g2s(sp + 16 + 4 * PIPE_CHUNK_U + 2 * PIPE_CHUNK_E, a.val + e0, vb, &full[st]);
-                    }
-                    __syncwarp();
-                }
-            }
-        }
-        if (!ok && lane == 0 && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
-        // copies still in flight land before the CTA may exit
-        if (lane == 0)
-            for (long q = (g > NS ? g - NS : 0); q < g; ++q) mbar_wait(&full[q % NS], (unsigned)((q / NS) & 1));
-        return;
-    }
     // ---------------------------------------------------------------- consumers
-    long g = 0;
     int4 ta, tb, na, nb4;
     sched_of(0, ta, tb);
     for (int i = 0; ta.x >= 0; ++i, ta = na, tb = nb4) {
         sched_of(i + 1, na, nb4);
         const int yb = i & 1;
-        const int u0 = ta.y, s0 = ta.z, s1 = ta.w, c0 = tb.x, c1 = tb.y;
+        const int u0 = ta.y, s0 = ta.z, s1 = ta.w, u1 = tb.x;
+        // this thread's row of the final sums, loaded before the wait
         int rv = -1, re0 = 0, re1 = 0;
         T rsub = T(0);
         if ((int)threadIdx.x < (s1 - s0) * 32) {
@@ -386,34 +332,35 @@ __global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 2), 1) k_spmv_tiled_pip
         }
         if (ok) ok = __all_sync(FULL, mbar_wait(&yfull[yb], (unsigned)((i >> 1) & 1)));
         const T* ysm = ybuf + (size_t)yb * pa.ybuf_elems;
-        for (int c = c0; c < c1; ++c, ++g) {
-            const int st = (int)(g % NS);
-            if (ok) ok = __all_sync(FULL, mbar_wait(&full[st], (unsigned)((g / NS) & 1)));
-            if (ok) {
-                const unsigned char* sp = ring + (size_t)st * pa.stage_bytes;
-                const int j0 = reinterpret_cast<const int*>(sp)[0], nu = reinterpret_cast<const int*>(sp)[1];
-                const unsigned* sd = reinterpret_cast<const unsigned*>(sp + 16);
-                const unsigned short* sl = reinterpret_cast<const unsigned short*>(sp + 16 + 4 * PIPE_CHUNK_U);
-                const V* sv = reinterpret_cast<const V*>(sp + 16 + 4 * PIPE_CHUNK_U + 2 * PIPE_CHUNK_E);
-                for (int j = j0 + ((warp - j0) % PIPE_CONSUMERS + PIPE_CONSUMERS) % PIPE_CONSUMERS; j < j0 + nu;
-                     j += PIPE_CONSUMERS) {
-                    const unsigned d = sd[j - j0];
-                    const int rel = (int)(d >> 8), steps = (int)(d & 0xffu);
-                    const unsigned short* li = sl + rel * 32 + lane;
-                    const V* va = sv + rel * 32 + lane;
-                    RowAcc<T> acc;
-#pragma unroll 4
-                    for (int q = 0; q < steps; ++q) madd(acc, (typename TVT<V>::type)va[32 * q], ysm[li[32 * q]]);
-                    psm[j * 32 + lane] = acc.value();
+        if (ok) {
+            for (int w = u0 + warp; w < u1; w += PIPE_CONSUMERS) {
+                const int sl = __ldg(a.unit_slice + w);
+                const long long off = a.slice_off[sl];
+                const int len = (int)((a.slice_off[sl + 1] - off) >> 5);
+                const int k0 = __ldg(a.unit_k0 + w), k1 = min(len, k0 + TILED_UNIT_K);
+                const unsigned short* __restrict__ li = a.lidx + off + lane;
+                const V* __restrict__ va = a.val + off + lane;
+                RowAcc<T> acc;
+                int k = k0;
+                for (; k + U <= k1; k += U) {
+                    unsigned short ii[U];
+                    VV vv[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        ii[u] = __ldcs(li + 32 * (k + u));
+                        vv[u] = (VV)Acc<VV, V>::load(va + 32 * (k + u));
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) madd(acc, vv[u], ysm[ii[u]]);
                 }
+                for (; k < k1; ++k) madd(acc, (VV)Acc<VV, V>::load(va + 32 * k), ysm[__ldcs(li + 32 * k)]);
+                psm[(w - u0) * 32 + lane] = acc.value();
             }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[st]);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&yempty[yb]);
         named_sync(1, 32 * PIPE_CONSUMERS);  // every unit's partials are in psm
-        if (rv >= 0) {
+        if (ok && rv >= 0) {
             T sum = T(0);
             for (int e = re0; e < re1; ++e) sum += psm[e * 32 + lane];
             out[rv] = (EPI == SPMV_SUB) ? sum - rsub : sum;
@@ -619,20 +566,16 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
     // the attribute is per kernel, shared by every operator: always the full budget
     set_smem_attr<T, V>(max_smem);
     // kept for the pipelined form, built on first use
-    h_soff = std::move(soff);
     h_tsl = std::move(tsl);
     h_tunit = std::move(tunit);
-    h_uslice = std::move(uslice);
-    h_uk0 = std::move(uk0);
     pipe_tried = false;
     pipe_ok = false;
     TV3_CUDA(cudaStreamSynchronize(s));
     ok = true;
 }
 
-// Chunk tables and padded ray lists of the pipelined form, when its shared
-// memory (ring of at least two stages, two y buffers, the ray list and the
-// unit partials) fits one CTA.
+// Tile records and padded ray lists of the pipelined form, when its shared
+// memory (two y buffers, the ray list and the unit partials) fits one CTA.
 template <class T, class V>
 bool TiledT<T, V>::ensure_pipe() const {
     if (!pipe_tried) {
@@ -644,52 +587,16 @@ bool TiledT<T, V>::ensure_pipe() const {
 
 template <class T, class V>
 void TiledT<T, V>::build_pipe() {
-    const std::vector<long long>& soff = h_soff;
     const std::vector<int>& tsl = h_tsl;
     const std::vector<int>& tunit = h_tunit;
-    const std::vector<int>& uslice = h_uslice;
-    const std::vector<unsigned short>& uk0 = h_uk0;
-    const cudaStream_t s = 0;
     pipe_ok = false;
     if (!(std::is_same<V, float>::value || std::is_same<V, double>::value) || ntiles <= 0) return;
     int dev = 0, optin = 0;
     TV3_CUDA(cudaGetDevice(&dev));
     TV3_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const int sb = (16 + 4 * PIPE_CHUNK_U + 2 * PIPE_CHUNK_E + (int)sizeof(V) * PIPE_CHUNK_E + 127) / 128 * 128;
     const int ybe = (max_rays + 3) & ~3;
-    const size_t fixed = PIPE_BAR_BYTES + 2 * (size_t)ybe * sizeof(T) + (size_t)ybe * 4 + (size_t)max_units * 32 * sizeof(T);
-    int ns = PIPE_MAX_STAGES;
-    while (ns >= 2 && fixed + (size_t)ns * sb > (size_t)optin) --ns;
-    if (ns < 2) return;
-    TV3_CUDA(cudaStreamSynchronize(s));  // ray lists were built on s
-    // chunks: consecutive units of one tile, their entries contiguous
-    std::vector<int> tch(ntiles + 1);
-    std::vector<int4> ci;
-    std::vector<unsigned> ud;
-    for (int t = 0; t < ntiles; ++t) {
-        tch[t] = (int)ci.size();
-        int u = tunit[t];
-        while (u < tunit[t + 1]) {
-            const long long e0 = soff[uslice[u]] + 32LL * uk0[u];
-            const int d0 = (int)ud.size(), j0 = u - tunit[t];
-            int ne = 0, nu = 0;
-            while (u < tunit[t + 1] && nu < PIPE_CHUNK_U) {
-                const int sl = uslice[u];
-                const long len = (long)((soff[sl + 1] - soff[sl]) / 32);
-                const int steps = (int)std::min<long>(len - uk0[u], TILED_UNIT_K);
-                if (nu > 0 && ne + 32 * steps > PIPE_CHUNK_E) break;
-                ud.push_back(((unsigned)(ne / 32) << 8) | (unsigned)steps);
-                ne += 32 * steps;
-                ++nu;
-                ++u;
-            }
-            while (ud.size() % 4) ud.push_back(0u);
-            if (e0 / 32 > 0x7fffffffLL || j0 >= (1 << 23)) return;  // beyond the packed record
-            ci.push_back(make_int4((int)(e0 / 32), ne, d0, (j0 << 8) | nu));
-        }
-    }
-    tch[ntiles] = (int)ci.size();
-    nchunks = (int)ci.size();
+    const size_t smem = 64 + 2 * (size_t)ybe * sizeof(T) + (size_t)ybe * 4 + (size_t)max_units * 32 * sizeof(T);
+    if (smem > (size_t)optin) return;
     // ray lists starting at multiples of four entries (16-byte bulk copies)
     std::vector<int> roff(ntiles + 1);
     TV3_CUDA(cudaMemcpy(roff.data(), ray_off.p, (ntiles + 1) * sizeof(int), cudaMemcpyDeviceToHost));
@@ -710,24 +617,18 @@ void TiledT<T, V>::build_pipe() {
     for (int k = 0; k < nwork; ++k) {
         const int t = ord[k];
         sc[2 * k] = make_int4(t, tunit[t], tsl[t], tsl[t + 1]);
-        sc[2 * k + 1] = make_int4(tch[t], tch[t + 1], roff[t + 1] - roff[t], rpo[t]);
+        sc[2 * k + 1] = make_int4(tunit[t + 1], 0, roff[t + 1] - roff[t], rpo[t]);
     }
-    auto up = [&](auto& d, const auto& h) {
-        d.alloc(std::max<size_t>(h.size(), 1));
-        if (!h.empty()) TV3_CUDA(cudaMemcpy(d.p, h.data(), h.size() * sizeof(h[0]), cudaMemcpyHostToDevice));
-    };
-    up(sched, sc);
-    up(cinfo, ci);
-    up(udesc, ud);
-    up(rays_pad, rp);
-    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiled_pipe<T, V, SPMV_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    sched.alloc(sc.size());
+    TV3_CUDA(cudaMemcpy(sched.p, sc.data(), sc.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    rays_pad.alloc(rp.size());
+    TV3_CUDA(cudaMemcpy(rays_pad.p, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice));
+    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiled_pipe<T, V, SPMV_PLAIN, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   optin));
-    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiled_pipe<T, V, SPMV_SUB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiled_pipe<T, V, SPMV_SUB, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   optin));
-    pipe_stages = ns;
-    pipe_stage_bytes = sb;
     pipe_ybe = ybe;
-    pipe_smem = fixed + (size_t)ns * sb;
+    pipe_smem = smem;
     pipe_ok = true;
 }
 
@@ -742,11 +643,11 @@ void TiledT<T, V>::apply_pipe(const TiledArgs<T, V>& a, int epi, cudaStream_t s)
     b.nwork = nwork;
     b.zrows = zrows.p;
     b.nzero = nzero;
-    PipeArgs pa{sched.p, cinfo.p, udesc.p, rays_pad.p, pipe_stages, pipe_stage_bytes, pipe_ybe};
+    PipeArgs pa{sched.p, rays_pad.p, pipe_ybe};
     const int grid = std::max(1, num_sms());
-    const int threads = 32 * (PIPE_CONSUMERS + 2);
-    if (epi == SPMV_SUB) k_spmv_tiled_pipe<T, V, SPMV_SUB><<<grid, threads, pipe_smem, s>>>(b, pa);
-    else k_spmv_tiled_pipe<T, V, SPMV_PLAIN><<<grid, threads, pipe_smem, s>>>(b, pa);
+    const int threads = 32 * (PIPE_CONSUMERS + 1);
+    if (epi == SPMV_SUB) launch_k(k_spmv_tiled_pipe<T, V, SPMV_SUB, 8>, dim3(grid), dim3(threads), pipe_smem, s, b, pa);
+    else launch_k(k_spmv_tiled_pipe<T, V, SPMV_PLAIN, 8>, dim3(grid), dim3(threads), pipe_smem, s, b, pa);
     TV3_CUDA(cudaGetLastError());
 }
 

@@ -40,27 +40,17 @@ struct TiledArgs {
     long nzero;
 };
 
-// Chunk tables of the pipelined A^T*y (k_spmv_tiled_pipe): each tile's work
-// units cut into chunks of consecutive units (at most PIPE_CHUNK_E entries and
-// PIPE_CHUNK_U units), streamed into a shared-memory ring by bulk copies.
-constexpr int PIPE_CHUNK_E = 2048;
-constexpr int PIPE_CHUNK_U = 64;
-constexpr int PIPE_CONSUMERS = 16;  // consumer warps; two more warps produce
-constexpr int PIPE_MAX_STAGES = 8;
-constexpr int PIPE_BAR_BYTES = 256;  // the ring's and y buffers' barriers: (2 * stages + 5) * 8 bytes
+// Pipelined A^T*y (k_spmv_tiled_pipe): one persistent CTA per SM of
+// PIPE_CONSUMERS consumer warps and one producer warp that stages the next
+// tile's y values while the consumers sum the current tile.
+constexpr int PIPE_CONSUMERS = 31;
 
 struct PipeArgs {
     // per position k of the largest-first order, two 16-byte records:
-    // {tile, first unit, first slice, end slice}, {first chunk, end chunk,
-    // rays, start of the ray list in rays_pad}
+    // {tile, first unit, first slice, end slice}, {end unit, 0, rays, start of
+    // the ray list in rays_pad}
     const int4* sched;
-    // per chunk: {first entry / 32, entries, first descriptor, first unit
-    // relative to the tile's first << 8 | units}
-    const int4* cinfo;
-    const unsigned* udesc;       // per unit: (first entry - chunk's first) / 32 << 8 | steps
     const int* rays_pad;         // ray lists, each starting at a multiple of 4 entries
-    int stages;                  // ring depth
-    int stage_bytes;
     int ybuf_elems;              // y elements per buffer (max rays rounded up to 4)
 };
 
@@ -83,23 +73,20 @@ struct TiledT {
     void build(long n, long m, int p, int q, int r, const int* tptr, const int* tind, const V* tval, long nnz,
                size_t max_smem, cudaStream_t s);
     void apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) const;
-    // pipelined form: one CTA per SM, a producer warp streams the units in
-    // chunks through a shared-memory ring (bulk copies) and gathers the next
-    // tile's y values with asynchronous copies; FP32/FP64 values only
+    // pipelined form: one CTA per SM; a producer warp gathers the next tile's
+    // y values (bulk copy of the ray list, then asynchronous copies) while 31
+    // consumer warps sum the current tile; FP32/FP64 values only
     mutable bool pipe_ok = false;
-    mutable int nchunks = 0, pipe_stages = 0, pipe_stage_bytes = 0, pipe_ybe = 0;
+    mutable int pipe_ybe = 0;
     mutable size_t pipe_smem = 0;
-    mutable DBuf<int4> sched, cinfo;
+    mutable DBuf<int4> sched;
     mutable DBuf<int> rays_pad;
-    mutable DBuf<unsigned> udesc;
     void apply_pipe(const TiledArgs<T, V>& a, int epi, cudaStream_t s) const;
     // the pipelined form's tables are built on first use (a caller pinning
     // variant 2); the slice and unit layout they need is kept from build()
     bool ensure_pipe() const;
     mutable bool pipe_tried = false;
-    std::vector<long long> h_soff;
-    std::vector<int> h_tsl, h_tunit, h_uslice;
-    std::vector<unsigned short> h_uk0;
+    std::vector<int> h_tsl, h_tunit;
     void build_pipe();
 };
 
