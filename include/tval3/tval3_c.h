@@ -265,10 +265,12 @@ TVAL3_API tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const
  * known (geometry operators, or any operator once a solver has been created
  * on it): variant 0 = CSR kernels, 1 = tile-staged (the vector staged per
  * voxel tile in shared memory), 2 (A^T only, FP32/FP64 matrix values) =
- * tile-staged and pipelined (one CTA per SM; the matrix streamed into a
- * shared-memory ring by bulk copies; same sums as variant 1, bit for bit).
- * The library picks the fastest by timing when it builds the tiled form;
- * pinning a variant makes a program's results independent of that timing.
+ * tile-staged and pipelined (one CTA per SM; a producer warp stages the next
+ * tile's y with bulk and asynchronous copies while the other warps sum the
+ * current tile; same sums as variant 1, bit for bit; built on first use and
+ * never chosen by the timing).  The library picks between CSR and
+ * tile-staged by timing when it builds the tiled form; pinning a variant
+ * makes a program's results independent of that timing.
  * TVAL3_ERR_UNSUPPORTED if the variant is not available. */
 TVAL3_API tval3_status tval3_op_set_variant(tval3_op op, int trans, int variant);
 TVAL3_API tval3_status tval3_op_get_variant(tval3_op op, int trans, int* variant);

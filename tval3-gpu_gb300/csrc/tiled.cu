@@ -28,6 +28,7 @@
 // partials in order after a barrier (deterministic).
 #include <cub/cub.cuh>
 #include <algorithm>
+#include <memory>
 #include <type_traits>
 #include <vector>
 #include "ops.h"
@@ -472,17 +473,19 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
         ray_off.release();
         return;
     }
-    std::vector<unsigned long long> hk(n);
-    TV3_CUDA(cudaMemcpy(hk.data(), rkey_s.p, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    // host copies are written whole by the copy: no zero fill
+    std::unique_ptr<unsigned long long[]> hk(new unsigned long long[n]);
+    TV3_CUDA(cudaMemcpy(hk.get(), rkey_s.p, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
     std::vector<int> trow(ntiles + 1, (int)n), tsl(ntiles + 1, 0);
     for (long i = n - 1; i >= 0; --i) trow[hk[i] >> 16] = (int)i;
     for (int t = ntiles - 1; t >= 0; --t) trow[t] = std::min(trow[t], trow[t + 1]);
     // rows are sorted longest first inside each tile, so the rows without
     // nonzeros are a suffix of the tile's rows; they leave the slices and go
     // to one list of voxels whose result is 0 (or -sub)
-    std::vector<int> hvox(n);
-    TV3_CUDA(cudaMemcpy(hvox.data(), vox.p, n * sizeof(int), cudaMemcpyDeviceToHost));
+    std::unique_ptr<int[]> hvox(new int[n]);
+    TV3_CUDA(cudaMemcpy(hvox.get(), vox.p, n * sizeof(int), cudaMemcpyDeviceToHost));
     std::vector<int> zlist;
+    zlist.reserve(n);
     std::vector<long long> soff(1, 0);
     for (int t = 0; t < ntiles; ++t) {
         tsl[t] = (int)(soff.size() - 1);
@@ -919,8 +922,8 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
         TV3_CUDA(cudaStreamSynchronize(s));
     }
     // slices (host): tiles' segment ranges and 32-segment slices
-    std::vector<unsigned long long> hk(nseg);
-    TV3_CUDA(cudaMemcpy(hk.data(), k_slice_s.p, nseg * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    std::unique_ptr<unsigned long long[]> hk(new unsigned long long[nseg]);  // written whole by the copy
+    TV3_CUDA(cudaMemcpy(hk.get(), k_slice_s.p, nseg * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
     std::vector<int> tseg(ntiles + 1, (int)nseg), tsl(ntiles + 1, 0);
     for (long i = nseg - 1; i >= 0; --i) tseg[hk[i] >> 16] = (int)i;
     for (int t = ntiles - 1; t >= 0; --t) tseg[t] = std::min(tseg[t], tseg[t + 1]);
