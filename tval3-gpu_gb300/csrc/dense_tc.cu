@@ -17,7 +17,8 @@
 // Kernel structure (one CTA = one 128-row tile of D and one split of K; four
 // warps):
 //   - thread 0 issues the TMA loads of a STAGES-deep ring (A tile 128 x 64,
-//     B tiles Npad x 64 for hi and lo, 128-byte swizzle) and the
+//     one contiguous block of the blocked copy of A or A^T; B tiles Npad x 64
+//     for hi and lo; 128-byte swizzle) and the
 //     tcgen05.mma instructions (M = 128, N = Npad, K = 16 each), then commits
 //     each stage's MMAs to the stage's "empty" barrier before refilling it;
 //   - warp 0 allocates and frees the TMEM accumulator (Npad columns);
@@ -113,7 +114,7 @@ struct GemmArgs {
     Ctl* ctl;        // error word and launch counter (may be null)
 };
 
-__global__ void __launch_bounds__(128, 2) k_umma_gemm(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(128, 3) k_umma_gemm(const __grid_constant__ CUtensorMap tmA,
                                                        const __grid_constant__ CUtensorMap tmBh,
                                                        const __grid_constant__ CUtensorMap tmBl, GemmArgs g) {
     count_launch(g.ctl);
@@ -164,7 +165,7 @@ __global__ void __launch_bounds__(128, 2) k_umma_gemm(const __grid_constant__ CU
             mbar_expect_tx(&full[s], stage_bytes);
             const int jj = (j + rot) % nkb;
             const int kx = (int)((kb0 + jj) * UK);
-            tma_load_2d(st, &tmA, kx, (int)(mt * UM), &full[s]);
+            tma_load_2d(st, &tmA, 0, (int)((mt * KB + kb0 + jj) * UM), &full[s]);
             tma_load_2d(st + a_bytes, &tmBh, kx, 0, &full[s]);
             tma_load_2d(st + a_bytes + b_bytes, &tmBl, kx, 0, &full[s]);
         };
@@ -292,19 +293,35 @@ __global__ void __launch_bounds__(256) k_umma_reduce(long M, int L, int splits, 
     }
 }
 
-// transpose of a BF16 row-major m x n array into n x mp (row pitch mp)
-__global__ void k_bf16_transpose(long m, long n, long mp, const __nv_bfloat16* __restrict__ a,
-                                 __nv_bfloat16* __restrict__ at) {
-    __shared__ __nv_bfloat16 t[32][33];
-    const long c0 = (long)blockIdx.x * 32, r0 = (long)blockIdx.y * 32;
-    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-        const long r = r0 + j, c = c0 + threadIdx.x;
-        t[j][threadIdx.x] = (r < m && c < n) ? a[r * n + c] : __float2bfloat16_rn(0.f);
-    }
-    __syncthreads();
-    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-        const long c = c0 + j, r = r0 + threadIdx.x;
-        if (c < n && r < mp) at[c * mp + r] = (r < m) ? t[threadIdx.x][j] : __float2bfloat16_rn(0.f);
+// A (trans = 0) or A^T (trans = 1) of the row-major m x n BF16 array `a` in
+// 128 x 64 blocks: block (row tile rt, k-block kb) holds rows rt*128.. and
+// columns kb*64.. of the operand, row-major and contiguous (16 KB), blocks in
+// (rt, kb) order, zeros outside the matrix.  One TMA box of the GEMM is then a
+// single contiguous 16 KB read and one split of K a contiguous run of blocks,
+// instead of 128 pieces of 128 bytes one matrix row apart.
+__global__ void __launch_bounds__(256) k_bf16_tile(long m, long n, int trans, long KB, long nblocks,
+                                                   const __nv_bfloat16* __restrict__ a,
+                                                   __nv_bfloat16* __restrict__ dst) {
+    __shared__ __nv_bfloat16 t[UK][UM + 2];
+    const long R = trans ? n : m, C = trans ? m : n;
+    for (long b = blockIdx.x; b < nblocks; b += gridDim.x) {
+        const long rt = b / KB, kb = b - rt * KB;
+        __nv_bfloat16* __restrict__ o = dst + (size_t)b * (UM * UK);
+        if (!trans) {
+            for (int idx = threadIdx.x; idx < UM * UK; idx += blockDim.x) {
+                const long i = rt * UM + (idx >> 6), k = kb * UK + (idx & 63);
+                o[idx] = (i < R && k < C) ? a[i * n + k] : __float2bfloat16_rn(0.f);
+            }
+        } else {
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < UM * UK; idx += blockDim.x) {
+                const int c = idx >> 7, r = idx & 127;  // operand row rt*128+r = column of a
+                const long i = rt * UM + r, k = kb * UK + c;
+                t[c][r] = (i < R && k < C) ? a[k * n + i] : __float2bfloat16_rn(0.f);
+            }
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < UM * UK; idx += blockDim.x) o[idx] = t[idx & 63][idx >> 6];
+        }
     }
 }
 
@@ -348,7 +365,7 @@ CUtensorMap make_map(const void* base, long inner, long outer, long pitch, int b
 struct UmmaPlan {
     long m = 0, n = 0, mp = 0, np = 0;
     int L = 0, Npad = 0, tmem_cols = 0;
-    DBuf<__nv_bfloat16> at;          // Aq^T, n x mp
+    DBuf<__nv_bfloat16> tN, tT;      // Aq and Aq^T in 128 x 64 blocks (k_bf16_tile)
     DBuf<__nv_bfloat16> bN_h, bN_l;  // B of A*X: Npad x np
     DBuf<__nv_bfloat16> bT_h, bT_l;  // B of A^T*Y: Npad x mp
     DBuf<float> part;
@@ -365,8 +382,21 @@ static void plan_split(long M, long K, int& splits, int& kb_per) {
     splits = (int)((KB + kb_per - 1) / kb_per);
 }
 
+// rows of the blocked copy of an M x K operand (TMA row coordinates are int)
+static long blocked_rows(long M, long K) { return (M + UM - 1) / UM * ((K + UK - 1) / UK) * UM; }
+
 bool umma_supported(long m, long n, int L) {
-    return L > 1 && L <= 256 && n % 8 == 0 && m > 0 && n > 0;
+    return L > 1 && L <= 256 && n % 8 == 0 && m > 0 && n > 0 && blocked_rows(m, n) < (1L << 31) &&
+           blocked_rows(n, m) < (1L << 31);
+}
+
+static void tile_operand(long m, long n, int trans, const __nv_bfloat16* Aq, DBuf<__nv_bfloat16>& dst) {
+    const long M = trans ? n : m, K = trans ? m : n;
+    const long KB = (K + UK - 1) / UK, nblocks = (M + UM - 1) / UM * KB;
+    dst.alloc((size_t)blocked_rows(M, K) * UK);
+    const int g = (int)std::min<long>(nblocks, (long)num_sms() * 8);
+    k_bf16_tile<<<g, 256>>>(m, n, trans, KB, nblocks, Aq, dst.p);
+    TV3_CUDA(cudaGetLastError());
 }
 
 UmmaPlan* umma_plan_create(long m, long n, int L, const __nv_bfloat16* Aq) {
@@ -379,10 +409,8 @@ UmmaPlan* umma_plan_create(long m, long n, int L, const __nv_bfloat16* Aq) {
         int tc = 32;
         while (tc < p->Npad) tc <<= 1;
         p->tmem_cols = tc;
-        p->at.alloc((size_t)n * p->mp);
-        dim3 tb(32, 8), tg((unsigned)((n + 31) / 32), (unsigned)((p->mp + 31) / 32));
-        k_bf16_transpose<<<tg, tb>>>(m, n, p->mp, Aq, p->at.p);
-        TV3_CUDA(cudaGetLastError());
+        tile_operand(m, n, 0, Aq, p->tN);
+        tile_operand(m, n, 1, Aq, p->tT);
         p->bN_h.alloc((size_t)p->Npad * p->np);
         p->bN_l.alloc((size_t)p->Npad * p->np);
         p->bT_h.alloc((size_t)p->Npad * p->mp);
@@ -394,14 +422,14 @@ UmmaPlan* umma_plan_create(long m, long n, int L, const __nv_bfloat16* Aq) {
         plan_split(m, n, p->splitsN, p->kbN);
         plan_split(n, m, p->splitsT, p->kbT);
         p->part.alloc(std::max((size_t)p->splitsN * m * L, (size_t)p->splitsT * n * L));
-        p->mapA = make_map(Aq, n, m, n, UM);
-        p->mapAt = make_map(p->at.p, m, n, p->mp, UM);
+        p->mapA = make_map(p->tN.p, UK, blocked_rows(m, n), UK, UM);
+        p->mapAt = make_map(p->tT.p, UK, blocked_rows(n, m), UK, UM);
         p->mapBNh = make_map(p->bN_h.p, n, p->Npad, p->np, p->Npad);
         p->mapBNl = make_map(p->bN_l.p, n, p->Npad, p->np, p->Npad);
         p->mapBTh = make_map(p->bT_h.p, m, p->Npad, p->mp, p->Npad);
         p->mapBTl = make_map(p->bT_l.p, m, p->Npad, p->mp, p->Npad);
         const size_t stage = (size_t)UM * 128 + 2 * (size_t)p->Npad * 128;
-        const size_t budget = 100 * 1024;  // two CTAs per SM
+        const size_t budget = 72 * 1024;  // three CTAs per SM while a stage is <= 24 KB (Npad <= 32)
         const int st = (int)std::min<size_t>(MAX_STAGES, std::max<size_t>(2, budget / stage));
         p->stagesN = p->stagesT = st;
         p->smemN = p->smemT = st * stage + 1024;
