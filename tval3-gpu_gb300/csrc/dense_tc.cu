@@ -237,20 +237,34 @@ __global__ void __launch_bounds__(128, 3) k_umma_gemm(const __grid_constant__ CU
 }
 
 // B operand of one product: v = x (or rs .* x) as BF16 hi and lo parts, K-major
-// rows per right-hand side: B[l * Kp + k].  Rows l >= L stay zero.
-__global__ void k_umma_quant(long K, int L, long Kp, const float* __restrict__ rs, MatIO<float> io,
-                             __nv_bfloat16* __restrict__ bh, __nv_bfloat16* __restrict__ bl) {
+// rows per right-hand side: B[l * Kp + k].  Rows l >= L stay zero.  A block
+// moves QK consecutive k of all L right-hand sides through shared memory, so
+// both the interleaved read of x (x[k * L + l]) and the row-wise writes of B
+// are coalesced.
+constexpr int QK = 32;
+__global__ void __launch_bounds__(256) k_umma_quant(long K, int L, long Kp, const float* __restrict__ rs,
+                                                    MatIO<float> io, __nv_bfloat16* __restrict__ bh,
+                                                    __nv_bfloat16* __restrict__ bl) {
     count_launch(io.ctl);
-    const int sel = io.by_parity ? io.ctl->parity : 0;
-    const float* __restrict__ x = io.x[sel];
-    const long tot = K * L;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long)gridDim.x * blockDim.x) {
-        const long l = t / K, k = t - l * K;
-        float v = x[k * L + l];
-        if (rs) v *= rs[k];
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        bh[l * Kp + k] = h;
-        bl[l * Kp + k] = __float2bfloat16_rn(v - __bfloat162float(h));
+    __shared__ float t[QK][257];
+    const float* __restrict__ x = (io.by_parity && io.ctl->parity) ? io.x[1] : io.x[0];
+    for (long k0 = (long)blockIdx.x * QK; k0 < K; k0 += (long)gridDim.x * QK) {
+        const int kn = (int)min((long)QK, K - k0);
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < kn * L; idx += blockDim.x) {
+            const int kk = idx / L;
+            t[kk][idx - kk * L] = x[k0 * L + idx];
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < QK * L; idx += blockDim.x) {
+            const int l = idx / QK, kk = idx % QK;
+            if (kk >= kn) continue;
+            float v = t[kk][l];
+            if (rs) v *= rs[k0 + kk];
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            bh[l * Kp + k0 + kk] = h;
+            bl[l * Kp + k0 + kk] = __float2bfloat16_rn(v - __bfloat162float(h));
+        }
     }
 }
 
@@ -448,8 +462,7 @@ void umma_apply(const UmmaPlan* p, int trans, const MatIO<float>& io, int epi, c
     const long M = trans ? p->n : p->m, K = trans ? p->m : p->n, Kp = trans ? p->mp : p->np;
     __nv_bfloat16* bh = trans ? p->bT_h.p : p->bN_h.p;
     __nv_bfloat16* bl = trans ? p->bT_l.p : p->bN_l.p;
-    const long qn = K * p->L;
-    const int qg = (int)std::max<long>(1, std::min<long>((qn + 255) / 256, (long)num_sms() * 8));
+    const int qg = (int)std::max<long>(1, std::min<long>((K + QK - 1) / QK, (long)num_sms() * 8));
     k_umma_quant<<<qg, 256, 0, s>>>(K, p->L, Kp, trans ? rs : nullptr, io, bh, bl);
     GemmArgs g;
     g.M = M; g.K = K; g.L = p->L; g.Npad = p->Npad; g.tmem_cols = p->tmem_cols;
