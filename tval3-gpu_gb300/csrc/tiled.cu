@@ -376,6 +376,83 @@ __global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 1), 1) k_spmv_tiled_pip
     }
 }
 
+// ---- slicing tables from rows sorted by key (tile << 16) | (0xffff - length):
+// tiles in order, longest rows first, rows without entries last
+__global__ void k_fill_value(long n, int v, int* __restrict__ a) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) a[i] = v;
+}
+
+// first[t]: the tile's first row; nzend[t]: its first row without entries
+__global__ void k_tile_bounds(long N, const unsigned long long* __restrict__ key, int* __restrict__ first,
+                              int* __restrict__ nzend) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+        const unsigned long long k = key[i];
+        const int t = (int)(k >> 16);
+        const bool head = (i == 0) || (int)(key[i - 1] >> 16) != t;
+        if (head) first[t] = (int)i;
+        if ((k & 0xffff) == 0xffff && (head || (key[i - 1] & 0xffff) != 0xffff)) nzend[t] = (int)i;
+    }
+}
+
+// every 32nd row of a tile's rows with entries opens a slice as long as that row
+__global__ void k_slice_len(long N, const unsigned long long* __restrict__ key, const int* __restrict__ first,
+                            const int* __restrict__ nzend, const int* __restrict__ tsl, int* __restrict__ slen) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+        const unsigned long long k = key[i];
+        const int t = (int)(k >> 16);
+        const long j = i - first[t];
+        if ((j & 31) == 0 && i < nzend[t]) slen[tsl[t] + j / 32] = 0xffff - (int)(k & 0xffff);
+    }
+}
+
+__global__ void k_empty_flags(long N, const unsigned long long* __restrict__ key, char* __restrict__ f) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+        f[i] = (key[i] & 0xffff) == 0xffff;
+}
+
+// Host copies of the slicing tables, computed by two passes on the device:
+// first[t] (first[ntiles] = N) and nzend[t] bound tile t's rows and its rows
+// with entries; tile t owns slices tsl[t] .. tsl[t+1]-1; slen[sl] is the
+// length of slice sl.  first_d receives first[] for the fill kernels.
+struct SliceTables {
+    std::vector<int> first, nzend, tsl, slen;
+};
+
+void slice_tables(long N, int ntiles, const unsigned long long* key_s, TmpBuf<int>& first_d, cudaStream_t s,
+                  SliceTables& o) {
+    TmpBuf<int> nz_d(ntiles), tsl_d(ntiles + 1);
+    k_fill_value<<<ewt(ntiles + 1), 256, 0, s>>>(ntiles + 1, (int)N, first_d.p);
+    TV3_CUDA(cudaMemsetAsync(nz_d.p, 0xff, ntiles * sizeof(int), s));
+    k_tile_bounds<<<ewt(N), 256, 0, s>>>(N, key_s, first_d.p, nz_d.p);
+    TV3_CUDA(cudaGetLastError());
+    o.first.assign(ntiles + 1, 0);
+    o.nzend.assign(ntiles, 0);
+    TV3_CUDA(cudaMemcpyAsync(o.first.data(), first_d.p, ntiles * sizeof(int), cudaMemcpyDeviceToHost, s));
+    TV3_CUDA(cudaMemcpyAsync(o.nzend.data(), nz_d.p, ntiles * sizeof(int), cudaMemcpyDeviceToHost, s));
+    TV3_CUDA(cudaStreamSynchronize(s));
+    o.first[ntiles] = (int)N;
+    // a tile without rows starts where the next one does
+    for (int t = ntiles - 1; t >= 0; --t) o.first[t] = std::min(o.first[t], o.first[t + 1]);
+    o.tsl.assign(ntiles + 1, 0);
+    for (int t = 0; t < ntiles; ++t) {
+        if (o.nzend[t] < 0) o.nzend[t] = o.first[t + 1];
+        o.tsl[t + 1] = o.tsl[t] + (o.nzend[t] - o.first[t] + 31) / 32;
+    }
+    const int ns = o.tsl[ntiles];
+    o.slen.assign(std::max(ns, 1), 0);
+    TV3_CUDA(cudaMemcpyAsync(first_d.p, o.first.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+    TV3_CUDA(cudaMemcpyAsync(nz_d.p, o.nzend.data(), ntiles * sizeof(int), cudaMemcpyHostToDevice, s));
+    TV3_CUDA(cudaMemcpyAsync(tsl_d.p, o.tsl.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (ns > 0) {
+        TmpBuf<int> slen_d(ns);
+        k_slice_len<<<ewt(N), 256, 0, s>>>(N, key_s, first_d.p, nz_d.p, tsl_d.p, slen_d.p);
+        TV3_CUDA(cudaGetLastError());
+        TV3_CUDA(cudaMemcpyAsync(o.slen.data(), slen_d.p, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
+        TV3_CUDA(cudaStreamSynchronize(s));
+    }
+    TV3_CUDA(cudaStreamSynchronize(s));
+}
+
 template <class T, class V>
 void set_smem_attr(size_t smem) {
     const int b = (int)smem;
@@ -473,32 +550,30 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
         ray_off.release();
         return;
     }
-    // host copies are written whole by the copy: no zero fill
-    std::unique_ptr<unsigned long long[]> hk(new unsigned long long[n]);
-    TV3_CUDA(cudaMemcpy(hk.get(), rkey_s.p, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-    std::vector<int> trow(ntiles + 1, (int)n), tsl(ntiles + 1, 0);
-    for (long i = n - 1; i >= 0; --i) trow[hk[i] >> 16] = (int)i;
-    for (int t = ntiles - 1; t >= 0; --t) trow[t] = std::min(trow[t], trow[t + 1]);
-    // rows are sorted longest first inside each tile, so the rows without
-    // nonzeros are a suffix of the tile's rows; they leave the slices and go
-    // to one list of voxels whose result is 0 (or -sub)
-    std::unique_ptr<int[]> hvox(new int[n]);
-    TV3_CUDA(cudaMemcpy(hvox.get(), vox.p, n * sizeof(int), cudaMemcpyDeviceToHost));
-    std::vector<int> zlist;
-    zlist.reserve(n);
-    std::vector<long long> soff(1, 0);
-    for (int t = 0; t < ntiles; ++t) {
-        tsl[t] = (int)(soff.size() - 1);
-        long nz_end = trow[t];
-        while (nz_end < trow[t + 1] && (hk[nz_end] & 0xffff) != 0xffff) ++nz_end;
-        for (long i = trow[t]; i < nz_end; i += 32) {
-            const long len = 0xffff - (long)(hk[i] & 0xffff);  // the slice's first row is its longest
-            soff.push_back(soff.back() + 32 * len);
-        }
-        for (long i = nz_end; i < trow[t + 1]; ++i) zlist.push_back(hvox[i]);
-    }
-    tsl[ntiles] = (int)(soff.size() - 1);
+    // slices: each tile's rows with entries in runs of 32; the rows without
+    // entries (sorted last in their tile) go to one list of voxels whose
+    // result is 0 (or -sub), in row order
+    TmpBuf<int> trow_d(ntiles + 1);
+    SliceTables st;
+    slice_tables(n, ntiles, rkey_s.p, trow_d, s, st);
+    std::vector<int>& tsl = st.tsl;
     nslices = tsl[ntiles];
+    std::vector<long long> soff(nslices + 1, 0);
+    for (int sl = 0; sl < nslices; ++sl) soff[sl + 1] = soff[sl] + 32LL * st.slen[sl];
+    long nz = 0;
+    for (int t = 0; t < ntiles; ++t) nz += st.first[t + 1] - st.nzend[t];
+    nzero = nz;
+    zrows.alloc(std::max<long>(nzero, 1));
+    if (nzero) {
+        TmpBuf<char> flags(n);
+        TmpBuf<int> nsel(1);
+        k_empty_flags<<<ewt(n), 256, 0, s>>>(n, rkey_s.p, flags.p);
+        size_t fb = 0;
+        TV3_CUDA(cub::DeviceSelect::Flagged(nullptr, fb, vox.p, flags.p, zrows.p, nsel.p, (int)n, s));
+        TmpBuf<char> tmp(std::max<size_t>(fb, 1));
+        TV3_CUDA(cub::DeviceSelect::Flagged(tmp.p, fb, vox.p, flags.p, zrows.p, nsel.p, (int)n, s));
+        TV3_CUDA(cudaStreamSynchronize(s));
+    }
     // tiles with work, largest first: the longest tiles start in the first
     // wave and the last wave is made of the smallest ones
     {
@@ -511,9 +586,6 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
         nwork = (int)o.size();
         tile_order.alloc(std::max(nwork, 1));
         if (nwork) TV3_CUDA(cudaMemcpy(tile_order.p, o.data(), nwork * sizeof(int), cudaMemcpyHostToDevice));
-        nzero = (long)zlist.size();
-        zrows.alloc(std::max<long>(nzero, 1));
-        if (nzero) TV3_CUDA(cudaMemcpy(zrows.p, zlist.data(), nzero * sizeof(int), cudaMemcpyHostToDevice));
     }
     // work units of at most TILED_UNIT_K steps per slice (a slice of length 0 still gets one)
     std::vector<int> uslice, tunit(ntiles + 1, 0), sunit(nslices + 1, 0);
@@ -554,8 +626,6 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
     slice_off.alloc(nslices + 1);
     TV3_CUDA(cudaMemcpy(tile_slice.p, tsl.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
     TV3_CUDA(cudaMemcpy(slice_off.p, soff.data(), (nslices + 1) * sizeof(long long), cudaMemcpyHostToDevice));
-    TmpBuf<int> trow_d(ntiles + 1);
-    TV3_CUDA(cudaMemcpy(trow_d.p, trow.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
     lidx.alloc(std::max<long long>(padded, 1));
     val.alloc(std::max<long long>(padded, 1));
     row_voxel.alloc((size_t)std::max(nslices, 1) * 32);
@@ -921,22 +991,14 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
         TV3_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, sb, rcount.p, rseg.p, (int)(m + 1), s));
         TV3_CUDA(cudaStreamSynchronize(s));
     }
-    // slices (host): tiles' segment ranges and 32-segment slices
-    std::unique_ptr<unsigned long long[]> hk(new unsigned long long[nseg]);  // written whole by the copy
-    TV3_CUDA(cudaMemcpy(hk.get(), k_slice_s.p, nseg * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-    std::vector<int> tseg(ntiles + 1, (int)nseg), tsl(ntiles + 1, 0);
-    for (long i = nseg - 1; i >= 0; --i) tseg[hk[i] >> 16] = (int)i;
-    for (int t = ntiles - 1; t >= 0; --t) tseg[t] = std::min(tseg[t], tseg[t + 1]);
-    std::vector<long long> soff(1, 0);
-    for (int t = 0; t < ntiles; ++t) {
-        tsl[t] = (int)(soff.size() - 1);
-        for (long i = tseg[t]; i < tseg[t + 1]; i += 32) {
-            const long len = 0xffff - (long)(hk[i] & 0xffff);
-            soff.push_back(soff.back() + 32 * len);
-        }
-    }
-    tsl[ntiles] = (int)(soff.size() - 1);
+    // slices: each tile's segments in runs of 32 (every segment has entries)
+    TmpBuf<int> tseg_d(ntiles + 1);
+    SliceTables st;
+    slice_tables(nseg, ntiles, k_slice_s.p, tseg_d, s, st);
+    std::vector<int>& tsl = st.tsl;
     nslices = tsl[ntiles];
+    std::vector<long long> soff(nslices + 1, 0);
+    for (int sl = 0; sl < nslices; ++sl) soff[sl + 1] = soff[sl] + 32LL * st.slen[sl];
     {
         std::vector<std::pair<long long, int>> w;
         for (int t = 0; t < ntiles; ++t)
@@ -951,10 +1013,8 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     const long long padded = soff.back();
     tile_slice.alloc(ntiles + 1);
     slice_off.alloc(nslices + 1);
-    TmpBuf<int> tseg_d(ntiles + 1);
     TV3_CUDA(cudaMemcpy(tile_slice.p, tsl.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
     TV3_CUDA(cudaMemcpy(slice_off.p, soff.data(), (nslices + 1) * sizeof(long long), cudaMemcpyHostToDevice));
-    TV3_CUDA(cudaMemcpy(tseg_d.p, tseg.data(), (ntiles + 1) * sizeof(int), cudaMemcpyHostToDevice));
     lidx.alloc(std::max<long long>(padded, 1));
     val.alloc(std::max<long long>(padded, 1));
     slot_dest.alloc((size_t)std::max(nslices, 1) * 32);
