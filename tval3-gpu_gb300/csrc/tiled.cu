@@ -45,6 +45,13 @@ int ewt(long n) {
     return (int)std::max<long>(1, std::min(g, cap));
 }
 
+// bits that hold the indices 0 .. count-1 (at least 1)
+int index_bits(long count) {
+    int b = 1;
+    while (b < 62 && (1L << b) < count) ++b;
+    return b;
+}
+
 template <class V> struct TVT { using type = float; };
 template <> struct TVT<double> { using type = double; };
 
@@ -63,34 +70,37 @@ __global__ void k_rows_of(long rows, const int* __restrict__ ptr, int* __restric
         for (int k = ptr[r] + lane; k < ptr[r + 1]; k += 32) rowof[k] = (int)r;
 }
 
+// (tile, ray) keys: the ray index in the low rb bits, the tile above it, so a
+// radix sort needs only the bits the two indices occupy
 __global__ void k_keys(long nnz, const int* __restrict__ rowof, const int* __restrict__ tind,
-                       const int* __restrict__ tile_of, unsigned long long* __restrict__ key, int* __restrict__ idx) {
+                       const int* __restrict__ tile_of, int rb, unsigned long long* __restrict__ key,
+                       int* __restrict__ idx) {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
-        key[k] = ((unsigned long long)(unsigned)tile_of[rowof[k]] << 32) | (unsigned)tind[k];
+        key[k] = ((unsigned long long)(unsigned)tile_of[rowof[k]] << rb) | (unsigned)tind[k];
         idx[k] = (int)k;
     }
 }
 
 // first-of-(tile, ray) flags of the sorted keys, and each tile's first position
-__global__ void k_flags(long nnz, const unsigned long long* __restrict__ key, int* __restrict__ newray,
+__global__ void k_flags(long nnz, const unsigned long long* __restrict__ key, int rb, int* __restrict__ newray,
                         int* __restrict__ tile_first) {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
         const unsigned long long c = key[k];
         newray[k] = (k == 0 || key[k - 1] != c) ? 1 : 0;
-        if (k == 0 || (key[k - 1] >> 32) != (c >> 32)) tile_first[c >> 32] = (int)k;
+        if (k == 0 || (key[k - 1] >> rb) != (c >> rb)) tile_first[c >> rb] = (int)k;
     }
 }
 
 // uniq[k] = number of distinct (tile, ray) pairs up to and including k
-__global__ void k_local(long nnz, const unsigned long long* __restrict__ key, const int* __restrict__ uniq,
+__global__ void k_local(long nnz, const unsigned long long* __restrict__ key, int rb, const int* __restrict__ uniq,
                         const int* __restrict__ idx, const int* __restrict__ tile_first, int* __restrict__ rays,
                         unsigned short* __restrict__ local_of_entry) {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
         const unsigned long long c = key[k];
-        const int t = (int)(c >> 32);
+        const int t = (int)(c >> rb);
         const int u = uniq[k] - 1;                 // this (tile, ray) in the concatenated lists
         const int base = uniq[tile_first[t]] - 1;  // the tile's first
-        if (k == 0 || key[k - 1] != c) rays[u] = (int)(unsigned)(c & 0xffffffffu);
+        if (k == 0 || key[k - 1] != c) rays[u] = (int)(unsigned)(c & ((1ull << rb) - 1));
         local_of_entry[idx[k]] = (unsigned short)(u - base);
     }
 }
@@ -484,10 +494,9 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
         TmpBuf<unsigned long long> key(nnz), key_s(nnz);
         k_tile_of_voxel<<<ewt(n), 256, 0, s>>>(n, p, q, ty, tx, tz, nty, ntx, tile_of.p, iota.p);
         k_rows_of<<<ewt(n * 32), 256, 0, s>>>(n, tptr, rowof.p);
-        k_keys<<<ewt(nnz), 256, 0, s>>>(nnz, rowof.p, tind, tile_of.p, key.p, idx.p);
+        const int ray_bits = index_bits(m), end_bit = ray_bits + index_bits(ntiles);
+        k_keys<<<ewt(nnz), 256, 0, s>>>(nnz, rowof.p, tind, tile_of.p, ray_bits, key.p, idx.p);
         TV3_CUDA(cudaGetLastError());
-        int end_bit = 33;
-        while (end_bit < 64 && (1LL << (end_bit - 32)) < ntiles) ++end_bit;
         size_t tb = 0;
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, key.p, key_s.p, idx.p, idx_s.p, (int)nnz, 0, end_bit, s));
         {
@@ -497,7 +506,7 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
             TV3_CUDA(cudaStreamSynchronize(s));
         }
         TV3_CUDA(cudaMemsetAsync(tile_first.p, 0xff, ntiles * sizeof(int), s));
-        k_flags<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, newray.p, tile_first.p);
+        k_flags<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, ray_bits, newray.p, tile_first.p);
         size_t sb = 0;
         TV3_CUDA(cub::DeviceScan::InclusiveSum(nullptr, sb, newray.p, uniq.p, (int)nnz, s));
         {
@@ -507,7 +516,7 @@ void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, 
         }
         TV3_CUDA(cudaMemcpy(&nuniq, uniq.p + nnz - 1, sizeof(int), cudaMemcpyDeviceToHost));
         rays.alloc(std::max(nuniq, 1));
-        k_local<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, uniq.p, idx_s.p, tile_first.p, rays.p, local_of.p);
+        k_local<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, ray_bits, uniq.p, idx_s.p, tile_first.p, rays.p, local_of.p);
         TV3_CUDA(cudaGetLastError());
         // per-tile ray offsets: start of tile t's list = uniq[tile_first[t]] - 1;
         // a tile without nonzeros takes the next tile's start
@@ -743,10 +752,12 @@ void TiledT<T, V>::apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) cons
 // ---------------------------------------------------------------------------
 namespace {
 
+// (tile, ray) keys, the ray in the low rb bits
 __global__ void k_n_keys(long nnz, const int* __restrict__ rowof, const int* __restrict__ ind,
-                         const int* __restrict__ tile_of, unsigned long long* __restrict__ key, int* __restrict__ idx) {
+                         const int* __restrict__ tile_of, int rb, unsigned long long* __restrict__ key,
+                         int* __restrict__ idx) {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long)gridDim.x * blockDim.x) {
-        key[k] = ((unsigned long long)(unsigned)tile_of[ind[k]] << 32) | (unsigned)rowof[k];
+        key[k] = ((unsigned long long)(unsigned)tile_of[ind[k]] << rb) | (unsigned)rowof[k];
         idx[k] = (int)k;
     }
 }
@@ -768,8 +779,8 @@ __global__ void k_n_segs(long nnz, const unsigned long long* __restrict__ key, c
 
 // segment keys for the slicing sort (tile, longest first) and the ray-major sort (ray, tile)
 __global__ void k_n_segkeys(long nseg, const unsigned long long* __restrict__ seg_key, const int* __restrict__ seg_start,
-                            long nnz, unsigned long long* __restrict__ k_slice, unsigned long long* __restrict__ k_ray,
-                            int* __restrict__ iota, int* __restrict__ too_long) {
+                            long nnz, int rb, int tb, unsigned long long* __restrict__ k_slice,
+                            unsigned long long* __restrict__ k_ray, int* __restrict__ iota, int* __restrict__ too_long) {
     for (long s = (long)blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += (long)gridDim.x * blockDim.x) {
         const unsigned long long c = seg_key[s];
         const long end = (s + 1 < nseg) ? seg_start[s + 1] : nnz;
@@ -778,18 +789,18 @@ __global__ void k_n_segkeys(long nseg, const unsigned long long* __restrict__ se
             *too_long = 1;
             len = 0xffff;
         }
-        const unsigned tile = (unsigned)(c >> 32), ray = (unsigned)(c & 0xffffffffu);
+        const unsigned tile = (unsigned)(c >> rb), ray = (unsigned)(c & ((1ull << rb) - 1));
         k_slice[s] = ((unsigned long long)tile << 16) | (unsigned)(0xffff - len);
-        k_ray[s] = ((unsigned long long)ray << 32) | tile;
+        k_ray[s] = ((unsigned long long)ray << tb) | tile;
         iota[s] = (int)s;
     }
 }
 
 __global__ void k_n_dest(long nseg, const int* __restrict__ by_ray, const unsigned long long* __restrict__ k_ray_s,
-                         int* __restrict__ dest, int* __restrict__ rcount) {
+                         int tb, int* __restrict__ dest, int* __restrict__ rcount) {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nseg; i += (long)gridDim.x * blockDim.x) {
         dest[by_ray[i]] = (int)i;
-        atomicAdd(rcount + (k_ray_s[i] >> 32), 1);
+        atomicAdd(rcount + (k_ray_s[i] >> tb), 1);
     }
 }
 
@@ -925,10 +936,9 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     TmpBuf<unsigned long long> key(nnz), key_s(nnz);
     k_tile_of_voxel<<<ewt(n), 256, 0, s>>>(n, p, q, ty, tx, tz, nty, ntx, tile_of.p, iota_v.p);
     k_rows_of<<<ewt(m * 32), 256, 0, s>>>(m, ptr, rowof.p);
-    k_n_keys<<<ewt(nnz), 256, 0, s>>>(nnz, rowof.p, ind, tile_of.p, key.p, idx.p);
+    const int ray_bits = index_bits(m), tile_bits = index_bits(ntiles), end_bit = ray_bits + tile_bits;
+    k_n_keys<<<ewt(nnz), 256, 0, s>>>(nnz, rowof.p, ind, tile_of.p, ray_bits, key.p, idx.p);
     TV3_CUDA(cudaGetLastError());
-    int end_bit = 33;
-    while (end_bit < 64 && (1LL << (end_bit - 32)) < ntiles) ++end_bit;
     {
         size_t tb = 0;
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, key.p, key_s.p, idx.p, idx_s.p, (int)nnz, 0, end_bit, s));
@@ -953,7 +963,8 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     TmpBuf<int> seg_start(nseg), iota_s(nseg), order(nseg), by_ray(nseg), dest(nseg), too_long(1), rcount(m + 1);
     k_n_segs<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, segid.p, seg_key.p, seg_start.p);
     TV3_CUDA(cudaMemsetAsync(too_long.p, 0, sizeof(int), s));
-    k_n_segkeys<<<ewt(nseg), 256, 0, s>>>(nseg, seg_key.p, seg_start.p, nnz, k_slice.p, k_ray.p, iota_s.p, too_long.p);
+    k_n_segkeys<<<ewt(nseg), 256, 0, s>>>(nseg, seg_key.p, seg_start.p, nnz, ray_bits, tile_bits, k_slice.p, k_ray.p,
+                                          iota_s.p, too_long.p);
     // slicing order: (tile, longest first), stable
     int sbits = 17;
     while (sbits < 64 && (1LL << (sbits - 16)) < ntiles) ++sbits;
@@ -967,8 +978,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
         TV3_CUDA(cudaStreamSynchronize(s));
     }
     // ray-major order of the partials: (ray, tile)
-    int rbits = 33;
-    while (rbits < 64 && (1LL << (rbits - 32)) < m) ++rbits;
+    const int rbits = ray_bits + tile_bits;
     {
         size_t tb = 0;
         TV3_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, k_ray.p, k_ray_s.p, iota_s.p, by_ray.p, (int)nseg, 0,
@@ -982,7 +992,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     TV3_CUDA(cudaMemcpy(&tl, too_long.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (tl) return;
     TV3_CUDA(cudaMemsetAsync(rcount.p, 0, (m + 1) * sizeof(int), s));
-    k_n_dest<<<ewt(nseg), 256, 0, s>>>(nseg, by_ray.p, k_ray_s.p, dest.p, rcount.p);
+    k_n_dest<<<ewt(nseg), 256, 0, s>>>(nseg, by_ray.p, k_ray_s.p, tile_bits, dest.p, rcount.p);
     rseg.alloc(m + 1);
     {
         size_t sb = 0;
