@@ -226,14 +226,19 @@ struct CsrOp : LinOp<T> {
         if (this->nnz >= (1L << 22)) {
             for (int trans = 0; trans < 2; ++trans) {
                 if (!(trans ? tiled.ok : tiledN.ok)) continue;
-                const float t1 = time_product(trans, 1);
+                // one round each; two more only when the kernels are within 25 %
+                float t1 = time_product(trans, 1, 1);
                 const unsigned keep = pend;
                 pend &= ~(1u << trans);
-                float t0 = time_product(trans, 0);
+                float t0 = time_product(trans, 0, 1);
                 pend = keep;
                 if (t0 < 1.5f * t1 && ((pend >> trans) & 1u)) {
                     tune_pending(trans);
-                    t0 = time_product(trans, 0);
+                    t0 = time_product(trans, 0, 1);
+                }
+                if (std::max(t0, t1) < 1.25f * std::min(t0, t1)) {
+                    t1 = std::min(t1, time_product(trans, 1, 2));
+                    t0 = std::min(t0, time_product(trans, 0, 2));
                 }
                 (trans ? varT : varN) = (t0 < t1) ? 0 : 1;
             }
@@ -249,8 +254,9 @@ struct CsrOp : LinOp<T> {
     }
     int variant(int trans) const override { return trans ? varT : varN; }
 
-    // milliseconds of three products (after one warm-up) with kernel variant use_variant
-    float time_product(int trans, int use_variant) const {
+    // milliseconds of three products with kernel variant use_variant, best of
+    // `rounds` rounds after one warm-up
+    float time_product(int trans, int use_variant, int rounds) const {
         int& flag = trans ? varT : varN;
         const int keep = flag;
         flag = use_variant;
@@ -262,9 +268,8 @@ struct CsrOp : LinOp<T> {
         TV3_CUDA(cudaEventCreate(&e1));
         MatIO<T> io = plain_io<T>(x.p, y.p);
         apply(trans, io, SPMV_PLAIN, 0);
-        // best of three rounds of three launches: robust to one-off noise
         float best = 1e30f;
-        for (int round = 0; round < 3; ++round) {
+        for (int round = 0; round < rounds; ++round) {
             TV3_CUDA(cudaEventRecord(e0, 0));
             for (int k = 0; k < 3; ++k) apply(trans, io, SPMV_PLAIN, 0);
             TV3_CUDA(cudaEventRecord(e1, 0));
