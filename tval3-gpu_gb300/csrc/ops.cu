@@ -18,7 +18,13 @@ void tmp_pool_init() {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev]) return;
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-        unsigned long long keep = 4ull << 30;
+        // The threshold counts memory in use too: with live operators holding
+        // more than it, every synchronize would return all freed memory to the
+        // driver and the next build would map its temporaries again.  Keep up
+        // to 1/16 of the device (17.8 GB on a 284 GB part), at least 4 GB.
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) total_b = 0;
+        unsigned long long keep = std::max<unsigned long long>(4ull << 30, (unsigned long long)total_b / 16);
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
     done[dev] = true;
