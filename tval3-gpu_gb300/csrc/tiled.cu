@@ -28,7 +28,6 @@
 // partials in order after a barrier (deterministic).
 #include <cub/cub.cuh>
 #include <algorithm>
-#include <memory>
 #include <type_traits>
 #include <vector>
 #include "ops.h"
