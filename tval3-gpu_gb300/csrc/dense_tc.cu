@@ -463,7 +463,9 @@ void umma_apply(const UmmaPlan* p, int trans, const MatIO<float>& io, int epi, c
     __nv_bfloat16* bh = trans ? p->bT_h.p : p->bN_h.p;
     __nv_bfloat16* bl = trans ? p->bT_l.p : p->bN_l.p;
     const int qg = (int)std::max<long>(1, std::min<long>((K + QK - 1) / QK, (long)num_sms() * 8));
-    k_umma_quant<<<qg, 256, 0, s>>>(K, p->L, Kp, trans ? rs : nullptr, io, bh, bl);
+    // dependent launches: each kernel waits for its predecessor at entry
+    // (count_launch), so its launch overlaps the previous kernel's tail
+    launch_k(k_umma_quant, dim3(qg), dim3(256), 0, s, K, p->L, Kp, trans ? rs : nullptr, io, bh, bl);
     GemmArgs g;
     g.M = M; g.K = K; g.L = p->L; g.Npad = p->Npad; g.tmem_cols = p->tmem_cols;
     g.stages = trans ? p->stagesT : p->stagesN;
@@ -472,17 +474,19 @@ void umma_apply(const UmmaPlan* p, int trans, const MatIO<float>& io, int epi, c
     g.ctl = io.ctl;
     const int splits = trans ? p->splitsT : p->splitsN;
     dim3 grid((unsigned)splits, (unsigned)((M + UM - 1) / UM));
-    k_umma_gemm<<<grid, 128, trans ? p->smemT : p->smemN, s>>>(trans ? p->mapAt : p->mapA,
-                                                               trans ? p->mapBTh : p->mapBNh,
-                                                               trans ? p->mapBTl : p->mapBNl, g);
+    launch_k(k_umma_gemm, grid, dim3(128), trans ? p->smemT : p->smemN, s, trans ? p->mapAt : p->mapA,
+             trans ? p->mapBTh : p->mapBNh, trans ? p->mapBTl : p->mapBNl, g);
     const long tot = M * p->L;
     const int rg = (int)std::max<long>(1, std::min<long>((tot + 255) / 256, (long)num_sms() * 4));
     const float* post = trans ? nullptr : rs;
+    auto reduce = [&](auto kernel) {
+        launch_k(kernel, dim3(rg), dim3(256), 0, s, M, p->L, splits, (const float*)p->part.p, post, io);
+    };
     switch (epi) {
-        case SPMV_SUB: k_umma_reduce<SPMV_SUB><<<rg, 256, 0, s>>>(M, p->L, splits, p->part.p, post, io); break;
-        case SPMV_LAM35: k_umma_reduce<SPMV_LAM35><<<rg, 256, 0, s>>>(M, p->L, splits, p->part.p, post, io); break;
-        case SPMV_NORM2: k_umma_reduce<SPMV_NORM2><<<rg, 256, 0, s>>>(M, p->L, splits, p->part.p, post, io); break;
-        default: k_umma_reduce<SPMV_PLAIN><<<rg, 256, 0, s>>>(M, p->L, splits, p->part.p, post, io); break;
+        case SPMV_SUB: reduce(k_umma_reduce<SPMV_SUB>); break;
+        case SPMV_LAM35: reduce(k_umma_reduce<SPMV_LAM35>); break;
+        case SPMV_NORM2: reduce(k_umma_reduce<SPMV_NORM2>); break;
+        default: reduce(k_umma_reduce<SPMV_PLAIN>); break;
     }
     TV3_CUDA(cudaGetLastError());
 }
