@@ -11,8 +11,8 @@
 // The FP32 right-hand side is split into two BF16 parts (hi = bf16(v),
 // lo = bf16(v - hi)), so the products carry about 16 mantissa bits of the
 // vector and the BF16 rounding of A stays the only quantisation; A^T*Y uses
-// the same BF16 values as A*X (a stored transpose), so it is the exact adjoint
-// of the quantised A.
+// the same BF16 values as A*X (a blocked copy of the transpose), so it is the
+// exact adjoint of the quantised A.
 //
 // Kernel structure (one CTA = one 128-row tile of D and one split of K; four
 // warps):
