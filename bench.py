@@ -367,14 +367,17 @@ def run_ours(args):
     peak, peak_kind = peaks()
     dom = ("spmv_AT", tT, bT) if tT >= tN else ("spmv_A", tN, bN)
     ach = dom[2] / dom[1] / 1e9
+    # DRAM bytes of one launch of the kernel(s) that ran, from an ncu capture
+    # of that same variant (null when none was captured)
+    dom_variant = {0: "csr", 1: "tiled", 2: "tiled_pipe"}[op.variant(1 if dom[0] == "spmv_AT" else 0)]
     traffic = None
     tf = ROOT / "profiles" / "spmv_traffic.json"
     if tf.exists():
         try:
-            traffic = json.loads(tf.read_text()).get(f"{dom[0]}_{head}_{args.size}")
+            traffic = json.loads(tf.read_text()).get(f"{dom[0]}_{dom_variant}_{head}_{args.size}")
         except Exception:
             traffic = None
-    roofline = {"kernel": dom[0], "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+    roofline = {"kernel": dom[0], "variant": dom_variant, "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                 "bytes_per_launch": dom[2], "launch_us": round(dom[1] * 1e6, 2),
                 "pair": {"A_us": round(tN * 1e6, 2), "AT_us": round(tT * 1e6, 2),
