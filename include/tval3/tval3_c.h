@@ -53,8 +53,13 @@ typedef enum tval3_precision {
     TVAL3_PREC_BF16 = 2, /* BF16 values with per-row FP32 scale, FP32 accumulation */
     TVAL3_PREC_FP16 = 3, /* FP16 values with per-row FP32 scale, FP32 accumulation */
     TVAL3_PREC_FP32_F64VEC = 4, /* FP32 values, FP64 vectors, products and reductions */
-    TVAL3_PREC_FP32_DF64 = 5    /* FP32 values; vectors, products and reductions in double-float
+    TVAL3_PREC_FP32_DF64 = 5,   /* FP32 values; vectors, products and reductions in double-float
                                    (pairs of FP32, ~48 bits) on the FP32 pipes; FP64 at the interface */
+    TVAL3_PREC_BF16_DF64 = 6,   /* mixed: BF16 values with a per-row FP32 scale (the matrix stream
+                                   shrinks to 2 bytes per value); vectors, products, the step size,
+                                   line-search inner products and stopping norms in double-float;
+                                   FP64 at the interface */
+    TVAL3_PREC_FP16_DF64 = 7    /* mixed: as TVAL3_PREC_BF16_DF64 with FP16 values */
 } tval3_precision;
 
 typedef enum tval3_trans { TVAL3_OP_N = 0, TVAL3_OP_T = 1 } tval3_trans;
@@ -85,7 +90,9 @@ typedef struct tval3_options {
     int tv_type;      /* tval3_tv; the reference is anisotropic */
     int precision;    /* internal arithmetic of the host entry points: -1 = the entry point's
                          type; TVAL3_PREC_FP32_DF64 with an _f64 entry and FP32 matrix values
-                         runs the solve in double-float */
+                         runs the solve in double-float; TVAL3_PREC_BF16_DF64 / FP16_DF64
+                         with an _f64 sparse or geometry entry store the matrix in 16 bits
+                         (per-row FP32 scale) and run the solve in double-float */
 } tval3_options;
 
 /* Result summary (tval3_info, 2d/tval3_types.h:37-43; outer_secs
@@ -210,6 +217,24 @@ TVAL3_API tval3_status tval3_gpu_3d_geometry_sparse_f32(float* U, int dim_y, int
                                                         int b_len, const tval3_options* opts, const float* Ut,
                                                         int Ut_len, int pagelocked, int mainGPU, int numGPUs,
                                                         const int* gpuArray, tval3_info* info);
+/* double instantiations of the geometry overloads, 3d/tval3_gpu_3d.cpp:58-69:
+ * the ray matrix is built on the device and stored with FP32 values (the
+ * reference evaluates it on the fly); the solve runs with FP64 vectors, or in
+ * double-float (opts->precision = TVAL3_PREC_FP32_DF64), or in double-float
+ * over a BF16/FP16 copy of the matrix (TVAL3_PREC_BF16_DF64 / FP16_DF64). */
+TVAL3_API tval3_status tval3_gpu_3d_geometry_f64(double* U, int dim_y, int dim_x, int dim_z,
+                                                 const tval3_geometry_host* A, const double* b, int b_len,
+                                                 const tval3_options* opts, const double* Ut, int Ut_len,
+                                                 int pagelocked, int mainGPU, int numGPUs, const int* gpuArray,
+                                                 tval3_info* info);
+/* (U, geometry_host, sparse_mat_host<double>, ...): A*x from the geometry's
+ * ray matrix, A^T*y from A_mat, FP64 vectors. */
+TVAL3_API tval3_status tval3_gpu_3d_geometry_sparse_f64(double* U, int dim_y, int dim_x, int dim_z,
+                                                        const tval3_geometry_host* A_geo,
+                                                        const tval3_sparse_host* A_mat, const double* b,
+                                                        int b_len, const tval3_options* opts, const double* Ut,
+                                                        int Ut_len, int pagelocked, int mainGPU, int numGPUs,
+                                                        const int* gpuArray, tval3_info* info);
 /* 2D: tval3_gpu(U, sparse_mat_host A, b, opts, Ut, pagelocked), 2d/tval3_gpu.h:9-13;
  * U is rows x cols (dim_y x dim_x), periodic D in 2D (2d/tval3.cu:202-331).
  * layers = b_len / A.rows columns of b share A (2d/tval3.cu:1406-1426): U
@@ -235,7 +260,11 @@ typedef struct tval3_op_s* tval3_op;
 
 /* From host CSR (+ optional CSR of A^T).  precision selects the stored value
  * type: FP32, BF16 or FP16 (the vector type of products is FP32), or FP64
- * (vector type FP64).  The transpose is built on the device when absent. */
+ * (vector type FP64), FP32_F64VEC (FP32 values, vector type FP64), or
+ * FP32_DF64 / BF16_DF64 / FP16_DF64 (FP32, BF16 or FP16 values, vector type
+ * double-float).  16-bit values carry a per-row FP32 scale (the row's largest
+ * magnitude), quantised from FP32 values.  The transpose is built on the
+ * device when absent. */
 TVAL3_API tval3_status tval3_op_create_sparse(tval3_op* op, const tval3_sparse_host* A, int precision);
 /* From device CSR arrays (copied; the caller keeps ownership).  val is FP32. */
 TVAL3_API tval3_status tval3_op_create_sparse_device(tval3_op* op, int rows, int cols, int nnz, const int* d_ptr,
@@ -250,13 +279,25 @@ TVAL3_API tval3_status tval3_op_destroy(tval3_op op);
 TVAL3_API tval3_status tval3_op_shape(tval3_op op, int* rows, int* cols, int64_t* nnz);
 /* Copy the device CSR (A and A^T) of a stored operator to host arrays
  * (ptr: rows+1 / cols+1 ints, ind: nnz ints, val: nnz floats); any pointer may
- * be NULL to skip that array.  Values are FP32 (dequantised for BF16/FP16). */
+ * be NULL to skip that array.  Values are FP32 (dequantised for the 16-bit
+ * storages: the FP32 rounding of value x row scale). */
 TVAL3_API tval3_status tval3_op_export_csr(tval3_op op, int* ptr, int* ind, float* val, int* tptr, int* tind,
                                            float* tval);
+/* The stored matrix as the products see it: values val/tval (FP32) and a
+ * per-row scale row_scale (rows floats), so that entry (r, c) is exactly
+ * val * row_scale[r] (and tval * row_scale[r] in the CSR of A^T) when
+ * evaluated in FP64.  For 16-bit storage val holds the 16-bit values widened
+ * to FP32 (exact) and row_scale the per-ray scales; for other storage
+ * row_scale is all ones and val is what tval3_op_export_csr returns.  Lets a
+ * checker rebuild the quantised matrix without the rounding of an FP32
+ * product.  Any pointer may be NULL.  No counterpart in the reference. */
+TVAL3_API tval3_status tval3_op_export_csr_scaled(tval3_op op, int* ptr, int* ind, float* val, float* row_scale,
+                                                  int* tptr, int* tind, float* tval);
 /* mat_vec_mul(trans, A, x, y, stream): y = A x (trans = 0) or y = A^T x.
  * x, y are device pointers of the operator's vector type: float (FP32, BF16,
  * FP16 operators), double (FP64, FP32_F64VEC), or double-float pairs
- * {float hi, lo} (FP32_DF64; see tval3_df64_from_f64).  Batched multi-RHS
+ * {float hi, lo} (FP32_DF64, BF16_DF64, FP16_DF64; see tval3_df64_from_f64).
+ * Batched multi-RHS
  * form: nrhs columns, leading dimension = vector length (the reference's
  * `layers`, 2d/mat_vec_mul.h:65-71, :96-99). */
 TVAL3_API tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, void* stream);

@@ -73,6 +73,11 @@ def lib():
         L.oracle_tval3_csr.restype = C.c_int
         L.oracle_tval3_csr.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_long, P, P, P, P, P, P, P,
                                        C.POINTER(OracleOpts), P, P, C.POINTER(OracleInfo), P, P, P]
+        L.oracle_tval3_csr_scaled.restype = C.c_int
+        L.oracle_tval3_csr_scaled.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_long, P, P, P, P, P, P, P, P,
+                                              C.POINTER(OracleOpts), P, P, C.POINTER(OracleInfo), P, P, P]
+        L.oracle_spmv_scaled_f64.restype = None
+        L.oracle_spmv_scaled_f64.argtypes = [C.c_long, P, P, P, P, P, P]
         L.oracle_tval3_dense.restype = C.c_int
         L.oracle_tval3_dense.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_long, P, P,
                                          C.POINTER(OracleOpts), P, P, C.POINTER(OracleInfo), P]
@@ -141,10 +146,15 @@ def transpose(m, n, ptr, ind, val):
     return tptr, tind, tval
 
 
-def spmv(ptr, ind, val, x):
+def spmv(ptr, ind, val, x, rscale=None):
+    """y = A x in FP64; rscale: optional per-row scale (entry = val * rscale[row])."""
     x = np.ascontiguousarray(x, np.float64).reshape(-1)
     y = np.empty(ptr.size - 1, np.float64)
-    lib().oracle_spmv_f64(ptr.size - 1, _p(ptr), _p(ind), _p(val), _p(x), _p(y))
+    if rscale is None:
+        lib().oracle_spmv_f64(ptr.size - 1, _p(ptr), _p(ind), _p(val), _p(x), _p(y))
+    else:
+        rs = np.ascontiguousarray(rscale, np.float32)
+        lib().oracle_spmv_scaled_f64(ptr.size - 1, _p(ptr), _p(ind), _p(val), _p(rs), _p(x), _p(y))
     return y
 
 
@@ -186,8 +196,11 @@ def make_opts(**kw) -> OracleOpts:
 
 
 def tval3_csr(dims, ptr, ind, val, b, opts=None, prec=0, Ut=None, tptr=None, tind=None, tval=None, trace=False,
-              xstar=None):
+              xstar=None, rscale=None):
     """Solve with the oracle.  prec 0: FP64 vectors, 1: FP32 vectors.
+    rscale: optional per-row scale of A (entry (r, c) = val * rscale[r]; the
+    library's 16-bit storage as tval3_op_export_csr_scaled returns it), with
+    tval then holding the unscaled values of the transpose.
     Returns (U as [z, x, y] array, info dict[, per-iteration f][, per-iteration
     relative error vs xstar])."""
     p, q, r = dims
@@ -204,8 +217,14 @@ def tval3_csr(dims, ptr, ind, val, b, opts=None, prec=0, Ut=None, tptr=None, tin
     tr = np.zeros(max(o.maxit, 1), np.float64) if trace else None
     xs = None if xstar is None else np.ascontiguousarray(xstar, np.float64).reshape(-1)
     te = None if xs is None else np.full(max(o.maxit, 1), np.nan)
-    lib().oracle_tval3_csr(prec, p, q, r, m, _p(ptr), _p(ind), _p(val), _p(tptr), _p(tind), _p(tval), _p(b),
-                           C.byref(o), _p(U), _p(Ut_a), C.byref(info), _p(tr), _p(xs), _p(te))
+    if rscale is None:
+        lib().oracle_tval3_csr(prec, p, q, r, m, _p(ptr), _p(ind), _p(val), _p(tptr), _p(tind), _p(tval), _p(b),
+                               C.byref(o), _p(U), _p(Ut_a), C.byref(info), _p(tr), _p(xs), _p(te))
+    else:
+        rs = np.ascontiguousarray(rscale, np.float32)
+        lib().oracle_tval3_csr_scaled(prec, p, q, r, m, _p(ptr), _p(ind), _p(val), _p(rs), _p(tptr), _p(tind),
+                                      _p(tval), _p(b), C.byref(o), _p(U), _p(Ut_a), C.byref(info), _p(tr), _p(xs),
+                                      _p(te))
     out = (U.reshape(r, q, p), info.as_dict())
     if trace:
         out = out + (tr,)

@@ -136,21 +136,28 @@ struct Op {
     virtual ~Op() {}
 };
 
+// rs (optional): a per-row scale of A, entry (r, c) = val * rs[r], applied to
+// the row sum of A*x and to the gathered y of A^T*y (the library's order for
+// its 16-bit storage, where val holds the 16-bit values exactly)
 template <class T>
 struct CsrOp : Op<T> {
     const int *ptr, *ind, *tptr, *tind;
     const float *val, *tval;
+    const float* rs = nullptr;
     void N(const T* x, T* y) const override {
         pfor(this->m, [&](long r) {
             T s = 0;
             for (int k = ptr[r]; k < ptr[r + 1]; ++k) s += (T)val[k] * x[ind[k]];
-            y[r] = s;
+            y[r] = rs ? s * (T)rs[r] : s;
         });
     }
     void Tr(const T* y, T* x) const override {
         pfor(this->n, [&](long c) {
             T s = 0;
-            for (int k = tptr[c]; k < tptr[c + 1]; ++k) s += (T)tval[k] * y[tind[k]];
+            if (rs)
+                for (int k = tptr[c]; k < tptr[c + 1]; ++k) s += (T)tval[k] * (y[tind[k]] * (T)rs[tind[k]]);
+            else
+                for (int k = tptr[c]; k < tptr[c + 1]; ++k) s += (T)tval[k] * y[tind[k]];
             x[c] = s;
         });
     }
@@ -836,6 +843,36 @@ int oracle_tval3_csr(int prec, int p, int q, int r, long m, const int* ptr, cons
     CsrOp<float> A;
     A.m = m; A.n = g.n(); A.ptr = ptr; A.ind = ind; A.val = val; A.tptr = tptr; A.tind = tind; A.tval = tval;
     return solve<float>(g, A, (const float*)b, *o, (float*)U_out, (const float*)Ut, info, trace_f, xstar, trace_err);
+}
+
+// The same with a per-row scale of A (rs, m floats; NULL = none): entry
+// (r, c) = val * rs[r], as the library stores 16-bit matrices.
+int oracle_tval3_csr_scaled(int prec, int p, int q, int r, long m, const int* ptr, const int* ind, const float* val,
+                            const float* rs, const int* tptr, const int* tind, const float* tval, const void* b,
+                            const oracle_opts* o, void* U_out, const void* Ut, oracle_info* info, double* trace_f,
+                            const double* xstar, double* trace_err) {
+    Dims g{p, q, r};
+    if (prec == 0) {
+        CsrOp<double> A;
+        A.m = m; A.n = g.n(); A.ptr = ptr; A.ind = ind; A.val = val; A.tptr = tptr; A.tind = tind; A.tval = tval;
+        A.rs = rs;
+        return solve<double>(g, A, (const double*)b, *o, (double*)U_out, (const double*)Ut, info, trace_f, xstar,
+                             trace_err);
+    }
+    CsrOp<float> A;
+    A.m = m; A.n = g.n(); A.ptr = ptr; A.ind = ind; A.val = val; A.tptr = tptr; A.tind = tind; A.tval = tval;
+    A.rs = rs;
+    return solve<float>(g, A, (const float*)b, *o, (float*)U_out, (const float*)Ut, info, trace_f, xstar, trace_err);
+}
+
+// y = A x with a per-row scale (FP64 vectors).
+void oracle_spmv_scaled_f64(long m, const int* ptr, const int* ind, const float* val, const float* rs,
+                            const double* x, double* y) {
+    pfor(m, [&](long r) {
+        double s = 0;
+        for (int k = ptr[r]; k < ptr[r + 1]; ++k) s += (double)val[k] * x[ind[k]];
+        y[r] = rs ? s * (double)rs[r] : s;
+    });
 }
 
 // TVAL3 with a dense row-major m x n matrix.

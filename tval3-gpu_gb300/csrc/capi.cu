@@ -23,11 +23,23 @@ struct tval3_op_s {
     int precision = 0;
     LinOp<float>* f = nullptr;
     LinOp<double>* d = nullptr;
-    LinOp<df64>* q = nullptr;  // double-float view of d (TVAL3_PREC_FP32_DF64)
+    // double-float products: a view of d (TVAL3_PREC_FP32_DF64), or an
+    // operator of its own with 16-bit storage and d null (BF16_DF64, FP16_DF64)
+    LinOp<df64>* q = nullptr;
     ~tval3_op_s() {
         delete q;
         delete f;
         delete d;
+    }
+    // shape and stored arrays: the owning operator of whichever kind
+    long rows() const { return d ? d->m : (q ? q->m : f->m); }
+    long cols() const { return d ? d->n : (q ? q->n : f->n); }
+    long nnz() const { return d ? d->nnz : (q ? q->nnz : f->nnz); }
+    template <class F>
+    void with_store(F fn) const {
+        if (d) fn(*d);
+        else if (q) fn(*q);
+        else fn(*f);
     }
 };
 
@@ -201,6 +213,55 @@ void to_device(DBuf<T>& d, const void* h, long n, int src_type) {
     }
 }
 
+// FP32 device copies of a host sparse matrix (FP64 values are narrowed on the
+// host), with the CSR of A built on the device when only the CSC was given
+struct F32Csr {
+    DBuf<int> ptr, ind, tptr, tind;
+    DBuf<float> val, tval;
+};
+
+void upload_f32(const tval3_sparse_host* A, bool dev_check, F32Csr& c) {
+    const long m = A->rows, n = A->cols, nnz = A->nnz;
+    if (A->format & TVAL3_SPARSE_CSR) {
+        c.ptr.alloc(m + 1);
+        c.ind.alloc(std::max<long>(nnz, 1));
+        TV3_CUDA(cudaMemcpy(c.ptr.p, A->csr_ptr, (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        if (nnz) TV3_CUDA(cudaMemcpy(c.ind.p, A->csr_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
+        to_device(c.val, A->csr_val, nnz, A->val_type);
+    }
+    if (A->format & TVAL3_SPARSE_CSC) {
+        c.tptr.alloc(n + 1);
+        c.tind.alloc(std::max<long>(nnz, 1));
+        TV3_CUDA(cudaMemcpy(c.tptr.p, A->csc_ptr, (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        if (nnz) TV3_CUDA(cudaMemcpy(c.tind.p, A->csc_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
+        to_device(c.tval, A->csc_val, nnz, A->val_type);
+    }
+    if (dev_check) {
+        if (A->format & TVAL3_SPARSE_CSR) validate_device<float>(c.ptr.p, m, c.ind.p, c.val.p, nnz, n, "CSR");
+        if (A->format & TVAL3_SPARSE_CSC) validate_device<float>(c.tptr.p, n, c.tind.p, c.tval.p, nnz, m, "CSC");
+    }
+    if (!(A->format & TVAL3_SPARSE_CSR)) {
+        c.ptr.alloc(m + 1);
+        c.ind.alloc(std::max<long>(nnz, 1));
+        c.val.alloc(std::max<long>(nnz, 1));
+        csr_transpose_device<float>(n, m, nnz, c.tptr.p, c.tind.p, c.tval.p, c.ptr.p, c.ind.p, c.val.p, 0);
+    }
+}
+
+// mixed-precision operator (TVAL3_PREC_BF16_DF64 / FP16_DF64) from a host
+// sparse matrix: FP32 values uploaded, then quantised on the device
+LinOp<df64>* sparse_op_mixed(const tval3_sparse_host* A, int precision) {
+    if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+    const bool dev_check = A->nnz > DEVICE_CHECK_NNZ && A->val_type == TVAL3_PREC_FP32;
+    check_sparse(A, !dev_check);
+    F32Csr c;
+    upload_f32(A, dev_check, c);
+    return make_csr_op_df64q(A->rows, A->cols, A->nnz, c.ptr.p, c.ind.p, c.val.p, c.tptr.p,
+                             c.tptr.p ? c.tind.p : nullptr, c.tptr.p ? c.tval.p : nullptr, precision, 0);
+}
+
+bool is_mixed(int precision) { return precision == TVAL3_PREC_BF16_DF64 || precision == TVAL3_PREC_FP16_DF64; }
+
 // device operator from a host sparse matrix.  FP32 values under FP64 vectors
 // (TVAL3_PREC_FP32_F64VEC) go up as FP32 and stay FP32.  tune = false skips
 // the lane timing (an operator that only backs a double-float view).
@@ -213,36 +274,10 @@ LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision, bool tune = true)
     const long m = A->rows, n = A->cols, nnz = A->nnz;
     if constexpr (std::is_same<T, double>::value) {
         if (precision == TVAL3_PREC_FP32_F64VEC && A->val_type == TVAL3_PREC_FP32) {
-            DBuf<int> ptr, ind, tptr, tind;
-            DBuf<float> val, tval;
-            if (A->format & TVAL3_SPARSE_CSR) {
-                ptr.alloc(m + 1);
-                ind.alloc(std::max<long>(nnz, 1));
-                val.alloc(std::max<long>(nnz, 1));
-                TV3_CUDA(cudaMemcpy(ptr.p, A->csr_ptr, (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
-                if (nnz) TV3_CUDA(cudaMemcpy(ind.p, A->csr_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
-                if (nnz) TV3_CUDA(cudaMemcpy(val.p, A->csr_val, nnz * sizeof(float), cudaMemcpyHostToDevice));
-            }
-            if (A->format & TVAL3_SPARSE_CSC) {
-                tptr.alloc(n + 1);
-                tind.alloc(std::max<long>(nnz, 1));
-                tval.alloc(std::max<long>(nnz, 1));
-                TV3_CUDA(cudaMemcpy(tptr.p, A->csc_ptr, (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
-                if (nnz) TV3_CUDA(cudaMemcpy(tind.p, A->csc_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
-                if (nnz) TV3_CUDA(cudaMemcpy(tval.p, A->csc_val, nnz * sizeof(float), cudaMemcpyHostToDevice));
-            }
-            if (dev_check) {
-                if (A->format & TVAL3_SPARSE_CSR) validate_device<float>(ptr.p, m, ind.p, val.p, nnz, n, "CSR");
-                if (A->format & TVAL3_SPARSE_CSC) validate_device<float>(tptr.p, n, tind.p, tval.p, nnz, m, "CSC");
-            }
-            if (!(A->format & TVAL3_SPARSE_CSR)) {
-                ptr.alloc(m + 1);
-                ind.alloc(std::max<long>(nnz, 1));
-                val.alloc(std::max<long>(nnz, 1));
-                csr_transpose_device<float>(n, m, nnz, tptr.p, tind.p, tval.p, ptr.p, ind.p, val.p, 0);
-            }
-            return make_csr_op_f64vec(m, n, nnz, ptr.p, ind.p, val.p, tptr.p, tptr.p ? tind.p : nullptr,
-                                      tptr.p ? tval.p : nullptr, 0, tune);
+            F32Csr c;
+            upload_f32(A, dev_check, c);
+            return make_csr_op_f64vec(m, n, nnz, c.ptr.p, c.ind.p, c.val.p, c.tptr.p, c.tptr.p ? c.tind.p : nullptr,
+                                      c.tptr.p ? c.tval.p : nullptr, 0, tune);
         }
     }
     DBuf<int> ptr, ind, tptr, tind;
@@ -410,6 +445,12 @@ tval3_status tval3_gpu_3d_sparse_f64(double* U, int dim_y, int dim_x, int dim_z,
                              t0);
             return;
         }
+        if (is_mixed(opts->precision)) {
+            // 16-bit matrix with per-ray scales, double-float solve
+            solve_host<df64>(sparse_op_mixed(A, opts->precision), U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len,
+                             info, t0);
+            return;
+        }
         solve_host<double>(sparse_op<double>(A, prec), U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len, info, t0);
     });
 }
@@ -505,17 +546,86 @@ tval3_status tval3_gpu_3d_geometry_sparse_f32(float* U, int dim_y, int dim_x, in
     });
 }
 
+tval3_status tval3_gpu_3d_geometry_f64(double* U, int dim_y, int dim_x, int dim_z, const tval3_geometry_host* A,
+                                       const double* b, int b_len, const tval3_options* opts, const double* Ut,
+                                       int Ut_len, int, int, int, const int*, tval3_info* info) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_opts(opts);
+        if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+        if (A->rv_y != dim_y || A->rv_x != dim_x || A->rv_z != dim_z)
+            arg_error(TVAL3_ERR_SHAPE, "Argument error: the volume of U must equal the geometry's rv_y x rv_x x rv_z!");
+        // the ray matrix is built on the device and stored (FP32 path lengths);
+        // the solve runs in FP64, double-float, or double-float over a 16-bit
+        // copy of the matrix, as opts->precision asks
+        const int pr = opts->precision;
+        if (pr == TVAL3_PREC_FP32_DF64 || is_mixed(pr)) {
+            std::unique_ptr<LinOp<double>> base;
+            LinOp<df64>* op = nullptr;
+            if (pr == TVAL3_PREC_FP32_DF64) {
+                base.reset(make_geometry_op<double>(A, 0, TVAL3_PREC_FP32_DF64, 0));
+                op = make_df64_view(base.get());
+            } else {
+                op = make_geometry_op<df64>(A, 0, pr, 0);
+            }
+            try {
+                check_problem(U, dim_y, dim_x, dim_z, op->m, op->n, b, b_len, Ut, Ut_len);
+            } catch (...) {
+                delete op;
+                throw;
+            }
+            solve_host<df64>(op, U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len, info, t0);
+            return;
+        }
+        LinOp<double>* op = make_geometry_op<double>(A, 0, TVAL3_PREC_FP32_F64VEC, 0);
+        try {
+            check_problem(U, dim_y, dim_x, dim_z, op->m, op->n, b, b_len, Ut, Ut_len);
+        } catch (...) {
+            delete op;
+            throw;
+        }
+        solve_host<double>(op, U, dim_y, dim_x, dim_z, b, b_len, opts, Ut, Ut_len, info, t0);
+    });
+}
+
+tval3_status tval3_gpu_3d_geometry_sparse_f64(double* U, int dim_y, int dim_x, int dim_z,
+                                              const tval3_geometry_host* A_geo, const tval3_sparse_host* A_mat,
+                                              const double* b, int b_len, const tval3_options* opts,
+                                              const double* Ut, int Ut_len, int, int, int, const int*,
+                                              tval3_info* info) {
+    return guard([&] {
+        auto t0 = std::chrono::steady_clock::now();
+        check_opts(opts);
+        if (!A_geo || !A_mat) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
+        if (A_geo->rv_y != dim_y || A_geo->rv_x != dim_x || A_geo->rv_z != dim_z)
+            arg_error(TVAL3_ERR_SHAPE, "Argument error: the volume of U must equal the geometry's rv_y x rv_x x rv_z!");
+        check_problem(U, dim_y, dim_x, dim_z, A_mat->rows, A_mat->cols, b, b_len, Ut, Ut_len);
+        // A*x from the geometry's ray matrix (built on the device), A^T*y from
+        // the given sparse matrix, both with FP64 vectors
+        std::unique_ptr<LinOp<double>> geo(make_geometry_op<double>(A_geo, 0, TVAL3_PREC_FP32_F64VEC, 0));
+        const int prec = (A_mat->val_type == TVAL3_PREC_FP32) ? TVAL3_PREC_FP32_F64VEC : TVAL3_PREC_FP64;
+        std::unique_ptr<LinOp<double>> mat(sparse_op<double>(A_mat, prec));
+        if (geo->m != mat->m || geo->n != mat->n)
+            arg_error(TVAL3_ERR_SHAPE, "Argument error: geometry and sparse matrix disagree in shape!");
+        solve_host<double>(new SplitOp<double>(std::move(geo), std::move(mat)), U, dim_y, dim_x, dim_z, b, b_len,
+                           opts, Ut, Ut_len, info, t0);
+    });
+}
+
 // ---------------------------------------------------------------------------
 // operators
 // ---------------------------------------------------------------------------
 tval3_status tval3_op_create_sparse(tval3_op* op, const tval3_sparse_host* A, int precision) {
     return guard([&] {
         if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
-        if (precision < 0 || precision > 5) arg_error(TVAL3_ERR_ARG, "Argument error: unknown precision!");
+        if (precision < 0 || precision > 7) arg_error(TVAL3_ERR_ARG, "Argument error: unknown precision!");
         auto* h = new tval3_op_s();
         try {
             h->precision = precision;
-            if (precision == TVAL3_PREC_FP32_DF64) {
+            if (is_mixed(precision)) {
+                h->dbl = 1;
+                h->q = sparse_op_mixed(A, precision);
+            } else if (precision == TVAL3_PREC_FP32_DF64) {
                 h->dbl = 1;
                 h->d = sparse_op<double>(A, TVAL3_PREC_FP32_F64VEC, false);
                 h->q = make_df64_view(h->d);
@@ -557,14 +667,17 @@ tval3_status tval3_op_create_geometry(tval3_op* op, const tval3_geometry_host* G
     return guard([&] {
         if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
         if (mode < 0 || mode > 1) arg_error(TVAL3_ERR_ARG, "Argument error: unknown geometry mode!");
-        if (precision == TVAL3_PREC_FP64 || precision < 0 || precision > 5)
+        if (precision == TVAL3_PREC_FP64 || precision < 0 || precision > 7)
             arg_error(TVAL3_ERR_UNSUPPORTED, "geometry operators store FP32/BF16/FP16 values");
         if (mode == 1 && precision != TVAL3_PREC_FP32)
             arg_error(TVAL3_ERR_UNSUPPORTED, "on-the-fly traversal stores nothing; use FP32");
         auto* h = new tval3_op_s();
         try {
             h->precision = precision;
-            if (precision == TVAL3_PREC_FP32_F64VEC || precision == TVAL3_PREC_FP32_DF64) {
+            if (is_mixed(precision)) {
+                h->dbl = 1;
+                h->q = make_geometry_op<df64>(G, mode, precision, 0);
+            } else if (precision == TVAL3_PREC_FP32_F64VEC || precision == TVAL3_PREC_FP32_DF64) {
                 h->dbl = 1;
                 h->d = make_geometry_op<double>(G, mode, precision, 0);
                 if (precision == TVAL3_PREC_FP32_DF64) h->q = make_df64_view(h->d);
@@ -614,19 +727,27 @@ tval3_status tval3_op_destroy(tval3_op op) {
 tval3_status tval3_op_shape(tval3_op op, int* rows, int* cols, int64_t* nnz) {
     return guard([&] {
         if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
-        long m = op->dbl ? op->d->m : op->f->m, n = op->dbl ? op->d->n : op->f->n;
-        long z = op->dbl ? op->d->nnz : op->f->nnz;
-        if (rows) *rows = (int)m;
-        if (cols) *cols = (int)n;
-        if (nnz) *nnz = z;
+        if (rows) *rows = (int)op->rows();
+        if (cols) *cols = (int)op->cols();
+        if (nnz) *nnz = op->nnz();
     });
 }
 
 tval3_status tval3_op_export_csr(tval3_op op, int* ptr, int* ind, float* val, int* tptr, int* tind, float* tval) {
     return guard([&] {
         if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
-        if (op->dbl) op->d->export_csr(ptr, ind, val, tptr, tind, tval);
-        else op->f->export_csr(ptr, ind, val, tptr, tind, tval);
+        op->with_store([&](auto& A) { A.export_csr(ptr, ind, val, tptr, tind, tval); });
+    });
+}
+
+tval3_status tval3_op_export_csr_scaled(tval3_op op, int* ptr, int* ind, float* val, float* row_scale, int* tptr,
+                                        int* tind, float* tval) {
+    return guard([&] {
+        if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
+        op->with_store([&](auto& A) {
+            A.export_csr(ptr, ind, nullptr, tptr, tind, nullptr);
+            A.export_scaled(val, row_scale, tval);
+        });
     });
 }
 
@@ -736,7 +857,7 @@ tval3_status tval3_solver_create(tval3_solver* s, tval3_op A, int dim_y, int dim
         if (!s || !A) arg_error(TVAL3_ERR_ARG, "Argument error: NULL solver or operator!");
         check_opts(opts);
         const long n = (long)dim_y * dim_x * dim_z;
-        long cols = A->dbl ? A->d->n : A->f->n;
+        const long cols = A->cols();
         if (dim_y <= 0 || dim_x <= 0 || dim_z <= 0 || n != cols)
             arg_error(TVAL3_ERR_SHAPE, "Argument error: the length of U must be equal to A.dim_x!");
         auto* h = new tval3_solver_s();
@@ -760,7 +881,7 @@ tval3_status tval3_solver_create_layers(tval3_solver* s, tval3_op A, int dim_y, 
         if (layers < 1) arg_error(TVAL3_ERR_ARG, "Argument error: layers must be positive!");
         check_opts(opts);
         const long n = (long)dim_y * dim_x * dim_z;
-        long cols = A->q ? A->q->n : (A->dbl ? A->d->n : A->f->n);
+        const long cols = A->cols();
         if (dim_y <= 0 || dim_x <= 0 || dim_z <= 0 || n != cols)
             arg_error(TVAL3_ERR_SHAPE, "Argument error: the length of U must be equal to A.dim_x!");
         auto* h = new tval3_solver_s();
@@ -896,7 +1017,7 @@ tval3_status tval3_batch_create(tval3_batch* batch, const tval3_op* ops, const i
                 arg_error(TVAL3_ERR_ARG, "Argument error: all operators of a batch must have the same vector type!");
             const int* d = dims + 3 * (long)i;
             const long n = (long)d[0] * d[1] * d[2];
-            const long cols = ops[i]->q ? ops[i]->q->n : (ops[i]->dbl ? ops[i]->d->n : ops[i]->f->n);
+            const long cols = ops[i]->cols();
             if (d[0] <= 0 || d[1] <= 0 || d[2] <= 0 || n != cols)
                 arg_error(TVAL3_ERR_SHAPE, "Argument error: the length of U must be equal to A.dim_x!");
         }

@@ -5,6 +5,7 @@
 // (3d/mat_vec_mul_sparse.h:1599-1781).
 #include <cub/cub.cuh>
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 #include "dbuf.h"
 #include "ops.h"
@@ -340,6 +341,7 @@ struct CsrOp : LinOp<T> {
     }
 
     void export_csr(int* hptr, int* hind, float* hval, int* htptr, int* htind, float* htval) const override;
+    void export_scaled(float* hval, float* hrs, float* htval) const override;
     bool multi_rhs() const override { return true; }
 };
 
@@ -363,8 +365,8 @@ void export_vals<double, double>(const CsrOp<double, double>& op, float* hval, f
         TV3_CUDA(cudaMemcpy(htval, tmp.p, op.nnz * sizeof(float), cudaMemcpyDeviceToHost));
     }
 }
-template <class V>
-static void export_q(const CsrOp<float, V>& op, float* hval, float* htval) {
+template <class T, class V>
+static void export_q(const CsrOp<T, V>& op, float* hval, float* htval) {
     DBuf<float> tmp(std::max<long>(op.nnz, 1));
     if (hval) {
         k_dequant_rows<V><<<ew(op.m * 32), 256>>>(op.m, op.ptr.p, op.val.p, op.rs.p, tmp.p);
@@ -382,6 +384,45 @@ void export_vals<float, __nv_bfloat16>(const CsrOp<float, __nv_bfloat16>& op, fl
 template <>
 void export_vals<float, __half>(const CsrOp<float, __half>& op, float* hval, float* htval) {
     export_q(op, hval, htval);
+}
+template <>
+void export_vals<df64, __nv_bfloat16>(const CsrOp<df64, __nv_bfloat16>& op, float* hval, float* htval) {
+    export_q(op, hval, htval);
+}
+template <>
+void export_vals<df64, __half>(const CsrOp<df64, __half>& op, float* hval, float* htval) {
+    export_q(op, hval, htval);
+}
+
+// 16-bit values widened to FP32 (exact), in the layout of the stored arrays
+template <class V>
+__global__ void k_widen(long n, const V* __restrict__ q, float* __restrict__ out) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x)
+        out[k] = from_v<V>(q[k]);
+}
+
+template <class V>
+static constexpr bool is_16bit() {
+    return std::is_same<V, __nv_bfloat16>::value || std::is_same<V, __half>::value;
+}
+
+template <class T, class V>
+void CsrOp<T, V>::export_scaled(float* hval, float* hrs, float* htval) const {
+    if constexpr (is_16bit<V>()) {
+        DBuf<float> tmp(std::max<long>(this->nnz, 1));
+        if (hval && this->nnz) {
+            k_widen<V><<<ew(this->nnz), 256>>>(this->nnz, val.p, tmp.p);
+            TV3_CUDA(cudaMemcpy(hval, tmp.p, this->nnz * sizeof(float), cudaMemcpyDeviceToHost));
+        }
+        if (htval && this->nnz) {
+            k_widen<V><<<ew(this->nnz), 256>>>(this->nnz, tval.p, tmp.p);
+            TV3_CUDA(cudaMemcpy(htval, tmp.p, this->nnz * sizeof(float), cudaMemcpyDeviceToHost));
+        }
+        if (hrs && this->m) TV3_CUDA(cudaMemcpy(hrs, rs.p, this->m * sizeof(float), cudaMemcpyDeviceToHost));
+    } else {
+        export_vals<T, V>(*this, hval, htval);
+        if (hrs) std::fill(hrs, hrs + this->m, 1.0f);
+    }
 }
 
 template <class T, class V>
@@ -579,12 +620,15 @@ LinOp<double>* make_csr_op_device<double>(long rows, long cols, long nnz, const 
     return op;
 }
 
-template <class V>
-static LinOp<float>* make_q(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind, const float* d_val,
-                            const int* d_tptr, const int* d_tind, const float* d_tval, cudaStream_t s) {
-    auto* op = new CsrOp<float, V>();
+// 16-bit values with a per-ray FP32 scale (the row's largest magnitude) from
+// FP32 device arrays; T is the vector type of the products (float, or df64
+// for the mixed-precision modes)
+template <class T, class V>
+static LinOp<T>* make_q(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind, const float* d_val,
+                        const int* d_tptr, const int* d_tind, const float* d_tval, cudaStream_t s) {
+    auto* op = new CsrOp<T, V>();
     try {
-        copy_structure<float>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
+        copy_structure<T>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
         DBuf<float> tv(std::max<long>(nnz, 1));
         if (d_tptr) {
             TV3_CUDA(cudaMemcpy(op->tptr.p, d_tptr, (cols + 1) * sizeof(int), cudaMemcpyDeviceToDevice));
@@ -615,8 +659,9 @@ template <>
 LinOp<float>* make_csr_op_device<float>(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind,
                                         const float* d_val, const int* d_tptr, const int* d_tind, const float* d_tval,
                                         int precision, cudaStream_t s) {
-    if (precision == 2) return make_q<__nv_bfloat16>(rows, cols, nnz, d_ptr, d_ind, d_val, d_tptr, d_tind, d_tval, s);
-    if (precision == 3) return make_q<__half>(rows, cols, nnz, d_ptr, d_ind, d_val, d_tptr, d_tind, d_tval, s);
+    if (precision == 2)
+        return make_q<float, __nv_bfloat16>(rows, cols, nnz, d_ptr, d_ind, d_val, d_tptr, d_tind, d_tval, s);
+    if (precision == 3) return make_q<float, __half>(rows, cols, nnz, d_ptr, d_ind, d_val, d_tptr, d_tind, d_tval, s);
     auto* op = new CsrOp<float, float>();
     try {
         copy_structure<float>(op, op->ptr, op->ind, op->tptr, op->tind, rows, cols, nnz, d_ptr, d_ind);
@@ -639,6 +684,15 @@ LinOp<float>* make_csr_op_device<float>(long rows, long cols, long nnz, const in
         throw;
     }
     return op;
+}
+
+LinOp<df64>* make_csr_op_df64q(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind,
+                               const float* d_val, const int* d_tptr, const int* d_tind, const float* d_tval,
+                               int precision, cudaStream_t s) {
+    if (precision == 6)
+        return make_q<df64, __nv_bfloat16>(rows, cols, nnz, d_ptr, d_ind, d_val, d_tptr, d_tind, d_tval, s);
+    if (precision == 7) return make_q<df64, __half>(rows, cols, nnz, d_ptr, d_ind, d_val, d_tptr, d_tind, d_tval, s);
+    throw Error{7, "mixed-precision operators store BF16 or FP16 values"};
 }
 
 // column-major (rows x k) <-> interleaved (row * k + column)

@@ -102,6 +102,10 @@ struct LinOp {
     virtual void export_csr(int*, int*, float*, int*, int*, float*) const {
         throw Error{7, "operator has no stored CSR"};
     }
+    // the stored values and per-row scales as the products apply them: entry
+    // (r, c) = val * row_scale[r] exactly (16-bit storage: the 16-bit values
+    // widened to FP32; other storage: the FP32 values and scales of one)
+    virtual void export_scaled(float*, float*, float*) const { throw Error{7, "operator has no stored CSR"}; }
 };
 
 // A*x from one operator, A^T*y from another: the reference's sparse_geom_mm
@@ -146,6 +150,14 @@ LinOp<double>* make_csr_op_f64vec(long rows, long cols, long nnz, const int* d_p
 // Double-float products over the arrays of an FP32-value / FP64-vector CSR
 // operator (precision TVAL3_PREC_FP32_DF64); the view does not own the arrays.
 LinOp<df64>* make_df64_view(const LinOp<double>* base);
+
+// Mixed precision (TVAL3_PREC_BF16_DF64 = 6, TVAL3_PREC_FP16_DF64 = 7): the
+// FP32 device CSR quantised to 16-bit values with a per-ray FP32 scale,
+// products and vectors in double-float.  The transpose is built when d_tptr
+// is null.
+LinOp<df64>* make_csr_op_df64q(long rows, long cols, long nnz, const int* d_ptr, const int* d_ind,
+                               const float* d_val, const int* d_tptr, const int* d_tind, const float* d_tval,
+                               int precision, cudaStream_t s);
 void convert_to_df64(const double* in, void* out, long n, cudaStream_t s);
 void convert_from_df64(const void* in, double* out, long n, cudaStream_t s);
 

@@ -500,4 +500,14 @@ LinOp<double>* make_geometry_op<double>(const void* gh, int mode, int precision,
                               precision == 4);
 }
 
+template <>
+LinOp<df64>* make_geometry_op<df64>(const void* gh, int mode, int precision, cudaStream_t s) {
+    // precision 6 / 7: the ray matrix in BF16 / FP16 with per-ray FP32 scales,
+    // double-float products
+    if (mode != 0 || (precision != 6 && precision != 7))
+        throw Error{7, "mixed-precision geometry operators are stored (mode 0) with BF16 or FP16 values"};
+    RayCsr c = build_ray_csr(static_cast<const tval3_geometry_host*>(gh), s);
+    return make_csr_op_df64q(c.m, c.n, c.nnz, c.ptr.p, c.ind.p, c.val.p, nullptr, nullptr, nullptr, precision, s);
+}
+
 }  // namespace tv3

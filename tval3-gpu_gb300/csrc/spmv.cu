@@ -305,5 +305,7 @@ template void launch_spmv<double, float>(const SpmvArgs<double, float>&, int, in
 template void launch_spmv<df64, float>(const SpmvArgs<df64, float>&, int, int, int, cudaStream_t);
 template void launch_spmv<float, __nv_bfloat16>(const SpmvArgs<float, __nv_bfloat16>&, int, int, int, cudaStream_t);
 template void launch_spmv<float, __half>(const SpmvArgs<float, __half>&, int, int, int, cudaStream_t);
+template void launch_spmv<df64, __nv_bfloat16>(const SpmvArgs<df64, __nv_bfloat16>&, int, int, int, cudaStream_t);
+template void launch_spmv<df64, __half>(const SpmvArgs<df64, __half>&, int, int, int, cudaStream_t);
 
 }  // namespace tv3

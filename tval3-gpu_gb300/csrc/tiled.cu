@@ -1064,6 +1064,8 @@ template struct TiledN<double, float>;
 template struct TiledN<df64, float>;
 template struct TiledN<float, __nv_bfloat16>;
 template struct TiledN<float, __half>;
+template struct TiledN<df64, __nv_bfloat16>;
+template struct TiledN<df64, __half>;
 
 template struct TiledT<float, float>;
 template struct TiledT<double, double>;
@@ -1071,5 +1073,7 @@ template struct TiledT<double, float>;
 template struct TiledT<df64, float>;
 template struct TiledT<float, __nv_bfloat16>;
 template struct TiledT<float, __half>;
+template struct TiledT<df64, __nv_bfloat16>;
+template struct TiledT<df64, __half>;
 
 }  // namespace tv3

@@ -210,7 +210,8 @@ def tval3_gpu_3d(shape, A, b, opts=None, Ut=None, *, dtype=np.float32, pagelocke
     if isinstance(A, tuple):
         geo, mat = A
         gs, ms = geo.struct(), mat.struct()
-        st = lib.tval3_gpu_3d_geometry_sparse_f32(_ptr(U), dim_y, dim_x, dim_z, C.byref(gs), C.byref(ms), *common)
+        fn = lib.tval3_gpu_3d_geometry_sparse_f64 if dt == np.float64 else lib.tval3_gpu_3d_geometry_sparse_f32
+        st = fn(_ptr(U), dim_y, dim_x, dim_z, C.byref(gs), C.byref(ms), *common)
     elif isinstance(A, SparseMatrix):
         s = A.struct()
         fn = lib.tval3_gpu_3d_sparse_f64 if dt == np.float64 else lib.tval3_gpu_3d_sparse_f32
@@ -221,7 +222,8 @@ def tval3_gpu_3d(shape, A, b, opts=None, Ut=None, *, dtype=np.float32, pagelocke
         st = fn(_ptr(U), dim_y, dim_x, dim_z, C.byref(s), *common)
     elif isinstance(A, Geometry):
         s = A.struct()
-        st = lib.tval3_gpu_3d_geometry_f32(_ptr(U), dim_y, dim_x, dim_z, C.byref(s), *common)
+        fn = lib.tval3_gpu_3d_geometry_f64 if dt == np.float64 else lib.tval3_gpu_3d_geometry_f32
+        st = fn(_ptr(U), dim_y, dim_x, dim_z, C.byref(s), *common)
     else:
         raise TypeError(f"unsupported matrix type {type(A).__name__}")
     check(st)
@@ -319,6 +321,18 @@ class Operator:
         check(load().tval3_op_export_csr(self._h, _ptr(ptr), _ptr(ind), _ptr(val), _ptr(tptr), _ptr(tind),
                                          _ptr(tval)))
         return ptr, ind, val, tptr, tind, tval
+
+    def export_csr_scaled(self):
+        """(ptr, ind, val, row_scale, tptr, tind, tval): entry (r, c) is exactly
+        val * row_scale[r] in FP64 (16-bit storage: val holds the 16-bit values,
+        row_scale the per-ray scales; otherwise row_scale is all ones)."""
+        m, n, z = self.rows, self.cols, self.nnz
+        ptr, tptr = np.empty(m + 1, np.int32), np.empty(n + 1, np.int32)
+        ind, tind = np.empty(z, np.int32), np.empty(z, np.int32)
+        val, tval, rs = np.empty(z, np.float32), np.empty(z, np.float32), np.empty(m, np.float32)
+        check(load().tval3_op_export_csr_scaled(self._h, _ptr(ptr), _ptr(ind), _ptr(val), _ptr(rs), _ptr(tptr),
+                                                _ptr(tind), _ptr(tval)))
+        return ptr, ind, val, rs, tptr, tind, tval
 
     def close(self):
         if self._h:

@@ -15,6 +15,7 @@ TVAL3_OK = 0
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_SHAPE", 3: "ERR_CUDA", 4: "ERR_NOMEM", 5: "ERR_TIMEOUT",
           6: "ERR_NONFINITE", 7: "ERR_UNSUPPORTED"}
 PREC_FP32, PREC_FP64, PREC_BF16, PREC_FP16, PREC_FP32_F64VEC, PREC_FP32_DF64 = 0, 1, 2, 3, 4, 5
+PREC_BF16_DF64, PREC_FP16_DF64 = 6, 7
 TV_ANISO, TV_ISO = 0, 1
 SPARSE_CSR, SPARSE_CSC, SPARSE_BOTH = 1, 2, 3
 TRAV_BRESENHAM, TRAV_SIDDON = 0, 1
@@ -87,6 +88,8 @@ _SIG = {
     "tval3_gpu_3d_dense_f64": (_I, [_P, _I, _I, _I, _P, _P, _I, _P, _P, _I, _I, _I, _I, _P, _P]),
     "tval3_gpu_3d_geometry_f32": (_I, [_P, _I, _I, _I, _P, _P, _I, _P, _P, _I, _I, _I, _I, _P, _P]),
     "tval3_gpu_3d_geometry_sparse_f32": (_I, [_P, _I, _I, _I, _P, _P, _P, _I, _P, _P, _I, _I, _I, _I, _P, _P]),
+    "tval3_gpu_3d_geometry_f64": (_I, [_P, _I, _I, _I, _P, _P, _I, _P, _P, _I, _I, _I, _I, _P, _P]),
+    "tval3_gpu_3d_geometry_sparse_f64": (_I, [_P, _I, _I, _I, _P, _P, _P, _I, _P, _P, _I, _I, _I, _I, _P, _P]),
     "tval3_gpu_sparse": (_I, [_P, _I, _I, _P, _P, _I, _P, _P, _I, _I, _P]),
     "tval3_gpu_dense": (_I, [_P, _I, _I, _P, _P, _I, _P, _P, _I, _I, _P]),
     "tval3_op_create_sparse": (_I, [_P, _P, _I]),
@@ -96,6 +99,7 @@ _SIG = {
     "tval3_op_destroy": (_I, [_P]),
     "tval3_op_shape": (_I, [_P, _P, _P, _P]),
     "tval3_op_export_csr": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "tval3_op_export_csr_scaled": (_I, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "tval3_mat_vec_mul": (_I, [_P, _I, _P, _P, _P]),
     "tval3_mat_mat_mul": (_I, [_P, _I, _I, _P, _P, _P]),
     "tval3_mat_mat_mul_interleaved": (_I, [_P, _I, _I, _P, _P, _P]),
