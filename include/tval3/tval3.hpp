@@ -3,7 +3,7 @@
 //
 //   tval3_gpu_3d(U, A, b, opts, Ut, pagelocked, mainGPU, numGPUs, gpuArray)
 //       3d/tval3_gpu_3d.cpp:23-69 (sparse, dense, geometry, geometry+sparse;
-//       float and double)
+//       float and double: all eight overloads)
 //   tval3_gpu(U, A, b, opts, Ut, pagelocked)        2d/tval3_gpu.h:9-19
 //   mat_host / sparse_mat_host / geometry_host      2d/container_host.h:25-127,
 //                                                   3d/container_device.h:103-172
@@ -265,7 +265,33 @@ inline const tval3_info<float> tval3_gpu_3d(mat_host<float>& U, const geometry_h
     return tval3::to_info<float>(i);
 }
 
-// 2D (2d/tval3_gpu.h:9-19): U is rows x cols
+inline const tval3_info<double> tval3_gpu_3d(mat_host<double>& U, const geometry_host& A, const mat_host<double>& b,
+                                             const tval3_options<double>& opts, const mat_host<double>& Ut,
+                                             bool pagelocked = true, int mainGPU = -1, int numGPUs = 0,
+                                             int* gpuArray = nullptr) {
+    tval3c::tval3_options o = opts.to_c();
+    tval3c::tval3_info i;
+    tval3::check(tval3c::tval3_gpu_3d_geometry_f64(U.data(), U.dim_y, U.dim_x, U.dim_z, &A, b.data(), b.len, &o,
+                                                   Ut.data(), Ut.len, pagelocked, mainGPU, numGPUs, gpuArray, &i));
+    return tval3::to_info<double>(i);
+}
+
+inline const tval3_info<double> tval3_gpu_3d(mat_host<double>& U, const geometry_host& A_geo,
+                                             sparse_mat_host<double>& A_mat, const mat_host<double>& b,
+                                             const tval3_options<double>& opts, const mat_host<double>& Ut,
+                                             bool pagelocked = true, int mainGPU = -1, int numGPUs = 0,
+                                             int* gpuArray = nullptr) {
+    tval3c::tval3_sparse_host a = A_mat.to_c();
+    tval3c::tval3_options o = opts.to_c();
+    tval3c::tval3_info i;
+    tval3::check(tval3c::tval3_gpu_3d_geometry_sparse_f64(U.data(), U.dim_y, U.dim_x, U.dim_z, &A_geo, &a, b.data(),
+                                                          b.len, &o, Ut.data(), Ut.len, pagelocked, mainGPU, numGPUs,
+                                                          gpuArray, &i));
+    return tval3::to_info<double>(i);
+}
+
+// 2D (2d/tval3_gpu.h:9-19): U is rows x cols.  The 2D reference's untemplated
+// containers are in tval3_2d.hpp; these overloads take the 3D templates.
 inline const tval3_info<float> tval3_gpu(mat_host<float>& U, const sparse_mat_host<float>& A,
                                          const mat_host<float>& b, const tval3_options<float>& opts,
                                          const mat_host<float>* Ut = nullptr, bool pagelocked = true) {

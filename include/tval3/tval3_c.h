@@ -299,7 +299,11 @@ TVAL3_API tval3_status tval3_op_export_csr_scaled(tval3_op op, int* ptr, int* in
  * {float hi, lo} (FP32_DF64, BF16_DF64, FP16_DF64; see tval3_df64_from_f64).
  * Batched multi-RHS
  * form: nrhs columns, leading dimension = vector length (the reference's
- * `layers`, 2d/mat_vec_mul.h:65-71, :96-99). */
+ * `layers`, 2d/mat_vec_mul.h:65-71, :96-99).  Products on the tensor cores
+ * (BF16 dense operators with several right-hand sides) have bounded device
+ * waits: these calls then wait for the stream and return TVAL3_ERR_TIMEOUT
+ * if a wait ran out (the output is incomplete); all other products return
+ * without waiting. */
 TVAL3_API tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, void* stream);
 TVAL3_API tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, void* Y, void* stream);
 /* Kernel of the single-vector products of a stored operator whose volume is
@@ -319,7 +323,9 @@ TVAL3_API tval3_status tval3_op_get_variant(tval3_op op, int trans, int* variant
  * row * nrhs + j, the layout the multi-layer solver keeps.  One SpMM (CSR),
  * tensor-core GEMM (BF16 dense) or SIMT GEMM (FP32/FP64 dense) launch
  * sequence; the first call for a given nrhs sets up the operator's scratch
- * (make it before any stream capture), later calls allocate nothing. */
+ * (make it before any stream capture), later calls allocate nothing.  On the
+ * tensor-core path the call waits for the stream and reports a timed-out
+ * device wait as TVAL3_ERR_TIMEOUT (see tval3_mat_vec_mul). */
 TVAL3_API tval3_status tval3_mat_mat_mul_interleaved(tval3_op op, int trans, int nrhs, const void* X, void* Y,
                                                      void* stream);
 /* Device conversions between double and the double-float pairs used by
@@ -435,9 +441,11 @@ TVAL3_API tval3_status tval3_shrink_adjoint_f64(int64_t n, const double* d_v, do
  * row-major, one ray per row), y (rows) and x (cols) are the caller's device
  * arrays; the slab partial sums live in one static device array of
  * 1,048,576 floats, so cols must not exceed that (TVAL3_ERR_SHAPE
- * otherwise).  The first call on a device looks up that array's address:
- * make it before any stream capture.  Calls that overlap in time on one
- * device share the array and race; order them.
+ * otherwise).  A call on a stream that is not capturing looks up that
+ * array's address on the current device; calls under capture use the
+ * address remembered from an earlier call, so make the first call on a
+ * device before any stream capture.  Calls that overlap in time on one
+ * device share the array and race; order them.  rows = 0 writes x = 0.
  * ---------------------------------------------------------------------- */
 #define TVAL3_NOALLOC_SCRATCH_FLOATS 1048576
 TVAL3_API tval3_status tval3_dense_rmatvec_f32_noalloc(int rows, int cols, const float* d_A, const float* d_y,

@@ -751,6 +751,17 @@ tval3_status tval3_op_export_csr_scaled(tval3_op op, int* ptr, int* ind, float* 
     });
 }
 
+// a bounded device wait of a standalone product that ran out (the product's
+// output is incomplete)
+void check_product(tval3_op op, cudaStream_t s) {
+    int e = 0;
+    if (op->q) e = op->q->take_error(s);
+    else if (op->d) e = op->d->take_error(s);
+    else e = op->f->take_error(s);
+    if (e) arg_error(TVAL3_ERR_TIMEOUT, "a bounded device wait of the product ran out (error bits " +
+                                            std::to_string(e) + "); the output is incomplete");
+}
+
 tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, void* stream) {
     return guard([&] {
         if (!op || !x || !y) arg_error(TVAL3_ERR_ARG, "Argument error: NULL operator or vector!");
@@ -758,6 +769,7 @@ tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, v
         if (op->q) op->q->apply(trans ? 1 : 0, plain_io<df64>((const df64*)x, (df64*)y), SPMV_PLAIN, s);
         else if (op->dbl) op->d->apply(trans ? 1 : 0, plain_io<double>((const double*)x, (double*)y), SPMV_PLAIN, s);
         else op->f->apply(trans ? 1 : 0, plain_io<float>((const float*)x, (float*)y), SPMV_PLAIN, s);
+        check_product(op, s);
     });
 }
 
@@ -768,6 +780,7 @@ tval3_status tval3_mat_mat_mul(tval3_op op, int trans, int nrhs, const void* X, 
         if (op->q) op->q->apply_multi(trans ? 1 : 0, nrhs, (const df64*)X, (df64*)Y, s);
         else if (op->dbl) op->d->apply_multi(trans ? 1 : 0, nrhs, (const double*)X, (double*)Y, s);
         else op->f->apply_multi(trans ? 1 : 0, nrhs, (const float*)X, (float*)Y, s);
+        check_product(op, s);
     });
 }
 
@@ -804,6 +817,7 @@ tval3_status tval3_mat_mat_mul_interleaved(tval3_op op, int trans, int nrhs, con
         if (op->q) run(op->q, (const df64*)X, (df64*)Y);
         else if (op->dbl) run(op->d, (const double*)X, (double*)Y);
         else run(op->f, (const float*)X, (float*)Y);
+        check_product(op, s);
     });
 }
 

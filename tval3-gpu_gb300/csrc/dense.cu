@@ -19,6 +19,7 @@ bool umma_supported(long m, long n, int L);
 UmmaPlan* umma_plan_create(long m, long n, int L, const __nv_bfloat16* Aq);
 void umma_plan_destroy(UmmaPlan* p);
 void umma_apply(const UmmaPlan* p, int trans, const MatIO<float>& io, int epi, const float* rs, cudaStream_t s);
+int umma_take_error(const UmmaPlan* p, cudaStream_t s);
 
 template <class T, class V, int EPI>
 __global__ void __launch_bounds__(256) k_dense_N(long m, long n, const V* __restrict__ A, const float* __restrict__ rs,
@@ -228,6 +229,7 @@ struct DenseOp : LinOp<T> {
         if constexpr (std::is_same<T, float>::value && std::is_same<V, __nv_bfloat16>::value) {
             if (umma && umma_L == L) {
                 umma_apply(umma, trans, io, epi, rs.p, s);
+                if (!io.ctl) umma_unchecked = true;
                 return;
             }
         }
@@ -285,6 +287,18 @@ struct DenseOp : LinOp<T> {
     }
     mutable DBuf<T> part_l;  // slab partials of the multi-RHS A^T*Y
     bool multi_rhs() const override { return true; }
+    // standalone tensor-core products record a timed-out wait in the plan's
+    // own error word; read (and clear) it once the products have completed
+    int take_error(cudaStream_t s) const override {
+        if constexpr (std::is_same<T, float>::value && std::is_same<V, __nv_bfloat16>::value) {
+            if (umma && umma_unchecked) {
+                umma_unchecked = false;
+                return umma_take_error(umma, s);
+            }
+        }
+        return 0;
+    }
+    mutable bool umma_unchecked = false;  // a standalone tensor-core product whose error word is unread
     mutable UmmaPlan* umma = nullptr;  // tensor-core plan of the multi-RHS products (BF16 only)
     mutable int umma_L = 0;
     int use_umma = 1;

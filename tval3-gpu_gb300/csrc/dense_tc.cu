@@ -111,7 +111,8 @@ struct GemmArgs {
     int stages;
     int kb_per_split;
     float* part;     // [split][M][L]
-    Ctl* ctl;        // error word and launch counter (may be null)
+    Ctl* ctl;        // launch counter (may be null)
+    int* err;        // error word: the solve's Ctl::err, or the plan's own for standalone products
 };
 
 __global__ void __launch_bounds__(128, 3) k_umma_gemm(const __grid_constant__ CUtensorMap tmA,
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(128, 3) k_umma_gemm(const __grid_constant__ CU
         if (ok) ok = mbar_wait(&done, 0u);
         if (!ok) {
             failed = 1;
-            if (g.ctl) atomicOr(&g.ctl->err, (int)ERR_UMMA_TIMEOUT);
+            if (g.err) atomicOr(g.err, (int)ERR_UMMA_TIMEOUT);
             // let this CTA's copies and MMAs finish before its shared memory goes away
             for (int j = consumed; j < issued; ++j) mbar_wait(&full[j % S], (unsigned)((j / S) & 1));
             mbar_wait(&done, 0u);
@@ -383,6 +384,7 @@ struct UmmaPlan {
     DBuf<__nv_bfloat16> bN_h, bN_l;  // B of A*X: Npad x np
     DBuf<__nv_bfloat16> bT_h, bT_l;  // B of A^T*Y: Npad x mp
     DBuf<float> part;
+    DBuf<int> err;  // error word of products made outside a solve (zero: no error)
     CUtensorMap mapA, mapAt, mapBNh, mapBNl, mapBTh, mapBTl;
     int splitsN = 1, kbN = 1, stagesN = 1, splitsT = 1, kbT = 1, stagesT = 1;
     size_t smemN = 0, smemT = 0;
@@ -436,6 +438,8 @@ UmmaPlan* umma_plan_create(long m, long n, int L, const __nv_bfloat16* Aq) {
         plan_split(m, n, p->splitsN, p->kbN);
         plan_split(n, m, p->splitsT, p->kbT);
         p->part.alloc(std::max((size_t)p->splitsN * m * L, (size_t)p->splitsT * n * L));
+        p->err.alloc(1);
+        TV3_CUDA(cudaMemset(p->err.p, 0, sizeof(int)));
         p->mapA = make_map(p->tN.p, UK, blocked_rows(m, n), UK, UM);
         p->mapAt = make_map(p->tT.p, UK, blocked_rows(n, m), UK, UM);
         p->mapBNh = make_map(p->bN_h.p, n, p->Npad, p->np, p->Npad);
@@ -458,6 +462,16 @@ UmmaPlan* umma_plan_create(long m, long n, int L, const __nv_bfloat16* Aq) {
 
 void umma_plan_destroy(UmmaPlan* p) { delete p; }
 
+// the error word of the plan's standalone products (after they completed on
+// s), cleared for the next product
+int umma_take_error(const UmmaPlan* p, cudaStream_t s) {
+    int e = 0;
+    TV3_CUDA(cudaMemcpyAsync(&e, p->err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TV3_CUDA(cudaStreamSynchronize(s));
+    if (e) TV3_CUDA(cudaMemsetAsync(p->err.p, 0, sizeof(int), s));
+    return e;
+}
+
 void umma_apply(const UmmaPlan* p, int trans, const MatIO<float>& io, int epi, const float* rs, cudaStream_t s) {
     const long M = trans ? p->n : p->m, K = trans ? p->m : p->n, Kp = trans ? p->mp : p->np;
     __nv_bfloat16* bh = trans ? p->bT_h.p : p->bN_h.p;
@@ -472,6 +486,7 @@ void umma_apply(const UmmaPlan* p, int trans, const MatIO<float>& io, int epi, c
     g.kb_per_split = trans ? p->kbT : p->kbN;
     g.part = p->part.p;
     g.ctl = io.ctl;
+    g.err = io.ctl ? &io.ctl->err : p->err.p;
     const int splits = trans ? p->splitsT : p->splitsN;
     dim3 grid((unsigned)splits, (unsigned)((M + UM - 1) / UM));
     launch_k(k_umma_gemm, grid, dim3(128), trans ? p->smemT : p->smemN, s, trans ? p->mapAt : p->mapA,

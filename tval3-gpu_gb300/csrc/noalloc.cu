@@ -16,9 +16,14 @@
 //
 // Limits and rules:
 //  - cols <= TVAL3_NOALLOC_SCRATCH_FLOATS (1,048,576); larger is rejected.
-//  - the first call on a device looks up the scratch address for that device
-//    (cudaGetSymbolAddress with the device current); make it before any
-//    stream capture, e.g. once during start-up.
+//  - a call on a stream that is not being captured looks up the scratch
+//    address of the current device (cudaGetSymbolAddress with that device
+//    current) and remembers it; a call on a stream under capture uses the
+//    remembered address, so the first call on a device must come before any
+//    capture, e.g. once during start-up.  Looking the address up again on
+//    every uncaptured call keeps it right after a cudaDeviceReset (which
+//    reloads the module); a graph captured before such a reset must not be
+//    replayed after it.
 //  - nothing in the scratch has to start at zero: the partial pass writes
 //    every (slab, column) entry that the sum pass reads in the same call.
 //  - the scratch is shared by all calls on a device: calls that overlap in
@@ -42,19 +47,25 @@ namespace {
 float* g_scratch_ptr[NOALLOC_MAX_DEVICES] = {};
 std::mutex g_scratch_mu;
 
-// Address of the static scratch on the current device (looked up once).
-float* scratch_for_current_device() {
+// Address of the static scratch on the current device: looked up when `s`
+// is not capturing, remembered for calls made under capture.
+float* scratch_for_current_device(cudaStream_t s) {
     int dev = 0;
     TV3_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) throw Error{TVAL3_ERR_UNSUPPORTED, "device ordinal out of range"};
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    TV3_CUDA(cudaStreamIsCapturing(s, &cs));
     std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (cs == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             throw Error{TVAL3_ERR_CUDA, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
                                             cudaGetErrorString(e)};
         g_scratch_ptr[dev] = (float*)p;
+    } else if (!g_scratch_ptr[dev]) {
+        throw Error{TVAL3_ERR_ARG, "Argument error: the first no-allocation call on a device must come before any "
+                                   "stream capture!"};
     }
     return g_scratch_ptr[dev];
 }
@@ -88,7 +99,7 @@ void dense_rmatvec_noalloc_f32(long rows, long cols, const float* A, const float
                                          std::to_string(NOALLOC_SCRATCH_FLOATS) + " floats!"};
     if (cols == 0) return;
     if ((!A && rows > 0) || (!y && rows > 0) || !x) throw Error{TVAL3_ERR_ARG, "Argument error: NULL device array!"};
-    float* part = scratch_for_current_device();
+    float* part = scratch_for_current_device(s);
     if (rows == 0) {
         TV3_CUDA(cudaMemsetAsync(x, 0, (size_t)cols * sizeof(float), s));
         return;

@@ -106,6 +106,14 @@ struct LinOp {
     // (r, c) = val * row_scale[r] exactly (16-bit storage: the 16-bit values
     // widened to FP32; other storage: the FP32 values and scales of one)
     virtual void export_scaled(float*, float*, float*) const { throw Error{7, "operator has no stored CSR"}; }
+    // operators whose kernels have bounded device waits (the tensor-core
+    // products) record a timeout of a product made outside a solve in an
+    // error word of their own: this waits for the stream, returns the word
+    // (0 = none) and clears it.  Operators without such waits return 0 at once.
+    virtual int take_error(cudaStream_t s) const {
+        (void)s;
+        return 0;
+    }
 };
 
 // A*x from one operator, A^T*y from another: the reference's sparse_geom_mm
@@ -133,6 +141,7 @@ struct SplitOp : LinOp<T> {
         top->ready();
     }
     bool set_variant(int trans, int v) const override { return (trans ? top : nop)->set_variant(trans, v); }
+    int take_error(cudaStream_t s) const override { return nop->take_error(s) | top->take_error(s); }
     int variant(int trans) const override { return (trans ? top : nop)->variant(trans); }
 };
 

@@ -1038,15 +1038,18 @@ __global__ void k_Dt_plain(Geo g, long n, const T* __restrict__ V, T* __restrict
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-static int g_sms = 0;
+// SM count of the current device, looked up once per device
 int num_sms() {
-    if (!g_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = 1;
+    constexpr int MAXDEV = 64;
+    static int sms[MAXDEV] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAXDEV) dev = 0;
+    if (!sms[dev]) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+        sms[dev] = v;
     }
-    return g_sms;
+    return sms[dev];
 }
 
 // Blocks of a grid-stride reducing kernel (256 threads): `want` (about one per
