@@ -828,50 +828,132 @@ __global__ void k_n_fill(long nseg, const int* __restrict__ order, const unsigne
     }
 }
 
-template <class T, class V, int U>
-__global__ void __launch_bounds__(512) k_spmv_tiledN(TiledNArgs<T, V> a) {
+// a matrix value read from shared memory, in the accumulation type
+__device__ __forceinline__ float smem_val(float v) { return v; }
+__device__ __forceinline__ double smem_val(double v) { return v; }
+__device__ __forceinline__ float smem_val(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ float smem_val(__half v) { return __half2float(v); }
+
+constexpr size_t align128(size_t b) { return (b + 127) & ~(size_t)127; }
+template <class V> constexpr size_t bulk_stage_bytes() {
+    return align128((size_t)BULK_CHUNK * 2) + align128((size_t)BULK_CHUNK * sizeof(V));
+}
+
+// Tile-staged A*x, one tile per CTA of BULK_NC consumer warps and one
+// producer warp.  The tile's slices are consecutive in memory; the producer
+// (one lane) bulk-copies them chunk by chunk into a ring of BULK_STAGES
+// shared-memory stages (positions and values, mbarrier full[s] counting the
+// bytes), so the matrix stream is in flight without registers or per-warp
+// load chains; the consumers stage the tile's x, then sum the slices of each
+// landed chunk (slice j of a chunk to warp j mod BULK_NC, one segment per
+// lane, steps in order) and release the stage (mbarrier empty[s], one
+// arrival per consumer warp).  Every wait is bounded: on a timeout a warp
+// records ERR_TILED_TIMEOUT and stops computing but keeps releasing stages,
+// and the producer waits (bounded) for its last copies before it returns, so
+// no copy lands after the CTA exits.
+template <class T, class V>
+__global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T, V> a, BulkArgs bk) {
     count_launch(a.ctl);
     using VV = typename TVT<V>::type;
-    extern __shared__ __align__(16) unsigned char sm_raw[];
-    T* xsm = reinterpret_cast<T*>(sm_raw);
-    const int sel = a.by_parity ? a.ctl->parity : 0;
-    const T* __restrict__ x = a.x[sel];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int tvox = a.ty * a.tx * a.tz;
+    constexpr int S = BULK_STAGES, NC = BULK_NC;
+    constexpr size_t LB = align128((size_t)BULK_CHUNK * 2), SB = bulk_stage_bytes<V>();
+    extern __shared__ __align__(128) unsigned char sm_raw[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm_raw);
+    uint64_t* empty = full + S;
+    unsigned char* stages = sm_raw + 128;
+    T* xsm = reinterpret_cast<T*>(stages + S * SB);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int t = __ldg(a.tile_order + blockIdx.x);  // tiles with segments, largest first
+    const int c0 = __ldg(bk.tile_chunk + t), nch = __ldg(bk.tile_chunk + t + 1) - c0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < S; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], NC);
+        }
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (warp == NC) {
+        // ---- producer: one lane issues the bulk copies of every chunk
+        if (lane == 0) {
+            bool ok = true;
+            int issued = 0;
+            for (int i = 0; i < nch; ++i) {
+                const int st = i % S;
+                if (i >= S && !mbar_wait(&empty[st], (unsigned)(((i / S) - 1) & 1))) {
+                    ok = false;
+                    break;
+                }
+                const long long e0 = __ldg(bk.chunk_e0 + c0 + i), ne = __ldg(bk.chunk_e0 + c0 + i + 1) - e0;
+                const unsigned bl = (unsigned)(ne * 2), bv = (unsigned)(ne * sizeof(V));
+                unsigned char* dst = stages + st * SB;
+                mbar_expect_tx(&full[st], bl + bv);
+                bulk_g2s(dst, a.lidx + e0, bl, &full[st]);
+                bulk_g2s(dst + LB, a.val + e0, bv, &full[st]);
+                issued = i + 1;
+            }
+            // the last copies of each stage land before this thread (and so the CTA) exits
+            for (int i = max(0, issued - S); i < issued; ++i)
+                if (!mbar_wait(&full[i % S], (unsigned)((i / S) & 1))) ok = false;
+            if (!ok && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
+        }
+        return;
+    }
+    // ---- consumers: stage x of the tile
+    const T* __restrict__ x = a.x[a.by_parity ? a.ctl->parity : 0];
     {
-        const int t = __ldg(a.tile_order + blockIdx.x);  // tiles with segments, largest first
-        const int s0 = __ldg(a.tile_slice + t), s1 = __ldg(a.tile_slice + t + 1);
+        const int tvox = a.ty * a.tx * a.tz;
         const int tzi = t / (a.nty * a.ntx), rem = t - tzi * a.nty * a.ntx, txi = rem / a.nty, tyi = rem - txi * a.nty;
         const long y0 = (long)tyi * a.ty, x0 = (long)txi * a.tx, z0 = (long)tzi * a.tz;
-        for (int j = threadIdx.x; j < tvox; j += blockDim.x) {
+        for (int j = threadIdx.x; j < tvox; j += 32 * NC) {
             const int ly = j % a.ty, lx = (j / a.ty) % a.tx, lz = j / (a.ty * a.tx);
             const long yy = y0 + ly, xx = x0 + lx, zz = z0 + lz;
             xsm[j] = (yy < a.p && xx < a.q && zz < a.r) ? x[yy + (long)a.p * (xx + (long)a.q * zz)] : T(0);
         }
-        __syncthreads();
-        for (int sl = s0 + warp; sl < s1; sl += nwarps) {
-            const long long off = a.slice_off[sl];
-            const int len = (int)((a.slice_off[sl + 1] - off) >> 5);
-            const unsigned short* __restrict__ li = a.lidx + off + lane;
-            const V* __restrict__ va = a.val + off + lane;
-            RowAcc<T> acc;
-            int k = 0;
-            for (; k + U <= len; k += U) {
-                unsigned short ii[U];
-                VV vv[U];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    ii[u] = __ldcs(li + 32 * (k + u));
-                    vv[u] = (VV)Acc<VV, V>::load(va + 32 * (k + u));
-                }
-#pragma unroll
-                for (int u = 0; u < U; ++u) madd(acc, vv[u], xsm[ii[u]]);
-            }
-            for (; k < len; ++k) madd(acc, (VV)Acc<VV, V>::load(va + 32 * k), xsm[__ldcs(li + 32 * k)]);
-            const int d = __ldg(a.slot_dest + (long)sl * 32 + lane);
-            if (d >= 0) a.part[d] = acc.value();
-        }
     }
+    named_sync(1, 32 * NC);
+    bool ok = true;
+    for (int i = 0; i < nch; ++i) {
+        const int st = i % S;
+        const int cs0 = __ldg(bk.chunk_slice + c0 + i), cs1 = __ldg(bk.chunk_slice + c0 + i + 1);
+        // this warp's slices of the chunk are cs0 + warp + j NC; lane j holds the j-th one's place
+        int2 rl = make_int2(0, 0);
+        {
+            const int sl = cs0 + warp + lane * NC;
+            if (sl < cs1) rl = __ldg(bk.slice_rel + sl);
+        }
+        if (ok) ok = mbar_wait(&full[st], (unsigned)((i / S) & 1));
+        if (ok) {
+            const unsigned short* L = reinterpret_cast<const unsigned short*>(stages + st * SB);
+            const V* W = reinterpret_cast<const V*>(stages + st * SB + LB);
+            for (int j = 0;; ++j) {
+                const int sl = cs0 + warp + j * NC;
+                if (sl >= cs1) break;
+                const int off = __shfl_sync(FULL, rl.x, j), len = __shfl_sync(FULL, rl.y, j);
+                const int d = __ldg(a.slot_dest + (long)sl * 32 + lane);
+                const unsigned short* li = L + off + lane;
+                const V* wv = W + off + lane;
+                RowAcc<T> acc;
+                int k = 0;
+                for (; k + 4 <= len; k += 4) {
+                    unsigned short ii[4];
+                    VV vv[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        ii[u] = li[32 * (k + u)];
+                        vv[u] = (VV)smem_val(wv[32 * (k + u)]);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) madd(acc, vv[u], xsm[ii[u]]);
+                }
+                for (; k < len; ++k) madd(acc, (VV)smem_val(wv[32 * k]), xsm[li[32 * k]]);
+                if (d >= 0) a.part[d] = acc.value();
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);
+    }
+    if (!ok && lane == 0 && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
 }
 
 template <class T, class V, int EPI>
@@ -1035,19 +1117,59 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
                                           seg_start.p, nnz, idx_s.p, ind, valin, dest.p, p, q, ty, tx, tz, lidx.p,
                                           val.p, slot_dest.p);
     TV3_CUDA(cudaGetLastError());
-    const int smem = (int)std::max<size_t>((size_t)ty * tx * tz * sizeof(T), 16);
-    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiledN<T, V, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  std::max(smem, 48 * 1024)));
+    // chunks of the streamed form: per tile, runs of consecutive slices with
+    // at most BULK_CHUNK entries and 32 slices per consumer warp
+    {
+        std::vector<int> tch(ntiles + 1, 0), csl;
+        std::vector<long long> ce0;
+        std::vector<int2> srel(std::max(nslices, 1), make_int2(0, 0));
+        for (int t = 0; t < ntiles; ++t) {
+            tch[t] = (int)csl.size();
+            int sl = tsl[t];
+            while (sl < tsl[t + 1]) {
+                csl.push_back(sl);
+                ce0.push_back(soff[sl]);
+                long long ent = 0;
+                int cnt = 0;
+                while (sl < tsl[t + 1] && cnt < 32 * BULK_NC && ent + (soff[sl + 1] - soff[sl]) <= BULK_CHUNK) {
+                    srel[sl] = make_int2((int)(soff[sl] - ce0.back()), (int)((soff[sl + 1] - soff[sl]) / 32));
+                    ent += soff[sl + 1] - soff[sl];
+                    ++cnt;
+                    ++sl;
+                }
+                if (cnt == 0) return;  // a slice longer than a chunk (not met by ray segments of a tile)
+            }
+        }
+        tch[ntiles] = (int)csl.size();
+        csl.push_back(nslices);
+        ce0.push_back(soff[nslices]);
+        tile_chunk.alloc(ntiles + 1);
+        chunk_slice.alloc(csl.size());
+        chunk_e0.alloc(ce0.size());
+        slice_rel.alloc(srel.size());
+        TV3_CUDA(cudaMemcpy(tile_chunk.p, tch.data(), tch.size() * sizeof(int), cudaMemcpyHostToDevice));
+        TV3_CUDA(cudaMemcpy(chunk_slice.p, csl.data(), csl.size() * sizeof(int), cudaMemcpyHostToDevice));
+        TV3_CUDA(cudaMemcpy(chunk_e0.p, ce0.data(), ce0.size() * sizeof(long long), cudaMemcpyHostToDevice));
+        TV3_CUDA(cudaMemcpy(slice_rel.p, srel.data(), srel.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    }
+    TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiledN<T, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem_bytes()));
     TV3_CUDA(cudaStreamSynchronize(s));
     ok = true;
 }
 
 template <class T, class V>
+size_t TiledN<T, V>::smem_bytes() const {
+    return 128 + BULK_STAGES * bulk_stage_bytes<V>() + (size_t)ty * tx * tz * sizeof(T);
+}
+
+template <class T, class V>
 void TiledN<T, V>::apply(const TiledNArgs<T, V>& a, int epi, cudaStream_t s) const {
-    const size_t smem = std::max<size_t>((size_t)ty * tx * tz * sizeof(T), 16);
     TiledNArgs<T, V> b = a;
     b.tile_order = tile_order.p;
-    if (nwork > 0) launch_k(k_spmv_tiledN<T, V, 8>, dim3(nwork), dim3(512), smem, s, b);
+    const BulkArgs bk{tile_chunk.p, chunk_slice.p, chunk_e0.p, slice_rel.p};
+    if (nwork > 0)
+        launch_k(k_spmv_tiledN<T, V>, dim3(nwork), dim3(32 * (BULK_NC + 1)), smem_bytes(), s, b, bk);
     const int g = (int)std::max<long>(1, std::min<long>((a.m + 255) / 256, (long)num_sms() * 4));
     switch (epi) {
         case SPMV_SUB: launch_k(k_tiledN_reduce<T, V, SPMV_SUB>, dim3(g), dim3(256), 0, s, b); break;
