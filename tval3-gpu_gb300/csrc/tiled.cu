@@ -835,28 +835,34 @@ __device__ __forceinline__ float smem_val(__nv_bfloat16 v) { return __bfloat162f
 __device__ __forceinline__ float smem_val(__half v) { return __half2float(v); }
 
 constexpr size_t align128(size_t b) { return (b + 127) & ~(size_t)127; }
+// one stage: positions, values, the slices' destinations (32 each), places
+constexpr size_t BULK_LB = align128((size_t)BULK_CHUNK * 2);
+template <class V> constexpr size_t bulk_val_bytes() { return align128((size_t)BULK_CHUNK * sizeof(V)); }
+constexpr size_t BULK_DB = (size_t)BULK_MAXS * 32 * 4;
 template <class V> constexpr size_t bulk_stage_bytes() {
-    return align128((size_t)BULK_CHUNK * 2) + align128((size_t)BULK_CHUNK * sizeof(V));
+    return BULK_LB + bulk_val_bytes<V>() + BULK_DB + (size_t)BULK_MAXS * 16;
 }
 
 // Tile-staged A*x, one tile per CTA of BULK_NC consumer warps and one
 // producer warp.  The tile's slices are consecutive in memory; the producer
 // (one lane) bulk-copies them chunk by chunk into a ring of BULK_STAGES
-// shared-memory stages (positions and values, mbarrier full[s] counting the
-// bytes), so the matrix stream is in flight without registers or per-warp
-// load chains; the consumers stage the tile's x, then sum the slices of each
-// landed chunk (slice j of a chunk to warp j mod BULK_NC, one segment per
-// lane, steps in order) and release the stage (mbarrier empty[s], one
-// arrival per consumer warp).  Every wait is bounded: on a timeout a warp
-// records ERR_TILED_TIMEOUT and stops computing but keeps releasing stages,
-// and the producer waits (bounded) for its last copies before it returns, so
-// no copy lands after the CTA exits.
+// shared-memory stages (positions, values, and the chunk's per-slice
+// destinations and places; mbarrier full[s] counts the bytes), so the
+// matrix stream is in flight without registers or per-warp load chains and
+// the consumers read no table from global memory while they sum.  The
+// consumers stage the tile's x, then sum the slices of each landed chunk
+// (slice j of a chunk to warp j mod BULK_NC, one segment per lane, steps in
+// order) and release the stage (mbarrier empty[s], one arrival per consumer
+// warp).  Every wait is bounded: on a timeout a warp records
+// ERR_TILED_TIMEOUT and stops computing but keeps releasing stages, and the
+// producer waits (bounded) for its last copies before it returns, so no copy
+// lands after the CTA exits.
 template <class T, class V>
 __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T, V> a, BulkArgs bk) {
     count_launch(a.ctl);
     using VV = typename TVT<V>::type;
     constexpr int S = BULK_STAGES, NC = BULK_NC;
-    constexpr size_t LB = align128((size_t)BULK_CHUNK * 2), SB = bulk_stage_bytes<V>();
+    constexpr size_t VB = bulk_val_bytes<V>(), SB = bulk_stage_bytes<V>();
     extern __shared__ __align__(128) unsigned char sm_raw[];
     uint64_t* full = reinterpret_cast<uint64_t*>(sm_raw);
     uint64_t* empty = full + S;
@@ -885,11 +891,15 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
                     break;
                 }
                 const long long e0 = __ldg(bk.chunk_e0 + c0 + i), ne = __ldg(bk.chunk_e0 + c0 + i + 1) - e0;
+                const int cs0 = __ldg(bk.chunk_slice + c0 + i), ns = __ldg(bk.chunk_slice + c0 + i + 1) - cs0;
                 const unsigned bl = (unsigned)(ne * 2), bv = (unsigned)(ne * sizeof(V));
+                const unsigned bd = (unsigned)ns * 128u, bi = (unsigned)ns * 16u;
                 unsigned char* dst = stages + st * SB;
-                mbar_expect_tx(&full[st], bl + bv);
+                mbar_expect_tx(&full[st], bl + bv + bd + bi);
                 bulk_g2s(dst, a.lidx + e0, bl, &full[st]);
-                bulk_g2s(dst + LB, a.val + e0, bv, &full[st]);
+                bulk_g2s(dst + BULK_LB, a.val + e0, bv, &full[st]);
+                bulk_g2s(dst + BULK_LB + VB, a.slot_dest + (long)cs0 * 32, bd, &full[st]);
+                bulk_g2s(dst + BULK_LB + VB + BULK_DB, bk.slice_info + cs0, bi, &full[st]);
                 issued = i + 1;
             }
             // the last copies of each stage land before this thread (and so the CTA) exits
@@ -899,7 +909,9 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
         }
         return;
     }
-    // ---- consumers: stage x of the tile
+    // ---- consumers: the tile's chunk bounds (lane i holds chunk i's first
+    // slice), then x of the tile
+    const int cfirst = (lane <= nch) ? __ldg(bk.chunk_slice + c0 + lane) : 0;
     const T* __restrict__ x = a.x[a.by_parity ? a.ctl->parity : 0];
     {
         const int tvox = a.ty * a.tx * a.tz;
@@ -915,22 +927,24 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
     bool ok = true;
     for (int i = 0; i < nch; ++i) {
         const int st = i % S;
-        const int cs0 = __ldg(bk.chunk_slice + c0 + i), cs1 = __ldg(bk.chunk_slice + c0 + i + 1);
-        // this warp's slices of the chunk are cs0 + warp + j NC; lane j holds the j-th one's place
-        int2 rl = make_int2(0, 0);
-        {
-            const int sl = cs0 + warp + lane * NC;
-            if (sl < cs1) rl = __ldg(bk.slice_rel + sl);
+        int cs0, cs1;
+        if (i < 31) {
+            cs0 = __shfl_sync(FULL, cfirst, i);
+            cs1 = __shfl_sync(FULL, cfirst, i + 1);
+        } else {  // a tile of more than 31 chunks: read the bounds directly
+            cs0 = __ldg(bk.chunk_slice + c0 + i);
+            cs1 = __ldg(bk.chunk_slice + c0 + i + 1);
         }
         if (ok) ok = mbar_wait(&full[st], (unsigned)((i / S) & 1));
         if (ok) {
-            const unsigned short* L = reinterpret_cast<const unsigned short*>(stages + st * SB);
-            const V* W = reinterpret_cast<const V*>(stages + st * SB + LB);
-            for (int j = 0;; ++j) {
-                const int sl = cs0 + warp + j * NC;
-                if (sl >= cs1) break;
-                const int off = __shfl_sync(FULL, rl.x, j), len = __shfl_sync(FULL, rl.y, j);
-                const int d = __ldg(a.slot_dest + (long)sl * 32 + lane);
+            const unsigned char* base = stages + st * SB;
+            const unsigned short* L = reinterpret_cast<const unsigned short*>(base);
+            const V* W = reinterpret_cast<const V*>(base + BULK_LB);
+            const int* D = reinterpret_cast<const int*>(base + BULK_LB + VB);
+            const int4* I = reinterpret_cast<const int4*>(base + BULK_LB + VB + BULK_DB);
+            for (int j = warp; j < cs1 - cs0; j += NC) {
+                const int4 info = I[j];
+                const int off = info.x, len = info.y;
                 const unsigned short* li = L + off + lane;
                 const V* wv = W + off + lane;
                 RowAcc<T> acc;
@@ -947,6 +961,7 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
                     for (int u = 0; u < 4; ++u) madd(acc, vv[u], xsm[ii[u]]);
                 }
                 for (; k < len; ++k) madd(acc, (VV)smem_val(wv[32 * k]), xsm[li[32 * k]]);
+                const int d = D[j * 32 + lane];
                 if (d >= 0) a.part[d] = acc.value();
             }
         }
@@ -956,29 +971,55 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
     if (!ok && lane == 0 && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
 }
 
+// Each ray's partials in tile order, one warp per 32 consecutive rays: the
+// warp's partials are contiguous (ray-major), so it loads them coalesced
+// into shared memory, 256 at a time, and every lane adds its ray's range in
+// order; then the solver epilogues.
 template <class T, class V, int EPI>
 __global__ void __launch_bounds__(256) k_tiledN_reduce(TiledNArgs<T, V> a) {
     count_launch(a.ctl);
+    constexpr int W = 256;
+    __shared__ T buf[8][W];
     const int sel = a.by_parity ? a.ctl->parity : 0;
     T* __restrict__ y = a.y[sel];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T* wb = buf[warp];
     double acc0 = 0.0, acc1 = 0.0;
-    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < a.m; r += (long)gridDim.x * blockDim.x) {
-        const int e0 = __ldg(a.rseg + r), e1 = __ldg(a.rseg + r + 1);
+    const long nwarps = (long)gridDim.x * 8;
+    for (long rb = ((long)blockIdx.x * 8 + warp) * 32; rb < a.m; rb += nwarps * 32) {
+        const long r = rb + lane;
+        const int elo = __ldg(a.rseg + rb), ehi = __ldg(a.rseg + min(rb + 32, a.m));
+        const int ra = (r < a.m) ? __ldg(a.rseg + r) : 0, rz = (r < a.m) ? __ldg(a.rseg + r + 1) : 0;
         T s = T(0);
-        for (int e = e0; e < e1; ++e) s += a.part[e];
-        if (a.rscale) s *= (T)__ldg(a.rscale + r);
-        if (EPI == SPMV_PLAIN) {
-            y[r] = s;
-        } else if (EPI == SPMV_SUB) {
-            y[r] = s - a.sub[r];
-        } else if (EPI == SPMV_LAM35) {
-            y[r] = s;
-            double t = acc_d(to_acc(s) - to_acc(a.b[r]));
-            acc0 += t * t;
-            acc1 += acc_d(to_acc(a.delta[r])) * t;
-        } else if (EPI == SPMV_NORM2) {
-            const double sd = acc_d(to_acc(s));
-            acc0 += sd * sd;
+        for (int base = elo; base < ehi; base += W) {
+            T v[W / 32];
+#pragma unroll
+            for (int u = 0; u < W / 32; ++u) {
+                const int e = base + lane + 32 * u;
+                v[u] = (e < ehi) ? a.part[e] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < W / 32; ++u) wb[lane + 32 * u] = v[u];
+            __syncwarp();
+            const int e1 = min(rz, base + W);
+            for (int e = max(ra, base); e < e1; ++e) s += wb[e - base];
+            __syncwarp();
+        }
+        if (r < a.m) {
+            if (a.rscale) s *= (T)__ldg(a.rscale + r);
+            if (EPI == SPMV_PLAIN) {
+                y[r] = s;
+            } else if (EPI == SPMV_SUB) {
+                y[r] = s - a.sub[r];
+            } else if (EPI == SPMV_LAM35) {
+                y[r] = s;
+                double t = acc_d(to_acc(s) - to_acc(a.b[r]));
+                acc0 += t * t;
+                acc1 += acc_d(to_acc(a.delta[r])) * t;
+            } else if (EPI == SPMV_NORM2) {
+                const double sd = acc_d(to_acc(s));
+                acc0 += sd * sd;
+            }
         }
     }
     if (EPI == SPMV_LAM35 || EPI == SPMV_NORM2) {
@@ -1122,7 +1163,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     {
         std::vector<int> tch(ntiles + 1, 0), csl;
         std::vector<long long> ce0;
-        std::vector<int2> srel(std::max(nslices, 1), make_int2(0, 0));
+        std::vector<int4> sinfo(std::max(nslices, 1), make_int4(0, 0, 0, 0));
         for (int t = 0; t < ntiles; ++t) {
             tch[t] = (int)csl.size();
             int sl = tsl[t];
@@ -1131,8 +1172,8 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
                 ce0.push_back(soff[sl]);
                 long long ent = 0;
                 int cnt = 0;
-                while (sl < tsl[t + 1] && cnt < 32 * BULK_NC && ent + (soff[sl + 1] - soff[sl]) <= BULK_CHUNK) {
-                    srel[sl] = make_int2((int)(soff[sl] - ce0.back()), (int)((soff[sl + 1] - soff[sl]) / 32));
+                while (sl < tsl[t + 1] && cnt < BULK_MAXS && ent + (soff[sl + 1] - soff[sl]) <= BULK_CHUNK) {
+                    sinfo[sl] = make_int4((int)(soff[sl] - ce0.back()), (int)((soff[sl + 1] - soff[sl]) / 32), 0, 0);
                     ent += soff[sl + 1] - soff[sl];
                     ++cnt;
                     ++sl;
@@ -1146,11 +1187,11 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
         tile_chunk.alloc(ntiles + 1);
         chunk_slice.alloc(csl.size());
         chunk_e0.alloc(ce0.size());
-        slice_rel.alloc(srel.size());
+        slice_info.alloc(sinfo.size());
         TV3_CUDA(cudaMemcpy(tile_chunk.p, tch.data(), tch.size() * sizeof(int), cudaMemcpyHostToDevice));
         TV3_CUDA(cudaMemcpy(chunk_slice.p, csl.data(), csl.size() * sizeof(int), cudaMemcpyHostToDevice));
         TV3_CUDA(cudaMemcpy(chunk_e0.p, ce0.data(), ce0.size() * sizeof(long long), cudaMemcpyHostToDevice));
-        TV3_CUDA(cudaMemcpy(slice_rel.p, srel.data(), srel.size() * sizeof(int2), cudaMemcpyHostToDevice));
+        TV3_CUDA(cudaMemcpy(slice_info.p, sinfo.data(), sinfo.size() * sizeof(int4), cudaMemcpyHostToDevice));
     }
     TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiledN<T, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem_bytes()));
@@ -1167,10 +1208,10 @@ template <class T, class V>
 void TiledN<T, V>::apply(const TiledNArgs<T, V>& a, int epi, cudaStream_t s) const {
     TiledNArgs<T, V> b = a;
     b.tile_order = tile_order.p;
-    const BulkArgs bk{tile_chunk.p, chunk_slice.p, chunk_e0.p, slice_rel.p};
+    const BulkArgs bk{tile_chunk.p, chunk_slice.p, chunk_e0.p, slice_info.p};
     if (nwork > 0)
         launch_k(k_spmv_tiledN<T, V>, dim3(nwork), dim3(32 * (BULK_NC + 1)), smem_bytes(), s, b, bk);
-    const int g = (int)std::max<long>(1, std::min<long>((a.m + 255) / 256, (long)num_sms() * 4));
+    const int g = (int)std::max<long>(1, std::min<long>((a.m + 255) / 256, (long)num_sms() * 8));
     switch (epi) {
         case SPMV_SUB: launch_k(k_tiledN_reduce<T, V, SPMV_SUB>, dim3(g), dim3(256), 0, s, b); break;
         case SPMV_LAM35: launch_k(k_tiledN_reduce<T, V, SPMV_LAM35>, dim3(g), dim3(256), 0, s, b); break;
