@@ -30,16 +30,19 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
 }
-// bounded wait for the completion of phase `parity`; false on timeout
+// bounded wait for the completion of phase `parity`; false on timeout.  Each
+// try_wait may suspend the thread until the phase completes or about a
+// microsecond passes (the suspend-time hint), so a waiting warp does not
+// spin on the issue slots that the working warps of its SM need.
 __device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
     const unsigned a = smem_u32(b);
     const long long t0 = clock64();
     for (;;) {
         unsigned ok;
         asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(ok)
-            : "r"(a), "r"(parity)
+            : "r"(a), "r"(parity), "r"(1000u)
             : "memory");
         if (ok) return true;
         if (clock64() - t0 > WAIT_CYCLES) return false;
@@ -67,6 +70,13 @@ __device__ __forceinline__ void cp_async_arrive(uint64_t* b) {
     asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(b)) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// close the thread's current group of cp.async copies
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// wait until at most N of the thread's committed groups are still in flight
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 // named barrier over `threads` threads (a multiple of 32) of the CTA
 __device__ __forceinline__ void named_sync(int id, int threads) {

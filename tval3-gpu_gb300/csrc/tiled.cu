@@ -843,20 +843,38 @@ template <class V> constexpr size_t bulk_stage_bytes() {
     return BULK_LB + bulk_val_bytes<V>() + BULK_DB + (size_t)BULK_MAXS * 16;
 }
 
-// Tile-staged A*x, one tile per CTA of BULK_NC consumer warps and one
-// producer warp.  The tile's slices are consecutive in memory; the producer
-// (one lane) bulk-copies them chunk by chunk into a ring of BULK_STAGES
-// shared-memory stages (positions, values, and the chunk's per-slice
-// destinations and places; mbarrier full[s] counts the bytes), so the
-// matrix stream is in flight without registers or per-warp load chains and
-// the consumers read no table from global memory while they sum.  The
-// consumers stage the tile's x, then sum the slices of each landed chunk
-// (slice j of a chunk to warp j mod BULK_NC, one segment per lane, steps in
-// order) and release the stage (mbarrier empty[s], one arrival per consumer
-// warp).  Every wait is bounded: on a timeout a warp records
-// ERR_TILED_TIMEOUT and stops computing but keeps releasing stages, and the
-// producer waits (bounded) for its last copies before it returns, so no copy
-// lands after the CTA exits.
+// x values of tile t into xs (shared memory) by asynchronous copies; voxels
+// outside the volume (boundary tiles) are zero
+template <class T, class V>
+__device__ __forceinline__ void stage_x_async(const TiledNArgs<T, V>& a, const T* __restrict__ x, int t, T* xs) {
+    const int tvox = a.ty * a.tx * a.tz;
+    const int tzi = t / (a.nty * a.ntx), rem = t - tzi * a.nty * a.ntx, txi = rem / a.nty, tyi = rem - txi * a.nty;
+    const long y0 = (long)tyi * a.ty, x0 = (long)txi * a.tx, z0 = (long)tzi * a.tz;
+    for (int j = threadIdx.x; j < tvox; j += 32 * BULK_NC) {
+        const int ly = j % a.ty, lx = (j / a.ty) % a.tx, lz = j / (a.ty * a.tx);
+        const long yy = y0 + ly, xx = x0 + lx, zz = z0 + lz;
+        if (yy < a.p && xx < a.q && zz < a.r) cp_async<(int)sizeof(T)>(xs + j, x + yy + (long)a.p * (xx + (long)a.q * zz));
+        else xs[j] = T(0);
+    }
+    cp_async_commit();
+}
+
+// Tile-staged A*x.  A persistent CTA of BULK_NC consumer warps and one
+// producer warp takes the tiles with segments in largest-first order,
+// snaking over the CTAs (position k*G + b for even k, k*G + G-1-b for odd
+// k).  The tiles' slices are consecutive in memory; the producer (one lane)
+// bulk-copies them chunk by chunk, across tile boundaries, into a ring of
+// BULK_STAGES shared-memory stages (positions, values, and the chunk's
+// per-slice destinations and places; mbarrier full[s] counts the bytes), so
+// the matrix stream stays in flight without registers or per-warp load
+// chains and without draining between tiles.  The consumers keep two x
+// buffers: while they sum tile k, the x values of tile k+1 arrive by
+// asynchronous copies.  A chunk's slice j goes to warp j mod BULK_NC (one
+// segment per lane, steps in order); the warp releases the stage (mbarrier
+// empty[s], one arrival per consumer warp).  Every wait is bounded: on a
+// timeout a warp records ERR_TILED_TIMEOUT and stops computing but keeps
+// releasing stages, and the producer waits (bounded) for its last copies
+// before it returns, so no copy lands after the CTA exits.
 template <class T, class V>
 __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T, V> a, BulkArgs bk) {
     count_launch(a.ctl);
@@ -867,10 +885,13 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
     uint64_t* full = reinterpret_cast<uint64_t*>(sm_raw);
     uint64_t* empty = full + S;
     unsigned char* stages = sm_raw + 128;
-    T* xsm = reinterpret_cast<T*>(stages + S * SB);
+    T* xbuf = reinterpret_cast<T*>(stages + S * SB);
+    const int xstride = (a.ty * a.tx * a.tz + 1) & ~1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int t = __ldg(a.tile_order + blockIdx.x);  // tiles with segments, largest first
-    const int c0 = __ldg(bk.tile_chunk + t), nch = __ldg(bk.tile_chunk + t + 1) - c0;
+    const int G = gridDim.x, b = blockIdx.x;
+    auto tile_pos = [&](int k) { return k * G + ((k & 1) ? G - 1 - b : b); };  // this CTA's k-th tile position
+    int ntl = 0;  // tiles of this CTA
+    while (tile_pos(ntl) < bk.nwork) ++ntl;
     if (threadIdx.x == 0) {
         for (int i = 0; i < S; ++i) {
             mbar_init(&full[i], 1);
@@ -880,101 +901,117 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
     }
     __syncthreads();
     if (warp == NC) {
-        // ---- producer: one lane issues the bulk copies of every chunk
+        // ---- producer: one lane issues the bulk copies of every chunk of every tile
         if (lane == 0) {
             bool ok = true;
-            int issued = 0;
-            for (int i = 0; i < nch; ++i) {
-                const int st = i % S;
-                if (i >= S && !mbar_wait(&empty[st], (unsigned)(((i / S) - 1) & 1))) {
-                    ok = false;
-                    break;
+            int i = 0;  // chunks issued
+            for (int k = 0; k < ntl && ok; ++k) {
+                const int t = __ldg(a.tile_order + tile_pos(k));
+                const int c0 = __ldg(bk.tile_chunk + t), c1 = __ldg(bk.tile_chunk + t + 1);
+                for (int c = c0; c < c1; ++c, ++i) {
+                    const int st = i % S;
+                    if (i >= S && !mbar_wait(&empty[st], (unsigned)(((i / S) - 1) & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    const long long e0 = __ldg(bk.chunk_e0 + c), ne = __ldg(bk.chunk_e0 + c + 1) - e0;
+                    const int cs0 = __ldg(bk.chunk_slice + c), ns = __ldg(bk.chunk_slice + c + 1) - cs0;
+                    const unsigned bl = (unsigned)(ne * 2), bv = (unsigned)(ne * sizeof(V));
+                    const unsigned bd = (unsigned)ns * 128u, bi = (unsigned)ns * 16u;
+                    unsigned char* dst = stages + st * SB;
+                    mbar_expect_tx(&full[st], bl + bv + bd + bi);
+                    bulk_g2s(dst, a.lidx + e0, bl, &full[st]);
+                    bulk_g2s(dst + BULK_LB, a.val + e0, bv, &full[st]);
+                    bulk_g2s(dst + BULK_LB + VB, a.slot_dest + (long)cs0 * 32, bd, &full[st]);
+                    bulk_g2s(dst + BULK_LB + VB + BULK_DB, bk.slice_info + cs0, bi, &full[st]);
                 }
-                const long long e0 = __ldg(bk.chunk_e0 + c0 + i), ne = __ldg(bk.chunk_e0 + c0 + i + 1) - e0;
-                const int cs0 = __ldg(bk.chunk_slice + c0 + i), ns = __ldg(bk.chunk_slice + c0 + i + 1) - cs0;
-                const unsigned bl = (unsigned)(ne * 2), bv = (unsigned)(ne * sizeof(V));
-                const unsigned bd = (unsigned)ns * 128u, bi = (unsigned)ns * 16u;
-                unsigned char* dst = stages + st * SB;
-                mbar_expect_tx(&full[st], bl + bv + bd + bi);
-                bulk_g2s(dst, a.lidx + e0, bl, &full[st]);
-                bulk_g2s(dst + BULK_LB, a.val + e0, bv, &full[st]);
-                bulk_g2s(dst + BULK_LB + VB, a.slot_dest + (long)cs0 * 32, bd, &full[st]);
-                bulk_g2s(dst + BULK_LB + VB + BULK_DB, bk.slice_info + cs0, bi, &full[st]);
-                issued = i + 1;
             }
             // the last copies of each stage land before this thread (and so the CTA) exits
-            for (int i = max(0, issued - S); i < issued; ++i)
-                if (!mbar_wait(&full[i % S], (unsigned)((i / S) & 1))) ok = false;
+            for (int j = max(0, i - S); j < i; ++j)
+                if (!mbar_wait(&full[j % S], (unsigned)((j / S) & 1))) ok = false;
             if (!ok && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
         }
         return;
     }
-    // ---- consumers: the tile's chunk bounds (lane i holds chunk i's first
-    // slice), then x of the tile
-    const int cfirst = (lane <= nch) ? __ldg(bk.chunk_slice + c0 + lane) : 0;
+    // ---- consumers
     const T* __restrict__ x = a.x[a.by_parity ? a.ctl->parity : 0];
-    {
-        const int tvox = a.ty * a.tx * a.tz;
-        const int tzi = t / (a.nty * a.ntx), rem = t - tzi * a.nty * a.ntx, txi = rem / a.nty, tyi = rem - txi * a.nty;
-        const long y0 = (long)tyi * a.ty, x0 = (long)txi * a.tx, z0 = (long)tzi * a.tz;
-        for (int j = threadIdx.x; j < tvox; j += 32 * NC) {
-            const int ly = j % a.ty, lx = (j / a.ty) % a.tx, lz = j / (a.ty * a.tx);
-            const long yy = y0 + ly, xx = x0 + lx, zz = z0 + lz;
-            xsm[j] = (yy < a.p && xx < a.q && zz < a.r) ? x[yy + (long)a.p * (xx + (long)a.q * zz)] : T(0);
-        }
-    }
-    named_sync(1, 32 * NC);
     bool ok = true;
-    for (int i = 0; i < nch; ++i) {
-        const int st = i % S;
-        int cs0, cs1;
-        if (i < 31) {
-            cs0 = __shfl_sync(FULL, cfirst, i);
-            cs1 = __shfl_sync(FULL, cfirst, i + 1);
-        } else {  // a tile of more than 31 chunks: read the bounds directly
-            cs0 = __ldg(bk.chunk_slice + c0 + i);
-            cs1 = __ldg(bk.chunk_slice + c0 + i + 1);
+    int i = 0;  // chunks consumed
+    if (ntl > 0) stage_x_async(a, x, __ldg(a.tile_order + tile_pos(0)), xbuf);
+    for (int k = 0; k < ntl; ++k) {
+        const int t = __ldg(a.tile_order + tile_pos(k));
+        const int c0 = __ldg(bk.tile_chunk + t), nch = __ldg(bk.tile_chunk + t + 1) - c0;
+        const int cfirst = (lane <= nch) ? __ldg(bk.chunk_slice + c0 + lane) : 0;  // lane j: chunk j's first slice
+        named_sync(1, 32 * NC);  // every consumer is done with tile k-1: its x buffer is free
+        if (k + 1 < ntl) {
+            stage_x_async(a, x, __ldg(a.tile_order + tile_pos(k + 1)), xbuf + ((k + 1) & 1) * xstride);
+            cp_async_wait_group<1>();  // this thread's copies of tile k have landed
+        } else {
+            cp_async_wait_group<0>();
         }
-        if (ok) ok = mbar_wait(&full[st], (unsigned)((i / S) & 1));
-        if (ok) {
-            const unsigned char* base = stages + st * SB;
-            const unsigned short* L = reinterpret_cast<const unsigned short*>(base);
-            const V* W = reinterpret_cast<const V*>(base + BULK_LB);
-            const int* D = reinterpret_cast<const int*>(base + BULK_LB + VB);
-            const int4* I = reinterpret_cast<const int4*>(base + BULK_LB + VB + BULK_DB);
-            for (int j = warp; j < cs1 - cs0; j += NC) {
-                const int4 info = I[j];
-                const int off = info.x, len = info.y;
-                const unsigned short* li = L + off + lane;
-                const V* wv = W + off + lane;
-                RowAcc<T> acc;
-                int k = 0;
-                for (; k + 4 <= len; k += 4) {
-                    unsigned short ii[4];
-                    VV vv[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        ii[u] = li[32 * (k + u)];
-                        vv[u] = (VV)smem_val(wv[32 * (k + u)]);
-                    }
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) madd(acc, vv[u], xsm[ii[u]]);
-                }
-                for (; k < len; ++k) madd(acc, (VV)smem_val(wv[32 * k]), xsm[li[32 * k]]);
-                const int d = D[j * 32 + lane];
-                if (d >= 0) a.part[d] = acc.value();
+        named_sync(1, 32 * NC);  // ... and every thread's
+        const T* xsm = xbuf + (k & 1) * xstride;
+        for (int j = 0; j < nch; ++j, ++i) {
+            const int st = i % S;
+            int cs0, cs1;
+            if (j < 31) {
+                cs0 = __shfl_sync(FULL, cfirst, j);
+                cs1 = __shfl_sync(FULL, cfirst, j + 1);
+            } else {  // a tile of more than 31 chunks: read the bounds directly
+                cs0 = __ldg(bk.chunk_slice + c0 + j);
+                cs1 = __ldg(bk.chunk_slice + c0 + j + 1);
             }
+            if (ok) ok = mbar_wait(&full[st], (unsigned)((i / S) & 1));
+            if (ok) {
+                const unsigned char* base = stages + st * SB;
+                const unsigned short* L = reinterpret_cast<const unsigned short*>(base);
+                const V* W = reinterpret_cast<const V*>(base + BULK_LB);
+                const int* D = reinterpret_cast<const int*>(base + BULK_LB + VB);
+                const int4* I = reinterpret_cast<const int4*>(base + BULK_LB + VB + BULK_DB);
+                for (int js = warp; js < cs1 - cs0; js += NC) {
+                    const int4 info = I[js];
+                    const int off = info.x, len = info.y;
+                    const unsigned short* li = L + off + lane;
+                    const V* wv = W + off + lane;
+                    // two independent accumulations (even and odd steps), so
+                    // that the dependent chain of one step is half as long
+                    RowAcc<T> acc0, acc1;
+                    int kk = 0;
+                    for (; kk + 4 <= len; kk += 4) {
+                        unsigned short ii[4];
+                        VV vv[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            ii[u] = li[32 * (kk + u)];
+                            vv[u] = (VV)smem_val(wv[32 * (kk + u)]);
+                        }
+                        madd(acc0, vv[0], xsm[ii[0]]);
+                        madd(acc1, vv[1], xsm[ii[1]]);
+                        madd(acc0, vv[2], xsm[ii[2]]);
+                        madd(acc1, vv[3], xsm[ii[3]]);
+                    }
+                    for (; kk < len; ++kk) {
+                        if (kk & 1) madd(acc1, (VV)smem_val(wv[32 * kk]), xsm[li[32 * kk]]);
+                        else madd(acc0, (VV)smem_val(wv[32 * kk]), xsm[li[32 * kk]]);
+                    }
+                    combine(acc0, acc1);
+                    const int d = D[js * 32 + lane];
+                    if (d >= 0) a.part[d] = acc0.value();
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[st]);
     }
+    cp_async_wait_group<0>();
     if (!ok && lane == 0 && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
 }
 
 // Each ray's partials in tile order, one warp per 32 consecutive rays: the
 // warp's partials are contiguous (ray-major), so it loads them coalesced
 // into shared memory, 256 at a time, and every lane adds its ray's range in
-// order; then the solver epilogues.
+// order (for double-float partials a compensated sum: high parts by TwoSum,
+// low parts and errors in one FP32 term); then the solver epilogues.
 template <class T, class V, int EPI>
 __global__ void __launch_bounds__(256) k_tiledN_reduce(TiledNArgs<T, V> a) {
     count_launch(a.ctl);
@@ -990,7 +1027,7 @@ __global__ void __launch_bounds__(256) k_tiledN_reduce(TiledNArgs<T, V> a) {
         const long r = rb + lane;
         const int elo = __ldg(a.rseg + rb), ehi = __ldg(a.rseg + min(rb + 32, a.m));
         const int ra = (r < a.m) ? __ldg(a.rseg + r) : 0, rz = (r < a.m) ? __ldg(a.rseg + r + 1) : 0;
-        T s = T(0);
+        RowAcc<T> acc;
         for (int base = elo; base < ehi; base += W) {
             T v[W / 32];
 #pragma unroll
@@ -1002,9 +1039,10 @@ __global__ void __launch_bounds__(256) k_tiledN_reduce(TiledNArgs<T, V> a) {
             for (int u = 0; u < W / 32; ++u) wb[lane + 32 * u] = v[u];
             __syncwarp();
             const int e1 = min(rz, base + W);
-            for (int e = max(ra, base); e < e1; ++e) s += wb[e - base];
+            for (int e = max(ra, base); e < e1; ++e) add(acc, wb[e - base]);
             __syncwarp();
         }
+        T s = acc.value();
         if (r < a.m) {
             if (a.rscale) s *= (T)__ldg(a.rscale + r);
             if (EPI == SPMV_PLAIN) {
@@ -1195,22 +1233,27 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     }
     TV3_CUDA(cudaFuncSetAttribute(k_spmv_tiledN<T, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem_bytes()));
+    // persistent CTAs: as many as fit on the GPU at once (at most one per tile)
+    int per = 0;
+    TV3_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmv_tiledN<T, V>, 32 * (BULK_NC + 1),
+                                                           smem_bytes()));
+    grid_n = std::max(1, std::min(std::max(nwork, 1), std::max(per, 1) * num_sms()));
     TV3_CUDA(cudaStreamSynchronize(s));
     ok = true;
 }
 
 template <class T, class V>
 size_t TiledN<T, V>::smem_bytes() const {
-    return 128 + BULK_STAGES * bulk_stage_bytes<V>() + (size_t)ty * tx * tz * sizeof(T);
+    const size_t xs = ((size_t)ty * tx * tz + 1) & ~(size_t)1;
+    return 128 + BULK_STAGES * bulk_stage_bytes<V>() + 2 * xs * sizeof(T);
 }
 
 template <class T, class V>
 void TiledN<T, V>::apply(const TiledNArgs<T, V>& a, int epi, cudaStream_t s) const {
     TiledNArgs<T, V> b = a;
     b.tile_order = tile_order.p;
-    const BulkArgs bk{tile_chunk.p, chunk_slice.p, chunk_e0.p, slice_info.p};
-    if (nwork > 0)
-        launch_k(k_spmv_tiledN<T, V>, dim3(nwork), dim3(32 * (BULK_NC + 1)), smem_bytes(), s, b, bk);
+    const BulkArgs bk{tile_chunk.p, chunk_slice.p, chunk_e0.p, slice_info.p, nwork};
+    if (nwork > 0) launch_k(k_spmv_tiledN<T, V>, dim3(grid_n), dim3(32 * (BULK_NC + 1)), smem_bytes(), s, b, bk);
     const int g = (int)std::max<long>(1, std::min<long>((a.m + 255) / 256, (long)num_sms() * 8));
     switch (epi) {
         case SPMV_SUB: launch_k(k_tiledN_reduce<T, V, SPMV_SUB>, dim3(g), dim3(256), 0, s, b); break;

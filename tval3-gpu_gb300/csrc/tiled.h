@@ -97,19 +97,20 @@ struct TiledT {
 // tile order and applies the epilogues.
 // Streaming of a tile's slices through shared memory (tile-staged A*x): a
 // producer warp bulk-copies chunks of consecutive slices (at most
-// BULK_CHUNK entries and BULK_MAXS slices, with the slices' destinations and
-// places) into a ring of BULK_STAGES stages while BULK_NC consumer warps sum
-// the slices of the chunks already landed.
+// BULK_CHUNK entries and BULK_MAXS slices, two per consumer warp, with the
+// slices' destinations and places) into a ring of BULK_STAGES stages while
+// BULK_NC consumer warps sum the slices of the chunks already landed.
 constexpr int BULK_NC = 8;
-constexpr int BULK_STAGES = 3;
-constexpr int BULK_CHUNK = 2816;
-constexpr int BULK_MAXS = 32;
+constexpr int BULK_STAGES = 2;
+constexpr int BULK_CHUNK = 4096;
+constexpr int BULK_MAXS = 2 * BULK_NC;
 
 struct BulkArgs {
     const int* tile_chunk;        // ntiles + 1: the tile's chunks
     const int* chunk_slice;       // nchunks + 1: the chunk's first slice (the next chunk's first ends it)
     const long long* chunk_e0;    // nchunks + 1: the chunk's first entry
     const int4* slice_info;       // per slice: {first entry - its chunk's first entry, steps, 0, 0}
+    int nwork;                    // tiles with segments (positions of tile_order)
 };
 
 template <class T, class V>
@@ -152,6 +153,7 @@ struct TiledN {
     DBuf<int> tile_chunk, chunk_slice;
     DBuf<long long> chunk_e0;
     DBuf<int4> slice_info;
+    mutable int grid_n = 0;  // persistent CTAs of the streamed A*x
     size_t smem_bytes() const;
     // build from the CSR of A (m ray rows over the p x q x r volume)
     void build(long m, int p, int q, int r, const int* ptr, const int* ind, const V* val, long nnz, cudaStream_t s);

@@ -62,6 +62,24 @@ template <> struct RowAcc<df64> {
     __device__ __forceinline__ RowAcc() : s(0.f), c(0.f) {}
     __device__ __forceinline__ df64 value() const { return fast_two_sum(s, c); }
 };
+// a + b of two partial accumulations (b's terms after a's)
+__device__ __forceinline__ void combine(RowAcc<float>& a, const RowAcc<float>& b) { a.s += b.s; }
+__device__ __forceinline__ void combine(RowAcc<double>& a, const RowAcc<double>& b) { a.s += b.s; }
+__device__ __forceinline__ void combine(RowAcc<df64>& a, const RowAcc<df64>& b) {
+    const df64 t = two_sum(a.s, b.s);
+    a.s = t.hi;
+    a.c = __fadd_rn(a.c, __fadd_rn(b.c, t.lo));
+}
+// one more summand p (sums of partial results): for df64 the high parts are
+// added with TwoSum and the low parts and rounding errors collected in the
+// compensation term, as in madd
+__device__ __forceinline__ void add(RowAcc<float>& a, float p) { a.s += p; }
+__device__ __forceinline__ void add(RowAcc<double>& a, double p) { a.s += p; }
+__device__ __forceinline__ void add(RowAcc<df64>& a, df64 p) {
+    const df64 t = two_sum(a.s, p.hi);
+    a.s = t.hi;
+    a.c = __fadd_rn(a.c, __fadd_rn(t.lo, p.lo));
+}
 __device__ __forceinline__ void madd(RowAcc<float>& a, float v, float x) { a.s = fmaf(v, x, a.s); }
 __device__ __forceinline__ void madd(RowAcc<double>& a, float v, double x) { a.s = fma((double)v, x, a.s); }
 __device__ __forceinline__ void madd(RowAcc<double>& a, double v, double x) { a.s = fma(v, x, a.s); }
