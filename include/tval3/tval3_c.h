@@ -170,6 +170,14 @@ typedef struct tval3_geometry_host {
 /* ---------------------------------------------------------------------- */
 TVAL3_API void tval3_options_default(tval3_options* opts);
 TVAL3_API const char* tval3_last_error_message(void);
+/* Seconds spent in the phases of the calling thread's last call of a
+ * reference entry point (tval3_gpu_3d_* / tval3_gpu_*): [0] operator (input
+ * checks, upload, transpose or quantisation, ray-matrix build), [1] set-up
+ * (b upload, solver workspace, tile-staged layouts and kernel choice), [2]
+ * solve (graph capture and instantiation on first use, then the solve), [3]
+ * download of U.  n entries are written (at most 4).  No counterpart in the
+ * reference. */
+TVAL3_API tval3_status tval3_last_call_phases(double* secs, int n);
 TVAL3_API const char* tval3_version(void);
 
 /* ---------------------------------------------------------------------- *

@@ -69,6 +69,11 @@ struct tval3_solver_s {
 namespace {
 
 thread_local std::string g_err;
+// seconds of the phases of this thread's last reference entry-point call:
+// operator (input checks, upload, transpose / quantisation, ray-matrix build),
+// set-up (b upload, solver workspace, tile-staged layouts and kernel choice),
+// solve (graph capture on first use, then the solve), download of U
+thread_local double g_phase[4] = {0, 0, 0, 0};
 
 tval3_status fail(int st, const std::string& msg) {
     g_err = msg;
@@ -341,6 +346,8 @@ void solve_host(LinOp<T>* op, Ext<T>* U, int dim_y, int dim_x, int dim_z, const 
                 std::chrono::steady_clock::time_point t0, int layers = 1) {
     using E = Ext<T>;
     std::unique_ptr<LinOp<T>> hold(op);
+    using clk = std::chrono::steady_clock;
+    const auto ta = clk::now();
     const long n = (long)dim_y * dim_x * dim_z * layers;
     DBuf<E> db, dU, dUt;
     db.alloc(std::max<long>(b_len, 1));
@@ -353,10 +360,19 @@ void solve_host(LinOp<T>* op, Ext<T>* U, int dim_y, int dim_x, int dim_z, const 
     }
     Solver<T> s(op, dim_y, dim_x, dim_z, *opts, layers);
     s.mode = 1;  // the whole solve as one graph launch
+    TV3_CUDA(cudaDeviceSynchronize());
+    const auto tb = clk::now();
     tval3_info inf{};
     s.solve(db.p, dU.p, use_ut ? dUt.p : nullptr, &inf, 0);
+    const auto tc = clk::now();
     TV3_CUDA(cudaMemcpy(U, dU.p, n * sizeof(E), cudaMemcpyDeviceToHost));
-    inf.outer_secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    const auto td = clk::now();
+    auto sec = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+    g_phase[0] = sec(t0, ta);
+    g_phase[1] = sec(ta, tb);
+    g_phase[2] = sec(tb, tc);
+    g_phase[3] = sec(tc, td);
+    inf.outer_secs = sec(t0, td);
     if (info) *info = inf;
 }
 
@@ -413,6 +429,13 @@ void tval3_options_default(tval3_options* o) {
 }
 
 const char* tval3_last_error_message(void) { return g_err.c_str(); }
+
+tval3_status tval3_last_call_phases(double* secs, int n) {
+    return guard([&] {
+        if (!secs || n < 0) arg_error(TVAL3_ERR_ARG, "Argument error: NULL phase array!");
+        for (int i = 0; i < n && i < 4; ++i) secs[i] = g_phase[i];
+    });
+}
 const char* tval3_version(void) { return "tval3-gb300 0.1 (sm_103a)"; }
 
 tval3_status tval3_gpu_3d_sparse_f32(float* U, int dim_y, int dim_x, int dim_z, const tval3_sparse_host* A,

@@ -22,6 +22,7 @@ from .capi import (PREC_BF16, PREC_FP16, PREC_FP32, PREC_FP64, SPARSE_BOTH, SPAR
                    TRAV_BRESENHAM, TRAV_SIDDON, Info, Options, check, default_options, load)
 
 __all__ = ["SparseMatrix", "DenseMatrix", "Geometry", "tval3_gpu_3d", "tval3_gpu", "Operator", "Solver",
+           "last_call_phases",
            "D", "Dt", "default_options", "Options", "Info"]
 
 
@@ -229,6 +230,14 @@ def tval3_gpu_3d(shape, A, b, opts=None, Ut=None, *, dtype=np.float32, pagelocke
     check(st)
     assert U.size == n
     return U, info.as_dict()
+
+
+def last_call_phases() -> dict:
+    """Seconds of the phases of this thread's last reference entry-point
+    call: operator, setup, solve, download (tval3_last_call_phases)."""
+    out = (C.c_double * 4)()
+    check(load().tval3_last_call_phases(out, 4))
+    return dict(zip(("operator_s", "setup_s", "solve_s", "download_s"), list(out)))
 
 
 def tval3_gpu(shape, A, b, opts=None, Ut=None, pagelocked=True):
