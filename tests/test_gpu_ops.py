@@ -208,3 +208,34 @@ def test_empty_rays_and_empty_matrix(cuda, oracle):
     op.mat_vec_mul(0, torch.ones(op.cols, device=cuda), y)
     torch.cuda.synchronize()
     assert float(y[0]) == 0.0
+
+
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_multi_mp_geometry_bitexact(cuda, oracle, traversal):
+    """Two measurement positions (numMPs = 2: the transducer coordinates of
+    each position one after the other) and a partial use_path mask: the ray
+    list follows 3d/mat_vec_mul_dynamic.h:477-556 (signal i of position k:
+    emitter k*E + i/R, receiver k*R + i%R, only flagged pairs), and the
+    device-built CSR equals the oracle's bit for bit (Bresenham and Siddon)."""
+    from tval3_gb300 import Geometry, Operator
+    from tval3_gb300 import workloads as W
+    g1 = W.hemisphere_geometry(24, 20, 16, seed=3)
+    g2 = W.hemisphere_geometry(24, 20, 16, seed=9)  # the second position: a rotated lattice
+    cat = lambda a, b: np.concatenate([a, b])
+    use = (np.random.default_rng(5).random(20 * 16) < 0.6).astype(np.uint32)
+    pos = tuple(cat(a, b) for a, b in zip(g1.pos, g2.pos))
+    geo = Geometry(rv_x=24, rv_y=24, rv_z=24,
+                   x_emitters=cat(g1.x_emitters, g2.x_emitters), y_emitters=cat(g1.y_emitters, g2.y_emitters),
+                   z_emitters=cat(g1.z_emitters, g2.z_emitters), x_receivers=cat(g1.x_receivers, g2.x_receivers),
+                   y_receivers=cat(g1.y_receivers, g2.y_receivers), z_receivers=cat(g1.z_receivers, g2.z_receivers),
+                   num_emitters=20, num_receivers=16, numMPs=2, use_path=use, scale_factor=1.0,
+                   traversal=traversal, pos=pos)
+    assert geo.nrays == 2 * int(use.sum())
+    pairs = oracle.ray_list(2, 20, 16, use)
+    assert np.array_equal(pairs, geo.ray_pairs())
+    ref = oracle.bresenham_csr(geo) if traversal == 0 else oracle.siddon_csr(geo)
+    op = Operator.from_geometry(geo, mode=0)
+    ptr, ind, val, tptr, tind, tval = op.export_csr()
+    assert op.rows == geo.nrays
+    assert np.array_equal(ptr, ref[0]) and np.array_equal(ind, ref[1])
+    assert np.array_equal(val.view(np.uint32), ref[2].view(np.uint32))
