@@ -211,7 +211,9 @@ TVAL3_API tval3_status tval3_gpu_3d_dense_f64(double* U, int dim_y, int dim_x, i
                                               const tval3_options* opts, const double* Ut, int Ut_len,
                                               int pagelocked, int mainGPU, int numGPUs, const int* gpuArray,
                                               tval3_info* info);
-/* tval3_gpu_3d(U, geometry_host A, ...), 3d/tval3_gpu_3d.cpp:35-39, :1533-1600 */
+/* tval3_gpu_3d(U, geometry_host A, ...), 3d/tval3_gpu_3d.cpp:35-39, :1533-1600:
+ * evaluated on the fly as in the reference (no matrix stored), for Bresenham
+ * and Siddon rays; A^T*y is deterministic (tile runs summed in a fixed order). */
 TVAL3_API tval3_status tval3_gpu_3d_geometry_f32(float* U, int dim_y, int dim_x, int dim_z,
                                                  const tval3_geometry_host* A, const float* b, int b_len,
                                                  const tval3_options* opts, const float* Ut, int Ut_len,
@@ -279,12 +281,19 @@ TVAL3_API tval3_status tval3_op_create_sparse_device(tval3_op* op, int rows, int
                                                      const int* d_ind, const float* d_val, int precision,
                                                      void* stream);
 /* From a geometry: the ray matrix (Bresenham or Siddon) is built on the
- * device.  mode 0: stored as CSR; mode 1: on-the-fly traversal (A*x gathers,
- * A^T*y scatters), nothing stored. */
+ * device.  mode 0: stored as CSR; mode 1 (FP32 only): on-the-fly traversal,
+ * no matrix stored: A*x walks every ray and gathers x; A^T*y resumes each
+ * ray's runs through a voxel tile (16 bytes a run, plus 88 bytes a Siddon
+ * ray) and sums the tile's voxels in shared memory in a fixed order, so it is
+ * deterministic.  The implied matrix equals the mode-0 CSR bit for bit. */
 TVAL3_API tval3_status tval3_op_create_geometry(tval3_op* op, const tval3_geometry_host* G, int mode, int precision);
 TVAL3_API tval3_status tval3_op_create_dense(tval3_op* op, const tval3_dense_host* A, int precision);
 TVAL3_API tval3_status tval3_op_destroy(tval3_op op);
 TVAL3_API tval3_status tval3_op_shape(tval3_op op, int* rows, int* cols, int64_t* nnz);
+/* Device memory the operator kept from its creation (matrix storage, the
+ * transposed copy, tile layouts, geometry tables); layouts that a solver
+ * builds later on first use are not included. */
+TVAL3_API tval3_status tval3_op_device_bytes(tval3_op op, int64_t* bytes);
 /* Copy the device CSR (A and A^T) of a stored operator to host arrays
  * (ptr: rows+1 / cols+1 ints, ind: nnz ints, val: nnz floats); any pointer may
  * be NULL to skip that array.  Values are FP32 (dequantised for the 16-bit

@@ -125,26 +125,83 @@ def test_double_float_products(cuda, oracle):
     assert np.linalg.norm(Aty - ref_Aty) <= 1e-12 * np.linalg.norm(ref_Aty)
 
 
-def test_on_the_fly_bresenham_matches_csr(cuda, oracle):
-    """On-the-fly traversal (dyn_calc_kernel's mode) equals the stored CSR
-    product: A x within FP32 summation order, A^T y (atomic scatter) likewise."""
+def _box_geometry(nx, ny, nz, ne, nr, seed):
+    """Transducers on the ellipsoid inscribed in an nx x ny x nz box, 80 % of
+    the pairs in use, scale factor 0.5."""
+    from tval3_gb300.api import Geometry
+    rng = np.random.default_rng(seed)
+    half = np.array([nx, ny, nz], dtype=np.float64) / 2.0
+
+    def pts(k):
+        u = rng.normal(size=(k, 3))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        return half + 0.98 * half * u
+
+    em, rc = pts(ne), pts(nr)
+    dims = (nx, ny, nz)
+    ie = [np.clip(np.floor(em[:, a]), 0, dims[a] - 1).astype(np.int32) for a in range(3)]
+    ir = [np.clip(np.floor(rc[:, a]), 0, dims[a] - 1).astype(np.int32) for a in range(3)]
+    use = (rng.random(ne * nr) < 0.8).astype(np.uint32)
+    return Geometry(rv_x=nx, rv_y=ny, rv_z=nz, x_emitters=ie[0], y_emitters=ie[1], z_emitters=ie[2],
+                    x_receivers=ir[0], y_receivers=ir[1], z_receivers=ir[2], num_emitters=ne, num_receivers=nr,
+                    numMPs=1, use_path=use, scale_factor=0.5, traversal=1,
+                    pos=tuple(em[:, a].copy() for a in range(3)) + tuple(rc[:, a].copy() for a in range(3)))
+
+
+@pytest.mark.parametrize("which", ["hemi", "ring", "odd"])
+@pytest.mark.parametrize("traversal", [0, 1])
+def test_on_the_fly_matches_oracle(cuda, oracle, which, traversal):
+    """On-the-fly traversal (Bresenham: dyn_calc_kernel's mode; Siddon: the
+    builder's FP64 walk per ray) against the oracle's products of its CSR:
+    A x and A^T y within FP32 summation order, the adjoint identity
+    <Ax, y> = <x, A^T y>, the implied matrix's nonzero count, the stored CSR
+    operator's products, and A^T y (tile runs summed in a fixed order)
+    bit-identical over repeats.  Volumes: 40^3 hemisphere (8^3 tiles, partial
+    edge tiles), 64^2 ring (16^2 tiles) and 33 x 17 x 9 (ragged tiles)."""
     torch = _torch()
     from tval3_gb300 import Operator
-    cfg, geo, _ = _small_3d(40, 48)
-    geo = geo.with_traversal(0)
-    ptr, ind, val = oracle.bresenham_csr(geo)
-    tptr, tind, tval = oracle.transpose(ptr.size - 1, 40 ** 3, ptr, ind, val)
+    from tval3_gb300 import workloads as W
+    if which == "hemi":
+        geo = _small_3d(40, 48)[1]
+    elif which == "ring":
+        geo = W.ring_geometry(64, 128)
+    else:
+        geo = _box_geometry(33, 17, 9, 24, 20, seed=2)
+    geo = geo.with_traversal(traversal)
+    ptr, ind, val = oracle.bresenham_csr(geo) if traversal == 0 else oracle.siddon_csr(geo)
     op = Operator.from_geometry(geo, mode=1)
+    n = op.cols
+    assert op.nnz == ind.size
+    tptr, tind, tval = oracle.transpose(ptr.size - 1, n, ptr, ind, val)
     x, y = _vecs(torch, op, torch.float32)
+    x32, y32 = x.float(), y.float()
     Ax = torch.empty(op.rows, device=cuda)
-    Aty = torch.empty(op.cols, device=cuda)
-    op.mat_vec_mul(0, x.to(cuda, torch.float32), Ax)
-    op.mat_vec_mul(1, y.to(cuda, torch.float32), Aty)
+    Aty = torch.empty(n, device=cuda)
+    op.mat_vec_mul(0, x32.to(cuda), Ax)
+    op.mat_vec_mul(1, y32.to(cuda), Aty)
     torch.cuda.synchronize()
-    ref_Ax = oracle.spmv(ptr, ind, val, x.numpy())
-    ref_Aty = oracle.spmv(tptr, tind, tval, y.numpy())
-    assert np.linalg.norm(Ax.double().cpu().numpy() - ref_Ax) <= 1e-5 * np.linalg.norm(ref_Ax)
-    assert np.linalg.norm(Aty.double().cpu().numpy() - ref_Aty) <= 1e-5 * np.linalg.norm(ref_Aty)
+    ref_Ax = oracle.spmv(ptr, ind, val, x32.double().numpy())
+    ref_Aty = oracle.spmv(tptr, tind, tval, y32.double().numpy())
+    Axn, Atyn = Ax.double().cpu().numpy(), Aty.double().cpu().numpy()
+    assert np.linalg.norm(Axn - ref_Ax) <= 1e-5 * np.linalg.norm(ref_Ax)
+    assert np.linalg.norm(Atyn - ref_Aty) <= 1e-5 * np.linalg.norm(ref_Aty)
+    # empty rows and columns are exact zeros
+    assert np.all(Axn[np.diff(ptr) == 0] == 0) and np.all(Atyn[np.diff(tptr) == 0] == 0)
+    lhs, rhs = float(np.dot(Axn, y32.double().numpy())), float(np.dot(x32.double().numpy(), Atyn))
+    assert abs(lhs - rhs) <= 1e-5 * np.linalg.norm(Axn) * np.linalg.norm(y32.double().numpy())
+    # the stored CSR operator of the same geometry gives the same products
+    st = Operator.from_geometry(geo, mode=0)
+    Ax2 = torch.empty_like(Ax)
+    Aty2 = torch.empty_like(Aty)
+    st.mat_vec_mul(0, x32.to(cuda), Ax2)
+    st.mat_vec_mul(1, y32.to(cuda), Aty2)
+    for _ in range(3):
+        again = torch.empty_like(Aty)
+        op.mat_vec_mul(1, y32.to(cuda), again)
+        torch.cuda.synchronize()
+        assert torch.equal(again, Aty)
+    assert torch.allclose(Ax2, Ax, rtol=1e-5, atol=1e-5 * float(Ax.abs().max()))
+    assert torch.allclose(Aty2, Aty, rtol=1e-5, atol=1e-5 * float(Aty.abs().max()))
 
 
 @pytest.mark.parametrize("dims", [(7, 5, 3), (64, 64, 1), (33, 17, 9)])

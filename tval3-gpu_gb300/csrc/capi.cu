@@ -26,6 +26,7 @@ struct tval3_op_s {
     // double-float products: a view of d (TVAL3_PREC_FP32_DF64), or an
     // operator of its own with 16-bit storage and d null (BF16_DF64, FP16_DF64)
     LinOp<df64>* q = nullptr;
+    long long device_bytes = 0;  // device memory its creation kept
     ~tval3_op_s() {
         delete q;
         delete f;
@@ -538,9 +539,9 @@ tval3_status tval3_gpu_3d_geometry_f32(float* U, int dim_y, int dim_x, int dim_z
         if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
         if (A->rv_y != dim_y || A->rv_x != dim_x || A->rv_z != dim_z)
             arg_error(TVAL3_ERR_SHAPE, "Argument error: the volume of U must equal the geometry's rv_y x rv_x x rv_z!");
-        // the reference evaluates this overload on the fly (geom_mm_multGPU); Bresenham runs on the fly here too
-        const int mode = (A->traversal == TVAL3_TRAVERSAL_BRESENHAM) ? 1 : 0;
-        LinOp<float>* op = make_geometry_op<float>(A, mode, TVAL3_PREC_FP32, 0);
+        // the reference evaluates this overload on the fly (geom_mm_multGPU): no matrix is stored, for
+        // Bresenham and Siddon rays alike
+        LinOp<float>* op = make_geometry_op<float>(A, 1, TVAL3_PREC_FP32, 0);
         try {
             check_problem(U, dim_y, dim_x, dim_z, op->m, op->n, b, b_len, Ut, Ut_len);
         } catch (...) {
@@ -642,6 +643,7 @@ tval3_status tval3_op_create_sparse(tval3_op* op, const tval3_sparse_host* A, in
     return guard([&] {
         if (!op) arg_error(TVAL3_ERR_ARG, "Argument error: op is NULL!");
         if (precision < 0 || precision > 7) arg_error(TVAL3_ERR_ARG, "Argument error: unknown precision!");
+        const long long b0 = dbuf_live_bytes;
         auto* h = new tval3_op_s();
         try {
             h->precision = precision;
@@ -662,6 +664,7 @@ tval3_status tval3_op_create_sparse(tval3_op* op, const tval3_sparse_host* A, in
             delete h;
             throw;
         }
+        h->device_bytes = dbuf_live_bytes - b0;
         *op = h;
     });
 }
@@ -673,6 +676,7 @@ tval3_status tval3_op_create_sparse_device(tval3_op* op, int rows, int cols, int
         if (rows < 0 || cols < 0 || nnz < 0 || !d_ptr) arg_error(TVAL3_ERR_ARG, "Argument error: bad device CSR!");
         if (precision == TVAL3_PREC_FP64 || precision < 0 || precision > 3)
             arg_error(TVAL3_ERR_UNSUPPORTED, "device CSR input takes FP32 values (FP32/BF16/FP16 storage)");
+        const long long b0 = dbuf_live_bytes;
         auto* h = new tval3_op_s();
         try {
             h->precision = precision;
@@ -682,6 +686,7 @@ tval3_status tval3_op_create_sparse_device(tval3_op* op, int rows, int cols, int
             delete h;
             throw;
         }
+        h->device_bytes = dbuf_live_bytes - b0;
         *op = h;
     });
 }
@@ -694,6 +699,7 @@ tval3_status tval3_op_create_geometry(tval3_op* op, const tval3_geometry_host* G
             arg_error(TVAL3_ERR_UNSUPPORTED, "geometry operators store FP32/BF16/FP16 values");
         if (mode == 1 && precision != TVAL3_PREC_FP32)
             arg_error(TVAL3_ERR_UNSUPPORTED, "on-the-fly traversal stores nothing; use FP32");
+        const long long b0 = dbuf_live_bytes;
         auto* h = new tval3_op_s();
         try {
             h->precision = precision;
@@ -717,6 +723,7 @@ tval3_status tval3_op_create_geometry(tval3_op* op, const tval3_geometry_host* G
             delete h;
             throw;
         }
+        h->device_bytes = dbuf_live_bytes - b0;
         *op = h;
     });
 }
@@ -726,6 +733,7 @@ tval3_status tval3_op_create_dense(tval3_op* op, const tval3_dense_host* A, int 
         if (!op || !A || !A->data || A->rows < 0 || A->cols < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad dense matrix!");
         if (precision == TVAL3_PREC_FP16 || precision < 0 || precision > 3)
             arg_error(TVAL3_ERR_UNSUPPORTED, "dense storage: FP32, FP64 or BF16");
+        const long long b0 = dbuf_live_bytes;
         auto* h = new tval3_op_s();
         try {
             h->precision = precision;
@@ -739,6 +747,7 @@ tval3_status tval3_op_create_dense(tval3_op* op, const tval3_dense_host* A, int 
             delete h;
             throw;
         }
+        h->device_bytes = dbuf_live_bytes - b0;
         *op = h;
     });
 }
@@ -753,6 +762,13 @@ tval3_status tval3_op_shape(tval3_op op, int* rows, int* cols, int64_t* nnz) {
         if (rows) *rows = (int)op->rows();
         if (cols) *cols = (int)op->cols();
         if (nnz) *nnz = op->nnz();
+    });
+}
+
+tval3_status tval3_op_device_bytes(tval3_op op, int64_t* bytes) {
+    return guard([&] {
+        if (!op || !bytes) arg_error(TVAL3_ERR_ARG, "Argument error: op or bytes is NULL!");
+        *bytes = op->device_bytes;
     });
 }
 

@@ -14,6 +14,10 @@ namespace tv3 {
 
 void tmp_pool_init();
 
+// bytes of DBuf memory allocated and not yet released by the calling thread
+// (the operator entry points report their creation's growth of it)
+inline thread_local long long dbuf_live_bytes = 0;
+
 template <class T>
 struct DBuf {
     T* p = nullptr;
@@ -30,6 +34,7 @@ struct DBuf {
             TV3_CUDA(cudaStreamSynchronize(0));
             p = static_cast<T*>(q);
             n = n_;
+            dbuf_live_bytes += (long long)(n_ * sizeof(T));
         }
     }
     void view(T* q, size_t n_) {
@@ -42,6 +47,7 @@ struct DBuf {
         if (p && own) {
             cudaDeviceSynchronize();
             cudaFreeAsync(p, 0);
+            dbuf_live_bytes -= (long long)(n * sizeof(T));
         }
         p = nullptr;
         n = 0;
@@ -85,6 +91,7 @@ struct TmpBuf {
             TV3_CUDA(cudaMallocAsync(&q, n_ * sizeof(T), 0));
             p = static_cast<T*>(q);
             n = n_;
+            dbuf_live_bytes += (long long)(n_ * sizeof(T));
         }
     }
     void release() {

@@ -474,11 +474,26 @@ void set_smem_attr(size_t smem) {
 template <class T, class V>
 void TiledT<T, V>::build(long n_, long m, int p, int q, int r, const int* tptr, const int* tind, const V* tval,
                          long nnz, size_t max_smem, cudaStream_t s) {
+    // tile shapes, largest first: 8 x 8 x 8 voxels in 3D (16 x 16 in 2D); a
+    // volume crossed by so many rays that a tile's ray list overflows shared
+    // memory takes smaller tiles (fewer rays cross each)
+    static const int shapes3[][3] = {{8, 8, 8}, {8, 8, 4}, {4, 4, 4}, {4, 4, 2}};
+    static const int shapes2[][3] = {{16, 16, 1}, {8, 8, 1}, {4, 4, 1}};
+    const bool flat = r <= 1;
+    const int ns = flat ? 3 : 4;
+    for (int i = 0; i < ns && !ok; ++i) {
+        const int* sh = flat ? shapes2[i] : shapes3[i];
+        build_shape(n_, m, p, q, r, tptr, tind, tval, nnz, max_smem, s, sh[0], sh[1], sh[2]);
+    }
+}
+
+template <class T, class V>
+void TiledT<T, V>::build_shape(long n_, long m, int p, int q, int r, const int* tptr, const int* tind, const V* tval,
+                               long nnz, size_t max_smem, cudaStream_t s, int ty0, int tx0, int tz0) {
     ok = false;
     n = n_;
     if (nnz <= 0 || n <= 0 || m <= 0 || (long)p * q * r != n || nnz >= (1L << 31)) return;
-    // tile shape: 8 x 8 x 8 voxels in 3D, 16 x 16 in 2D
-    const int ty = std::min(p, r > 1 ? 8 : 16), tx = std::min(q, r > 1 ? 8 : 16), tz = std::min(r, 8);
+    const int ty = std::min(p, ty0), tx = std::min(q, tx0), tz = std::min(r, tz0);
     const int nty = (p + ty - 1) / ty, ntx = (q + tx - 1) / tx, ntz = (r + tz - 1) / tz;
     const long nt = (long)nty * ntx * ntz;
     if (nt >= (1L << 24) || (long)ty * tx * tz > 512) return;  // the kernel gives each row of a tile one thread

@@ -68,10 +68,13 @@ struct TiledT {
     DBuf<unsigned short> lidx;
     DBuf<V> val;
     // build from the CSR of A^T (n voxel rows, ray indices < m) of a p x q x r
-    // volume; leaves ok = false when some tile's ray list exceeds max_smem
-    // bytes of T or 65,535 entries
+    // volume; leaves ok = false when, with the smallest tiles, some tile's ray
+    // list exceeds max_smem bytes of T or 65,535 entries
     void build(long n, long m, int p, int q, int r, const int* tptr, const int* tind, const V* tval, long nnz,
                size_t max_smem, cudaStream_t s);
+    // one attempt with tiles of ty x tx x tz voxels (clipped to the volume)
+    void build_shape(long n, long m, int p, int q, int r, const int* tptr, const int* tind, const V* tval, long nnz,
+                     size_t max_smem, cudaStream_t s, int ty, int tx, int tz);
     void apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) const;
     // pipelined form: one CTA per SM; a producer warp gathers the next tile's
     // y values (bulk copy of the ray list, then asynchronous copies) while 31

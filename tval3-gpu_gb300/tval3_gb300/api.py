@@ -302,6 +302,13 @@ class Operator:
     def handle(self):
         return self._h
 
+    @property
+    def device_bytes(self) -> int:
+        """Device memory the operator kept from its creation."""
+        z = C.c_int64()
+        check(load().tval3_op_device_bytes(self._h, C.byref(z)))
+        return z.value
+
     def mat_vec_mul(self, trans: int, x, y, stream=None) -> None:
         check(load().tval3_mat_vec_mul(self._h, int(trans), _ptr(x), _ptr(y), _stream(stream)))
 

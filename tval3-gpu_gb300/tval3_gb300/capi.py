@@ -99,6 +99,7 @@ _SIG = {
     "tval3_op_create_dense": (_I, [_P, _P, _I]),
     "tval3_op_destroy": (_I, [_P]),
     "tval3_op_shape": (_I, [_P, _P, _P, _P]),
+    "tval3_op_device_bytes": (_I, [_P, _P]),
     "tval3_op_export_csr": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "tval3_op_export_csr_scaled": (_I, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "tval3_mat_vec_mul": (_I, [_P, _I, _P, _P, _P]),
