@@ -175,8 +175,11 @@ TVAL3_API const char* tval3_last_error_message(void);
  * checks, upload, transpose or quantisation, ray-matrix build), [1] set-up
  * (b upload, solver workspace, tile-staged layouts and kernel choice), [2]
  * solve (graph capture and instantiation on first use, then the solve), [3]
- * download of U.  n entries are written (at most 4).  No counterpart in the
- * reference. */
+ * download of U; then parts of those: [4] matrix upload, [5] input
+ * validation, [6] operator layout (device copies, transpose, quantisation,
+ * ray-matrix build), [7] tile-staged layouts and kernel choice, [8] graph
+ * capture and instantiation.  n entries are written (at most 9).  No
+ * counterpart in the reference. */
 TVAL3_API tval3_status tval3_last_call_phases(double* secs, int n);
 TVAL3_API const char* tval3_version(void);
 

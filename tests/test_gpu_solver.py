@@ -206,6 +206,27 @@ def test_geometry_siddon_on_the_fly_solve(cuda, oracle, iso):
     assert np.linalg.norm(U1 - Uo64) <= 0.2 * np.linalg.norm(Uo64)
 
 
+def test_entry_phases_reported(cuda, oracle):
+    """tval3_last_call_phases after a host entry call: nine non-negative
+    figures; the upload, validation and layout parts fit inside the operator
+    phase, the tile and graph parts inside set-up plus solve, and the four
+    main phases inside the call's wall time."""
+    import time
+    from tval3_gb300 import SparseMatrix, tval3_gpu_3d
+    from tval3_gb300.api import last_call_phases
+    geo, x, ptr, ind, val, b = _problem(oracle, 64, 128, seed=0)
+    A = SparseMatrix(ptr.size - 1, x.size, ptr, ind, val)
+    t0 = time.perf_counter()
+    tval3_gpu_3d((64, 64, 1), A, b, dict(OPTS, maxit=20))
+    wall = time.perf_counter() - t0
+    ph = last_call_phases()
+    assert len(ph) == 9 and all(v >= 0.0 for v in ph.values())
+    main = ph["operator_s"] + ph["setup_s"] + ph["solve_s"] + ph["download_s"]
+    assert 0.0 < main <= wall
+    assert ph["upload_s"] + ph["validate_s"] + ph["layout_s"] <= ph["operator_s"] + 1e-6
+    assert ph["tiles_s"] + ph["graph_s"] <= ph["setup_s"] + ph["solve_s"] + 1e-6
+
+
 def test_dense_entry_points(cuda, oracle):
     from tval3_gb300 import DenseMatrix, tval3_gpu
     geo, x, ptr, ind, val, b = _problem(oracle)

@@ -75,6 +75,12 @@ thread_local std::string g_err;
 // set-up (b upload, solver workspace, tile-staged layouts and kernel choice),
 // solve (graph capture on first use, then the solve), download of U
 thread_local double g_phase[4] = {0, 0, 0, 0};
+// start of a host entry call: clears the phase records
+std::chrono::steady_clock::time_point entry_clock() {
+    for (double& v : sub_phase) v = 0.0;
+    for (double& v : g_phase) v = 0.0;
+    return std::chrono::steady_clock::now();
+}
 
 tval3_status fail(int st, const std::string& msg) {
     g_err = msg;
@@ -228,6 +234,7 @@ struct F32Csr {
 
 void upload_f32(const tval3_sparse_host* A, bool dev_check, F32Csr& c) {
     const long m = A->rows, n = A->cols, nnz = A->nnz;
+    std::unique_ptr<PhaseTimer> up(new PhaseTimer(0));
     if (A->format & TVAL3_SPARSE_CSR) {
         c.ptr.alloc(m + 1);
         c.ind.alloc(std::max<long>(nnz, 1));
@@ -242,6 +249,8 @@ void upload_f32(const tval3_sparse_host* A, bool dev_check, F32Csr& c) {
         if (nnz) TV3_CUDA(cudaMemcpy(c.tind.p, A->csc_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
         to_device(c.tval, A->csc_val, nnz, A->val_type);
     }
+    up.reset();
+    PhaseTimer pv(1);
     if (dev_check) {
         if (A->format & TVAL3_SPARSE_CSR) validate_device<float>(c.ptr.p, m, c.ind.p, c.val.p, nnz, n, "CSR");
         if (A->format & TVAL3_SPARSE_CSC) validate_device<float>(c.tptr.p, n, c.tind.p, c.tval.p, nnz, m, "CSC");
@@ -262,6 +271,7 @@ LinOp<df64>* sparse_op_mixed(const tval3_sparse_host* A, int precision) {
     check_sparse(A, !dev_check);
     F32Csr c;
     upload_f32(A, dev_check, c);
+    PhaseTimer pl(2);
     return make_csr_op_df64q(A->rows, A->cols, A->nnz, c.ptr.p, c.ind.p, c.val.p, c.tptr.p,
                              c.tptr.p ? c.tind.p : nullptr, c.tptr.p ? c.tval.p : nullptr, precision, 0);
 }
@@ -282,6 +292,7 @@ LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision, bool tune = true)
         if (precision == TVAL3_PREC_FP32_F64VEC && A->val_type == TVAL3_PREC_FP32) {
             F32Csr c;
             upload_f32(A, dev_check, c);
+            PhaseTimer pl(2);
             return make_csr_op_f64vec(m, n, nnz, c.ptr.p, c.ind.p, c.val.p, c.tptr.p, c.tptr.p ? c.tind.p : nullptr,
                                       c.tptr.p ? c.tval.p : nullptr, 0, tune);
         }
@@ -289,6 +300,7 @@ LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision, bool tune = true)
     DBuf<int> ptr, ind, tptr, tind;
     DBuf<T> val, tval;
     cudaStream_t s = 0;
+    std::unique_ptr<PhaseTimer> up(new PhaseTimer(0));
     if (A->format & TVAL3_SPARSE_CSR) {
         ptr.alloc(m + 1);
         ind.alloc(std::max<long>(nnz, 1));
@@ -303,10 +315,13 @@ LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision, bool tune = true)
         if (nnz) TV3_CUDA(cudaMemcpy(tind.p, A->csc_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
         to_device(tval, A->csc_val, nnz, A->val_type);
     }
+    up.reset();
     if (dev_check) {
+        PhaseTimer pv(1);
         if (A->format & TVAL3_SPARSE_CSR) validate_device<T>(ptr.p, m, ind.p, val.p, nnz, n, "CSR");
         if (A->format & TVAL3_SPARSE_CSC) validate_device<T>(tptr.p, n, tind.p, tval.p, nnz, m, "CSC");
     }
+    PhaseTimer pl(2);
     if (!(A->format & TVAL3_SPARSE_CSR)) {
         // only CSC given: its transpose is the CSR of A
         ptr.alloc(m + 1);
@@ -435,6 +450,7 @@ tval3_status tval3_last_call_phases(double* secs, int n) {
     return guard([&] {
         if (!secs || n < 0) arg_error(TVAL3_ERR_ARG, "Argument error: NULL phase array!");
         for (int i = 0; i < n && i < 4; ++i) secs[i] = g_phase[i];
+        for (int i = 4; i < n && i < 9; ++i) secs[i] = sub_phase[i - 4];
     });
 }
 const char* tval3_version(void) { return "tval3-gb300 0.1 (sm_103a)"; }
@@ -443,7 +459,7 @@ tval3_status tval3_gpu_3d_sparse_f32(float* U, int dim_y, int dim_x, int dim_z, 
                                      const float* b, int b_len, const tval3_options* opts, const float* Ut,
                                      int Ut_len, int, int, int, const int*, tval3_info* info) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         check_opts(opts);
         if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
         check_problem(U, dim_y, dim_x, dim_z, A->rows, A->cols, b, b_len, Ut, Ut_len);
@@ -456,7 +472,7 @@ tval3_status tval3_gpu_3d_sparse_f64(double* U, int dim_y, int dim_x, int dim_z,
                                      const double* b, int b_len, const tval3_options* opts, const double* Ut,
                                      int Ut_len, int, int, int, const int*, tval3_info* info) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         check_opts(opts);
         if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
         check_problem(U, dim_y, dim_x, dim_z, A->rows, A->cols, b, b_len, Ut, Ut_len);
@@ -482,7 +498,7 @@ tval3_status tval3_gpu_3d_sparse_f64(double* U, int dim_y, int dim_x, int dim_z,
 tval3_status tval3_gpu_sparse(float* U, int rows, int cols, const tval3_sparse_host* A, const float* b, int b_len,
                               const tval3_options* opts, const float* Ut, int Ut_len, int, tval3_info* info) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         check_opts(opts);
         if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
         const int layers = check_problem_2d(U, rows, cols, A->rows, A->cols, b, b_len, Ut, Ut_len);
@@ -495,7 +511,7 @@ tval3_status tval3_gpu_3d_dense_f32(float* U, int dim_y, int dim_x, int dim_z, c
                                     const float* b, int b_len, const tval3_options* opts, const float* Ut,
                                     int Ut_len, int, int, int, const int*, tval3_info* info) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         check_opts(opts);
         if (!A || !A->data || A->rows < 0 || A->cols < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad dense matrix!");
         check_problem(U, dim_y, dim_x, dim_z, A->rows, A->cols, b, b_len, Ut, Ut_len);
@@ -508,7 +524,7 @@ tval3_status tval3_gpu_3d_dense_f64(double* U, int dim_y, int dim_x, int dim_z, 
                                     const double* b, int b_len, const tval3_options* opts, const double* Ut,
                                     int Ut_len, int, int, int, const int*, tval3_info* info) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         check_opts(opts);
         if (!A || !A->data || A->rows < 0 || A->cols < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad dense matrix!");
         check_problem(U, dim_y, dim_x, dim_z, A->rows, A->cols, b, b_len, Ut, Ut_len);
@@ -520,7 +536,7 @@ tval3_status tval3_gpu_3d_dense_f64(double* U, int dim_y, int dim_x, int dim_z, 
 tval3_status tval3_gpu_dense(float* U, int rows, int cols, const tval3_dense_host* A, const float* b, int b_len,
                              const tval3_options* opts, const float* Ut, int Ut_len, int, tval3_info* info) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         check_opts(opts);
         if (!A || !A->data || A->rows < 0 || A->cols < 0) arg_error(TVAL3_ERR_ARG, "Argument error: bad dense matrix!");
         const int layers = check_problem_2d(U, rows, cols, A->rows, A->cols, b, b_len, Ut, Ut_len);
@@ -534,7 +550,7 @@ tval3_status tval3_gpu_3d_geometry_f32(float* U, int dim_y, int dim_x, int dim_z
                                        const float* b, int b_len, const tval3_options* opts, const float* Ut,
                                        int Ut_len, int, int, int, const int*, tval3_info* info) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         check_opts(opts);
         if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
         if (A->rv_y != dim_y || A->rv_x != dim_x || A->rv_z != dim_z)
@@ -557,7 +573,7 @@ tval3_status tval3_gpu_3d_geometry_sparse_f32(float* U, int dim_y, int dim_x, in
                                               const float* b, int b_len, const tval3_options* opts, const float* Ut,
                                               int Ut_len, int, int, int, const int*, tval3_info* info) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         check_opts(opts);
         if (!A_geo || !A_mat) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
         check_problem(U, dim_y, dim_x, dim_z, A_mat->rows, A_mat->cols, b, b_len, Ut, Ut_len);
@@ -574,7 +590,7 @@ tval3_status tval3_gpu_3d_geometry_f64(double* U, int dim_y, int dim_x, int dim_
                                        const double* b, int b_len, const tval3_options* opts, const double* Ut,
                                        int Ut_len, int, int, int, const int*, tval3_info* info) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         check_opts(opts);
         if (!A) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
         if (A->rv_y != dim_y || A->rv_x != dim_x || A->rv_z != dim_z)
@@ -618,7 +634,7 @@ tval3_status tval3_gpu_3d_geometry_sparse_f64(double* U, int dim_y, int dim_x, i
                                               const double* Ut, int Ut_len, int, int, int, const int*,
                                               tval3_info* info) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         check_opts(opts);
         if (!A_geo || !A_mat) arg_error(TVAL3_ERR_ARG, "Argument error: A is NULL!");
         if (A_geo->rv_y != dim_y || A_geo->rv_x != dim_x || A_geo->rv_z != dim_z)
@@ -1120,7 +1136,7 @@ tval3_status tval3_batch_destroy(tval3_batch batch) {
 tval3_status tval3_gpu_batched(const tval3_slice_host* slices, int count, const tval3_options* opts,
                                tval3_info* infos) {
     return guard([&] {
-        auto t0 = std::chrono::steady_clock::now();
+        auto t0 = entry_clock();
         if (!slices || count <= 0) arg_error(TVAL3_ERR_ARG, "Argument error: empty batch!");
         check_opts(opts);
         for (int i = 0; i < count; ++i) {

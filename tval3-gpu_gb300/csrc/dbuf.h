@@ -91,7 +91,6 @@ struct TmpBuf {
             TV3_CUDA(cudaMallocAsync(&q, n_ * sizeof(T), 0));
             p = static_cast<T*>(q);
             n = n_;
-            dbuf_live_bytes += (long long)(n_ * sizeof(T));
         }
     }
     void release() {

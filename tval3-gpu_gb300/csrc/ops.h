@@ -5,12 +5,28 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <chrono>
 #include <memory>
 #include <string>
 #include "launch.h"
 #include "tval3_internal.cuh"
 
 namespace tv3 {
+
+// Seconds spent in the parts of the last host entry call on this thread:
+// [0] matrix upload, [1] input validation, [2] operator layout (copies,
+// transposes, quantisation, ray-matrix build), [3] tile layouts and kernel
+// choice, [4] graph capture and instantiation.  Entry points reset it; a
+// PhaseTimer adds the wall time of its scope.
+inline thread_local double sub_phase[5] = {0, 0, 0, 0, 0};
+struct PhaseTimer {
+    int k;
+    std::chrono::steady_clock::time_point t0;
+    explicit PhaseTimer(int k_) : k(k_), t0(std::chrono::steady_clock::now()) {}
+    ~PhaseTimer() {
+        sub_phase[k] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
 
 template <class T> struct LinOp;
 // column-major k-column product through one interleaved multi-RHS apply (ops.cu)

@@ -64,6 +64,7 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
         throw Error{TVAL3_ERR_UNSUPPORTED, "voxels x layers exceeds the 32-bit index range of the stencil kernels"};
     A->prepare(L);
     if (L == 1) {
+        PhaseTimer pt(3);
         A->set_volume(p_, q_, r_);
         A->ready();
     }
@@ -433,6 +434,7 @@ void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const 
 
 template <class T>
 void Solver<T>::build_graph(const void* d_b, void* d_U, const void* d_Ut, cudaStream_t s) {
+    PhaseTimer pg(4);
     if (gexec) {
         cudaGraphExecDestroy(gexec);
         gexec = nullptr;

@@ -234,10 +234,14 @@ def tval3_gpu_3d(shape, A, b, opts=None, Ut=None, *, dtype=np.float32, pagelocke
 
 def last_call_phases() -> dict:
     """Seconds of the phases of this thread's last reference entry-point
-    call: operator, setup, solve, download (tval3_last_call_phases)."""
-    out = (C.c_double * 4)()
-    check(load().tval3_last_call_phases(out, 4))
-    return dict(zip(("operator_s", "setup_s", "solve_s", "download_s"), list(out)))
+    call: operator, setup, solve, download, and inside them the matrix
+    upload, validation, operator layout, tile layouts + kernel choice and
+    graph build (tval3_last_call_phases)."""
+    names = ("operator_s", "setup_s", "solve_s", "download_s", "upload_s", "validate_s", "layout_s", "tiles_s",
+             "graph_s")
+    out = (C.c_double * len(names))()
+    check(load().tval3_last_call_phases(out, len(names)))
+    return dict(zip(names, list(out)))
 
 
 def tval3_gpu(shape, A, b, opts=None, Ut=None, pagelocked=True):
