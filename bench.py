@@ -94,6 +94,9 @@ def parse():
                     help="right-hand sides of the dense multi-RHS leg (0 skips it); printed under 'dense_multi_rhs'")
     ap.add_argument("--only-dense", action="store_true", help="run only the dense multi-RHS products (development)")
     ap.add_argument("--no-fly", action="store_true", help="skip the on-the-fly operator's product timing")
+    ap.add_argument("--pin-tiled", action="store_true",
+                    help="pin the tile-staged kernels of both products (profiling runs, where the build-time "
+                         "timing under a profiler may pick others)")
     ap.add_argument("--only-fly", action="store_true", help="time only the on-the-fly products (development)")
     ap.add_argument("--solver-mode", type=int, default=1,
                     help="1: whole solve as one CUDA graph; 0: host-driven loop (same kernels; profilers "
@@ -317,6 +320,12 @@ def run_ours(args):
     for name, prec, dt in modes:
         op = op32 if prec == T.PREC_FP32 else T.Operator.from_geometry(geo, mode=0, precision=prec)
         ops[name] = op
+        if args.pin_tiled:
+            for trans in (0, 1):
+                try:
+                    op.set_variant(trans, 1)
+                except T.Tval3Error:
+                    pass
         s = T.Solver(op, dims, cfg.opts, mode=args.solver_mode)
         xs_t = xs_dev.to(dt)
         s.set_trace(xs_t)

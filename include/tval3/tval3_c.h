@@ -453,6 +453,53 @@ TVAL3_API tval3_status tval3_shrink_adjoint_f64(int64_t n, const double* d_v, do
                                                 double* d_gv, double* d_gt, void* stream);
 
 /* ---------------------------------------------------------------------- *
+ * One differentiable inner step of the TVAL3 u-subproblem and its adjoint
+ * (the autograd path; the reference's inner iteration,
+ * 3d/tval3_gpu_3d.cpp:823-1029, without the discrete Armijo decision):
+ *   DU = D U, W = shrink(DU - sigma/beta, 1/beta),
+ *   g2 = D^T (DU - W - sigma/beta), g = A^T (A U - b - delta/mu),
+ *   d = g2 + (mu/beta) g, tau = |<s,s>/<s,y>| with s = U - Up,
+ *   y = g2 - g2p + (mu/beta)(g - gp)   (first = 1: tau = |<d,d> /
+ *   (||D d||^2 + (mu/beta)||A d||^2)|, and Up, gp, g2p are not read),
+ *   Un = max(U - tau d, 0) (nonneg) or U - tau d.
+ * Device vectors: U, Up, gp, g2p, Un, g, g2 (dim_y*dim_x*dim_z), b, delta
+ * (op rows), sigma (3 volumes); sigma and delta may be NULL (zero).  mub is
+ * a device array {mu, beta}.  op's products must take the entry point's
+ * vector type (an FP32 operator for _f32, FP64 vectors for _f64).
+ * The adjoint takes the adjoints gUn, gg, gg2 of the outputs (any NULL =
+ * zero), recomputes the step's intermediates from the same inputs, and
+ * writes the adjoints of U, Up, gp, g2p (NULL to skip; not written for the
+ * first step), b (NULL to skip) and {mu, beta} (device array of 2, NULL to
+ * skip).  All work is queued on `stream`; scratch comes from the
+ * stream-ordered pool.
+ * ---------------------------------------------------------------------- */
+TVAL3_API tval3_status tval3_unroll_step_f32(tval3_op op, int dim_y, int dim_x, int dim_z, int first, int iso,
+                                             int nonneg, const double* d_mub, const float* d_U, const float* d_Up,
+                                             const float* d_gp, const float* d_g2p, const float* d_b,
+                                             const float* d_sigma, const float* d_delta, float* d_Un, float* d_g,
+                                             float* d_g2, void* stream);
+TVAL3_API tval3_status tval3_unroll_step_f64(tval3_op op, int dim_y, int dim_x, int dim_z, int first, int iso,
+                                             int nonneg, const double* d_mub, const double* d_U, const double* d_Up,
+                                             const double* d_gp, const double* d_g2p, const double* d_b,
+                                             const double* d_sigma, const double* d_delta, double* d_Un,
+                                             double* d_g, double* d_g2, void* stream);
+TVAL3_API tval3_status tval3_unroll_step_adjoint_f32(tval3_op op, int dim_y, int dim_x, int dim_z, int first,
+                                                     int iso, int nonneg, const double* d_mub, const float* d_U,
+                                                     const float* d_Up, const float* d_gp, const float* d_g2p,
+                                                     const float* d_b, const float* d_sigma, const float* d_delta,
+                                                     const float* d_gUn, const float* d_gg, const float* d_gg2,
+                                                     float* d_gU, float* d_gUp, float* d_ggp, float* d_gg2p,
+                                                     float* d_gb, double* d_gmub, void* stream);
+TVAL3_API tval3_status tval3_unroll_step_adjoint_f64(tval3_op op, int dim_y, int dim_x, int dim_z, int first,
+                                                     int iso, int nonneg, const double* d_mub, const double* d_U,
+                                                     const double* d_Up, const double* d_gp, const double* d_g2p,
+                                                     const double* d_b, const double* d_sigma,
+                                                     const double* d_delta, const double* d_gUn,
+                                                     const double* d_gg, const double* d_gg2, double* d_gU,
+                                                     double* d_gUp, double* d_ggp, double* d_gg2p, double* d_gb,
+                                                     double* d_gmub, void* stream);
+
+/* ---------------------------------------------------------------------- *
  * Dense A^T*y without any device allocation (no counterpart in the
  * reference; same result as tval3_mat_vec_mul(trans = 1) on a dense FP32
  * operator up to summation order).  For callers that must not allocate

@@ -1,7 +1,10 @@
 """Autograd binding: the hand-written adjoints (A^T, D^T, shrinkage
-subgradient) pass torch.autograd.gradcheck and dot-product tests in FP64,
-and the gradient of a loss through K unrolled TVAL3 iterations with respect
-to b, mu and beta agrees with central finite differences (h = 1e-5, FP64)."""
+subgradient, and the whole inner step's tval3_unroll_step_adjoint) pass
+torch.autograd.gradcheck and dot-product tests in FP64; the gradient of a
+loss through K unrolled TVAL3 iterations (each one fused _InnerStep) with
+respect to b, mu and beta agrees with central finite differences (h = 1e-5,
+FP64) and with the same map composed from the single-operator Functions
+(the eager reference below, kept only here)."""
 import numpy as np
 import pytest
 
@@ -113,18 +116,94 @@ def test_unrolled_gradient_vs_finite_differences(cuda, oracle, size, rays, iters
         fd_beta = (loss(b, mu0, beta0 * (1 + h)) - loss(b, mu0, beta0 * (1 - h))) / (2 * h * beta0)
     an_b = float((bb.grad * v).sum())
     for an, fd in ((an_b, float(fd_b)), (float(mu.grad), float(fd_mu)), (float(beta.grad), float(fd_beta))):
-        assert abs(an - fd) <= 2e-3 * max(abs(fd), 1e-8 * float(L)), (an, fd)
+        assert abs(an - fd) <= 2e-3 * max(abs(fd), 1e-8 * float(L.detach())), (an, fd)
 
 
-def test_checkpointing_matches_plain(cuda, oracle):
+def _eager_unrolled(op, b, dims, mu, beta, iters, iso=True, nonneg=True, sigma=None, delta=None):
+    """The unrolled map composed from the single-operator Functions (A, At,
+    D, Dt, shrink) and PyTorch elementwise ops: the reference the fused
+    _InnerStep is checked against."""
+    import torch
+    from tval3_gb300 import autograd as AG
+    dt = b.dtype
+    n = dims[0] * dims[1] * dims[2]
+    sig = sigma if sigma is not None else torch.zeros(3 * n, dtype=dt, device=b.device)
+    dl = delta if delta is not None else torch.zeros(b.numel(), dtype=dt, device=b.device)
+    dot = lambda x, y: (x * y).sum()
+
+    def grad_dir(U):
+        DU = AG.D(U, dims)
+        W = AG.shrink(DU - sig / beta, 1.0 / beta, iso)
+        g = AG.At(op, AG.A(op, U) - b) - AG.At(op, dl) / mu
+        g2 = AG.Dt(DU - W, dims) - AG.Dt(sig, dims) / beta
+        return g2 + (mu / beta) * g, g, g2
+
+    U = AG.At(op, b)
+    Up = gp = g2p = None
+    for k in range(iters):
+        d, g, g2 = grad_dir(U)
+        if k == 0:
+            Dd, Ad = AG.D(d, dims), AG.A(op, d)
+            tau = torch.abs(dot(d, d) / (dot(Dd, Dd) + (mu / beta) * dot(Ad, Ad)))
+        else:
+            s_ = U - Up
+            tau = torch.abs(dot(s_, s_) / dot(s_, (g2 - g2p) + (mu / beta) * (g - gp)))
+        Un = U - tau * d
+        if nonneg:
+            Un = torch.relu(Un)
+        Up, gp, g2p, U = U, g, g2, Un
+    return U
+
+
+@pytest.mark.parametrize("iso", [True, False])
+def test_fused_step_matches_eager_reference(cuda, oracle, iso):
+    """U_K and the gradients wrt b, mu, beta of the fused map equal those of
+    the eager composition (FP64; only summation orders differ), with nonzero
+    multipliers sigma and delta."""
     import torch
     from tval3_gb300 import autograd as AG
     cfg, op, b, xt = _loss_setup(oracle, 12, 8, 6, cuda)
+    g = torch.Generator().manual_seed(7)
+    n = xt.numel()
+    sig = (0.05 * torch.randn(3 * n, dtype=torch.float64, generator=g)).to(cuda)
+    dl = (0.05 * torch.randn(b.numel(), dtype=torch.float64, generator=g)).to(cuda)
     outs = []
-    for ck in (True, False):
+    for fn in (AG.unrolled_tval3, _eager_unrolled):
         bb = b.clone().requires_grad_()
-        U = AG.unrolled_tval3(op, bb, cfg.dims, 512.0, 64.0, iters=6, use_checkpoint=ck)
+        mu = torch.tensor(512.0, dtype=torch.float64, device=cuda, requires_grad=True)
+        beta = torch.tensor(64.0, dtype=torch.float64, device=cuda, requires_grad=True)
+        U = fn(op, bb, cfg.dims, mu, beta, iters=6, iso=iso, sigma=sig, delta=dl)
         ((U - xt) ** 2).sum().backward()
-        outs.append((U.detach(), bb.grad))
-    assert torch.allclose(outs[0][0], outs[1][0], rtol=0, atol=0)
-    assert torch.allclose(outs[0][1], outs[1][1], rtol=1e-12, atol=1e-14)
+        outs.append((U.detach(), bb.grad, mu.grad, beta.grad))
+    (U1, gb1, gm1, gbt1), (U2, gb2, gm2, gbt2) = outs
+    assert torch.allclose(U1, U2, rtol=1e-10, atol=1e-12 * float(U2.abs().max()))
+    assert torch.allclose(gb1, gb2, rtol=1e-8, atol=1e-10 * float(gb2.abs().max()))
+    assert abs(float(gm1) - float(gm2)) <= 1e-8 * abs(float(gm2)) + 1e-14
+    assert abs(float(gbt1) - float(gbt2)) <= 1e-8 * abs(float(gbt2)) + 1e-14
+
+
+@pytest.mark.parametrize("first", [True, False])
+def test_inner_step_gradcheck(cuda, oracle, first):
+    """torch.autograd.gradcheck of one fused step wrt U, Up, gp, g2p, b and
+    (mu, beta) (FP64, no projection so the map is smooth away from the
+    shrinkage kinks, which random inputs at eps = 1e-6 do not cross)."""
+    import torch
+    from tval3_gb300 import autograd as AG
+    cfg, geo, x, op = _op64(oracle, 6, 5, seed=4)
+    dims = cfg.dims
+    n, m = x.size, op.rows
+    g = torch.Generator().manual_seed(11)
+    mk = lambda k, sc=1.0: (sc * torch.randn(k, dtype=torch.float64, generator=g)).to(cuda).requires_grad_()
+    U, Up, gp, g2p = mk(n), mk(n), mk(n), mk(n)
+    b = mk(m)
+    mub = torch.tensor([4.0, 2.0], dtype=torch.float64, device=cuda, requires_grad=True)
+    sig = (0.1 * torch.randn(3 * n, dtype=torch.float64, generator=g)).to(cuda)
+
+    def f(U_, Up_, gp_, g2p_, b_, mub_):
+        if first:
+            outs = AG._InnerStep.apply(U_, None, None, None, b_, mub_, op, dims, True, True, False, sig, None)
+        else:
+            outs = AG._InnerStep.apply(U_, Up_, gp_, g2p_, b_, mub_, op, dims, False, True, False, sig, None)
+        return outs
+
+    assert torch.autograd.gradcheck(f, (U, Up, gp, g2p, b, mub), eps=1e-6, atol=1e-6, rtol=1e-5)

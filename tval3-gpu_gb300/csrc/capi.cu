@@ -424,6 +424,64 @@ int check_problem_2d(const T* U, int rows, int cols, long A_rows, long A_cols, c
     return layers;
 }
 
+// a product that timed out in a bounded device wait is an error of the call
+void check_product(tval3_op op, cudaStream_t s) {
+    int e = 0;
+    if (op->q) e = op->q->take_error(s);
+    else if (op->d) e = op->d->take_error(s);
+    else e = op->f->take_error(s);
+    if (e) arg_error(TVAL3_ERR_TIMEOUT, "a bounded device wait of the product ran out (error bits " +
+                                            std::to_string(e) + "); the output is incomplete");
+}
+
+// the operator of a handle whose products take vectors of type T
+template <class T>
+const LinOp<T>* vec_op(tval3_op op);
+template <>
+const LinOp<float>* vec_op<float>(tval3_op op) {
+    if (!op || !op->f) arg_error(TVAL3_ERR_ARG, "Argument error: the _f32 step needs an FP32-vector operator!");
+    return op->f;
+}
+template <>
+const LinOp<double>* vec_op<double>(tval3_op op) {
+    if (!op || !op->d || op->q) arg_error(TVAL3_ERR_ARG, "Argument error: the _f64 step needs an FP64-vector operator!");
+    return op->d;
+}
+
+template <class T>
+void unroll_checks(tval3_op op, int p, int q, int r, int first, const double* mub, const T* U, const T* Up,
+                   const T* gp, const T* g2p, const T* b) {
+    const LinOp<T>* A = vec_op<T>(op);
+    if (p <= 0 || q <= 0 || r <= 0 || (long)p * q * r != A->n)
+        arg_error(TVAL3_ERR_SHAPE, "Argument error: the volume must have A.cols voxels!");
+    if (!mub || !U || !b || (!first && (!Up || !gp || !g2p)))
+        arg_error(TVAL3_ERR_ARG, "Argument error: NULL input of the unrolled step!");
+}
+
+template <class T>
+void unroll_fwd_entry(tval3_op op, int p, int q, int r, int first, int iso, int nonneg, const double* mub, const T* U,
+                      const T* Up, const T* gp, const T* g2p, const T* b, const T* sig, const T* delta, T* Un, T* g,
+                      T* g2, void* stream) {
+    unroll_checks<T>(op, p, q, r, first, mub, U, Up, gp, g2p, b);
+    if (!Un || !g || !g2) arg_error(TVAL3_ERR_ARG, "Argument error: NULL output of the unrolled step!");
+    const LinOp<T>* A = vec_op<T>(op);
+    unroll_step<T>(A, p, q, r, first, iso, nonneg, mub, U, Up, gp, g2p, b, sig, delta, Un, g, g2, (cudaStream_t)stream);
+    check_product(op, (cudaStream_t)stream);
+}
+
+template <class T>
+void unroll_bwd_entry(tval3_op op, int p, int q, int r, int first, int iso, int nonneg, const double* mub, const T* U,
+                      const T* Up, const T* gp, const T* g2p, const T* b, const T* sig, const T* delta, const T* gUn,
+                      const T* gg, const T* gg2, T* gU, T* gUp, T* ggp, T* gg2p, T* gb, double* gmub, void* stream) {
+    unroll_checks<T>(op, p, q, r, first, mub, U, Up, gp, g2p, b);
+    if (!gU) arg_error(TVAL3_ERR_ARG, "Argument error: NULL adjoint of U!");
+    const LinOp<T>* A = vec_op<T>(op);
+    unroll_step_adjoint<T>(A, p, q, r, first, iso, nonneg, mub, U, Up, gp, g2p, b, sig, delta, gUn, gg, gg2, gU,
+                           first ? nullptr : gUp, first ? nullptr : ggp, first ? nullptr : gg2p, gb, gmub,
+                           (cudaStream_t)stream);
+    check_product(op, (cudaStream_t)stream);
+}
+
 }  // namespace
 
 namespace tv3 {
@@ -808,14 +866,6 @@ tval3_status tval3_op_export_csr_scaled(tval3_op op, int* ptr, int* ind, float* 
 
 // a bounded device wait of a standalone product that ran out (the product's
 // output is incomplete)
-void check_product(tval3_op op, cudaStream_t s) {
-    int e = 0;
-    if (op->q) e = op->q->take_error(s);
-    else if (op->d) e = op->d->take_error(s);
-    else e = op->f->take_error(s);
-    if (e) arg_error(TVAL3_ERR_TIMEOUT, "a bounded device wait of the product ran out (error bits " +
-                                            std::to_string(e) + "); the output is incomplete");
-}
 
 tval3_status tval3_mat_vec_mul(tval3_op op, int trans, const void* x, void* y, void* stream) {
     return guard([&] {
@@ -900,6 +950,47 @@ tval3_status tval3_shrink_adjoint_f64(int64_t n, const double* v, double t, int 
     return guard([&] {
         if (n < 0 || (n > 0 && (!v || !gW || !gv))) arg_error(TVAL3_ERR_ARG, "Argument error: bad shrinkage arrays!");
         shrink_bwd<double>((long)n, v, t, iso, gW, gv, gt, (cudaStream_t)stream);
+    });
+}
+
+tval3_status tval3_unroll_step_f32(tval3_op op, int p, int q, int r, int first, int iso, int nonneg,
+                                   const double* mub, const float* U, const float* Up, const float* gp,
+                                   const float* g2p, const float* b, const float* sig, const float* delta, float* Un,
+                                   float* g, float* g2, void* stream) {
+    return guard([&] {
+        unroll_fwd_entry<float>(op, p, q, r, first, iso, nonneg, mub, U, Up, gp, g2p, b, sig, delta, Un, g, g2,
+                                stream);
+    });
+}
+tval3_status tval3_unroll_step_f64(tval3_op op, int p, int q, int r, int first, int iso, int nonneg,
+                                   const double* mub, const double* U, const double* Up, const double* gp,
+                                   const double* g2p, const double* b, const double* sig, const double* delta,
+                                   double* Un, double* g, double* g2, void* stream) {
+    return guard([&] {
+        unroll_fwd_entry<double>(op, p, q, r, first, iso, nonneg, mub, U, Up, gp, g2p, b, sig, delta, Un, g, g2,
+                                 stream);
+    });
+}
+tval3_status tval3_unroll_step_adjoint_f32(tval3_op op, int p, int q, int r, int first, int iso, int nonneg,
+                                           const double* mub, const float* U, const float* Up, const float* gp,
+                                           const float* g2p, const float* b, const float* sig, const float* delta,
+                                           const float* gUn, const float* gg, const float* gg2, float* gU,
+                                           float* gUp, float* ggp, float* gg2p, float* gb, double* gmub,
+                                           void* stream) {
+    return guard([&] {
+        unroll_bwd_entry<float>(op, p, q, r, first, iso, nonneg, mub, U, Up, gp, g2p, b, sig, delta, gUn, gg, gg2,
+                                gU, gUp, ggp, gg2p, gb, gmub, stream);
+    });
+}
+tval3_status tval3_unroll_step_adjoint_f64(tval3_op op, int p, int q, int r, int first, int iso, int nonneg,
+                                           const double* mub, const double* U, const double* Up, const double* gp,
+                                           const double* g2p, const double* b, const double* sig,
+                                           const double* delta, const double* gUn, const double* gg,
+                                           const double* gg2, double* gU, double* gUp, double* ggp, double* gg2p,
+                                           double* gb, double* gmub, void* stream) {
+    return guard([&] {
+        unroll_bwd_entry<double>(op, p, q, r, first, iso, nonneg, mub, U, Up, gp, g2p, b, sig, delta, gUn, gg, gg2,
+                                 gU, gUp, ggp, gg2p, gb, gmub, stream);
     });
 }
 

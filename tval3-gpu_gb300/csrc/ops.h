@@ -191,6 +191,17 @@ template <class T> void shrink_fwd(long n, const T* v, double t, int iso, T* W, 
 template <class T>
 void shrink_bwd(long n, const T* v, double t, int iso, const T* gW, T* gv, T* gt, cudaStream_t s);
 
+// One differentiable TVAL3 inner step and its adjoint (unroll.cu).
+template <class T>
+void unroll_step(const LinOp<T>* op, int p, int q, int r, int first, int iso, int nonneg, const double* mub,
+                 const T* U, const T* Up, const T* gp, const T* g2p, const T* b, const T* sig, const T* delta, T* Un,
+                 T* g, T* g2, cudaStream_t s);
+template <class T>
+void unroll_step_adjoint(const LinOp<T>* op, int p, int q, int r, int first, int iso, int nonneg, const double* mub,
+                         const T* U, const T* Up, const T* gp, const T* g2p, const T* b, const T* sig, const T* delta,
+                         const T* gUn, const T* gg, const T* gg2, T* gU, T* gUp, T* ggp, T* gg2p, T* gb, double* gmub,
+                         cudaStream_t s);
+
 // Ray-geometry operators (ray.cu).
 struct RayList;  // compacted ray list and geometry on the device
 template <class T>

@@ -10,19 +10,22 @@ hand-written adjoint kernel:
     Dt     forward D^T                      backward D
     shrink forward shrinkage W(v, t)        backward subgradient (tval3_shrink_adjoint)
 
-`unrolled_tval3` composes them into K inner iterations of the TVAL3
-u-subproblem (3d/tval3_gpu_3d.cpp:823-1029): W = shrink(DU - sigma/beta,
-1/beta), d = D^T(DU - W) + mu/beta A^T(AU - b), Barzilai-Borwein step tau
-(first step |<d,d> / (||Dd||^2 + mu/beta ||Ad||^2)|), U <- max(U - tau d, 0).
-The nonmonotone Armijo test of the reference is a discrete decision and is
-not part of the differentiable map; everything else, including tau, is
-differentiated.  Each iteration is checkpointed (recomputed in the backward
-pass) so memory stays at one iteration's state.
+`unrolled_tval3` runs K inner iterations of the TVAL3 u-subproblem
+(3d/tval3_gpu_3d.cpp:823-1029), each one `_InnerStep` Function: W =
+shrink(DU - sigma/beta, 1/beta), d = D^T(DU - W - sigma/beta) + mu/beta
+A^T(AU - b - delta/mu), Barzilai-Borwein step tau (first step |<d,d> /
+(||Dd||^2 + mu/beta ||Ad||^2)|), U <- max(U - tau d, 0).  Its forward is one
+C call of fused kernels (tval3_unroll_step_*) and its backward one C call of
+hand-written adjoint kernels (tval3_unroll_step_adjoint_*: projection mask,
+BB quotient, transposed products, shrinkage subgradient).  The nonmonotone
+Armijo test of the reference is a discrete decision and is not part of the
+differentiable map; everything else, including tau, is differentiated.  A
+step keeps only its inputs and recomputes its intermediates in the backward
+pass (per-iteration checkpointing), so memory stays at U, g, g2 per step.
 """
 from __future__ import annotations
 
 import torch
-from torch.utils.checkpoint import checkpoint
 
 from . import capi
 from .api import Operator
@@ -128,58 +131,74 @@ def shrink(v: torch.Tensor, t, iso: bool = True) -> torch.Tensor:
     return _Shrink.apply(v, t, iso)
 
 
-def _dot(a, b):
-    return (a * b).sum()
+def _ptr(t):
+    return t.data_ptr() if t is not None else None
+
+
+class _InnerStep(torch.autograd.Function):
+    """One inner step of the TVAL3 u-subproblem as a single Function: the
+    forward is tval3_unroll_step_* (fused kernels), the backward
+    tval3_unroll_step_adjoint_* (hand-written adjoint kernels: projection
+    mask, BB quotient, the transposed products, shrinkage subgradient).  Only
+    the inputs are kept; the backward recomputes the step's intermediates, so
+    each step is its own checkpoint."""
+
+    @staticmethod
+    def forward(ctx, U, Up, gp, g2p, b, mub, op, dims, first, iso, nonneg, sigma, delta):
+        lib = capi.load()
+        f = lib.tval3_unroll_step_f64 if U.dtype == torch.float64 else lib.tval3_unroll_step_f32
+        U = U.contiguous()
+        b = b.contiguous()
+        mub = mub.detach().to(torch.float64).contiguous()
+        Un, g, g2 = torch.empty_like(U), torch.empty_like(U), torch.empty_like(U)
+        ins = [None, None, None] if first else [Up.contiguous(), gp.contiguous(), g2p.contiguous()]
+        capi.check(f(op.handle, *dims, int(first), int(iso), int(nonneg), mub.data_ptr(), U.data_ptr(),
+                     *[_ptr(t) for t in ins], b.data_ptr(), _ptr(sigma), _ptr(delta), Un.data_ptr(), g.data_ptr(),
+                     g2.data_ptr(), _stream()))
+        ctx.save_for_backward(U, *(t if t is not None else torch.empty(0, device=U.device) for t in ins), b, mub)
+        ctx.op, ctx.dims, ctx.first, ctx.iso, ctx.nonneg = op, dims, first, iso, nonneg
+        ctx.sigma, ctx.delta = sigma, delta
+        return Un, g, g2
+
+    @staticmethod
+    def backward(ctx, gUn, gg, gg2):
+        U, Up, gp, g2p, b, mub = ctx.saved_tensors
+        first = ctx.first
+        lib = capi.load()
+        f = lib.tval3_unroll_step_adjoint_f64 if U.dtype == torch.float64 else lib.tval3_unroll_step_adjoint_f32
+        gU = torch.empty_like(U)
+        gUp = ggp = gg2p = None
+        if not first:
+            gUp, ggp, gg2p = torch.empty_like(U), torch.empty_like(U), torch.empty_like(U)
+        gb = torch.empty_like(b)
+        gmub = torch.empty(2, dtype=torch.float64, device=U.device)
+        cont = lambda t: t.contiguous() if t is not None else None
+        ins = [None, None, None] if first else [Up, gp, g2p]
+        capi.check(f(ctx.op.handle, *ctx.dims, int(first), int(ctx.iso), int(ctx.nonneg), mub.data_ptr(),
+                     U.data_ptr(), *[_ptr(t) for t in ins], b.data_ptr(), _ptr(ctx.sigma), _ptr(ctx.delta),
+                     _ptr(cont(gUn)), _ptr(cont(gg)), _ptr(cont(gg2)), gU.data_ptr(), _ptr(gUp), _ptr(ggp),
+                     _ptr(gg2p), gb.data_ptr(), gmub.data_ptr(), _stream()))
+        return (gU, gUp, ggp, gg2p, gb, gmub, None, None, None, None, None, None, None)
 
 
 def unrolled_tval3(op: Operator, b: torch.Tensor, dims, mu, beta, iters: int = 20, iso: bool = True,
-                   nonneg: bool = True, sigma=None, delta=None, use_checkpoint: bool = True) -> torch.Tensor:
-    """K differentiable inner iterations of the TVAL3 u-subproblem from U = A^T b.
-    mu and beta may be tensors requiring grad; returns U_K (n-vector)."""
+                   nonneg: bool = True, sigma=None, delta=None) -> torch.Tensor:
+    """K differentiable inner iterations of the TVAL3 u-subproblem from
+    U = A^T b, each one _InnerStep (fused forward kernels, hand-written
+    adjoint kernels, recomputation in the backward pass as per-iteration
+    checkpointing).  mu and beta may be tensors requiring grad; b may require
+    grad; returns U_K (n-vector).  sigma (3n) and delta (m) are the fixed
+    multipliers (zero when None)."""
     dt = b.dtype
-    mu = mu if torch.is_tensor(mu) else torch.tensor(float(mu), dtype=dt, device=b.device)
-    beta = beta if torch.is_tensor(beta) else torch.tensor(float(beta), dtype=dt, device=b.device)
-    n = dims[0] * dims[1] * dims[2]
-    sig = sigma if sigma is not None else torch.zeros(3 * n, dtype=dt, device=b.device)
-    dl = delta if delta is not None else torch.zeros(b.numel(), dtype=dt, device=b.device)
-    Atb = At(op, b)
-
-    def grad_dir(U, mu, beta):
-        DU = D(U, dims)
-        W = shrink(DU - sig / beta, 1.0 / beta, iso)
-        g = At(op, A(op, U) - b) - At(op, dl) / mu
-        g2 = Dt(DU - W, dims) - Dt(sig, dims) / beta
-        return g2 + (mu / beta) * g, g, g2
-
-    def step(U, Up, gp, g2p, first, mu, beta):
-        d, g, g2 = grad_dir(U, mu, beta)
-        if first:
-            Dd = D(d, dims)
-            Ad = A(op, d)
-            tau = torch.abs(_dot(d, d) / (_dot(Dd, Dd) + (mu / beta) * _dot(Ad, Ad)))
-        else:
-            s = U - Up
-            tau = torch.abs(_dot(s, s) / _dot(s, (g2 - g2p) + (mu / beta) * (g - gp)))
-        Un = U - tau * d
-        if nonneg:
-            Un = torch.relu(Un)
-        return Un, g, g2
-
-    U = Atb
+    mu = mu if torch.is_tensor(mu) else torch.tensor(float(mu), dtype=torch.float64, device=b.device)
+    beta = beta if torch.is_tensor(beta) else torch.tensor(float(beta), dtype=torch.float64, device=b.device)
+    mub = torch.stack([mu.to(torch.float64).reshape(()), beta.to(torch.float64).reshape(())])
+    sig = sigma.to(dt).contiguous() if sigma is not None else None
+    dl = delta.to(dt).contiguous() if delta is not None else None
+    dims = tuple(int(v) for v in dims)
+    U = At(op, b)
     Up = gp = g2p = None
     for k in range(iters):
-        first = k == 0
-        if first:
-            def fn(U_, mu_, beta_):
-                return step(U_, None, None, None, True, mu_, beta_)
-            args = (U, mu, beta)
-        else:
-            def fn(U_, Up_, gp_, g2p_, mu_, beta_):
-                return step(U_, Up_, gp_, g2p_, False, mu_, beta_)
-            args = (U, Up, gp, g2p, mu, beta)
-        if use_checkpoint:
-            Un, g, g2 = checkpoint(fn, *args, use_reentrant=False)
-        else:
-            Un, g, g2 = fn(*args)
+        Un, g, g2 = _InnerStep.apply(U, Up, gp, g2p, b, mub, op, dims, k == 0, iso, nonneg, sig, dl)
         Up, gp, g2p, U = U, g, g2, Un
     return U

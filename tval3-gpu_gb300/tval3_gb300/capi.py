@@ -107,6 +107,10 @@ _SIG = {
     "tval3_mat_mat_mul_interleaved": (_I, [_P, _I, _I, _P, _P, _P]),
     "tval3_op_set_variant": (_I, [_P, _I, _I]),
     "tval3_op_get_variant": (_I, [_P, _I, _P]),
+    "tval3_unroll_step_f32": (_I, [_P, _I, _I, _I, _I, _I, _I] + [_P] * 12),
+    "tval3_unroll_step_f64": (_I, [_P, _I, _I, _I, _I, _I, _I] + [_P] * 12),
+    "tval3_unroll_step_adjoint_f32": (_I, [_P, _I, _I, _I, _I, _I, _I] + [_P] * 18),
+    "tval3_unroll_step_adjoint_f64": (_I, [_P, _I, _I, _I, _I, _I, _I] + [_P] * 18),
     "tval3_shrink_f32": (_I, [C.c_int64, _P, C.c_double, _I, _P, _P]),
     "tval3_shrink_f64": (_I, [C.c_int64, _P, C.c_double, _I, _P, _P]),
     "tval3_shrink_adjoint_f32": (_I, [C.c_int64, _P, C.c_double, _I, _P, _P, _P, _P]),
