@@ -83,6 +83,8 @@ def parse():
     ap.add_argument("--mixed-maxit", type=int, default=0,
                     help="iteration limit of the at-scale leg's oracle and device solves (0: the config's maxit)")
     ap.add_argument("--only-mixed", action="store_true", help="run only the mixed-precision at-scale leg")
+    ap.add_argument("--mixed-products-only", action="store_true",
+                    help="at-scale leg: time the products of both kernels only (no oracle, no solves; development)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-API measurement (profiling runs)")
     ap.add_argument("--only-spmv", default=None,
                     choices=["fp32", "fp64vec", "df64", "bf16", "fp16", "bf16df64", "fp16df64"],
@@ -643,7 +645,10 @@ def mixed_at_scale(args, T, torch, dev):
     del op32
     b = W.add_noise(csr_matvec64(ptr, ind, val, x_true.reshape(-1)), cfg.noise, cfg.seed).astype(np.float64)
     t0 = time.time()
-    xstar, oi = O.tval3_csr(dims, ptr, ind, val, b, opts, prec=0, tptr=tptr, tind=tind, tval=tval)
+    if args.mixed_products_only:
+        xstar, oi = None, {"total_iters": 0}
+    else:
+        xstar, oi = O.tval3_csr(dims, ptr, ind, val, b, opts, prec=0, tptr=tptr, tind=tind, tval=tval)
     oracle_s = time.time() - t0
     del ptr, ind, val, tptr, tind, tval
     out = {"workload": f"tval3 3d {args.mixed_size}^3, {args.mixed_rays}x{args.mixed_rays} hemisphere rays, "
@@ -681,7 +686,37 @@ def mixed_at_scale(args, T, torch, dev):
             prods["AT" if trans else "A"] = {"us": round(t * 1e6, 1), "GBs": round(bts / t / 1e9, 1),
                                              "frac": round(bts / t / 1e9 / peak, 4), "bytes": int(bts),
                                              "variant": {0: "csr", 1: "tiled", 2: "tiled_pipe"}[op.variant(trans)]}
+            if args.mixed_products_only:
+                # the other kernel of the same product, for comparison
+                chosen = op.variant(trans)
+                for other in (0, 1):
+                    if other == chosen:
+                        continue
+                    try:
+                        op.set_variant(trans, other)
+                    except T.Tval3Error:
+                        continue
+                    for _ in range(3):
+                        op.mat_vec_mul(trans, src, dst, stream=stream)
+                    tot = 0.0
+                    for _ in range(10):
+                        with torch.cuda.stream(stream):
+                            flush()
+                            e0 = torch.cuda.Event(enable_timing=True)
+                            e1 = torch.cuda.Event(enable_timing=True)
+                            e0.record(stream)
+                            op.mat_vec_mul(trans, src, dst, stream=stream)
+                            e1.record(stream)
+                        e1.synchronize()
+                        tot += e0.elapsed_time(e1) / 1000.0
+                    prods["AT" if trans else "A"][{0: "csr", 1: "tiled"}[other] + "_us"] = round(tot / 10 * 1e6, 1)
+                    op.set_variant(trans, chosen)
         del x, y, outm, outn
+        if args.mixed_products_only:
+            out[name] = {"device_build_s": round(bs, 3), "products": prods}
+            op.close()
+            del op
+            continue
         qp, qi, qv, rs, qtp, qti, qtv = op.export_csr_scaled()
         t0 = time.time()
         xq, oq = O.tval3_csr(dims, qp, qi, qv, b, opts, prec=0, rscale=rs, tptr=qtp, tind=qti, tval=qtv)

@@ -15,10 +15,17 @@ def _geo(kind):
     from tval3_gb300 import workloads as W
     if kind == "ring":
         return W.ring_geometry(64, 96)
+    if kind == "dense_ring":
+        # ~16,000 rays through each 16 x 16 tile: beyond the shared memory of
+        # a double-float ray list, so A^T falls back to smaller tiles
+        return W.ring_geometry(64, 320)
+    if kind == "big":
+        # 160^3 voxels (8,000 tiles of 8^3): A*x takes 16 x 8 x 8 tiles
+        return W.hemisphere_geometry(160, 24, 24, seed=2)
     return W.hemisphere_geometry(40, 48, 48, seed=1)
 
 
-@pytest.mark.parametrize("kind", ["ring", "hemi"])
+@pytest.mark.parametrize("kind", ["ring", "hemi", "dense_ring", "big"])
 @pytest.mark.parametrize("prec", ["fp32", "df64", "bf16"])
 @pytest.mark.parametrize("trans", [1, 0])
 def test_tiled_products_match_plain_csr(cuda, kind, prec, trans):

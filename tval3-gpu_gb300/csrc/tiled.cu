@@ -1042,6 +1042,18 @@ __global__ void __launch_bounds__(256) k_tiledN_reduce(TiledNArgs<T, V> a) {
         const long r = rb + lane;
         const int elo = __ldg(a.rseg + rb), ehi = __ldg(a.rseg + min(rb + 32, a.m));
         const int ra = (r < a.m) ? __ldg(a.rseg + r) : 0, rz = (r < a.m) ? __ldg(a.rseg + r + 1) : 0;
+        // the epilogue's inputs, loaded before the sums so their latency overlaps them
+        T eb = T(0), ed = T(0);
+        float esc = 1.f;
+        if (r < a.m) {
+            if (EPI == SPMV_LAM35) {
+                eb = a.b[r];
+                ed = a.delta[r];
+            } else if (EPI == SPMV_SUB) {
+                eb = a.sub[r];
+            }
+            if (a.rscale) esc = __ldg(a.rscale + r);
+        }
         RowAcc<T> acc;
         for (int base = elo; base < ehi; base += W) {
             T v[W / 32];
@@ -1059,16 +1071,16 @@ __global__ void __launch_bounds__(256) k_tiledN_reduce(TiledNArgs<T, V> a) {
         }
         T s = acc.value();
         if (r < a.m) {
-            if (a.rscale) s *= (T)__ldg(a.rscale + r);
+            if (a.rscale) s *= (T)esc;
             if (EPI == SPMV_PLAIN) {
                 y[r] = s;
             } else if (EPI == SPMV_SUB) {
-                y[r] = s - a.sub[r];
+                y[r] = s - eb;
             } else if (EPI == SPMV_LAM35) {
                 y[r] = s;
-                double t = acc_d(to_acc(s) - to_acc(a.b[r]));
+                double t = acc_d(to_acc(s) - to_acc(eb));
                 acc0 += t * t;
-                acc1 += acc_d(to_acc(a.delta[r])) * t;
+                acc1 += acc_d(to_acc(ed)) * t;
             } else if (EPI == SPMV_NORM2) {
                 const double sd = acc_d(to_acc(s));
                 acc0 += sd * sd;
@@ -1099,7 +1111,15 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     m = m_; p = p_; q = q_; r = r_;
     const long n = (long)p * q * r;
     if (nnz <= 0 || n <= 0 || m <= 0 || nnz >= (1L << 31) || m >= (1L << 31)) return;
+    // tile shape: 8 x 8 x 8 voxels in 3D (16 x 16 in 2D); a volume with many
+    // more tiles than the SMs can use takes 16 x 8 x 8 tiles, which halve the
+    // (ray, tile) segments and so the partials written and re-read, while
+    // still leaving dozens of tiles per SM for the load balance
     ty = std::min(p, r > 1 ? 8 : 16); tx = std::min(q, r > 1 ? 8 : 16); tz = std::min(r, 8);
+    if (r > 1) {
+        const long n8 = (long)((p + 7) / 8) * ((q + 7) / 8) * ((r + 7) / 8);
+        if (n8 >= 48L * num_sms()) ty = std::min(p, 16);
+    }
     nty = (p + ty - 1) / ty; ntx = (q + tx - 1) / tx;
     const int ntz = (r + tz - 1) / tz;
     const long nt = (long)nty * ntx * ntz;
