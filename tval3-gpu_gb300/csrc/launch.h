@@ -123,8 +123,6 @@ template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s);
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s);
 template <class T> void launch_g2_gradient(SolverBufs<T>& B, cudaStream_t s);  // g2 (update_W) + gradient, fused
-template <class T> void launch_g2_only(SolverBufs<T>& B, int spec, cudaStream_t s);  // g2 alone (spec: the speculative W)
-template <class T> void launch_gradient_g2in(SolverBufs<T>& B, cudaStream_t s);  // gradient with g2 already formed
 template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t s);
 template <class T> void launch_bt_coef(SolverBufs<T>& B, cudaStream_t s);
 template <class T> void launch_bt_apply(SolverBufs<T>& B, cudaStream_t s);

@@ -110,9 +110,6 @@ Solver<T>::~Solver() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (rexec) cudaGraphExecDestroy(rexec);
     if (hctl) cudaFreeHost(hctl);
-    if (ev_fork) cudaEventDestroy(ev_fork);
-    if (ev_join) cudaEventDestroy(ev_join);
-    if (side) cudaStreamDestroy(side);
 }
 
 template <class T>
@@ -233,26 +230,6 @@ void Solver<T>::get_g(int epi, cudaStream_t s, Body* body) {
                 launch_skip_copy<T>(B, 1, s);
             }
         }
-    } else if (epi == EPI_G2_DESCEND && split_g2()) {
-        // update_W's g2 of the speculative W depends only on the descent: in
-        // the graph it is a parallel branch beside A^T A U (both kernels leave
-        // issue slots and bandwidth unused), joined before the Armijo kernel
-        if (body) {
-            if (!side) {
-                TV3_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-                TV3_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-                TV3_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-            }
-            TV3_CUDA(cudaEventRecord(ev_fork, s));
-            TV3_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
-            launch_g2_only<T>(B, 1, side);
-            TV3_CUDA(cudaEventRecord(ev_join, side));
-            A->apply(1, io_AtAu(), SPMV_SUB, s);
-            TV3_CUDA(cudaStreamWaitEvent(s, ev_join, 0));
-        } else {
-            launch_g2_only<T>(B, 1, s);
-            A->apply(1, io_AtAu(), SPMV_SUB, s);
-        }
     } else {
         A->apply(1, io_AtAu(), SPMV_SUB, s);
     }
@@ -314,11 +291,9 @@ void Solver<T>::run_host(cudaStream_t s) {
             // update_W at the point taken (an accepted full step committed the
             // descent's W in the Armijo kernel instead)
             launch_shrink<T>(B, EPI_G2_UPDATE_W, s);
-            if (split_g2()) launch_g2_only<T>(B, 0, s);
         }
         // ---- g2 of update_W (:965-1029), gradient, RelChg
-        if (split_g2()) launch_gradient_g2in<T>(B, s);
-        else launch_g2_gradient<T>(B, s);
+        launch_g2_gradient<T>(B, s);
         read_ctl(s);
         fst = false;
         if (hctl->inner_break) {
@@ -400,12 +375,10 @@ void Solver<T>::add_to_graph(cudaGraph_t top, const void* d_b, void* d_U, const 
             // the descent's W in the Armijo kernel instead)
             ab.begin();
             launch_shrink<T>(B, EPI_G2_UPDATE_W, cs);
-            if (split_g2()) launch_g2_only<T>(B, 0, cs);
             ab.end();
         }
         ib.begin();
-        if (split_g2()) launch_gradient_g2in<T>(B, cs);  // sets h_inner
-        else launch_g2_gradient<T>(B, cs);
+        launch_g2_gradient<T>(B, cs);  // sets h_inner
         ib.end();
     };
     try {

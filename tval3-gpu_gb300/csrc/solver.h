@@ -38,14 +38,6 @@ struct Solver {
     cudaGraphExec_t rexec = nullptr;  // resume graph (mode 1)
     void* r_U = nullptr;
     const void* r_Ut = nullptr;
-    // after a descent, update_W's g2 (of the speculative W) runs on a branch
-    // of its own beside A^T A U: the stream that captures it and the events
-    // of the fork and the join
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // g2 formed apart from the gradient pass (all but the skip-A^T heuristic,
-    // whose conditional A^T product is captured in bodies of its own)
-    bool split_g2() const { return o.skipMulRatio == 0.0; }
 
     Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_, int L_ = 1);
     ~Solver();

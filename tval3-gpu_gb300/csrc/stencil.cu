@@ -591,61 +591,6 @@ __global__ void k_gradient(SolverBufs<T> B, int iter) {
     }
 }
 
-// g2 = D^T (DU - W) of the voxel pair (i, i+1) (y even, L = 1): -x and -z
-// neighbours are pairs, the -y neighbour of i+1 is i
-template <class T>
-__device__ __forceinline__ void g2_pair(const Geo& geo, const T* __restrict__ DU, const T* __restrict__ W, long n,
-                                        long i, T& g2a, T& g2b) {
-    const Nb nb = neighbours(geo, i);
-    Two<T> va[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const Two<T> du = ld2(DU + c * n + i), w = ld2(W + c * n + i);
-        va[c] = {du.a - w.a, du.b - w.b};
-    }
-    const T v0m = DU[nb.ym] - W[nb.ym];
-    const Two<T> dxm = ld2(DU + n + nb.xm), wxm = ld2(W + n + nb.xm);
-    const Two<T> dzm = ld2(DU + 2 * n + nb.zm), wzm = ld2(W + 2 * n + nb.zm);
-    g2a = v0m - va[0].a + (dxm.a - wxm.a) - va[1].a + (dzm.a - wzm.a) - va[2].a;
-    g2b = va[0].a - va[0].b + (dxm.b - wxm.b) - va[1].b + (dzm.b - wzm.b) - va[2].b;
-}
-
-template <class T>
-__device__ __forceinline__ T g2_one(const Geo& geo, const T* __restrict__ DU, const T* __restrict__ W, long n,
-                                    long i) {
-    const Nb nb = neighbours(geo, i);
-    const T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
-    const T v0m = DU[nb.ym] - W[nb.ym];
-    const T v1m = DU[n + nb.xm] - W[n + nb.xm];
-    const T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
-    return v0m - v0 + v1m - v1 + v2m - v2;
-}
-
-// update_W's g2 = D^T (DU - W) alone, with W the descent's speculative
-// update_W (spec = 1: before the Armijo kernel commits it, so this pass can
-// run beside the sparse products) or the current W (spec = 0: after a
-// backtracking step's shrinkage).  The same values k_g2_gradient forms
-// inline.
-template <class T>
-__global__ void __launch_bounds__(256, 4) k_g2_only(SolverBufs<T> B, Geo geo, int spec) {
-    Ctl* ctl = B.ctl;
-    count_launch(ctl);
-    const int cur = ctl->parity;
-    const long n = B.n;
-    const T* __restrict__ DU = B.DU[cur];
-    const T* __restrict__ W = B.W[spec ? 1 - ctl->wsel : ctl->wsel];
-    T* __restrict__ g2o = B.g2[cur];
-    if (geo.l.d == 1 && (geo.p.d % 2) == 0) {
-        GRID_STRIDE_PAIRS(i, n) {
-            T a, b;
-            g2_pair(geo, DU, W, n, i, a, b);
-            st2(g2o + i, a, b);
-        }
-    } else GRID_STRIDE(i, n) {
-        g2o[i] = g2_one(geo, DU, W, n, i);
-    }
-}
-
 // ---------------------------------------------------------------------------
 // The end of an inner iteration in one pass: update_W's g2 = D^T (DU - W)
 // (its lam2 and lam4 come from k_shrink) and get_gradient's d with the next
@@ -653,9 +598,7 @@ __global__ void __launch_bounds__(256, 4) k_g2_only(SolverBufs<T> B, Geo geo, in
 // used by the same thread, so the pass saves the store-and-reload of g2 and a
 // launch.
 // ---------------------------------------------------------------------------
-// G2IN: g2 was formed already (k_g2_only on a branch beside the sparse
-// products, or after a backtracking step) and is read instead of formed.
-template <class T, bool G2IN>
+template <class T>
 __global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
@@ -696,15 +639,19 @@ __global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo
         // voxel pairs (i, i+1) with y even: -x and -z neighbours are pairs, the
         // -y neighbour of i+1 is i
         GRID_STRIDE_PAIRS(i, n) {
-            T g2a, g2b;
-            if (G2IN) {
-                const Two<T> gg = ld2(g2o + i);
-                g2a = gg.a;
-                g2b = gg.b;
-            } else {
-                g2_pair(geo, DU, W, n, i, g2a, g2b);
-                st2(g2o + i, g2a, g2b);
+            const Nb nb = neighbours(geo, i);
+            Two<T> va[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const Two<T> du = ld2(DU + c * n + i), w = ld2(W + c * n + i);
+                va[c] = {du.a - w.a, du.b - w.b};
             }
+            const T v0m = DU[nb.ym] - W[nb.ym];
+            const Two<T> dxm = ld2(DU + n + nb.xm), wxm = ld2(W + n + nb.xm);
+            const Two<T> dzm = ld2(DU + 2 * n + nb.zm), wzm = ld2(W + 2 * n + nb.zm);
+            const T g2a = v0m - va[0].a + (dxm.a - wxm.a) - va[1].a + (dzm.a - wzm.a) - va[2].a;
+            const T g2b = va[0].a - va[0].b + (dxm.b - wxm.b) - va[1].b + (dzm.b - wzm.b) - va[2].b;
+            st2(g2o + i, g2a, g2b);
             const Two<T> gi = ld2(g + i), dt = ld2(dts + i), u = ld2(U + i), up = ld2(Up + i);
             const Two<T> gpi = ld2(gp + i), g2pi = ld2(g2p + i);
             T da, db;
@@ -713,13 +660,13 @@ __global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo
             st2(d + i, da, db);
         }
     } else GRID_STRIDE(i, n) {
-        T g2i;
-        if (G2IN) {
-            g2i = g2o[i];
-        } else {
-            g2i = g2_one(geo, DU, W, n, i);
-            g2o[i] = g2i;
-        }
+        const Nb nb = neighbours(geo, i);
+        const T v0 = DU[i] - W[i], v1 = DU[n + i] - W[n + i], v2 = DU[2 * n + i] - W[2 * n + i];
+        const T v0m = DU[nb.ym] - W[nb.ym];
+        const T v1m = DU[n + nb.xm] - W[n + nb.xm];
+        const T v2m = DU[2 * n + nb.zm] - W[2 * n + nb.zm];
+        const T g2i = v0m - v0 + v1m - v1 + v2m - v2;
+        g2o[i] = g2i;
         T di;
         grad(i, g2i, g[i], dts[i], U[i], Up[i], gp[i], g2p[i], di);
         d[i] = di;
@@ -1168,13 +1115,7 @@ template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s
     else rlaunch(k_shrink<T, false>, B.grid, s, B, mode);
 }
 template <class T> void launch_g2_gradient(SolverBufs<T>& B, cudaStream_t s) {
-    rlaunch(k_g2_gradient<T, false>, B.grid, s, B, geo_of(B));
-}
-template <class T> void launch_g2_only(SolverBufs<T>& B, int spec, cudaStream_t s) {
-    rlaunch(k_g2_only<T>, B.grid, s, B, geo_of(B), spec);
-}
-template <class T> void launch_gradient_g2in(SolverBufs<T>& B, cudaStream_t s) {
-    rlaunch(k_g2_gradient<T, true>, B.grid, s, B, geo_of(B));
+    rlaunch(k_g2_gradient<T>, B.grid, s, B, geo_of(B));
 }
 template <class T> void launch_gradient(SolverBufs<T>& B, int mode, cudaStream_t s) {
     rlaunch(k_gradient<T>, B.grid, s, B, mode);
@@ -1213,8 +1154,6 @@ template <class T> void launch_Dt_plain(int p, int q, int r, const T* V3, T* out
     template void launch_shrink<T>(SolverBufs<T>&, int, cudaStream_t);              \
     template void launch_gradient<T>(SolverBufs<T>&, int, cudaStream_t);            \
     template void launch_g2_gradient<T>(SolverBufs<T>&, cudaStream_t);              \
-    template void launch_g2_only<T>(SolverBufs<T>&, int, cudaStream_t);             \
-    template void launch_gradient_g2in<T>(SolverBufs<T>&, cudaStream_t);            \
     template void launch_bt_coef<T>(SolverBufs<T>&, cudaStream_t);                  \
     template void launch_bt_apply<T>(SolverBufs<T>&, cudaStream_t);                 \
     template void launch_outer_relchg<T>(SolverBufs<T>&, cudaStream_t);             \
