@@ -69,6 +69,61 @@ struct tval3_solver_s {
 
 namespace {
 
+// Upload of a caller's host array.  Where the device reads pageable host
+// memory through the host's own page tables (Grace systems over NVLink-C2C:
+// cudaDevAttrPageableMemoryAccessUsesHostPageTables), a copy kernel reads
+// the array in place at the link's rate, with no host thread staging it
+// through pinned buffers (so a busy host does not slow the upload);
+// elsewhere cudaMemcpy.  Synchronous like cudaMemcpy on return.
+__global__ void k_h2d16(const int4* __restrict__ src, int4* __restrict__ dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+__global__ void k_h2d1(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+bool device_reads_host_memory() {
+    constexpr int MAXDEV = 64;
+    static std::atomic<int> known[MAXDEV] = {};  // 0 unknown, 1 no, 2 yes
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAXDEV) return false;
+    int k = known[dev].load();
+    if (!k) {
+        int pma = 0, hpt = 0;
+        if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) pma = 0;
+        if (cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) hpt = 0;
+        k = (pma && hpt) ? 2 : 1;
+        known[dev].store(k);
+    }
+    return k == 2;
+}
+
+void h2d(void* dst, const void* src, size_t bytes) {
+    if (!bytes) return;
+    if (!device_reads_host_memory()) {
+        TV3_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+        return;
+    }
+    const int grid = num_sms() * 4;
+    const uintptr_t a = (uintptr_t)src, b = (uintptr_t)dst;
+    size_t head = 0;
+    if ((a % 16) == (b % 16)) {
+        head = std::min(bytes, (size_t)((16 - a % 16) % 16));
+        const size_t body = (bytes - head) / 16;
+        if (body) k_h2d16<<<grid, 256>>>((const int4*)((const char*)src + head), (int4*)((char*)dst + head), body);
+        const size_t done = head + body * 16;
+        if (head) k_h2d1<<<1, 32>>>((const unsigned char*)src, (unsigned char*)dst, head);
+        if (bytes > done)
+            k_h2d1<<<1, 256>>>((const unsigned char*)src + done, (unsigned char*)dst + done, bytes - done);
+    } else {
+        k_h2d1<<<grid, 256>>>((const unsigned char*)src, (unsigned char*)dst, bytes);
+    }
+    TV3_CUDA(cudaGetLastError());
+    TV3_CUDA(cudaStreamSynchronize(0));
+}
+
 thread_local std::string g_err;
 // seconds of the phases of this thread's last reference entry-point call:
 // operator (input checks, upload, transpose / quantisation, ray-matrix build),
@@ -214,7 +269,7 @@ void to_device(DBuf<T>& d, const void* h, long n, int src_type) {
     if (n <= 0) return;
     bool src_double = (src_type == TVAL3_PREC_FP64);
     if (src_double == (sizeof(T) == 8)) {
-        TV3_CUDA(cudaMemcpy(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice));
+        h2d(d.p, h, n * sizeof(T));
     } else {
         std::vector<T> tmp(n);
         if (src_double)
@@ -238,15 +293,15 @@ void upload_f32(const tval3_sparse_host* A, bool dev_check, F32Csr& c) {
     if (A->format & TVAL3_SPARSE_CSR) {
         c.ptr.alloc(m + 1);
         c.ind.alloc(std::max<long>(nnz, 1));
-        TV3_CUDA(cudaMemcpy(c.ptr.p, A->csr_ptr, (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
-        if (nnz) TV3_CUDA(cudaMemcpy(c.ind.p, A->csr_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
+        h2d(c.ptr.p, A->csr_ptr, (m + 1) * sizeof(int));
+        h2d(c.ind.p, A->csr_ind, nnz * sizeof(int));
         to_device(c.val, A->csr_val, nnz, A->val_type);
     }
     if (A->format & TVAL3_SPARSE_CSC) {
         c.tptr.alloc(n + 1);
         c.tind.alloc(std::max<long>(nnz, 1));
-        TV3_CUDA(cudaMemcpy(c.tptr.p, A->csc_ptr, (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
-        if (nnz) TV3_CUDA(cudaMemcpy(c.tind.p, A->csc_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
+        h2d(c.tptr.p, A->csc_ptr, (n + 1) * sizeof(int));
+        h2d(c.tind.p, A->csc_ind, nnz * sizeof(int));
         to_device(c.tval, A->csc_val, nnz, A->val_type);
     }
     up.reset();
@@ -304,15 +359,15 @@ LinOp<T>* sparse_op(const tval3_sparse_host* A, int precision, bool tune = true)
     if (A->format & TVAL3_SPARSE_CSR) {
         ptr.alloc(m + 1);
         ind.alloc(std::max<long>(nnz, 1));
-        TV3_CUDA(cudaMemcpy(ptr.p, A->csr_ptr, (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
-        if (nnz) TV3_CUDA(cudaMemcpy(ind.p, A->csr_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
+        h2d(ptr.p, A->csr_ptr, (m + 1) * sizeof(int));
+        h2d(ind.p, A->csr_ind, nnz * sizeof(int));
         to_device(val, A->csr_val, nnz, A->val_type);
     }
     if (A->format & TVAL3_SPARSE_CSC) {
         tptr.alloc(n + 1);
         tind.alloc(std::max<long>(nnz, 1));
-        TV3_CUDA(cudaMemcpy(tptr.p, A->csc_ptr, (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
-        if (nnz) TV3_CUDA(cudaMemcpy(tind.p, A->csc_ind, nnz * sizeof(int), cudaMemcpyHostToDevice));
+        h2d(tptr.p, A->csc_ptr, (n + 1) * sizeof(int));
+        h2d(tind.p, A->csc_ind, nnz * sizeof(int));
         to_device(tval, A->csc_val, nnz, A->val_type);
     }
     up.reset();
@@ -368,11 +423,11 @@ void solve_host(LinOp<T>* op, Ext<T>* U, int dim_y, int dim_x, int dim_z, const 
     DBuf<E> db, dU, dUt;
     db.alloc(std::max<long>(b_len, 1));
     dU.alloc(std::max<long>(n, 1));
-    if (b_len) TV3_CUDA(cudaMemcpy(db.p, b, b_len * sizeof(E), cudaMemcpyHostToDevice));
+    h2d(db.p, b, b_len * sizeof(E));
     const bool use_ut = Ut && Ut_len == n && n > 0;
     if (use_ut) {
         dUt.alloc(n);
-        TV3_CUDA(cudaMemcpy(dUt.p, Ut, n * sizeof(E), cudaMemcpyHostToDevice));
+        h2d(dUt.p, Ut, n * sizeof(E));
     }
     Solver<T> s(op, dim_y, dim_x, dim_z, *opts, layers);
     s.mode = 1;  // the whole solve as one graph launch

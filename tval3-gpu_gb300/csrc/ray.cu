@@ -144,7 +144,8 @@ __device__ __forceinline__ bool sid_setup(const double P0[3], const double P1[3]
         if (R.dv[a] == 0.0) continue;
         const int st = R.dv[a] > 0 ? 1 : -1;
         double pos = __dadd_rn(P0[a], __dmul_rn(tmin, R.dv[a]));
-        long k = (st > 0) ? (long)floor(pos) + 1 : (long)ceil(pos) - 1;
+        // (round-down / round-up conversions: floor and ceil in one instruction)
+        long k = (st > 0) ? (long)__double2ll_rd(pos) + 1 : (long)__double2ll_ru(pos) - 1;
         double tn = __ddiv_rn(__dsub_rn((double)k, P0[a]), R.dv[a]);
         for (int guard = 0; tn <= tmin && guard < 4; ++guard) {
             k += st;
@@ -175,7 +176,7 @@ __device__ __forceinline__ bool sid_event(const SidRay& R, const int N[3], doubl
         const double mid = __dmul_rn(0.5, __dadd_rn(s.t, te));
         for (int a = 0; a < 3; ++a) {
             const double cc = __dadd_rn(R.P0[a], __dmul_rn(mid, R.dv[a]));
-            long q = (long)floor(cc);
+            long q = (long)__double2ll_rd(cc);
             if (q < 0) q = 0;
             if (q > N[a] - 1) q = N[a] - 1;
             c[a] = (int)q;

@@ -888,8 +888,9 @@ __device__ __forceinline__ void stage_x_async(const TiledNArgs<T, V>& a, const T
 // segment per lane, steps in order); the warp releases the stage (mbarrier
 // empty[s], one arrival per consumer warp).  Every wait is bounded: on a
 // timeout a warp records ERR_TILED_TIMEOUT and stops computing but keeps
-// releasing stages, and the producer waits (bounded) for its last copies
-// before it returns, so no copy lands after the CTA exits.
+// releasing stages, each only after a second bounded wait for its copy, and
+// the producer waits (bounded) for its last copies before it returns, so no
+// copy lands in a released stage or after the CTA exits.
 template <class T, class V>
 __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T, V> a, BulkArgs bk) {
     count_launch(a.ctl);
@@ -976,7 +977,13 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
                 cs0 = __ldg(bk.chunk_slice + c0 + j);
                 cs1 = __ldg(bk.chunk_slice + c0 + j + 1);
             }
-            if (ok) ok = mbar_wait(&full[st], (unsigned)((i / S) & 1));
+            // a stage is released only after its copy has landed: a wait that
+            // ran out (or a warp already failed) waits once more for the copy,
+            // so the producer never re-arms a barrier whose phase is pending
+            if (!(ok && mbar_wait(&full[st], (unsigned)((i / S) & 1)))) {
+                ok = false;
+                mbar_wait(&full[st], (unsigned)((i / S) & 1));
+            }
             if (ok) {
                 const unsigned char* base = stages + st * SB;
                 const unsigned short* L = reinterpret_cast<const unsigned short*>(base);
