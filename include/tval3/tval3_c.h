@@ -411,6 +411,12 @@ TVAL3_API tval3_status tval3_batch_create(tval3_batch* batch, const tval3_op* op
  * NULL) get each problem's counters, and secs = the time of the whole batch. */
 TVAL3_API tval3_status tval3_batch_solve(tval3_batch batch, const void* const* d_b, void* const* d_U,
                                          const void* const* d_Ut, tval3_info* infos, void* stream);
+/* Elements per block of the vector kernels that the batch's first solve
+ * chose by timing short solves of the whole batch (512 ... 4,096; 1,024
+ * unless another was at least 3 % faster).  Solvers created later in the
+ * process for the same vector type and problem shape take the same grid, so
+ * their results equal the batch's bit for bit. */
+TVAL3_API tval3_status tval3_batch_tuned_grid(tval3_batch batch, int64_t* elems_per_block);
 TVAL3_API tval3_status tval3_batch_destroy(tval3_batch batch);
 
 /* Host form: tval3_gpu(U, sparse A, b, opts, Ut) of every slice (FP32,

@@ -7,7 +7,10 @@ of different sizes and geometries in one CUDA graph launch.
   - FP32: the batched host entry point gives bit-identical results and
     counters to solving each slice alone through tval3_gpu (the same kernels
     in the same order, only run side by side);
-  - a repeated batch solve reuses its graph and gives the same result.
+  - a repeated batch solve reuses its graph and gives the same result;
+  - the first batch solve tunes the vector kernels' grid on short solves of
+    the whole batch, and solvers created later for the same shapes take the
+    same grid (so the single solves above equal the batched ones).
 """
 import numpy as np
 import pytest
@@ -42,6 +45,8 @@ def test_batch_fp64_matches_oracle_per_slice(cuda, oracle):
     Us = [torch.empty(x.size, dtype=torch.float64, device=cuda) for (n, x, *_) in sl]
     Uts = [torch.tensor(x.reshape(-1), dtype=torch.float64, device=cuda) for (n, x, *_) in sl]
     infos = bt.solve(bs, Us, Uts)
+    # the first solve tuned the vector kernels' grid (one of the candidates)
+    assert bt.tuned_grid in (512, 1024, 2048, 4096)
     for (n, x, p, i, v, b), U, ig in zip(sl, Us, infos):
         Uo, io = oracle.tval3_csr((n, n, 1), p, i, v, b.astype(np.float64), OPTS, prec=0, Ut=x)
         assert (ig["total_iters"], ig["outer_iters"], ig["backtracks"], ig["restarts"]) == \

@@ -1275,6 +1275,13 @@ tval3_status tval3_batch_solve(tval3_batch batch, const void* const* d_b, void* 
     });
 }
 
+tval3_status tval3_batch_tuned_grid(tval3_batch batch, int64_t* elems_per_block) {
+    return guard([&] {
+        if (!batch || !elems_per_block) arg_error(TVAL3_ERR_ARG, "Argument error: batch or output is NULL!");
+        *elems_per_block = batch->q ? batch->q->grid_elems : (batch->d ? batch->d->grid_elems : batch->f->grid_elems);
+    });
+}
+
 tval3_status tval3_batch_destroy(tval3_batch batch) {
     return guard([&] { delete batch; });
 }

@@ -14,6 +14,10 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <typeinfo>
 #include <vector>
 #include "solver.h"
 
@@ -55,6 +59,13 @@ struct Body {
     }
 };
 
+
+// Elements per block of the vector and reduction kernels, per vector type,
+// device and problem shape, as a batch's tuning chose them: a later solver
+// of the same shape takes the same grid, so its reductions add in the same
+// order as the batch's (results identical to the batched ones).
+static std::mutex g_grid_mu;
+static std::map<std::string, long> g_grid_epb;
 
 template <class T>
 Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_, int L_)
@@ -100,9 +111,27 @@ Solver<T>::Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_option
     // 256 threads per SM (a full SM); each launcher trims it further to the
     // blocks its kernel can keep resident.  Partials of the widest reduction
     // (10 values) fit in `part` up to 6,553 blocks.
-    const long cap = std::max(1, std::min(num_sms() * 8, 6553));
-    B.grid = (int)std::max<long>(1, std::min<long>(cap, (std::max<long>(n, m) + 1023) / 1024));
+    set_grid_elems(1024);
+    {
+        std::lock_guard<std::mutex> lk(g_grid_mu);
+        auto it = g_grid_epb.find(grid_key());
+        if (it != g_grid_epb.end()) set_grid_elems(it->second);
+    }
     B.trace = trace.p;
+}
+
+template <class T>
+void Solver<T>::set_grid_elems(long epb) {
+    const long cap = std::max(1, std::min(num_sms() * 8, 6553));
+    B.grid = (int)std::max<long>(1, std::min<long>(cap, (std::max<long>(n, m) + epb - 1) / std::max<long>(epb, 1)));
+}
+
+template <class T>
+std::string Solver<T>::grid_key() const {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return std::string(typeid(T).name()) + "/" + std::to_string(dev) + "/" + std::to_string(n) + "/" +
+           std::to_string(m);
 }
 
 template <class T>
@@ -619,6 +648,86 @@ Batch<T>::~Batch() {
 }
 
 template <class T>
+cudaGraphExec_t Batch<T>::build(const void* const* b, void* const* U, const void* const* Ut) {
+    const size_t k = s.size();
+    cudaGraphExec_t ex = nullptr;
+    cudaGraph_t top;
+    TV3_CUDA(cudaGraphCreate(&top, 0));
+    cudaStream_t cs;
+    TV3_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    try {
+        for (size_t i = 0; i < k; ++i) {
+            s[i]->xstar = nullptr;
+            s[i]->B.xstar = nullptr;
+            s[i]->add_to_graph(top, b[i], U[i], Ut[i], cs);
+        }
+        TV3_CUDA(cudaGraphInstantiate(&ex, top, 0));
+    } catch (...) {
+        cudaStreamDestroy(cs);
+        cudaGraphDestroy(top);
+        throw;
+    }
+    cudaStreamDestroy(cs);
+    cudaGraphDestroy(top);
+    return ex;
+}
+
+// Tuning of the vector kernels' grid: small slices cannot fill the GPU one
+// by one, and how many blocks each slice's kernels take decides how well the
+// slices run side by side.  Each candidate runs the whole batch as one graph
+// for at most 12 iterations per slice (timed after a warm-up launch); the
+// default (1,024 elements per block) is kept unless another is 3 % faster.
+// The tuning solves write the caller's U, which the real solve overwrites.
+template <class T>
+void Batch<T>::tune(const void* const* b, void* const* U, const void* const* Ut, cudaStream_t st) {
+    const size_t k = s.size();
+    const long cand[] = {1024, 512, 2048, 4096};
+    std::vector<int> keep(k);
+    for (size_t i = 0; i < k; ++i) {
+        keep[i] = s[i]->o.maxit;
+        s[i]->o.maxit = std::min(s[i]->o.maxit, 12);
+    }
+    cudaEvent_t e0, e1;
+    TV3_CUDA(cudaEventCreate(&e0));
+    TV3_CUDA(cudaEventCreate(&e1));
+    float best = 0.f;
+    long best_c = 1024;
+    try {
+        for (long c : cand) {
+            for (auto* x : s) x->set_grid_elems(c);
+            cudaGraphExec_t ex = build(b, U, Ut);
+            TV3_CUDA(cudaGraphLaunch(ex, st));
+            TV3_CUDA(cudaEventRecord(e0, st));
+            TV3_CUDA(cudaGraphLaunch(ex, st));
+            TV3_CUDA(cudaEventRecord(e1, st));
+            TV3_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            TV3_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            cudaGraphExecDestroy(ex);
+            if (c == 1024 || ms < 0.97f * best) {
+                best = ms;
+                best_c = c;
+            }
+        }
+    } catch (...) {
+        for (size_t i = 0; i < k; ++i) s[i]->o.maxit = keep[i];
+        for (auto* x : s) x->set_grid_elems(1024);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (size_t i = 0; i < k; ++i) s[i]->o.maxit = keep[i];
+    grid_elems = best_c;
+    std::lock_guard<std::mutex> lk(g_grid_mu);
+    for (auto* x : s) {
+        x->set_grid_elems(best_c);
+        g_grid_epb[x->grid_key()] = best_c;
+    }
+}
+
+template <class T>
 void Batch<T>::solve(const void* const* b, void* const* U, const void* const* Ut, tval3_info* infos,
                      cudaStream_t st) {
     const size_t k = s.size();
@@ -629,24 +738,11 @@ void Batch<T>::solve(const void* const* b, void* const* U, const void* const* Ut
             cudaGraphExecDestroy(gexec);
             gexec = nullptr;
         }
-        cudaGraph_t top;
-        TV3_CUDA(cudaGraphCreate(&top, 0));
-        cudaStream_t cs;
-        TV3_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        try {
-            for (size_t i = 0; i < k; ++i) {
-                s[i]->xstar = nullptr;
-                s[i]->B.xstar = nullptr;
-                s[i]->add_to_graph(top, b[i], U[i], Ut[i], cs);
-            }
-            TV3_CUDA(cudaGraphInstantiate(&gexec, top, 0));
-        } catch (...) {
-            cudaStreamDestroy(cs);
-            cudaGraphDestroy(top);
-            throw;
+        if (!tuned) {
+            tuned = true;
+            if (k > 1) tune(b, U, Ut, st);
         }
-        cudaStreamDestroy(cs);
-        cudaGraphDestroy(top);
+        gexec = build(b, U, Ut);
         g_b.assign(b, b + k);
         g_U.assign(U, U + k);
         g_Ut.assign(Ut, Ut + k);

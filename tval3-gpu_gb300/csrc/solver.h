@@ -1,6 +1,7 @@
 // TVAL3 solver workspace and loop driver (internal).
 #pragma once
 
+#include <string>
 #include <vector>
 #include "dbuf.h"
 #include "ops.h"
@@ -40,6 +41,10 @@ struct Solver {
     const void* r_Ut = nullptr;
 
     Solver(const LinOp<T>* A_, int p_, int q_, int r_, const tval3_options& o_, int L_ = 1);
+    // grid of the vector and reduction kernels: about epb elements per block
+    // (1,024 by default, or the value a batch's tuning stored for this shape)
+    void set_grid_elems(long epb);
+    std::string grid_key() const;
     ~Solver();
     // b, U and Ut are device arrays of the caller-facing type Ext<T>
     // (float for float vectors, double for double and double-float vectors)
@@ -81,11 +86,19 @@ struct Batch {
     cudaGraphExec_t gexec = nullptr;
     std::vector<const void*> g_b, g_Ut;
     std::vector<void*> g_U;
+    bool tuned = false;
+    long grid_elems = 1024;  // the tuned elements per block of the vector kernels
 
     ~Batch();
     // b[i], U[i], Ut[i] (may be NULL): device arrays of the type Ext<T>;
     // infos[i].secs is the time of the whole batch
     void solve(const void* const* b, void* const* U, const void* const* Ut, tval3_info* infos, cudaStream_t st);
+
+   private:
+    cudaGraphExec_t build(const void* const* b, void* const* U, const void* const* Ut);
+    // times short solves of the whole batch with 512 ... 4,096 elements per
+    // block of the vector kernels and keeps the fastest
+    void tune(const void* const* b, void* const* U, const void* const* Ut, cudaStream_t st);
 };
 
 }  // namespace tv3

@@ -453,6 +453,13 @@ class Batch:
         check(load().tval3_batch_solve(self._h, pb, pU, pUt, infos, _stream(stream)))
         return [i.as_dict() for i in infos]
 
+    @property
+    def tuned_grid(self) -> int:
+        """Elements per block of the vector kernels chosen by the first solve."""
+        v = C.c_int64()
+        check(load().tval3_batch_tuned_grid(self._h, C.byref(v)))
+        return v.value
+
     def close(self):
         if self._h:
             load().tval3_batch_destroy(self._h)

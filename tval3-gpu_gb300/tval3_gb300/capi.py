@@ -135,6 +135,7 @@ _SIG = {
     "tval3_batch_create": (_I, [_P, _P, _P, _I, _P]),
     "tval3_batch_solve": (_I, [_P, _P, _P, _P, _P, _P]),
     "tval3_batch_destroy": (_I, [_P]),
+    "tval3_batch_tuned_grid": (_I, [_P, _P]),
     "tval3_gpu_batched": (_I, [_P, _I, _P, _P]),
     "tval3_dense_rmatvec_f32_noalloc": (_I, [_I, _I, _P, _P, _P, _P]),
 }
