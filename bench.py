@@ -472,6 +472,8 @@ def run_ours(args):
                "entry": ("tval3_gpu_3d_sparse_f64" if dtn == np.float64 else "tval3_gpu_3d_sparse_f32") +
                         f" (FP32 CSR+CSC values, host arrays, mode {head})",
                "phases_mean_s": {k: round(float(np.mean([p[k] for p in phases])), 5) for k in phases[0]},
+               "median_s": round(float(np.median(et)), 5),
+               "calls_s": [round(t, 5) for t in et], "upload_calls_s": [round(p["upload_s"], 5) for p in phases],
                "h2d_at_measured_rate_s": round(h2d / h2d_rate(torch, dev, h2d), 5)}
 
     batched = batched_2d(args, T, torch, dev) if args.batch > 0 else None

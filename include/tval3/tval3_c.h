@@ -178,8 +178,9 @@ TVAL3_API const char* tval3_last_error_message(void);
  * download of U; then parts of those: [4] matrix upload, [5] input
  * validation, [6] operator layout (device copies, transpose, quantisation,
  * ray-matrix build), [7] tile-staged layouts and kernel choice, [8] graph
- * capture and instantiation.  n entries are written (at most 9).  No
- * counterpart in the reference. */
+ * capture and instantiation, [9] the host-to-device copies alone (inside
+ * [4], which also holds the device allocations).  n entries are written (at
+ * most 10).  No counterpart in the reference. */
 TVAL3_API tval3_status tval3_last_call_phases(double* secs, int n);
 TVAL3_API const char* tval3_version(void);
 

@@ -207,7 +207,7 @@ def test_geometry_siddon_on_the_fly_solve(cuda, oracle, iso):
 
 
 def test_entry_phases_reported(cuda, oracle):
-    """tval3_last_call_phases after a host entry call: nine non-negative
+    """tval3_last_call_phases after a host entry call: ten non-negative
     figures; the upload, validation and layout parts fit inside the operator
     phase, the tile and graph parts inside set-up plus solve, and the four
     main phases inside the call's wall time."""
@@ -220,7 +220,8 @@ def test_entry_phases_reported(cuda, oracle):
     tval3_gpu_3d((64, 64, 1), A, b, dict(OPTS, maxit=20))
     wall = time.perf_counter() - t0
     ph = last_call_phases()
-    assert len(ph) == 9 and all(v >= 0.0 for v in ph.values())
+    assert len(ph) == 10 and all(v >= 0.0 for v in ph.values())
+    assert ph["copy_s"] <= ph["upload_s"] + ph["setup_s"] + 1e-6
     main = ph["operator_s"] + ph["setup_s"] + ph["solve_s"] + ph["download_s"]
     assert 0.0 < main <= wall
     assert ph["upload_s"] + ph["validate_s"] + ph["layout_s"] <= ph["operator_s"] + 1e-6

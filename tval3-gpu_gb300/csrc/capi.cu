@@ -102,6 +102,7 @@ bool device_reads_host_memory() {
 
 void h2d(void* dst, const void* src, size_t bytes) {
     if (!bytes) return;
+    PhaseTimer pc(5);
     if (!device_reads_host_memory()) {
         TV3_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
         return;
@@ -563,7 +564,7 @@ tval3_status tval3_last_call_phases(double* secs, int n) {
     return guard([&] {
         if (!secs || n < 0) arg_error(TVAL3_ERR_ARG, "Argument error: NULL phase array!");
         for (int i = 0; i < n && i < 4; ++i) secs[i] = g_phase[i];
-        for (int i = 4; i < n && i < 9; ++i) secs[i] = sub_phase[i - 4];
+        for (int i = 4; i < n && i < 10; ++i) secs[i] = sub_phase[i - 4];
     });
 }
 const char* tval3_version(void) { return "tval3-gb300 0.1 (sm_103a)"; }

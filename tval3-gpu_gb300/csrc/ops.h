@@ -16,9 +16,10 @@ namespace tv3 {
 // Seconds spent in the parts of the last host entry call on this thread:
 // [0] matrix upload, [1] input validation, [2] operator layout (copies,
 // transposes, quantisation, ray-matrix build), [3] tile layouts and kernel
-// choice, [4] graph capture and instantiation.  Entry points reset it; a
-// PhaseTimer adds the wall time of its scope.
-inline thread_local double sub_phase[5] = {0, 0, 0, 0, 0};
+// choice, [4] graph capture and instantiation, [5] the host-to-device copies
+// alone (inside [0]).  Entry points reset it; a PhaseTimer adds the wall time
+// of its scope.
+inline thread_local double sub_phase[6] = {0, 0, 0, 0, 0, 0};
 struct PhaseTimer {
     int k;
     std::chrono::steady_clock::time_point t0;

@@ -197,16 +197,19 @@ __global__ void __launch_bounds__(512) k_spmv_tiled(TiledArgs<T, V> a) {
             if (ray[u] >= 0) ysm[j0 + u * blockDim.x] = v[u];
     }
     __syncthreads();
-    // work units: at most UNIT_K steps of one slice, so warps get equal work
+    // work units: at most UNIT_K steps of one slice, so warps get equal work.
+    // A unit is one 16-byte descriptor (its first entry and its steps); the
+    // warp's next descriptor is loaded while it sums the current unit.
+    longlong2 dnext = make_longlong2(0, 0);
+    if (u0 + warp < u1) dnext = __ldg(a.unit_desc + u0 + warp);
     for (int w = u0 + warp; w < u1; w += nwarps) {
-        const int sl = __ldg(a.unit_slice + w);
-        const long long off = a.slice_off[sl];
-        const int len = (int)((a.slice_off[sl + 1] - off) >> 5);
-        const int k0 = __ldg(a.unit_k0 + w), k1 = min(len, k0 + TILED_UNIT_K);
-        const unsigned short* __restrict__ li = a.lidx + off + lane;
-        const V* __restrict__ va = a.val + off + lane;
+        const longlong2 dc = dnext;
+        if (w + nwarps < u1) dnext = __ldg(a.unit_desc + w + nwarps);
+        const unsigned short* __restrict__ li = a.lidx + dc.x + lane;
+        const V* __restrict__ va = a.val + dc.x + lane;
+        const int k1 = (int)dc.y;
         RowAcc<T> acc;
-        int k = k0;
+        int k = 0;
         for (; k + U <= k1; k += U) {
             unsigned short ii[U];
             VV vv[U];
@@ -634,6 +637,17 @@ void TiledT<T, V>::build_shape(long n_, long m, int p, int q, int r, const int* 
         return;
     }
     nunits = (int)uslice.size();
+    {
+        std::vector<longlong2> desc(std::max(nunits, 1), make_longlong2(0, 0));
+        for (int u = 0; u < nunits; ++u) {
+            const int sl = uslice[u];
+            const long long len = (soff[sl + 1] - soff[sl]) / 32;
+            const long long k0 = uk0[u], k1 = std::min(len, k0 + (long long)TILED_UNIT_K);
+            desc[u] = make_longlong2(soff[sl] + 32LL * k0, std::max(k1 - k0, 0LL));
+        }
+        unit_desc.alloc(desc.size());
+        TV3_CUDA(cudaMemcpy(unit_desc.p, desc.data(), desc.size() * sizeof(longlong2), cudaMemcpyHostToDevice));
+    }
     tile_unit.alloc(ntiles + 1);
     slice_unit.alloc(nslices + 1);
     unit_slice.alloc(std::max(nunits, 1));
@@ -755,6 +769,7 @@ void TiledT<T, V>::apply(const TiledArgs<T, V>& a, int epi, cudaStream_t s) cons
     b.nwork = nwork;
     b.zrows = zrows.p;
     b.nzero = nzero;
+    b.unit_desc = unit_desc.p;
     const long grid = std::max<long>((long)nwork, 1);
     if (epi == SPMV_SUB) launch_k(k_spmv_tiled<T, V, SPMV_SUB, 8>, dim3((unsigned)grid), dim3(512), smem, s, b);
     else launch_k(k_spmv_tiled<T, V, SPMV_PLAIN, 8>, dim3((unsigned)grid), dim3(512), smem, s, b);

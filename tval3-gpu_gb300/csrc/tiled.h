@@ -27,6 +27,7 @@ struct TiledArgs {
     const int* slice_unit;       // nslices + 1: the slice's work units
     const int* unit_slice;       // slice of each unit
     const unsigned short* unit_k0;  // first step of each unit
+    const longlong2* unit_desc;     // per unit: {its first entry (lane 0), its steps}
     int max_rays;                // shared memory: max_rays values of y, then 32 partials per unit
     const float* xscale;       // per-ray scale of the gathered y (16-bit storage), or null
     const T* x[2];             // y (the input of A^T), ping-pong by parity
@@ -64,6 +65,7 @@ struct TiledT {
     long long padded_entries = 0;
     DBuf<int> ray_off, rays, tile_slice, row_voxel, tile_unit, slice_unit, unit_slice;
     DBuf<unsigned short> unit_k0;
+    DBuf<longlong2> unit_desc;
     DBuf<long long> slice_off;
     DBuf<unsigned short> lidx;
     DBuf<V> val;

@@ -238,7 +238,7 @@ def last_call_phases() -> dict:
     upload, validation, operator layout, tile layouts + kernel choice and
     graph build (tval3_last_call_phases)."""
     names = ("operator_s", "setup_s", "solve_s", "download_s", "upload_s", "validate_s", "layout_s", "tiles_s",
-             "graph_s")
+             "graph_s", "copy_s")
     out = (C.c_double * len(names))()
     check(load().tval3_last_call_phases(out, len(names)))
     return dict(zip(names, list(out)))
