@@ -228,6 +228,26 @@ def test_entry_phases_reported(cuda, oracle):
     assert ph["tiles_s"] + ph["graph_s"] <= ph["setup_s"] + ph["solve_s"] + 1e-6
 
 
+def test_uploads_from_unaligned_host_arrays(cuda, oracle):
+    """Host arrays that start 4 bytes past a 16-byte boundary (numpy views)
+    upload like aligned ones: the host entry's result is bit-identical."""
+    from tval3_gb300 import SparseMatrix, tval3_gpu_3d
+    geo, x, ptr, ind, val, b = _problem(oracle, 32, 48, seed=3)
+
+    def shifted(a):
+        buf = np.zeros(a.size + 4, dtype=a.dtype)
+        out = buf[1:1 + a.size]
+        out[:] = a
+        return out
+
+    o = dict(OPTS, maxit=30)
+    U1, i1 = tval3_gpu_3d((32, 32, 1), SparseMatrix(ptr.size - 1, x.size, ptr, ind, val), b, o)
+    sp, si, sv, sb = shifted(ptr), shifted(ind), shifted(val), shifted(np.asarray(b, dtype=np.float32))
+    assert sp.ctypes.data % 16 != 0 and si.ctypes.data % 16 != 0
+    U2, i2 = tval3_gpu_3d((32, 32, 1), SparseMatrix(ptr.size - 1, x.size, sp, si, sv), sb, o)
+    assert np.array_equal(U1, U2) and i1["total_iters"] == i2["total_iters"]
+
+
 def test_dense_entry_points(cuda, oracle):
     from tval3_gb300 import DenseMatrix, tval3_gpu
     geo, x, ptr, ind, val, b = _problem(oracle)

@@ -69,60 +69,15 @@ struct tval3_solver_s {
 
 namespace {
 
-// Upload of a caller's host array.  Where the device reads pageable host
-// memory through the host's own page tables (Grace systems over NVLink-C2C:
-// cudaDevAttrPageableMemoryAccessUsesHostPageTables), a copy kernel reads
-// the array in place at the link's rate, with no host thread staging it
-// through pinned buffers (so a busy host does not slow the upload);
-// elsewhere cudaMemcpy.  Synchronous like cudaMemcpy on return.
-__global__ void k_h2d16(const int4* __restrict__ src, int4* __restrict__ dst, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        dst[i] = src[i];
-}
-__global__ void k_h2d1(const unsigned char* __restrict__ src, unsigned char* __restrict__ dst, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        dst[i] = src[i];
-}
-
-bool device_reads_host_memory() {
-    constexpr int MAXDEV = 64;
-    static std::atomic<int> known[MAXDEV] = {};  // 0 unknown, 1 no, 2 yes
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAXDEV) return false;
-    int k = known[dev].load();
-    if (!k) {
-        int pma = 0, hpt = 0;
-        if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) pma = 0;
-        if (cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) hpt = 0;
-        k = (pma && hpt) ? 2 : 1;
-        known[dev].store(k);
-    }
-    return k == 2;
-}
-
+// Upload of a caller's host array (timed as its own phase).  cudaMemcpy from
+// pageable memory runs at the link's rate on Grace systems (~190 GB/s for
+// 440 MB); a device copy kernel reading the array through the host's page
+// tables was as fast in steady state but now and then took 15-50 ms for the
+// same 440 MB, when the translations had to be walked again.
 void h2d(void* dst, const void* src, size_t bytes) {
     if (!bytes) return;
     PhaseTimer pc(5);
-    if (!device_reads_host_memory()) {
-        TV3_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
-        return;
-    }
-    const int grid = num_sms() * 4;
-    const uintptr_t a = (uintptr_t)src, b = (uintptr_t)dst;
-    size_t head = 0;
-    if ((a % 16) == (b % 16)) {
-        head = std::min(bytes, (size_t)((16 - a % 16) % 16));
-        const size_t body = (bytes - head) / 16;
-        if (body) k_h2d16<<<grid, 256>>>((const int4*)((const char*)src + head), (int4*)((char*)dst + head), body);
-        const size_t done = head + body * 16;
-        if (head) k_h2d1<<<1, 32>>>((const unsigned char*)src, (unsigned char*)dst, head);
-        if (bytes > done)
-            k_h2d1<<<1, 256>>>((const unsigned char*)src + done, (unsigned char*)dst + done, bytes - done);
-    } else {
-        k_h2d1<<<grid, 256>>>((const unsigned char*)src, (unsigned char*)dst, bytes);
-    }
-    TV3_CUDA(cudaGetLastError());
-    TV3_CUDA(cudaStreamSynchronize(0));
+    TV3_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
 }
 
 thread_local std::string g_err;
