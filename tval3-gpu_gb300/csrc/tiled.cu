@@ -253,8 +253,9 @@ __global__ void __launch_bounds__(512) k_spmv_tiled(TiledArgs<T, V> a) {
 //
 // Every mbarrier wait is bounded.  On a timeout the warp records
 // ERR_TILED_TIMEOUT, stops computing, keeps taking part in the consumers'
-// named barriers so no warp is left waiting, and the producer waits (bounded)
-// for its own copies in flight before it returns.
+// named barriers so no warp is left waiting, releases a y buffer only after a
+// second bounded wait for its gathers, and the producer waits (bounded) for
+// its own copies in flight before it returns.
 // ---------------------------------------------------------------------------
 template <class T, class V, int EPI, int U>
 __global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 1), 1) k_spmv_tiled_pipe(TiledArgs<T, V> a, PipeArgs pa) {
@@ -343,7 +344,12 @@ __global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 1), 1) k_spmv_tiled_pip
             re1 = __ldg(a.slice_unit + sl + 1) - u0;
             if (EPI == SPMV_SUB && rv >= 0) rsub = a.sub[rv];
         }
-        if (ok) ok = __all_sync(FULL, mbar_wait(&yfull[yb], (unsigned)((i >> 1) & 1)));
+        // the y buffer is released only after its gathers have landed: a wait
+        // that ran out (or a warp already failed) waits once more for them
+        if (!(ok && __all_sync(FULL, mbar_wait(&yfull[yb], (unsigned)((i >> 1) & 1))))) {
+            ok = false;
+            mbar_wait(&yfull[yb], (unsigned)((i >> 1) & 1));
+        }
         const T* ysm = ybuf + (size_t)yb * pa.ybuf_elems;
         if (ok) {
             for (int w = u0 + warp; w < u1; w += PIPE_CONSUMERS) {
