@@ -265,6 +265,34 @@ def test_empty_rays_and_empty_matrix(cuda, oracle):
     op.mat_vec_mul(0, torch.ones(op.cols, device=cuda), y)
     torch.cuda.synchronize()
     assert float(y[0]) == 0.0
+    # the on-the-fly operator of the same rays: the missing ray's row is 0,
+    # the other one's sum is the stored row's, A^T of a one-hot y is its column
+    fly = Operator.from_geometry(geo, mode=1)
+    assert fly.nnz == ind.size
+    yf = torch.full((op.rows,), 7.0, device=cuda)
+    fly.mat_vec_mul(0, torch.ones(op.cols, device=cuda), yf)
+    xt = torch.full((op.cols,), 7.0, device=cuda)
+    onehot = torch.zeros(op.rows, device=cuda)
+    onehot[1] = 1.0
+    fly.mat_vec_mul(1, onehot, xt)
+    torch.cuda.synchronize()
+    assert float(yf[0]) == 0.0 and abs(float(yf[1]) - float(y[1])) <= 1e-6 * abs(float(y[1]))
+    col = np.zeros(op.cols)
+    col[ind[ptr[1]:ptr[2]]] = val[ptr[1]:ptr[2]]
+    assert np.allclose(xt.cpu().numpy(), col, rtol=0, atol=1e-7)
+    # every ray misses: no tile runs at all, both products are zeros
+    miss = Geometry(rv_x=8, rv_y=8, rv_z=1, x_emitters=[0], y_emitters=[0], z_emitters=[0],
+                    x_receivers=[0], y_receivers=[0], z_receivers=[0], traversal=1,
+                    pos=(np.array([-2.0]), np.array([-2.0]), np.array([0.5]),
+                         np.array([-2.0]), np.array([9.0]), np.array([0.5])))
+    fm = Operator.from_geometry(miss, mode=1)
+    assert fm.nnz == 0
+    ym = torch.full((1,), 3.0, device=cuda)
+    xm = torch.full((64,), 3.0, device=cuda)
+    fm.mat_vec_mul(0, torch.ones(64, device=cuda), ym)
+    fm.mat_vec_mul(1, torch.ones(1, device=cuda), xm)
+    torch.cuda.synchronize()
+    assert float(ym[0]) == 0.0 and float(xm.abs().sum()) == 0.0
 
 
 @pytest.mark.parametrize("traversal", [0, 1])
