@@ -100,6 +100,10 @@ def parse():
                     help="pin the tile-staged kernels of both products (profiling runs, where the build-time "
                          "timing under a profiler may pick others)")
     ap.add_argument("--only-fly", action="store_true", help="time only the on-the-fly products (development)")
+    ap.add_argument("--only-e2e", type=int, default=0,
+                    help="time only this many host-entry calls (double-float, maxit = --e2e-maxit) and print each "
+                         "call's phases (development)")
+    ap.add_argument("--e2e-maxit", type=int, default=133, help="iterations of the --only-e2e calls (K* at 128^3)")
     ap.add_argument("--solver-mode", type=int, default=1,
                     help="1: whole solve as one CUDA graph; 0: host-driven loop (same kernels; profilers "
                          "cannot see kernels inside graphs with conditional nodes)")
@@ -276,6 +280,8 @@ def run_ours(args):
         return spmv_only(args, T, torch, geo, op32, n, m, nnz, dev)
     if args.only_fly:
         return {"on_the_fly": on_the_fly(args, T, torch, geo, op32, n, m, nnz, dev)}
+    if args.only_e2e:
+        return {"e2e_calls": e2e_calls(args, T, cfg, x_true, op32, n, m)}
     if args.only_batched:
         return {"batched_2d": batched_2d(args, T, torch, dev)}
     if args.only_dense:
@@ -995,6 +1001,27 @@ def spmv_only(args, T, torch, geo, op32, n, m, nnz, dev):
     peak, kind = peaks()
     return {"spmv_only": args.only_spmv, "nnz": nnz, "rows": m, "cols": n, "peak_GBs": peak, "peak_source": kind,
             **res}
+
+
+def e2e_calls(args, T, cfg, x_true, op32, n, m):
+    """args.only_e2e calls of the reference-facing entry point
+    (tval3_gpu_3d_sparse_f64, double-float, host CSR + CSC arrays) with the
+    phases of each call (tval3_last_call_phases), in ms."""
+    from tval3_gb300.api import last_call_phases
+    from tval3_gb300.workloads import add_noise
+    ptr, ind, val, tptr, tind, tval = op32.export_csr()
+    op32.close()
+    b = add_noise(csr_matvec64(ptr, ind, val, x_true.reshape(-1)), cfg.noise, cfg.seed).astype(np.float64)
+    A = T.SparseMatrix(m, n, ptr, ind, val, tptr, tind, tval)
+    opts = dict(cfg.opts, maxit=args.e2e_maxit, precision=T.PREC_FP32_DF64)
+    out = []
+    for _ in range(args.only_e2e):
+        t0 = time.perf_counter()
+        T.tval3_gpu_3d(cfg.dims, A, b, opts, dtype=np.float64)
+        dt = time.perf_counter() - t0
+        out.append(dict({"total_ms": round(dt * 1e3, 2)},
+                        **{k.replace("_s", "_ms"): round(v * 1e3, 2) for k, v in last_call_phases().items()}))
+    return out
 
 
 def on_the_fly(args, T, torch, geo, op32, n, m, nnz, dev, reps=10):
