@@ -182,6 +182,71 @@ def test_fused_step_matches_eager_reference(cuda, oracle, iso):
     assert abs(float(gbt1) - float(gbt2)) <= 1e-8 * abs(float(gbt2)) + 1e-14
 
 
+def _numpy_unrolled(ptr, ind, val, b, dims, mu, beta, iters, iso=True, nonneg=True):
+    """The unrolled map in numpy (FP64, CPU), from the formulas alone:
+    periodic forward differences on the [z, x, y] volume, isotropic or
+    anisotropic shrinkage, the Barzilai-Borwein step and the projection."""
+    import scipy.sparse as sp
+    p, q, r = dims
+    n = p * q * r
+    A = sp.csr_matrix((val.astype(np.float64), ind, ptr), shape=(ptr.size - 1, n))
+
+    def D(u):
+        v = u.reshape(r, q, p)
+        return np.concatenate([(np.roll(v, -1, 2) - v).ravel(), (np.roll(v, -1, 1) - v).ravel(),
+                               (np.roll(v, -1, 0) - v).ravel()])
+
+    def Dt(w):
+        a, c, e = (w[k * n:(k + 1) * n].reshape(r, q, p) for k in range(3))
+        return ((np.roll(a, 1, 2) - a) + (np.roll(c, 1, 1) - c) + (np.roll(e, 1, 0) - e)).ravel()
+
+    def shrink(v, t):
+        v3 = v.reshape(3, n)
+        if iso:
+            nv = np.sqrt((v3 * v3).sum(0))
+            sc = np.where(nv > t, (nv - t) / np.where(nv > 0, nv, 1.0), 0.0)
+            return (v3 * sc).ravel()
+        return (np.sign(v3) * np.maximum(np.abs(v3) - t, 0.0)).ravel()
+
+    kap = mu / beta
+    U = A.T @ b
+    Up = gp = g2p = None
+    for k in range(iters):
+        DU = D(U)
+        W = shrink(DU, 1.0 / beta)
+        g2 = Dt(DU - W)
+        g = A.T @ (A @ U - b)
+        d = g2 + kap * g
+        if k == 0:
+            Dd, Ad = D(d), A @ d
+            tau = abs(d @ d / (Dd @ Dd + kap * (Ad @ Ad)))
+        else:
+            s_ = U - Up
+            tau = abs(s_ @ s_ / (s_ @ ((g2 - g2p) + kap * (g - gp))))
+        Un = U - tau * d
+        if nonneg:
+            Un = np.maximum(Un, 0.0)
+        Up, gp, g2p, U = U, g, g2, Un
+    return U
+
+
+@pytest.mark.parametrize("iso", [True, False])
+def test_fused_forward_matches_numpy(cuda, oracle, iso):
+    """The fused unrolled map's U_K against a numpy evaluation of the same
+    formulas on the CPU (FP64; only summation orders differ): 8 steps on a
+    12^3 hemisphere problem."""
+    import torch
+    from tval3_gb300 import autograd as AG
+    cfg, geo, x, op = _op64(oracle, 12, 8, seed=5)
+    ptr, ind, val = oracle.siddon_csr(geo)
+    from tval3_gb300 import workloads as W
+    b = W.add_noise(oracle.spmv(ptr, ind, val, x), 0.01, 5).astype(np.float64)
+    b *= 1.5 / abs(b.max() - b.min())
+    U = AG.unrolled_tval3(op, torch.tensor(b, device=cuda), cfg.dims, 512.0, 64.0, iters=8, iso=iso)
+    Un = _numpy_unrolled(ptr, ind, val, b, cfg.dims, 512.0, 64.0, 8, iso=iso)
+    assert np.linalg.norm(U.cpu().numpy() - Un) <= 1e-10 * np.linalg.norm(Un)
+
+
 @pytest.mark.parametrize("first", [True, False])
 def test_inner_step_gradcheck(cuda, oracle, first):
     """torch.autograd.gradcheck of one fused step wrt U, Up, gp, g2p, b and
