@@ -288,12 +288,13 @@ def test_skip_heuristic_matches_oracle(cuda, oracle, max_rel):
     assert np.array_equal(outs[0], outs[1])
 
 
-@pytest.mark.parametrize("dims", [(15, 14, 1), (9, 7, 5), (16, 12, 6)])
+@pytest.mark.parametrize("dims", [(15, 14, 1), (9, 7, 5), (16, 12, 6), (70, 9, 3), (2, 3, 4), (130, 17, 2)])
 def test_fp64_odd_and_even_volumes(cuda, oracle, dims):
     """The pass-per-vector kernels take two voxels per 16-byte access when the
     fastest dimension (stencils) or the volume (plain streams) is even, one
     voxel otherwise; FP64 solves of odd and even volumes keep the oracle's
-    control flow and result."""
+    control flow and result (p = 2: a single voxel pair along y, its own
+    periodic neighbour)."""
     from tval3_gb300 import SparseMatrix, tval3_gpu_3d
     from tval3_gb300 import workloads as W
     p, q, r = dims
@@ -316,3 +317,4 @@ def test_fp64_odd_and_even_volumes(cuda, oracle, dims):
     assert (ig["total_iters"], ig["outer_iters"], ig["backtracks"], ig["restarts"]) == \
         (io["total_iters"], io["outer_iters"], io["backtracks"], io["restarts"])
     assert np.linalg.norm(Ug.reshape(-1) - Uo.reshape(-1)) <= 1e-7 * np.linalg.norm(Uo)
+
