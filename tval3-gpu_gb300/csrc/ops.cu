@@ -336,7 +336,9 @@ struct CsrOp : LinOp<T> {
             t.p = tiledN.p; t.q = tiledN.q; t.r = tiledN.r; t.ty = tiledN.ty; t.tx = tiledN.tx; t.tz = tiledN.tz;
             t.nty = tiledN.nty; t.ntx = tiledN.ntx;
             t.tile_slice = tiledN.tile_slice.p; t.slice_off = tiledN.slice_off.p; t.slot_dest = tiledN.slot_dest.p;
-            t.lidx = tiledN.lidx.p; t.val = tiledN.val.p; t.part = tiledN.part.p; t.rseg = tiledN.rseg.p;
+            t.lidx = tiledN.lidx.p; t.val = tiledN.val.p; t.part = tiledN.part.p;
+            t.sray = tiledN.sray.p; t.rlen = tiledN.rlen.p;
+            t.gbase = tiledN.gbase.p;
             t.m = this->m; t.rscale = rs.p;
             t.x[0] = io.x[0]; t.x[1] = io.x[1]; t.y[0] = io.y[0]; t.y[1] = io.y[1];
             t.by_parity = io.by_parity; t.sub = io.sub; t.b = io.b; t.delta = io.delta; t.ctl = io.ctl;

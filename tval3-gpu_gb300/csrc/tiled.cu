@@ -150,7 +150,7 @@ template <class T, class V, int EPI, int U>
 __global__ void __launch_bounds__(512) k_spmv_tiled(TiledArgs<T, V> a) {
     count_launch(a.ctl);
     using VV = typename TVT<V>::type;
-    extern __shared__ __align__(16) unsigned char sm_raw[];
+    extern __shared__ __align__(128) unsigned char sm_raw[];
     T* ysm = reinterpret_cast<T*>(sm_raw);
     T* psm = ysm + a.max_rays;  // partial sums: 32 per work unit
     const int sel = a.by_parity ? a.ctl->parity : 0;
@@ -261,7 +261,7 @@ template <class T, class V, int EPI, int U>
 __global__ void __launch_bounds__(32 * (PIPE_CONSUMERS + 1), 1) k_spmv_tiled_pipe(TiledArgs<T, V> a, PipeArgs pa) {
     count_launch(a.ctl);
     using VV = typename TVT<V>::type;
-    extern __shared__ __align__(16) unsigned char sm_raw[];
+    extern __shared__ __align__(128) unsigned char sm_raw[];
     uint64_t* yfull = reinterpret_cast<uint64_t*>(sm_raw);  // 2
     uint64_t* yempty = yfull + 2;                             // 2
     uint64_t* rbar = yempty + 2;                              // 1
@@ -831,11 +831,57 @@ __global__ void k_n_segkeys(long nseg, const unsigned long long* __restrict__ se
     }
 }
 
-__global__ void k_n_dest(long nseg, const int* __restrict__ by_ray, const unsigned long long* __restrict__ k_ray_s,
-                         int tb, int* __restrict__ dest, int* __restrict__ rcount) {
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nseg; i += (long)gridDim.x * blockDim.x) {
-        dest[by_ray[i]] = (int)i;
+// partials per lane that the per-ray reduction stages in shared memory
+constexpr int RED_K0 = 16;
+
+__global__ void k_n_count(long nseg, const unsigned long long* __restrict__ k_ray_s, int tb, int* __restrict__ rcount) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nseg; i += (long)gridDim.x * blockDim.x)
         atomicAdd(rcount + (k_ray_s[i] >> tb), 1);
+}
+
+// Layout of the partials.  The rays of each window of 256 consecutive rays are
+// ranked by their number of partials (longest first, ties by ray), and the
+// rank gives each ray a slot: slot 256 w + rank.  Slots 32G .. 32G+31 form
+// group G, whose partials are interleaved: partial k of the ray in slot s at
+// gbase[G] + 32 k + s % 32, the group padded to its longest ray (rays of
+// similar length share a group, so the padding is small).
+__global__ void __launch_bounds__(256) k_n_slots(long m, const int* __restrict__ rcount, int* __restrict__ rslot,
+                                                 int* __restrict__ sray, int* __restrict__ slen) {
+    __shared__ int wl[256];
+    const long r = (long)blockIdx.x * 256 + threadIdx.x;
+    const int len = (r < m) ? rcount[r] : -1;
+    wl[threadIdx.x] = len;
+    __syncthreads();
+    if (r >= m) return;
+    int rank = 0;
+    for (int j = 0; j < 256; ++j) {
+        const int lj = wl[j];
+        rank += (lj > len) || (lj == len && j < (int)threadIdx.x);
+    }
+    const long sl = (long)blockIdx.x * 256 + rank;
+    rslot[r] = (int)sl;
+    sray[sl] = (int)r;
+    slen[sl] = len;
+}
+
+__global__ void k_n_group_len(long m, const int* __restrict__ slen, long long* __restrict__ glen) {
+    const long ng = (m + 31) / 32;
+    for (long g = (long)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (long)gridDim.x * blockDim.x) {
+        int mx = 0;
+        for (long sl = 32 * g; sl < min(m, 32 * g + 32); ++sl) mx = max(mx, slen[sl]);
+        glen[g] = 32LL * mx;
+    }
+}
+
+// destination of each segment's partial; the ray-major order i (ray, then
+// tile) gives the segment's place k = i - rseg[ray] among its ray's partials
+__global__ void k_n_dest(long nseg, const int* __restrict__ by_ray, const unsigned long long* __restrict__ k_ray_s,
+                         int tb, const int* __restrict__ rseg, const int* __restrict__ rslot,
+                         const long long* __restrict__ gbase, int* __restrict__ dest) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nseg; i += (long)gridDim.x * blockDim.x) {
+        const long ray = (long)(k_ray_s[i] >> tb);
+        const long sl = rslot[ray];
+        dest[by_ray[i]] = (int)(gbase[sl >> 5] + 32LL * (i - rseg[ray]) + (sl & 31));
     }
 }
 
@@ -1050,26 +1096,35 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
     if (!ok && lane == 0 && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
 }
 
-// Each ray's partials in tile order, one warp per 32 consecutive rays: the
-// warp's partials are contiguous (ray-major), so it loads them coalesced
-// into shared memory, 256 at a time, and every lane adds its ray's range in
-// order (for double-float partials a compensated sum: high parts by TwoSum,
-// low parts and errors in one FP32 term); then the solver epilogues.
+// Each ray's partials in tile order, one warp per group of 32 ray slots and
+// one lane per slot (rays of similar length, from one window of 256 rays).
+// The group's partials are interleaved (partial k of the ray in lane l's slot
+// at gbase + 32 k + l), so the k-th copies of the 32 lanes are one coalesced
+// row.  Each lane copies its first K0 partials into
+// its own column of shared memory with asynchronous copies (all in flight at
+// once, no registers held), waits for its own copies and adds them in order
+// (for double-float partials a compensated sum: high parts by TwoSum, low
+// parts and errors in one FP32 term); longer rays load the rest directly.
+// Then the solver epilogues.
 template <class T, class V, int EPI>
 __global__ void __launch_bounds__(256) k_tiledN_reduce(TiledNArgs<T, V> a) {
     count_launch(a.ctl);
-    constexpr int W = 256;
-    __shared__ T buf[8][W];
+    constexpr int K0 = RED_K0;
+    __shared__ T stage[8][K0][32];
     const int sel = a.by_parity ? a.ctl->parity : 0;
     T* __restrict__ y = a.y[sel];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T* wb = buf[warp];
     double acc0 = 0.0, acc1 = 0.0;
     const long nwarps = (long)gridDim.x * 8;
-    for (long rb = ((long)blockIdx.x * 8 + warp) * 32; rb < a.m; rb += nwarps * 32) {
-        const long r = rb + lane;
-        const int elo = __ldg(a.rseg + rb), ehi = __ldg(a.rseg + min(rb + 32, a.m));
-        const int ra = (r < a.m) ? __ldg(a.rseg + r) : 0, rz = (r < a.m) ? __ldg(a.rseg + r + 1) : 0;
+    for (long g = (long)blockIdx.x * 8 + warp; 32 * g < a.m; g += nwarps) {
+        const long sl = 32 * g + lane;
+        const long r = (sl < a.m) ? __ldg(a.sray + sl) : a.m;  // the slot's ray
+        const int len = (sl < a.m) ? __ldg(a.rlen + sl) : 0;
+        const T* __restrict__ pp = a.part + __ldg(a.gbase + g) + lane;
+#pragma unroll
+        for (int u = 0; u < K0; ++u)
+            if (u < len) cp_async<(int)sizeof(T)>(&stage[warp][u][lane], pp + 32 * u);
+        cp_async_commit();
         // the epilogue's inputs, loaded before the sums so their latency overlaps them
         T eb = T(0), ed = T(0);
         float esc = 1.f;
@@ -1083,19 +1138,16 @@ __global__ void __launch_bounds__(256) k_tiledN_reduce(TiledNArgs<T, V> a) {
             if (a.rscale) esc = __ldg(a.rscale + r);
         }
         RowAcc<T> acc;
-        for (int base = elo; base < ehi; base += W) {
-            T v[W / 32];
+        cp_async_wait_group<0>();  // this lane's copies have landed
+        const int l0 = min(len, K0);
+        for (int u = 0; u < l0; ++u) add(acc, stage[warp][u][lane]);
+        for (int k = K0; k < len; k += 8) {
+            T v[8];
 #pragma unroll
-            for (int u = 0; u < W / 32; ++u) {
-                const int e = base + lane + 32 * u;
-                v[u] = (e < ehi) ? a.part[e] : T(0);
-            }
+            for (int u = 0; u < 8; ++u) v[u] = (k + u < len) ? pp[32 * (k + u)] : T(0);
 #pragma unroll
-            for (int u = 0; u < W / 32; ++u) wb[lane + 32 * u] = v[u];
-            __syncwarp();
-            const int e1 = min(rz, base + W);
-            for (int e = max(ra, base); e < e1; ++e) add(acc, wb[e - base]);
-            __syncwarp();
+            for (int u = 0; u < 8; ++u)
+                if (k + u < len) add(acc, v[u]);
         }
         T s = acc.value();
         if (r < a.m) {
@@ -1183,7 +1235,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     TV3_CUDA(cudaMemcpy(&ns, segid.p + nnz - 1, sizeof(int), cudaMemcpyDeviceToHost));
     nseg = ns;
     TmpBuf<unsigned long long> seg_key(nseg), k_slice(nseg), k_slice_s(nseg), k_ray(nseg), k_ray_s(nseg);
-    TmpBuf<int> seg_start(nseg), iota_s(nseg), order(nseg), by_ray(nseg), dest(nseg), too_long(1), rcount(m + 1);
+    TmpBuf<int> seg_start(nseg), iota_s(nseg), order(nseg), by_ray(nseg), dest(nseg), too_long(1);
     k_n_segs<<<ewt(nnz), 256, 0, s>>>(nnz, key_s.p, segid.p, seg_key.p, seg_start.p);
     TV3_CUDA(cudaMemsetAsync(too_long.p, 0, sizeof(int), s));
     k_n_segkeys<<<ewt(nseg), 256, 0, s>>>(nseg, seg_key.p, seg_start.p, nnz, ray_bits, tile_bits, k_slice.p, k_ray.p,
@@ -1214,16 +1266,30 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     int tl = 0;
     TV3_CUDA(cudaMemcpy(&tl, too_long.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (tl) return;
-    TV3_CUDA(cudaMemsetAsync(rcount.p, 0, (m + 1) * sizeof(int), s));
-    k_n_dest<<<ewt(nseg), 256, 0, s>>>(nseg, by_ray.p, k_ray_s.p, tile_bits, dest.p, rcount.p);
-    rseg.alloc(m + 1);
+    TmpBuf<int> rcnt(m + 1), rseg(m + 1), rslot(std::max<long>(m, 1));
+    TV3_CUDA(cudaMemsetAsync(rcnt.p, 0, (m + 1) * sizeof(int), s));
+    k_n_count<<<ewt(nseg), 256, 0, s>>>(nseg, k_ray_s.p, tile_bits, rcnt.p);
+    const long ngroups = (m + 31) / 32;
+    sray.alloc(std::max<long>(m, 1));
+    rlen.alloc(std::max<long>(m, 1));
+    if (m > 0) k_n_slots<<<(int)((m + 255) / 256), 256, 0, s>>>(m, rcnt.p, rslot.p, sray.p, rlen.p);
+    TmpBuf<long long> glen(ngroups + 1);
+    gbase.alloc(ngroups + 1);
+    TV3_CUDA(cudaMemsetAsync(glen.p + ngroups, 0, sizeof(long long), s));
+    k_n_group_len<<<ewt(ngroups), 256, 0, s>>>(m, rlen.p, glen.p);
     {
-        size_t sb = 0;
-        TV3_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, sb, rcount.p, rseg.p, (int)(m + 1), s));
-        TmpBuf<char> tmp(std::max<size_t>(sb, 1));
-        TV3_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, sb, rcount.p, rseg.p, (int)(m + 1), s));
+        size_t sb = 0, sg = 0;
+        TV3_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, sb, rcnt.p, rseg.p, (int)(m + 1), s));
+        TV3_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, sg, glen.p, gbase.p, (int)(ngroups + 1), s));
+        TmpBuf<char> tmp(std::max<size_t>(std::max(sb, sg), 1));
+        TV3_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, sb, rcnt.p, rseg.p, (int)(m + 1), s));
+        TV3_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, sg, glen.p, gbase.p, (int)(ngroups + 1), s));
         TV3_CUDA(cudaStreamSynchronize(s));
     }
+    long long npart = 0;
+    TV3_CUDA(cudaMemcpy(&npart, gbase.p + ngroups, sizeof(long long), cudaMemcpyDeviceToHost));
+    if (npart >= (1LL << 31)) return;  // destinations are int
+    k_n_dest<<<ewt(nseg), 256, 0, s>>>(nseg, by_ray.p, k_ray_s.p, tile_bits, rseg.p, rslot.p, gbase.p, dest.p);
     // slices: each tile's segments in runs of 32 (every segment has entries)
     TmpBuf<int> tseg_d(ntiles + 1);
     SliceTables st;
@@ -1251,7 +1317,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
     lidx.alloc(std::max<long long>(padded, 1));
     val.alloc(std::max<long long>(padded, 1));
     slot_dest.alloc((size_t)std::max(nslices, 1) * 32);
-    part.alloc(std::max<long>(nseg, 1));
+    part.alloc(std::max<long long>(npart, 1));
     TV3_CUDA(cudaMemsetAsync(lidx.p, 0, std::max<long long>(padded, 1) * sizeof(unsigned short), s));
     TV3_CUDA(cudaMemsetAsync(val.p, 0, std::max<long long>(padded, 1) * sizeof(V), s));
     TV3_CUDA(cudaMemsetAsync(slot_dest.p, 0xff, (size_t)std::max(nslices, 1) * 32 * sizeof(int), s));

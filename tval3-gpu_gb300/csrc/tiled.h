@@ -128,7 +128,9 @@ struct TiledNArgs {
     const unsigned short* lidx;  // local voxel of each nonzero in its tile (0 in padding)
     const V* val;                // value (0 in padding)
     T* part;                     // one partial per segment, ray-major
-    const int* rseg;             // m + 1: ray r's partials are part[rseg[r] .. rseg[r+1])
+    const int* sray;             // m: the ray of each slot (slots: rays ranked by length in windows of 256)
+    const int* rlen;             // m: partials (segments) of the ray in each slot
+    const long long* gbase;      // per 32 slots: partial k of the ray in slot s is part[gbase[s/32] + 32 k + s%32]
     long m;
     const float* rscale;         // per-ray scale of the row sum (16-bit storage), or null
     const T* x[2];
@@ -150,7 +152,8 @@ struct TiledN {
     DBuf<int> tile_order;
     int p = 0, q = 0, r = 0, ty = 0, tx = 0, tz = 0, nty = 0, ntx = 0;
     long m = 0, nseg = 0;
-    DBuf<int> tile_slice, slot_dest, rseg;
+    DBuf<int> tile_slice, slot_dest, sray, rlen;
+    DBuf<long long> gbase;
     DBuf<long long> slice_off;
     DBuf<unsigned short> lidx;
     DBuf<V> val;
