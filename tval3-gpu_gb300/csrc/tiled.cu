@@ -1106,8 +1106,14 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
 // (for double-float partials a compensated sum: high parts by TwoSum, low
 // parts and errors in one FP32 term); longer rays load the rest directly.
 // Then the solver epilogues.
+// Six blocks per SM for float and double-float partials (at most 40
+// registers): the shared-memory stage allows six, and the lam3/lam5 form
+// otherwise takes 56 registers and runs four.  FP64 partials would spill.
+template <class T>
+constexpr int red_min_blocks() { return std::is_same<T, double>::value ? 1 : 6; }
+
 template <class T, class V, int EPI>
-__global__ void __launch_bounds__(256) k_tiledN_reduce(TiledNArgs<T, V> a) {
+__global__ void __launch_bounds__(256, red_min_blocks<T>()) k_tiledN_reduce(TiledNArgs<T, V> a) {
     count_launch(a.ctl);
     constexpr int K0 = RED_K0;
     __shared__ T stage[8][K0][32];
