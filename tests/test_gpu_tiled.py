@@ -22,10 +22,33 @@ def _geo(kind):
     if kind == "big":
         # 160^3 voxels (8,000 tiles of 8^3): A*x takes 16 x 8 x 8 tiles
         return W.hemisphere_geometry(160, 24, 24, seed=2)
+    if kind == "mixed":
+        return _mixed_geometry()
     return W.hemisphere_geometry(40, 48, 48, seed=1)
 
 
-@pytest.mark.parametrize("kind", ["ring", "hemi", "dense_ring", "big"])
+def _mixed_geometry(nv=96, ne=25, nr=28, seed=3):
+    """Transducers on a sphere of radius 0.95 nv around a 96^3 volume: 700
+    rays (not a multiple of the reduction's 32-ray groups or 256-ray windows),
+    333 of them missing the grid (empty rows), 110 crossing more than 16 of
+    the 8^3 tiles (the per-ray reduction's loads past its staged partials)."""
+    from tval3_gb300.api import Geometry
+    rng = np.random.default_rng(seed)
+    c = nv / 2.0
+
+    def pts(k):
+        u = rng.normal(size=(k, 3))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        return c + 0.95 * nv * u
+
+    em, rc = pts(ne), pts(nr)
+    ie, ir = ([np.clip(np.floor(P[:, a]), 0, nv - 1).astype(np.int32) for a in range(3)] for P in (em, rc))
+    return Geometry(rv_x=nv, rv_y=nv, rv_z=nv, x_emitters=ie[0], y_emitters=ie[1], z_emitters=ie[2],
+                    x_receivers=ir[0], y_receivers=ir[1], z_receivers=ir[2], num_emitters=ne, num_receivers=nr,
+                    traversal=1, pos=tuple(em[:, a].copy() for a in range(3)) + tuple(rc[:, a].copy() for a in range(3)))
+
+
+@pytest.mark.parametrize("kind", ["ring", "hemi", "dense_ring", "big", "mixed"])
 @pytest.mark.parametrize("prec", ["fp32", "df64", "bf16"])
 @pytest.mark.parametrize("trans", [1, 0])
 def test_tiled_products_match_plain_csr(cuda, kind, prec, trans):

@@ -699,8 +699,10 @@ __global__ void __launch_bounds__(256, 4) k_g2_gradient(SolverBufs<T> B, Geo geo
 // either accepts the first admissible a or asks for the restart (cnt == 5,
 // :876-882).  k_bt_apply materialises the accepted point once.
 // ---------------------------------------------------------------------------
+// Three blocks per SM (80 registers): with the ten compensated accumulators
+// and the pair loads, 64 registers spill 24 bytes in double-float.
 template <class T>
-__global__ void __launch_bounds__(256, 4) k_bt_coef(SolverBufs<T> B) {
+__global__ void __launch_bounds__(256, 3) k_bt_coef(SolverBufs<T> B) {
     Ctl* ctl = B.ctl;
     count_launch(ctl);
     using A = acc_t<T>;
@@ -712,28 +714,50 @@ __global__ void __launch_bounds__(256, 4) k_bt_coef(SolverBufs<T> B) {
     // compensated product sums (ProdAcc), as in the other reductions
     ProdAcc<A> a2, b2, c2, a4, b4, a3, b3, c3, a5, b5;
     const long N = n > m ? n : m;
-    GRID_STRIDE(i, N) {
-        if (i < n) {
+    auto vox = [&](T dp, T w, T du, T sg) {
+        const A v0 = to_acc(dp - w), dv = to_acc(du - dp), s = to_acc(sg);
+        a2.add(v0, v0);
+        b2.add(v0, dv);
+        c2.add(dv, dv);
+        a4.add(s, v0);
+        b4.add(s, dv);
+    };
+    auto ray = [&](T ap, T b_, T au, T d_) {
+        const A r0 = to_acc(ap) - to_acc(b_), dr = to_acc(au) - to_acc(ap), d = to_acc(d_);
+        a3.add(r0, r0);
+        b3.add(r0, dr);
+        c3.add(dr, dr);
+        a5.add(d, r0);
+        b5.add(d, dr);
+    };
+    if (n % 2 == 0 && m % 2 == 0) {
+        // two elements per 16-byte (8-byte for float) access
+        GRID_STRIDE_PAIRS(i, N) {
+            if (i < n) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const long k = c * n + i;
-                const T dp = DUp[k];
-                const A v0 = to_acc(dp - W[k]), dv = to_acc(DU[k] - dp), s = to_acc(S[k]);
-                a2.add(v0, v0);
-                b2.add(v0, dv);
-                c2.add(dv, dv);
-                a4.add(s, v0);
-                b4.add(s, dv);
+                for (int c = 0; c < 3; ++c) {
+                    const long k = c * n + i;
+                    const Two<T> dp = ld2(DUp + k), w = ld2(W + k), du = ld2(DU + k), sg = ld2(S + k);
+                    vox(dp.a, w.a, du.a, sg.a);
+                    vox(dp.b, w.b, du.b, sg.b);
+                }
+            }
+            if (i < m) {
+                const Two<T> ap = ld2(Aup + i), b_ = ld2(bb + i), au = ld2(Au + i), d_ = ld2(dl + i);
+                ray(ap.a, b_.a, au.a, d_.a);
+                ray(ap.b, b_.b, au.b, d_.b);
             }
         }
-        if (i < m) {
-            const T ap = Aup[i];
-            const A r0 = to_acc(ap) - to_acc(bb[i]), dr = to_acc(Au[i]) - to_acc(ap), d = to_acc(dl[i]);
-            a3.add(r0, r0);
-            b3.add(r0, dr);
-            c3.add(dr, dr);
-            a5.add(d, r0);
-            b5.add(d, dr);
+    } else {
+        GRID_STRIDE(i, N) {
+            if (i < n) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const long k = c * n + i;
+                    vox(DUp[k], W[k], DU[k], S[k]);
+                }
+            }
+            if (i < m) ray(Aup[i], bb[i], Au[i], dl[i]);
         }
     }
     double v[10] = {a2.value(), b2.value(), c2.value(), a4.value(), b4.value(),
