@@ -1258,7 +1258,7 @@ void TiledN<T, V>::build(long m_, int p_, int q_, int r_, const int* ptr, const 
                                                  sbits, s));
         TV3_CUDA(cudaStreamSynchronize(s));
     }
-    // ray-major order of the partials: (ray, tile)
+    // segments in (ray, tile) order: each ray's partials are numbered in tile order
     const int rbits = ray_bits + tile_bits;
     {
         size_t tb = 0;

@@ -127,7 +127,7 @@ struct TiledNArgs {
     const int* slot_dest;        // 32 per slice: index of the segment's partial in `part` (-1: padding)
     const unsigned short* lidx;  // local voxel of each nonzero in its tile (0 in padding)
     const V* val;                // value (0 in padding)
-    T* part;                     // one partial per segment, ray-major
+    T* part;                     // one partial per segment, in groups of 32 ray slots (gbase)
     const int* sray;             // m: the ray of each slot (slots: rays ranked by length in windows of 256)
     const int* rlen;             // m: partials (segments) of the ray in each slot
     const long long* gbase;      // per 32 slots: partial k of the ray in slot s is part[gbase[s/32] + 32 k + s%32]
