@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(256) k_dense_N(long m, long n, const V* __rest
             if (EPI == SPMV_LAM35) {
                 c->lam3 = tot[0];
                 c->lam5 = tot[1];
+                lam35_post(c);
             } else {
                 c->Add = tot[0];
                 c->tau = fabs(c->dd / (c->dDd + c->muDbeta * c->Add));
@@ -158,6 +159,7 @@ __global__ void __launch_bounds__(256) k_dense_NL(long m, long n, int L, const V
             if (EPI == SPMV_LAM35) {
                 c->lam3 = tot[0];
                 c->lam5 = tot[1];
+                lam35_post(c);
             } else {
                 c->Add = tot[0];
                 c->tau = fabs(c->dd / (c->dDd + c->muDbeta * c->Add));

@@ -300,6 +300,7 @@ __global__ void __launch_bounds__(256) k_umma_reduce(long M, int L, int splits, 
             if (EPI == SPMV_LAM35) {
                 c->lam3 = tt[0];
                 c->lam5 = tt[1];
+                lam35_post(c);
             } else {
                 c->Add = tt[0];
                 c->tau = fabs(c->dd / (c->dDd + c->muDbeta * c->Add));

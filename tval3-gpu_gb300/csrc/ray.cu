@@ -318,6 +318,7 @@ __device__ __forceinline__ void ray_epi_finish(const MatIO<float>& io, double ac
             if (EPI == SPMV_LAM35) {
                 c->lam3 = tot[0];
                 c->lam5 = tot[1];
+                lam35_post(c);
             } else {
                 c->Add = tot[0];
                 c->tau = fabs(c->dd / (c->dDd + c->muDbeta * c->Add));

@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(256) k_spmv(SpmvArgs<T, V> a) {
             if (EPI == SPMV_LAM35) {
                 c->lam3 = tot[0];
                 c->lam5 = tot[1];
+                lam35_post(c);
             } else {
                 // first inner iteration: tau = |<d,d> / (||Dd||^2 + mu/beta ||Ad||^2)|
                 c->Add = tot[0];
@@ -239,6 +240,7 @@ __global__ void __launch_bounds__(256) k_spmm(SpmvArgs<T, V> a) {
             if (EPI == SPMV_LAM35) {
                 c->lam3 = tot[0];
                 c->lam5 = tot[1];
+                lam35_post(c);
             } else {
                 c->Add = tot[0];
                 c->tau = fabs(c->dd / (c->dDd + c->muDbeta * c->Add));

@@ -9,7 +9,8 @@
 // Reference counterparts (3d/tval3_gpu_3d.cpp unless noted):
 //   k_D_only / k_descend   D_gpu :271-314 (+ axpy and nonneg_kernel, :671-701;
 //                          k_descend also lam2_4_kernel's sums at the new point)
-//   k_armijo               f and the Armijo test, min_u_gpu :848-858
+//   armijo_decide          f and the Armijo test, min_u_gpu :848-858 (run by the A*U
+//                          product's lam3/lam5 epilogue, tval3_internal.cuh)
 //   k_Dd_norm              get_tau_gpu first iteration :583-600
 //   k_gradient (BB step)   get_tau_kernel, 3d/tval3_gpu_3d_kernels.cu:1017-1067
 //   k_g2                   V = DU - W, lam2_4_kernel, Dt_gpu (get_g_gpu :484-571)
@@ -265,7 +266,7 @@ __device__ __forceinline__ void shrink_voxel(T d0, T d1, T d2, T s0, T s1, T s2,
 // DU is in registers instead of by a second pass over DU, W and sigma).  The
 // same pass forms update_W's shrinkage of the full step into the free W slot
 // with its lam1, lam2, lam4: most steps pass the Armijo test, which then
-// commits it (k_armijo) and no shrinkage pass runs.  U at the forward
+// commits it (armijo_decide) and no shrinkage pass runs.  U at the forward
 // neighbours is recomputed from Up and d (same expression, so bit-identical
 // to the stored value).  Normal mode reads the current slot, writes the other
 // one and flips the parity (the previous values become Up, gp, g2p, Aup, DUp
@@ -360,6 +361,11 @@ __global__ void __launch_bounds__(256, 4) k_descend(SolverBufs<T> B, Geo g, int 
         ctl->lam2s = tot[3];
         ctl->lam4s = tot[4];
         if (!restart) ctl->parity = 1 - cur;
+        // the A*U product that follows takes the Armijo decision in its
+        // lam3/lam5 epilogue
+        ctl->post_mode = restart ? EPI_G2_RESTART : EPI_G2_DESCEND;
+        ctl->post_graph = B.use_graph;
+        ctl->post_h_arm = B.h_arm;
     }
 }
 
@@ -386,15 +392,6 @@ __global__ void k_Dd_norm(SolverBufs<T> B, Geo g) {
     }
 }
 
-__device__ __forceinline__ double fval(const Ctl* c) {
-    return c->lam1 + c->beta / 2 * c->lam2 + c->mu / 2 * c->lam3 - c->lam4 - c->lam5;
-}
-
-__device__ __forceinline__ void armijo(Ctl* c) {
-    // |f| > |C - alpha * c_armij| : step rejected (:848, :855)
-    const int fail = fabs(c->f) > fabs(c->C - c->alpha * c->c_armij);
-    c->armijo_fail = fail;
-}
 
 // ---------------------------------------------------------------------------
 // g2 = D^T (DU - W) with lam2 = ||DU - W||^2 and lam4 = <sigma, DU - W>
@@ -440,38 +437,6 @@ __global__ void k_g2(SolverBufs<T> B, Geo g) {
 // (:848-858): one thread, once A*U has supplied lam3 and lam5 (k_descend
 // supplied lam2 and lam4).  Sets the graph's Armijo IF condition.
 // ---------------------------------------------------------------------------
-template <class T>
-__global__ void k_armijo(SolverBufs<T> B, int mode) {
-    Ctl* ctl = B.ctl;
-    count_launch(ctl);
-    if (threadIdx.x != 0) return;
-    ctl->f = fval(ctl);
-    if (mode == EPI_G2_DESCEND) {
-        ctl->alpha = 1.0;
-        ctl->cnt = 0;
-        ctl->c_armij = ctl->dd * ctl->tau * ctl->c_arm * ctl->beta;
-        armijo(ctl);
-        if (ctl->armijo_fail) {
-            ctl->alpha *= ctl->gamma;
-        } else {
-            // full step accepted: update_W is the descent's speculative one
-            // (:1016-1029), then the nonmonotone reference values (:1176-1177)
-            ctl->wsel = 1 - ctl->wsel;
-            ctl->f -= ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
-            ctl->lam1 = ctl->lam1s;
-            ctl->lam2 = ctl->lam2s;
-            ctl->lam4 = ctl->lam4s;
-            ctl->f += ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
-            const double Qp = ctl->Q;
-            ctl->Q = ctl->gam * Qp + 1.0;
-            ctl->C = (ctl->gam * Qp * ctl->C + ctl->f) / ctl->Q;
-        }
-        if (B.use_graph) cudaGraphSetConditional(B.h_arm, ctl->armijo_fail ? 1u : 0u);
-    } else {
-        ctl->armijo_fail = 0;
-        if (mode == EPI_G2_RESTART) ctl->restarts += 1;
-    }
-}
 
 // ---------------------------------------------------------------------------
 // shrinkage: W = shrink(DU - sigma/beta, 1/beta), lam1 = TV(W), and the
@@ -1131,8 +1096,8 @@ template <class T> void launch_Dd_norm(SolverBufs<T>& B, cudaStream_t s) {
     rlaunch(k_Dd_norm<T>, B.grid, s, B, geo_of(B));
 }
 template <class T> void launch_g2(SolverBufs<T>& B, int mode, cudaStream_t s) {
-    if (mode == EPI_G2_DESCEND || mode == EPI_G2_RESTART) launch_k(k_armijo<T>, dim3(1), dim3(32), 0, s, B, mode);
-    else rlaunch(k_g2<T>, B.grid, s, B, geo_of(B));
+    // after a descent the A*U epilogue took the Armijo decision (lam35_post)
+    if (mode != EPI_G2_DESCEND && mode != EPI_G2_RESTART) rlaunch(k_g2<T>, B.grid, s, B, geo_of(B));
 }
 template <class T> void launch_shrink(SolverBufs<T>& B, int mode, cudaStream_t s) {
     if (B.n % 2 == 0) rlaunch(k_shrink<T, true>, B.grid, s, B, mode);

@@ -1180,6 +1180,7 @@ __global__ void __launch_bounds__(256, red_min_blocks<T>()) k_tiledN_reduce(Tile
             if (EPI == SPMV_LAM35) {
                 c->lam3 = tot[0];
                 c->lam5 = tot[1];
+                lam35_post(c);
             } else {
                 c->Add = tot[0];
                 c->tau = fabs(c->dd / (c->dDd + c->muDbeta * c->Add));

@@ -161,6 +161,12 @@ struct Ctl {
     // the Armijo test when the full step is accepted
     int wsel;
     double lam1s, lam2s, lam4s;
+    // The Armijo decision after a descent is taken by the one thread that
+    // finishes the A*U product's lam3/lam5 epilogue (lam35_post below):
+    // k_descend arms it (post_mode EPI_G2_DESCEND or EPI_G2_RESTART, with the
+    // graph's IF handle), and taking it clears post_mode.
+    int post_mode, post_graph;
+    unsigned long long post_h_arm;
 };
 
 // Programmatic dependent launch: a kernel launched with programmatic stream
@@ -187,6 +193,59 @@ enum Epi : int {
     EPI_G2_RESTART = 5,   // get_g after the restart descent: f
     EPI_G2_UPDATE_W = 6,  // update_W: f, Q, C
 };
+
+// f = lam1 + beta/2 lam2 + mu/2 lam3 - lam4 - lam5 (the augmented Lagrangian)
+__device__ __forceinline__ double fval(const Ctl* c) {
+    return c->lam1 + c->beta / 2 * c->lam2 + c->mu / 2 * c->lam3 - c->lam4 - c->lam5;
+}
+
+__device__ __forceinline__ void armijo(Ctl* c) {
+    // |f| > |C - alpha * c_armij| : step rejected (3d/tval3_gpu_3d.cpp:848, :855)
+    const int fail = fabs(c->f) > fabs(c->C - c->alpha * c->c_armij);
+    c->armijo_fail = fail;
+}
+
+// f and the nonmonotone Armijo test after a descent (min_u_gpu,
+// 3d/tval3_gpu_3d.cpp:848-858); one thread, once lam1..lam5 of the new point
+// are known.  After the restart descent only f is formed (:876-882).
+__device__ inline void armijo_decide(Ctl* ctl, int mode, int use_graph, unsigned long long h_arm) {
+    ctl->f = fval(ctl);
+    if (mode == EPI_G2_DESCEND) {
+        ctl->alpha = 1.0;
+        ctl->cnt = 0;
+        ctl->c_armij = ctl->dd * ctl->tau * ctl->c_arm * ctl->beta;
+        armijo(ctl);
+        if (ctl->armijo_fail) {
+            ctl->alpha *= ctl->gamma;
+        } else {
+            // full step accepted: update_W is the descent's speculative one
+            // (:1016-1029), then the nonmonotone reference values (:1176-1177)
+            ctl->wsel = 1 - ctl->wsel;
+            ctl->f -= ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
+            ctl->lam1 = ctl->lam1s;
+            ctl->lam2 = ctl->lam2s;
+            ctl->lam4 = ctl->lam4s;
+            ctl->f += ctl->lam1 + ctl->beta / 2 * ctl->lam2 - ctl->lam4;
+            const double Qp = ctl->Q;
+            ctl->Q = ctl->gam * Qp + 1.0;
+            ctl->C = (ctl->gam * Qp * ctl->C + ctl->f) / ctl->Q;
+        }
+        if (use_graph) cudaGraphSetConditional(h_arm, ctl->armijo_fail ? 1u : 0u);
+    } else {
+        ctl->armijo_fail = 0;
+        ctl->restarts += 1;
+    }
+}
+
+// Called by the thread that has just written lam3 and lam5 of an A*U
+// product: takes the Armijo decision that the descent armed, if any.
+__device__ __forceinline__ void lam35_post(Ctl* c) {
+    const int mode = c->post_mode;
+    if (mode) {
+        c->post_mode = 0;
+        armijo_decide(c, mode, c->post_graph, c->post_h_arm);
+    }
+}
 
 // ---------------------------------------------------------------------------
 // Value loads.  Matrix streams are read once per product: load them with the
