@@ -1096,22 +1096,22 @@ __global__ void __launch_bounds__(32 * (BULK_NC + 1)) k_spmv_tiledN(TiledNArgs<T
     if (!ok && lane == 0 && a.ctl) atomicOr(&a.ctl->err, (int)ERR_TILED_TIMEOUT);
 }
 
+// Blocks per SM of the per-ray reduction: six for float and double-float
+// partials (at most 40 registers), which its shared-memory stage allows; the
+// lam3/lam5 form otherwise takes 56 registers and runs four.  FP64 partials
+// would spill at 40.
+template <class T>
+constexpr int red_min_blocks() { return std::is_same<T, double>::value ? 1 : 6; }
+
 // Each ray's partials in tile order, one warp per group of 32 ray slots and
 // one lane per slot (rays of similar length, from one window of 256 rays).
 // The group's partials are interleaved (partial k of the ray in lane l's slot
 // at gbase + 32 k + l), so the k-th copies of the 32 lanes are one coalesced
-// row.  Each lane copies its first K0 partials into
-// its own column of shared memory with asynchronous copies (all in flight at
-// once, no registers held), waits for its own copies and adds them in order
-// (for double-float partials a compensated sum: high parts by TwoSum, low
-// parts and errors in one FP32 term); longer rays load the rest directly.
-// Then the solver epilogues.
-// Six blocks per SM for float and double-float partials (at most 40
-// registers): the shared-memory stage allows six, and the lam3/lam5 form
-// otherwise takes 56 registers and runs four.  FP64 partials would spill.
-template <class T>
-constexpr int red_min_blocks() { return std::is_same<T, double>::value ? 1 : 6; }
-
+// row.  Each lane copies its first K0 partials into its own column of shared
+// memory with asynchronous copies (all in flight at once, no registers held),
+// waits for its own copies and adds them in order (for double-float partials
+// a compensated sum: high parts by TwoSum, low parts and errors in one FP32
+// term); longer rays load the rest directly.  Then the solver epilogues.
 template <class T, class V, int EPI>
 __global__ void __launch_bounds__(256, red_min_blocks<T>()) k_tiledN_reduce(TiledNArgs<T, V> a) {
     count_launch(a.ctl);
