@@ -392,7 +392,6 @@ __global__ void k_Dd_norm(SolverBufs<T> B, Geo g) {
     }
 }
 
-
 // ---------------------------------------------------------------------------
 // g2 = D^T (DU - W) with lam2 = ||DU - W||^2 and lam4 = <sigma, DU - W>
 // (start-up get_g; after a descent lam2 and lam4 come from k_descend, and the
@@ -431,12 +430,6 @@ __global__ void k_g2(SolverBufs<T> B, Geo g) {
         ctl->armijo_fail = 0;
     }
 }
-
-// ---------------------------------------------------------------------------
-// The Lagrangian at a new point and, after a descent, the Armijo test
-// (:848-858): one thread, once A*U has supplied lam3 and lam5 (k_descend
-// supplied lam2 and lam4).  Sets the graph's Armijo IF condition.
-// ---------------------------------------------------------------------------
 
 // ---------------------------------------------------------------------------
 // shrinkage: W = shrink(DU - sigma/beta, 1/beta), lam1 = TV(W), and the
