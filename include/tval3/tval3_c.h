@@ -183,6 +183,12 @@ TVAL3_API const char* tval3_last_error_message(void);
  * most 10).  No counterpart in the reference. */
 TVAL3_API tval3_status tval3_last_call_phases(double* secs, int n);
 TVAL3_API const char* tval3_version(void);
+/* Self-test of the bounded device waits: one warp waits `cycles` of SM clock
+ * (at most 4e9, about two seconds) on an mbarrier phase that nothing
+ * completes.  *timed_out = 1 when the wait gave up, as it must;
+ * *waited_cycles = the cycles it waited.  The pipelined kernels use the same
+ * wait with a limit of 4e9 cycles.  No counterpart in the reference. */
+TVAL3_API tval3_status tval3_selftest_bounded_wait(int64_t cycles, int* timed_out, int64_t* waited_cycles);
 
 /* ---------------------------------------------------------------------- *
  * Reference entry points.  U (dim_y x dim_x x dim_z, column-major) is output

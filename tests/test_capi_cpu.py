@@ -84,6 +84,10 @@ def test_null_arguments(lib):
     assert lib.tval3_batch_create(None, None, None, 0, None) == 1
     assert lib.tval3_batch_solve(None, None, None, None, None, None) == 1
     assert lib.tval3_gpu_batched(None, 0, None, None) == 1
+    t, w = C.c_int(-1), C.c_int64(0)
+    assert lib.tval3_selftest_bounded_wait(1000, None, None) == 1
+    assert lib.tval3_selftest_bounded_wait(-1, C.byref(t), C.byref(w)) == 1  # limit out of range
+    assert lib.tval3_selftest_bounded_wait(5_000_000_000, C.byref(t), C.byref(w)) == 1
 
 
 def test_batched_slice_errors(lib):

@@ -850,6 +850,16 @@ tval3_status tval3_op_shape(tval3_op op, int* rows, int* cols, int64_t* nnz) {
     });
 }
 
+tval3_status tval3_selftest_bounded_wait(int64_t cycles, int* timed_out, int64_t* waited_cycles) {
+    return guard([&] {
+        if (!timed_out || !waited_cycles) arg_error(TVAL3_ERR_ARG, "Argument error: timed_out or waited_cycles is NULL!");
+        if (cycles < 0 || cycles > 4000000000LL) arg_error(TVAL3_ERR_ARG, "Argument error: cycles outside [0, 4e9]!");
+        long long w = 0;
+        selftest_bounded_wait((long long)cycles, timed_out, &w);
+        *waited_cycles = (int64_t)w;
+    });
+}
+
 tval3_status tval3_op_device_bytes(tval3_op op, int64_t* bytes) {
     return guard([&] {
         if (!op || !bytes) arg_error(TVAL3_ERR_ARG, "Argument error: op or bytes is NULL!");

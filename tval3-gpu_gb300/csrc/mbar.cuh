@@ -30,11 +30,12 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
 }
-// bounded wait for the completion of phase `parity`; false on timeout.  Each
-// try_wait may suspend the thread until the phase completes or about a
-// microsecond passes (the suspend-time hint), so a waiting warp does not
-// spin on the issue slots that the working warps of its SM need.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
+// bounded wait (`limit` cycles of SM clock) for the completion of phase
+// `parity`; false on timeout.  Each try_wait may suspend the thread until the
+// phase completes or about a microsecond passes (the suspend-time hint), so a
+// waiting warp does not spin on the issue slots that the working warps of its
+// SM need.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity, long long limit = WAIT_CYCLES) {
     const unsigned a = smem_u32(b);
     const long long t0 = clock64();
     for (;;) {
@@ -45,7 +46,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
             : "r"(a), "r"(parity), "r"(1000u)
             : "memory");
         if (ok) return true;
-        if (clock64() - t0 > WAIT_CYCLES) return false;
+        if (clock64() - t0 > limit) return false;
     }
 }
 

@@ -187,6 +187,10 @@ LinOp<df64>* make_csr_op_df64q(long rows, long cols, long nnz, const int* d_ptr,
 void convert_to_df64(const double* in, void* out, long n, cudaStream_t s);
 void convert_from_df64(const void* in, double* out, long n, cudaStream_t s);
 
+// Bounded-wait self-test (selftest.cu): one warp waits `cycles` of SM clock
+// on an mbarrier phase that nothing completes.
+void selftest_bounded_wait(long long cycles, int* timed_out, long long* waited);
+
 // Differentiable shrinkage (shrink_ad.cu): W = shrink(v, t) and its adjoint.
 template <class T> void shrink_fwd(long n, const T* v, double t, int iso, T* W, cudaStream_t s);
 template <class T>

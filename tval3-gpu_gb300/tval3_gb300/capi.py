@@ -82,6 +82,7 @@ _SIG = {
     "tval3_options_default": (None, [C.POINTER(Options)]),
     "tval3_last_error_message": (C.c_char_p, []),
     "tval3_version": (C.c_char_p, []),
+    "tval3_selftest_bounded_wait": (_I, [C.c_int64, _P, _P]),
     "tval3_last_call_phases": (_I, [_P, _I]),
     "tval3_gpu_3d_sparse_f32": (_I, [_P, _I, _I, _I, _P, _P, _I, _P, _P, _I, _I, _I, _I, _P, _P]),
     "tval3_gpu_3d_sparse_f64": (_I, [_P, _I, _I, _I, _P, _P, _I, _P, _P, _I, _I, _I, _I, _P, _P]),
